@@ -1,0 +1,171 @@
+// Shared device infrastructure for the persistent Krylov kernels.
+//
+//  * GridCtl / grid_sync: a software grid barrier for kernels launched with
+//    cudaLaunchCooperativeKernel (all blocks co-resident). Every wait is
+//    bounded by a %globaltimer deadline; on expiry the kernel records
+//    CARPIO_GPU_ETIMEOUT in the error word and every block leaves at its next
+//    barrier. Nothing spins without a limit.
+//  * block_sum / grid_allreduce: fixed-order warp-shuffle + shared-memory
+//    trees, then a fixed-order sum of the per-block partials done redundantly
+//    by every block, so each block holds the same bits and the result does not
+//    depend on scheduling.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/carpio_gpu.h"
+
+namespace cg_dev {
+
+constexpr int kThreads = 256;            // threads per block of every solver
+constexpr int kWarps = kThreads / 32;
+constexpr int kMaxReduce = 6;            // values per grid all-reduce
+
+__device__ __forceinline__ unsigned long long globaltimer() {
+	unsigned long long t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+
+// L2-coherent loads for data written by other blocks of the same launch
+template<class T> __device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }
+
+struct GridCtl {
+	unsigned* count;          // arrivals at the current barrier
+	unsigned* gen;            // barrier generation
+	int* err;                 // first error code (0 = none)
+	double* partials;         // [2 banks][kMaxReduce][gridDim.x]
+	unsigned long long wait_ns;   // bound of one barrier wait
+	unsigned long long solve_ns;  // bound of the whole launch
+	unsigned long long deadline;  // absolute %globaltimer bound, set by start()
+	// each block stamps its own deadline when it starts
+	__device__ __forceinline__ void start() { deadline = globaltimer() + solve_ns; }
+};
+
+__device__ __forceinline__ int read_err(const GridCtl& c) {
+	return *(volatile int*)c.err;
+}
+
+__device__ __forceinline__ void set_err(const GridCtl& c, int code) {
+	atomicCAS(c.err, 0, code);
+}
+
+// Returns false once any block has recorded an error (timeout included);
+// callers then leave the kernel. All threads of the block get the same answer.
+__device__ __forceinline__ bool grid_sync(const GridCtl& c) {
+	__shared__ int s_ok;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		volatile unsigned* vgen = c.gen;
+		unsigned g = *vgen;
+		__threadfence();
+		unsigned ticket = atomicAdd(c.count, 1u);
+		if (ticket == gridDim.x - 1) {
+			// the last arrival also enforces the solve deadline, so a launch
+			// whose blocks never wait (one block) is bounded as well
+			if (globaltimer() > c.deadline) set_err(c, CARPIO_GPU_ETIMEOUT);
+			atomicExch(c.count, 0u);
+			__threadfence();
+			atomicAdd(c.gen, 1u);
+		} else {
+			unsigned long long t0 = globaltimer();
+			while (*vgen == g) {
+				if (*(volatile int*)c.err) break;
+				unsigned long long t = globaltimer();
+				if (t - t0 > c.wait_ns || t > c.deadline) {
+					set_err(c, CARPIO_GPU_ETIMEOUT);
+					break;
+				}
+				__nanosleep(32);
+			}
+		}
+		__threadfence();
+		s_ok = (read_err(c) == 0);
+	}
+	__syncthreads();
+	return s_ok != 0;
+}
+
+// Sum of NV values over the block in a fixed tree; every thread gets it.
+template<class R, int NV>
+__device__ __forceinline__ void block_sum(R (&v)[NV]) {
+	__shared__ R s_w[NV][kWarps];
+	__shared__ R s_out[NV];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+	for (int m = 0; m < NV; ++m) {
+		R x = v[m];
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+		if (lane == 0) s_w[m][warp] = x;
+	}
+	__syncthreads();
+	if (warp == 0) {
+#pragma unroll
+		for (int m = 0; m < NV; ++m) {
+			R x = lane < kWarps ? s_w[m][lane] : R(0);
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+			if (lane == 0) s_out[m] = x;
+		}
+	}
+	__syncthreads();
+#pragma unroll
+	for (int m = 0; m < NV; ++m) v[m] = s_out[m];
+	__syncthreads();
+}
+
+// Max of a non-negative value over the block (NaN never wins, matching
+// std::max(max, v) with max first).
+__device__ __forceinline__ double block_max(double v) {
+	__shared__ double s_w[kWarps];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+	for (int o = 16; o > 0; o >>= 1) {
+		double y = __shfl_down_sync(0xffffffffu, v, o);
+		v = (v < y) ? y : v;
+	}
+	if (lane == 0) s_w[warp] = v;
+	__syncthreads();
+	if (warp == 0) {
+		v = lane < kWarps ? s_w[lane] : 0.0;
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) {
+			double y = __shfl_down_sync(0xffffffffu, v, o);
+			v = (v < y) ? y : v;
+		}
+		if (lane == 0) s_w[0] = v;
+	}
+	__syncthreads();
+	v = s_w[0];
+	__syncthreads();
+	return v;
+}
+
+// Grid-wide sum of NV values (R = double or float). `bank` alternates 0/1 on
+// consecutive calls so a fast block never overwrites partials a slow block is
+// still reading. Returns false on error.
+template<class R, int NV>
+__device__ __forceinline__ bool grid_allreduce(R (&v)[NV], const GridCtl& c,
+		int& bank) {
+	block_sum<R, NV>(v);
+	double* part = c.partials + (size_t)bank * kMaxReduce * gridDim.x;
+	if (threadIdx.x == 0) {
+#pragma unroll
+		for (int m = 0; m < NV; ++m) part[m * gridDim.x + blockIdx.x] = (double)v[m];
+	}
+	bank ^= 1;
+	if (!grid_sync(c)) return false;
+#pragma unroll
+	for (int m = 0; m < NV; ++m) {
+		R acc = 0;
+		for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+			acc += (R)ldcg(&part[m * gridDim.x + b]);
+		v[m] = acc;
+	}
+	block_sum<R, NV>(v);
+	return true;
+}
+
+}  // namespace cg_dev

@@ -1,0 +1,126 @@
+// Host-side internals shared by the translation units of libcarpio_gpu.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <mutex>
+#include <vector>
+
+#include "../../include/carpio_gpu.h"
+#include "krylov.cuh"
+
+namespace cg_host {
+
+#define CG_CK(expr)                                                          \
+	do {                                                                     \
+		cudaError_t _e = (expr);                                             \
+		if (_e != cudaSuccess) { ::cg_host::note_cuda_error(_e); return CARPIO_GPU_ECUDA; } \
+	} while (0)
+
+void note_cuda_error(cudaError_t e);
+
+// true if p is memory the device can address directly
+bool is_device_ptr(const void* p);
+
+struct Watchdog {
+	unsigned wait_ms = 2000;
+	unsigned solve_ms = 600000;
+};
+Watchdog& watchdog();
+
+// Device-side control block of one persistent launch: barrier words, error
+// word and the all-reduce partials; reset before every launch.
+struct Ctl {
+	unsigned count;
+	unsigned gen;
+	int err;
+	int pad;
+	cg_dev::SolveOut out;
+};
+
+// A growable device buffer.
+struct DevBuf {
+	void* p = nullptr;
+	size_t bytes = 0;
+	int ensure(size_t n);
+	void release();
+	~DevBuf() { release(); }
+	template<class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// Everything a persistent Krylov launch needs besides the problem data.
+struct LaunchWs {
+	DevBuf ctl;        // Ctl
+	DevBuf partials;   // 2 * kMaxReduce * max_blocks doubles
+	Ctl* host_ctl = nullptr;   // pinned mirror for the results
+	int ensure(int max_blocks);
+	~LaunchWs();
+};
+
+int sm_count();
+
+// Number of blocks for a cooperative launch of `kernel` over `nwork` cells:
+// enough blocks to give every thread a few cells, never more than can be
+// co-resident.
+int coop_blocks(const void* kernel, long nwork, int min_cells_per_thread);
+
+cg_dev::GridCtl make_gridctl(LaunchWs& ws);
+
+// Copy a host-or-device array into a device buffer (async on s).
+int to_device(DevBuf& dst, const void* src, size_t bytes, cudaStream_t s);
+
+}  // namespace cg_host
+
+namespace cg_host {
+
+// Matrix-free coefficients of StencilPoisson_ + GhostRegular_ for one
+// (grid, bc, beta): D in the field layout, off-diagonal face coefficients
+// ax[nx+1], ay[ny+1] (0 on boundary faces) and the boundary constants the
+// ghost substitution adds to the row's constant (fold[0..3] = segments
+// x-, x+, y-, y+; lengths ny, ny, nx, nx). FP32 copies for the mixed solver.
+struct StencilCoeffs {
+	bool valid = false;
+	carpio_gpu_bc bc;
+	double beta = 0;
+	DevBuf D, ax, ay, fold, D32, ax32, ay32;
+};
+
+struct PoissonWs {
+	LaunchWs lw;
+	DevBuf v64, v32, src, phi, hist, out;
+};
+
+int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
+		StencilCoeffs& c, cudaStream_t s);
+
+// Source of the right-hand side: a cell field, or the divergence of two face
+// fields (Operation_::Div(VecF), s_operation.hpp:100-120) as the NS projection
+// passes it.
+enum { SRC_FIELD = 0, SRC_DIV = 1 };
+
+// One persistent launch: b from the source, x from phi's normal cells,
+// optional mean removal, the solve, optional mean removal, x back into phi.
+// All pointers are device pointers; the result lands in *out_dev.
+int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
+		int src_mode, const double* src_a, const double* src_b, double* phi,
+		const carpio_gpu_solver_cfg& cfg, double* hist_dev, int hist_cap,
+		cg_dev::SolveOut* out_dev, cudaStream_t s);
+
+}  // namespace cg_host
+
+// Grid handle (defined here so poisson.cu and ns.cu share it).
+struct carpio_gpu_grid {
+	int nx, ny, gl;
+	int NI, NJ;        // rows / columns incl. ghosts
+	int P;             // device row pitch (doubles)
+	std::vector<double> cx, sx, cy, sy;
+	double *d_cx = nullptr, *d_sx = nullptr, *d_cy = nullptr, *d_sy = nullptr;
+	cudaStream_t stream = nullptr;
+	int device = 0;
+	std::mutex mu;
+	cg_host::StencilCoeffs coeffs;   // cache for carpio_gpu_poisson_solve
+	cg_host::PoissonWs pws;
+};
+

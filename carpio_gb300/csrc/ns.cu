@@ -1,0 +1,745 @@
+// Explicit projection step of NS_explicit_ (lib/structure/s_ns_explicit.hpp:
+// 118-229) on the GPU, plus the single Operation_ operators.
+//
+// This file is compiled with --fmad=false: every expression below rounds
+// exactly like the reference's C++ (no contraction), and divisions and sqrt
+// are IEEE round-to-nearest, so the operators reproduce the reference's
+// doubles bit for bit. The projection's Krylov solve lives in poisson.cu.
+//
+// Fields are the reference's full arrays (ghosts included) in the device
+// layout of the grid: cell (i, j), i, j in normal-cell coordinates, at
+// (i + gl) * P + (j + gl).
+#include "internal.hpp"
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+using namespace cg_dev;
+
+constexpr double kSmall = 1e-10;  // SMALL, lib/type_define.hpp
+
+struct Geo {
+	int nx, ny, gl, P, NI, NJ;
+	const double *cx, *sx, *cy, *sy;   // incl. ghosts
+	__device__ __forceinline__ int at(int i, int j) const { return (i + gl) * P + (j + gl); }
+	__device__ __forceinline__ double CX(int i) const { return cx[i + gl]; }
+	__device__ __forceinline__ double CY(int j) const { return cy[j + gl]; }
+	__device__ __forceinline__ double SX(int i) const { return sx[i + gl]; }
+	__device__ __forceinline__ double SY(int j) const { return sy[j + gl]; }
+};
+
+struct BcDev {
+	int type[4];
+	double value[4];
+};
+
+__host__ __device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
+__host__ __device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
+
+// ------------------------------------------------------------ ghost fill --
+// Value Equation_::apply_bc (s_equation.hpp:340-378) gives ghost (i, j) when
+// its source cell (oi, oj) holds `src`.
+__device__ __forceinline__ double ghost_value(const Geo& g, const BcDev& bc,
+		int i, int j, double src, int& oi, int& oj) {
+	int seg, a;
+	oi = i;
+	oj = j;
+	if (i < 0 || i >= g.nx) { a = 0; seg = i < 0 ? 0 : 1; oi = i < 0 ? 0 : g.nx - 1; }
+	else { a = 1; seg = j < 0 ? 2 : 3; oj = j < 0 ? 0 : g.ny - 1; }
+	(void)src;
+	double val = bc.value[seg];
+	double cgh = a == 0 ? g.CX(i) : g.CY(j);
+	double co = a == 0 ? g.CX(oi) : g.CY(oj);
+	if (bc.type[seg] == 1) {
+		double hs = (a == 0 ? g.SX(oi) : g.SY(oj)) * 0.5;
+		double cf = (seg == 1 || seg == 3) ? co + hs : co - hs;
+		double u = (cgh - cf) / (co - cf);
+		return (val * (1.0 - u)) + (src * u);
+	}
+	double dl = fabs(cgh - co);
+	return src - val * dl;
+}
+
+// source cell of a ghost without evaluating it
+__device__ __forceinline__ void ghost_src(const Geo& g, int i, int j, int& oi, int& oj) {
+	oi = i;
+	oj = j;
+	if (i < 0 || i >= g.nx) oi = i < 0 ? 0 : g.nx - 1;
+	else oj = j < 0 ? 0 : g.ny - 1;
+}
+
+// One block per field. The reference visits ghosts in IJK order (x fastest)
+// and writes in place, so a corner ghost (x and y out of range) reads the
+// y-ghost of the first/last normal column of its row: the old value for the
+// low-x corners (visited first), the new one for the high-x corners. Phase 1
+// captures the old values the low-x corners need; phase 2 writes everything.
+struct BcFields {
+	double* f[2];
+	BcDev bc[2];
+};
+
+__global__ void __launch_bounds__(1024) k_apply_bc(Geo g, BcFields bf) {
+	double* f = bf.f[blockIdx.x];
+	const BcDev bc = bf.bc[blockIdx.x];
+	const int gl = g.gl, nx = g.nx, ny = g.ny;
+	const int NI = g.NI, NJ = g.NJ;
+	extern __shared__ double s_old[];   // [2 * gl (rows) * gl (cols)]
+	const int ncorner = 2 * gl * gl;     // low-x corners: I < gl, J < gl or J >= NJ-gl
+	for (int t = threadIdx.x; t < ncorner; t += blockDim.x) {
+		int r = t / gl, c = t - r * gl;   // r: ghost row 0..2gl-1, c: ghost column
+		int J = r < gl ? r : NJ - 2 * gl + r;
+		int i = c - gl, j = J - gl;
+		int oi, oj;
+		ghost_src(g, i, j, oi, oj);
+		s_old[t] = f[g.at(oi, oj)];
+	}
+	__syncthreads();
+	const long total = (long)NI * NJ;
+	// walk the ghost frame: rows J < gl and J >= NJ-gl fully, columns I < gl
+	// and I >= NI-gl for the other rows
+	const int frame_rows = 2 * gl;
+	const long n_rows = (long)frame_rows * NI;
+	const long n_cols = (long)(NJ - 2 * gl) * 2 * gl;
+	for (long t = threadIdx.x; t < n_rows + n_cols; t += blockDim.x) {
+		int I, J;
+		if (t < n_rows) {
+			int r = (int)(t / NI);
+			I = (int)(t - (long)r * NI);
+			J = r < gl ? r : NJ - 2 * gl + r;
+		} else {
+			long u = t - n_rows;
+			int r = (int)(u / (2 * gl));
+			int c = (int)(u - (long)r * 2 * gl);
+			J = gl + r;
+			I = c < gl ? c : NI - 2 * gl + c;
+		}
+		int i = I - gl, j = J - gl;
+		int oi, oj;
+		ghost_src(g, i, j, oi, oj);
+		double src;
+		bool xg = i < 0 || i >= nx, yg = j < 0 || j >= ny;
+		if (xg && yg) {
+			if (i < 0) {
+				int r = J < gl ? J : J - (NJ - 2 * gl);
+				src = s_old[r * gl + I];
+			} else {
+				// the y-ghost (nx-1, j) as this same call has just written it
+				int oi2, oj2;
+				ghost_src(g, oi, oj, oi2, oj2);
+				src = ghost_value(g, bc, oi, oj, f[g.at(oi2, oj2)], oi2, oj2);
+			}
+		} else {
+			src = f[g.at(oi, oj)];
+		}
+		f[(long)I * g.P + J] = ghost_value(g, bc, i, j, src, oi, oj);
+	}
+	(void)total;
+}
+
+// ------------------------------------------------------ advection schemes --
+// s_operation.hpp:313-628 (+ minmod, src/calculation/advection.hpp:1079-1081)
+__device__ __forceinline__ double limiter(int sch, double r, double R) {
+	switch (sch) {
+	case CARPIO_GPU_VANLEER: return 0.5 * R * (r + fabs(r)) / (R - 1 + r);
+	case CARPIO_GPU_SUPERBEE: return smax(smax(0.0, smin(R * r, 1.0)), smin(r, R));
+	case CARPIO_GPU_WAHYD:
+		if (r <= 1.0) return 0.5 * R * (r + fabs(r)) / (R - 1 + r);
+		return smin((r + R * r * fabs(r)) / (R + r * r), R);
+	case CARPIO_GPU_QUICK: return 0.75 * r + 0.25;
+	case CARPIO_GPU_CUI: return 2.0 / 3.0 * r + 1.0 / 3.0;
+	case CARPIO_GPU_UPWIND2: return r;
+	case CARPIO_GPU_MINMOD: return smax(0.0, smin(1.0, r));
+	}
+	return 0.0;
+}
+
+// one axis of VdotNabla at cell (i, j); D = 0 x, 1 y
+template<int SCH, int D>
+__device__ __forceinline__ double adv_axis(const Geo& g, const double* face,
+		const double* f, int i, int j) {
+	const int st = D == 0 ? g.P : 1;
+	const int a = g.at(i, j);
+#define F(k) f[a + (k) * st]
+#define C(k) (D == 0 ? g.CX(i + (k)) : g.CY(j + (k)))
+#define S(k) (D == 0 ? g.SX(i + (k)) : g.SY(j + (k)))
+	double fa0 = face[a], fam = face[a - st];
+	double veo = (fa0 + fam) * 0.5;
+	if (SCH == CARPIO_GPU_UPWIND1) {
+		if (veo > 0.0) return veo * (F(0) - F(-1)) / (C(0) - C(-1));
+		if (veo < 0.0) return veo * (F(1) - F(0)) / (C(1) - C(0));
+		return 0.0;
+	} else if (SCH == CARPIO_GPU_CENTER) {
+		return veo * (F(1) - F(-1)) / (C(1) - C(-1));
+	} else if (SCH == CARPIO_GPU_CENTER4) {
+		double din = (F(1) - F(-1)) / (C(1) - C(-1));
+		double dout = (F(2) - F(-2)) / (C(2) - C(-2));
+		return (4.0 * din - dout) / 3.0;
+	} else {
+		int Cm, Um, Dm, Cp, Up, Dp;
+		if (veo >= 0.0) {
+			Dm = 0; Cm = -1; Um = -2;
+			Dp = 1; Cp = 0; Up = -1;
+		} else if (veo < 0.0) {
+			Dm = -1; Cm = 0; Um = 1;
+			Dp = 0; Cp = 1; Up = 2;
+		} else {
+			Dm = Cm = Um = Dp = Cp = Up = 0;
+		}
+		double R, r, fp, fm;
+		R = (S(Dp) + S(Cp)) / S(Cp);
+		r = (F(Cp) - F(Up)) * (S(Dp) + S(Cp)) / (F(Dp) - F(Cp) + kSmall) / (S(Cp) + S(Up));
+		fp = F(Cp) + limiter(SCH, r, R) / R * (F(Dp) - F(Cp));
+		R = (S(Dm) + S(Cm)) / S(Cm);
+		r = (F(Cm) - F(Um)) * (S(Dm) + S(Cm)) / (F(Dm) - F(Cm) + kSmall) / (S(Cm) + S(Um));
+		fm = F(Cm) + limiter(SCH, r, R) / R * (F(Dm) - F(Cm));
+		return (fa0 * fp - fam * fm) / S(0);
+	}
+#undef F
+#undef C
+#undef S
+}
+
+template<int SCH>
+__device__ __forceinline__ double adv_cell(const Geo& g, const double* uf,
+		const double* vf, const double* f, int i, int j) {
+	double a0 = adv_axis<SCH, 0>(g, uf, f, i, j);
+	double a1 = adv_axis<SCH, 1>(g, vf, f, i, j);
+	double s = 0.0;
+	s += a0;
+	s += a1;
+	return s;
+}
+
+// NablaMuNabla(Vt mu, ...) (s_operation.hpp:664-688)
+__device__ __forceinline__ double diffusion(const Geo& g, double mu,
+		const double* f, int i, int j) {
+	const int a = g.at(i, j);
+	double t0, t1;
+	{
+		double dm = mu * (f[a] - f[a - g.P]) / (g.CX(i) - g.CX(i - 1));
+		double dp = mu * (f[a + g.P] - f[a]) / (g.CX(i + 1) - g.CX(i));
+		t0 = (dp - dm) / g.SX(i);
+	}
+	{
+		double dm = mu * (f[a] - f[a - 1]) / (g.CY(j) - g.CY(j - 1));
+		double dp = mu * (f[a + 1] - f[a]) / (g.CY(j + 1) - g.CY(j));
+		t1 = (dp - dm) / g.SY(j);
+	}
+	double res = 0.0;
+	res += t0;
+	res += t1;
+	return res;
+}
+
+// ------------------------------------------------------------- NS kernels --
+struct StepScalars {
+	double dt;                // current time step (Time_::_dt)
+	double t;                 // current time
+	unsigned long long maxmag_bits;   // max |u_c| of this step (as bits)
+	unsigned done;            // blocks finished with the max reduction
+	unsigned step;            // current step
+};
+
+struct DtRule {
+	double cfl, diff_number, diff_coef;
+	double mins, minx, miny;  // Grid_::min_size() and per axis
+};
+
+// NS_::restrict_time (s_ns.hpp:146-169): max_magnitude over the normal cells,
+// then the last block updates dt (it can only shrink).
+__global__ void __launch_bounds__(kThreads) k_restrict_time(Geo g,
+		const double* u, const double* v, StepScalars* ss, DtRule rule,
+		double* step_dt, int st) {
+	double m = 0.0;
+	const long n = (long)g.nx * g.ny;
+	for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n;
+			k += (long)gridDim.x * blockDim.x) {
+		int i = (int)(k / g.ny), j = (int)(k - (long)i * g.ny);
+		int a = g.at(i, j);
+		double s = 0;
+		s += u[a] * u[a];
+		s += v[a] * v[a];
+		m = smax(m, sqrt(s));
+	}
+	m = block_max(m);
+	__shared__ bool last;
+	if (threadIdx.x == 0) {
+		atomicMax(&ss->maxmag_bits, (unsigned long long)__double_as_longlong(m));
+		__threadfence();
+		last = atomicAdd(&ss->done, 1u) == gridDim.x - 1;
+	}
+	__syncthreads();
+	if (last && threadIdx.x == 0) {
+		__threadfence();
+		double maxmag = __longlong_as_double((long long)atomicAdd(&ss->maxmag_bits, 0ull));
+		double rdt = rule.cfl * rule.mins / maxmag;
+		double dt = ss->dt;
+		double rdt2 = dt;
+		if (rule.diff_number < 100) {
+			double den = 0.0;
+			den += 1.0 / (rule.minx * rule.minx);
+			den += 1.0 / (rule.miny * rule.miny);
+			rdt2 = rule.diff_number / rule.diff_coef / den;
+		}
+		if (dt > smin(rdt, rdt2)) dt = smin(rdt, rdt2);
+		ss->dt = dt;
+		ss->maxmag_bits = 0ull;
+		ss->done = 0u;
+		if (step_dt) step_dt[st] = dt;
+	}
+}
+
+// VectorCenter_::max_magnitude (s_vector.hpp:89-103) alone
+__global__ void __launch_bounds__(kThreads) k_maxmag(Geo g, const double* u,
+		const double* v, unsigned long long* out) {
+	double m = 0.0;
+	const long n = (long)g.nx * g.ny;
+	for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n;
+			k += (long)gridDim.x * blockDim.x) {
+		int i = (int)(k / g.ny), j = (int)(k - (long)i * g.ny);
+		int a = g.at(i, j);
+		double s = 0;
+		s += u[a] * u[a];
+		s += v[a] * v[a];
+		m = smax(m, sqrt(s));
+	}
+	m = block_max(m);
+	if (threadIdx.x == 0) atomicMax(out, (unsigned long long)__double_as_longlong(m));
+}
+
+// u* = u + dt (-adv + diff / rho) for both components
+// (NS_explicit_::_veo_star_center, s_ns_explicit.hpp:173-229)
+template<int SCH>
+__global__ void __launch_bounds__(kThreads) k_predictor(Geo g, const double* u,
+		const double* v, const double* uf, const double* vf, double* us,
+		double* vs, const StepScalars* ss, double rho, double mu) {
+	const double dt = ss->dt;
+	const long n = (long)g.nx * g.ny;
+	for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n;
+			k += (long)gridDim.x * blockDim.x) {
+		int i = (int)(k / g.ny), j = (int)(k - (long)i * g.ny);
+		int a = g.at(i, j);
+		{
+			double adv = adv_cell<SCH>(g, uf, vf, u, i, j);
+			double dif = diffusion(g, mu, u, i, j);
+			double src = 0;
+			us[a] = (-adv + (dif + src) / rho) * dt + u[a];
+		}
+		{
+			double adv = adv_cell<SCH>(g, uf, vf, v, i, j);
+			double dif = diffusion(g, mu, v, i, j);
+			double src = 0;
+			vs[a] = (-adv + (dif + src) / rho) * dt + v[a];
+		}
+	}
+}
+
+// Operation_::InterpolateC2F(VecC, VecF) (s_operation.hpp:166-187)
+__global__ void __launch_bounds__(kThreads) k_c2f(Geo g, const double* u,
+		const double* v, double* fx, double* fy) {
+	const long n = (long)g.nx * g.ny;
+	for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n;
+			k += (long)gridDim.x * blockDim.x) {
+		int i = (int)(k / g.ny), j = (int)(k - (long)i * g.ny);
+		int a = g.at(i, j);
+		double vc = u[a];
+		double hs = g.SX(i) * 0.5, hsp = g.SX(i + 1) * 0.5;
+		fx[a] = (u[a + g.P] * hs + vc * hsp) / (hs + hsp);
+		if (i == 0) {
+			double hsm = g.SX(i - 1) * 0.5;
+			fx[a - g.P] = (u[a - g.P] * hs + vc * hsm) / (hs + hsm);
+		}
+		vc = v[a];
+		hs = g.SY(j) * 0.5;
+		hsp = g.SY(j + 1) * 0.5;
+		fy[a] = (v[a + 1] * hs + vc * hsp) / (hs + hsp);
+		if (j == 0) {
+			double hsm = g.SY(j - 1) * 0.5;
+			fy[a - 1] = (v[a - 1] * hs + vc * hsm) / (hs + hsm);
+		}
+	}
+}
+
+// face gradient of Operation_::Grad (s_operation.hpp:46-72) at x face (i, j)
+// (between i and i+1; i = -1 is the low wall face, computed from cell 0)
+__device__ __forceinline__ double gx_at(const Geo& g, const double* phi, int i, int j) {
+	if (i >= 0) return (phi[g.at(i + 1, j)] - phi[g.at(i, j)]) / (g.CX(i + 1) - g.CX(i));
+	return (phi[g.at(-1, j)] - phi[g.at(0, j)]) / (g.CX(-1) - g.CX(0));
+}
+__device__ __forceinline__ double gy_at(const Geo& g, const double* phi, int i, int j) {
+	if (j >= 0) return (phi[g.at(i, j + 1)] - phi[g.at(i, j)]) / (g.CY(j + 1) - g.CY(j));
+	return (phi[g.at(i, -1)] - phi[g.at(i, 0)]) / (g.CY(-1) - g.CY(0));
+}
+
+// The end of run_one_step (s_ns_explicit.hpp:140-153) over every array
+// element: gradphi = Grad(phi); p = phi, p *= 1/dt on normal cells;
+// uf = us_f - gradphi; u = us - InterpolateF2C(gradphi).
+__global__ void __launch_bounds__(kThreads) k_correct(Geo g, const double* phi,
+		const double* us, const double* vs, const double* usf,
+		const double* vsf, double* u, double* v, double* uf, double* vf,
+		double* p, const StepScalars* ss) {
+	const double inv = 1.0 / ss->dt;
+	const long n = (long)g.NI * g.NJ;
+	for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n;
+			k += (long)gridDim.x * blockDim.x) {
+		int I = (int)(k / g.NJ), J = (int)(k - (long)I * g.NJ);
+		int i = I - g.gl, j = J - g.gl;
+		int a = I * g.P + J;
+		bool jin = j >= 0 && j < g.ny, iin = i >= 0 && i < g.nx;
+		double gx = (jin && i >= -1 && i < g.nx) ? gx_at(g, phi, i, j) : 0.0;
+		double gy = (iin && j >= -1 && j < g.ny) ? gy_at(g, phi, i, j) : 0.0;
+		uf[a] = usf[a] - gx;
+		vf[a] = vsf[a] - gy;
+		double gcx = 0.0, gcy = 0.0;
+		if (iin && jin) {
+			gcx = (gx + gx_at(g, phi, i - 1, j)) * 0.5;
+			gcy = (gy + gy_at(g, phi, i, j - 1)) * 0.5;
+		}
+		u[a] = us[a] - gcx;
+		v[a] = vs[a] - gcy;
+		p[a] = (iin && jin) ? phi[a] * inv : phi[a];
+	}
+}
+
+// ----------------------------------------------------- single operators --
+__global__ void k_op(Geo g, int which, int sch, double coef, const double* a,
+		const double* b, const double* c, double* o1, double* o2) {
+	const long n = (long)g.nx * g.ny;
+	for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n;
+			k += (long)gridDim.x * blockDim.x) {
+		int i = (int)(k / g.ny), j = (int)(k - (long)i * g.ny);
+		int x = g.at(i, j);
+		switch (which) {
+		case 0:
+			o1[x] = gx_at(g, a, i, j);
+			if (i == 0) o1[x - g.P] = gx_at(g, a, -1, j);
+			o2[x] = gy_at(g, a, i, j);
+			if (j == 0) o2[x - 1] = gy_at(g, a, i, -1);
+			break;
+		case 1: {
+			double d = 0;
+			d += (a[x] - a[x - g.P]) / g.SX(i);
+			d += (b[x] - b[x - 1]) / g.SY(j);
+			o1[x] = d;
+			break;
+		}
+		case 2:
+			o1[x] = (a[x] + a[x - g.P]) * 0.5;
+			o2[x] = (b[x] + b[x - 1]) * 0.5;
+			break;
+		case 4: {
+			double r = 0;
+			switch (sch) {
+#define CASE(S) case S: r = adv_cell<S>(g, a, b, c, i, j); break;
+			CASE(CARPIO_GPU_UPWIND1) CASE(CARPIO_GPU_CENTER) CASE(CARPIO_GPU_CENTER4)
+			CASE(CARPIO_GPU_UPWIND2) CASE(CARPIO_GPU_VANLEER) CASE(CARPIO_GPU_SUPERBEE)
+			CASE(CARPIO_GPU_WAHYD) CASE(CARPIO_GPU_QUICK) CASE(CARPIO_GPU_CUI)
+			CASE(CARPIO_GPU_MINMOD)
+#undef CASE
+			}
+			o1[x] = r;
+			break;
+		}
+		case 5:
+			o1[x] = diffusion(g, coef, c, i, j);
+			break;
+		}
+	}
+}
+
+// ---------------------------------------------------------------- host --
+Geo make_geo(const carpio_gpu_grid* g) {
+	Geo e;
+	e.nx = g->nx;
+	e.ny = g->ny;
+	e.gl = g->gl;
+	e.P = g->P;
+	e.NI = g->NI;
+	e.NJ = g->NJ;
+	e.cx = g->d_cx;
+	e.sx = g->d_sx;
+	e.cy = g->d_cy;
+	e.sy = g->d_sy;
+	return e;
+}
+
+BcDev to_dev(const carpio_gpu_bc& b) {
+	BcDev d;
+	for (int k = 0; k < 4; ++k) {
+		d.type[k] = b.type[k];
+		d.value[k] = b.value[k];
+	}
+	return d;
+}
+
+int grid_blocks(long n) {
+	long b = (n + kThreads - 1) / kThreads;
+	long cap = (long)cg_host::sm_count() * 8;
+	return (int)(b < 1 ? 1 : (b > cap ? cap : b));
+}
+
+cudaError_t launch_bc(const Geo& geo, double* f0, const carpio_gpu_bc& b0,
+		double* f1, const carpio_gpu_bc* b1, cudaStream_t s) {
+	BcFields bf;
+	bf.f[0] = f0;
+	bf.bc[0] = to_dev(b0);
+	bf.f[1] = f1;
+	bf.bc[1] = b1 ? to_dev(*b1) : bf.bc[0];
+	size_t smem = sizeof(double) * 2 * geo.gl * geo.gl;
+	k_apply_bc<<<b1 ? 2 : 1, 1024, smem, s>>>(geo, bf);
+	return cudaGetLastError();
+}
+
+template<int SCH>
+cudaError_t launch_pred(const Geo& geo, int blocks, cudaStream_t s,
+		const double* u, const double* v, const double* uf, const double* vf,
+		double* us, double* vs, const StepScalars* ss, double rho, double mu) {
+	k_predictor<SCH><<<blocks, kThreads, 0, s>>>(geo, u, v, uf, vf, us, vs, ss, rho, mu);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_predictor(int sch, const Geo& geo, int blocks, cudaStream_t s,
+		const double* u, const double* v, const double* uf, const double* vf,
+		double* us, double* vs, const StepScalars* ss, double rho, double mu) {
+	switch (sch) {
+#define CASE(S) case S: return launch_pred<S>(geo, blocks, s, u, v, uf, vf, us, vs, ss, rho, mu);
+	CASE(CARPIO_GPU_UPWIND1) CASE(CARPIO_GPU_CENTER) CASE(CARPIO_GPU_CENTER4)
+	CASE(CARPIO_GPU_UPWIND2) CASE(CARPIO_GPU_VANLEER) CASE(CARPIO_GPU_SUPERBEE)
+	CASE(CARPIO_GPU_WAHYD) CASE(CARPIO_GPU_QUICK) CASE(CARPIO_GPU_CUI)
+	CASE(CARPIO_GPU_MINMOD)
+#undef CASE
+	}
+	return cudaErrorInvalidValue;
+}
+
+bool valid_bc(const carpio_gpu_bc& b) {
+	for (int k = 0; k < 4; ++k)
+		if (b.type[k] != 1 && b.type[k] != 2) return false;
+	return true;
+}
+
+}  // namespace
+
+struct carpio_gpu_ns {
+	carpio_gpu_grid* g;
+	carpio_gpu_ns_cfg cfg;
+	cg_host::DevBuf fields;       // u v uf vf phi p us vs usf vsf
+	double* f[10];
+	cg_host::DevBuf scal;         // StepScalars
+	cg_host::DevBuf rec, rec_dt;  // per-step records
+	cg_host::StencilCoeffs coeffs;
+	cg_host::PoissonWs pws;
+	cudaStream_t s;
+	DtRule rule;
+	double t_host = 0;
+};
+
+extern "C" {
+
+int carpio_gpu_ns_create(carpio_gpu_grid* g, const carpio_gpu_ns_cfg* cfg,
+		double dt0, carpio_gpu_ns** out) {
+	using namespace cg_host;
+	if (!g || !cfg || !out || !(dt0 > 0) || g->gl < 2 || cfg->scheme < 0
+			|| cfg->scheme > 9 || !valid_bc(cfg->bc_u) || !valid_bc(cfg->bc_v)
+			|| !(cfg->rho != 0) || cfg->projection.kind != CARPIO_GPU_CG)
+		return CARPIO_GPU_EINVAL;
+	*out = nullptr;
+	carpio_gpu_ns* ns = new carpio_gpu_ns();
+	ns->g = g;
+	ns->cfg = *cfg;
+	ns->s = g->stream;
+	const size_t NF = (size_t)g->NI * g->P;
+	if (ns->fields.ensure(sizeof(double) * NF * 10) || ns->scal.ensure(sizeof(StepScalars))) {
+		delete ns;
+		return CARPIO_GPU_ENOMEM;
+	}
+	for (int k = 0; k < 10; ++k) ns->f[k] = ns->fields.as<double>() + k * NF;
+	StepScalars ss;
+	std::memset(&ss, 0, sizeof ss);
+	ss.dt = dt0;
+	if (cudaMemsetAsync(ns->fields.p, 0, ns->fields.bytes, ns->s) != cudaSuccess
+			|| cudaMemcpyAsync(ns->scal.p, &ss, sizeof ss, cudaMemcpyHostToDevice, ns->s) != cudaSuccess
+			|| cudaStreamSynchronize(ns->s) != cudaSuccess) {
+		note_cuda_error(cudaGetLastError());
+		delete ns;
+		return CARPIO_GPU_ECUDA;
+	}
+	// Grid_::min_size (s_grid.hpp:173-185), cell sizes incl. ghosts
+	double mx = 1.79769313486231570815e308, my = mx;
+	for (double v : g->sx) mx = smin(mx, v);
+	for (double v : g->sy) my = smin(my, v);
+	ns->rule.cfl = cfg->cfl;
+	ns->rule.diff_number = cfg->diff_number;
+	ns->rule.diff_coef = cfg->diff_coef;
+	ns->rule.minx = mx;
+	ns->rule.miny = my;
+	ns->rule.mins = smin(smin(1.79769313486231570815e308, mx), my);
+	*out = ns;
+	return 0;
+}
+
+int carpio_gpu_ns_destroy(carpio_gpu_ns* ns) {
+	if (!ns) return CARPIO_GPU_EINVAL;
+	cudaStreamSynchronize(ns->s);
+	delete ns;
+	return 0;
+}
+
+static int copy_field(carpio_gpu_grid* g, double* dst, const double* src,
+		bool to_dev, cudaStream_t s) {
+	const size_t wb = sizeof(double) * g->NJ, pb = sizeof(double) * g->P;
+	if (to_dev) CG_CK(cudaMemcpy2DAsync(dst, pb, src, wb, wb, g->NI, cudaMemcpyDefault, s));
+	else CG_CK(cudaMemcpy2DAsync(dst, wb, src, pb, wb, g->NI, cudaMemcpyDefault, s));
+	return 0;
+}
+
+int carpio_gpu_ns_set_state(carpio_gpu_ns* ns, double dt, const double* u,
+		const double* v, const double* uf, const double* vf,
+		const double* phi, const double* p) {
+	if (!ns || !(dt > 0)) return CARPIO_GPU_EINVAL;
+	const double* in[6] = { u, v, uf, vf, phi, p };
+	for (int k = 0; k < 6; ++k) {
+		if (!in[k]) continue;
+		int rc = copy_field(ns->g, ns->f[k], in[k], true, ns->s);
+		if (rc) return rc;
+	}
+	CG_CK(cudaMemcpyAsync(&((StepScalars*)ns->scal.p)->dt, &dt, sizeof dt,
+			cudaMemcpyHostToDevice, ns->s));
+	CG_CK(cudaStreamSynchronize(ns->s));
+	return 0;
+}
+
+int carpio_gpu_ns_get_state(carpio_gpu_ns* ns, double* dt, double* u,
+		double* v, double* uf, double* vf, double* phi, double* p) {
+	if (!ns) return CARPIO_GPU_EINVAL;
+	double* out[6] = { u, v, uf, vf, phi, p };
+	for (int k = 0; k < 6; ++k) {
+		if (!out[k]) continue;
+		int rc = copy_field(ns->g, out[k], ns->f[k], false, ns->s);
+		if (rc) return rc;
+	}
+	if (dt)
+		CG_CK(cudaMemcpyAsync(dt, &((StepScalars*)ns->scal.p)->dt, sizeof *dt,
+				cudaMemcpyDeviceToHost, ns->s));
+	CG_CK(cudaStreamSynchronize(ns->s));
+	return 0;
+}
+
+int carpio_gpu_ns_run(carpio_gpu_ns* ns, int steps, double* step_dt,
+		int* step_iters, double* step_resid) {
+	using namespace cg_host;
+	if (!ns || steps < 0) return CARPIO_GPU_EINVAL;
+	if (steps == 0) return 0;
+	carpio_gpu_grid* g = ns->g;
+	cudaStream_t s = ns->s;
+	int rc;
+	carpio_gpu_bc bc_phi;
+	for (int k = 0; k < 4; ++k) { bc_phi.type[k] = 2; bc_phi.value[k] = 0.0; }
+	if ((rc = stencil_prepare(g, bc_phi, 1.0, ns->coeffs, s))) return rc;
+	if ((rc = ns->rec.ensure(sizeof(cg_dev::SolveOut) * (size_t)steps))) return rc;
+	if ((rc = ns->rec_dt.ensure(sizeof(double) * (size_t)steps))) return rc;
+	const Geo geo = make_geo(g);
+	double *u = ns->f[0], *v = ns->f[1], *uf = ns->f[2], *vf = ns->f[3],
+		   *phi = ns->f[4], *p = ns->f[5], *us = ns->f[6], *vs = ns->f[7],
+		   *usf = ns->f[8], *vsf = ns->f[9];
+	StepScalars* ss = ns->scal.as<StepScalars>();
+	const int nb = grid_blocks((long)g->nx * g->ny);
+	const int nbf = grid_blocks((long)g->NI * g->NJ);
+	const carpio_gpu_ns_cfg& c = ns->cfg;
+	cg_dev::SolveOut* rec = ns->rec.as<cg_dev::SolveOut>();
+	for (int st = 0; st < steps; ++st) {
+		k_restrict_time<<<nb, kThreads, 0, s>>>(geo, u, v, ss, ns->rule,
+				ns->rec_dt.as<double>(), st);
+		CG_CK(cudaGetLastError());
+		CG_CK(launch_bc(geo, u, c.bc_u, v, &c.bc_v, s));
+		CG_CK(launch_predictor(c.scheme, geo, nb, s, u, v, uf, vf, us, vs, ss, c.rho, c.mu));
+		CG_CK(launch_bc(geo, us, c.bc_u, vs, &c.bc_v, s));
+		k_c2f<<<nb, kThreads, 0, s>>>(geo, us, vs, usf, vsf);
+		CG_CK(cudaGetLastError());
+		if ((rc = poisson_launch(g, ns->coeffs, ns->pws, SRC_DIV, usf, vsf, phi,
+				c.projection, nullptr, 0, rec + st, s)))
+			return rc;
+		CG_CK(launch_bc(geo, phi, bc_phi, nullptr, nullptr, s));
+		k_correct<<<nbf, kThreads, 0, s>>>(geo, phi, us, vs, usf, vsf, u, v, uf,
+				vf, p, ss);
+		CG_CK(cudaGetLastError());
+	}
+	std::vector<cg_dev::SolveOut> h(steps);
+	std::vector<double> hdt(steps);
+	CG_CK(cudaMemcpyAsync(h.data(), rec, sizeof(cg_dev::SolveOut) * steps,
+			cudaMemcpyDeviceToHost, s));
+	CG_CK(cudaMemcpyAsync(hdt.data(), ns->rec_dt.p, sizeof(double) * steps,
+			cudaMemcpyDeviceToHost, s));
+	CG_CK(cudaStreamSynchronize(s));
+	int first = 0;
+	for (int st = 0; st < steps; ++st) {
+		if (step_dt) step_dt[st] = hdt[st];
+		if (step_iters) step_iters[st] = h[st].iters;
+		if (step_resid) step_resid[st] = h[st].tol;
+		if (!first && h[st].code) first = h[st].code;
+		ns->t_host += hdt[st];
+	}
+	return first;
+}
+
+int carpio_gpu_operator(carpio_gpu_grid* g, int which, int scheme,
+		double coef, const carpio_gpu_bc* bc, const double* a,
+		const double* b, const double* c, double* out1, double* out2,
+		double* scalar) {
+	using namespace cg_host;
+	if (!g || which < 0 || which > 7) return CARPIO_GPU_EINVAL;
+	if (which == 4 && (scheme < 0 || scheme > 9 || g->gl < (scheme >= 2 ? 2 : 1)))
+		return CARPIO_GPU_EINVAL;
+	if (which == 6 && (!bc || !valid_bc(*bc) || !out1)) return CARPIO_GPU_EINVAL;
+	std::lock_guard<std::mutex> lock(g->mu);
+	cudaStream_t s = g->stream;
+	const size_t NF = (size_t)g->NI * g->P;
+	DevBuf buf;
+	int rc;
+	if ((rc = buf.ensure(sizeof(double) * NF * 5))) return rc;
+	double* d[5];
+	for (int k = 0; k < 5; ++k) d[k] = buf.as<double>() + k * NF;
+	CG_CK(cudaMemsetAsync(buf.p, 0, buf.bytes, s));
+	const double* in[3] = { a, b, c };
+	for (int k = 0; k < 3; ++k)
+		if (in[k] && (rc = copy_field(g, d[k], in[k], true, s))) return rc;
+	if (which == 3) {  // C2F writes into the caller's face arrays
+		if (out1 && (rc = copy_field(g, d[3], out1, true, s))) return rc;
+		if (out2 && (rc = copy_field(g, d[4], out2, true, s))) return rc;
+	}
+	if (which == 6 && (rc = copy_field(g, d[3], out1, true, s))) return rc;
+	const Geo geo = make_geo(g);
+	const int nb = grid_blocks((long)g->nx * g->ny);
+	if (which == 3) {
+		k_c2f<<<nb, kThreads, 0, s>>>(geo, d[0], d[1], d[3], d[4]);
+	} else if (which == 6) {
+		CG_CK(launch_bc(geo, d[3], *bc, nullptr, nullptr, s));
+	} else if (which == 7) {
+		DevBuf mb;
+		if ((rc = mb.ensure(sizeof(unsigned long long)))) return rc;
+		CG_CK(cudaMemsetAsync(mb.p, 0, sizeof(unsigned long long), s));
+		k_maxmag<<<nb, kThreads, 0, s>>>(geo, d[0], d[1], mb.as<unsigned long long>());
+		CG_CK(cudaGetLastError());
+		unsigned long long bits = 0;
+		CG_CK(cudaMemcpyAsync(&bits, mb.p, sizeof bits, cudaMemcpyDeviceToHost, s));
+		CG_CK(cudaStreamSynchronize(s));
+		double mxm;
+		std::memcpy(&mxm, &bits, sizeof mxm);
+		if (scalar) *scalar = mxm;
+		return 0;
+	} else {
+		k_op<<<nb, kThreads, 0, s>>>(geo, which, scheme, coef, d[0], d[1], d[2], d[3], d[4]);
+	}
+	CG_CK(cudaGetLastError());
+	if (out1 && (rc = copy_field(g, out1, d[3], false, s))) return rc;
+	if (out2 && which != 1 && which != 4 && which != 5 && which != 6
+			&& (rc = copy_field(g, out2, d[4], false, s)))
+		return rc;
+	CG_CK(cudaStreamSynchronize(s));
+	return 0;
+}
+
+}  // extern "C"

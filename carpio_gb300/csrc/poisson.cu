@@ -1,0 +1,546 @@
+// Structure-level Poisson solve on the GPU: the matrix-free form of
+// StencilPoisson_ + GhostRegular_ (lib/structure/s_poisson.hpp:60-114,
+// s_ghost.hpp:140-179, 334-357) behind structure::Solver_<2>::solve
+// (s_solver.hpp:77-171), in one persistent cooperative launch.
+//
+// Coefficients are computed on the host with the reference's formulas in the
+// reference's order, so D, the face coefficients and the right-hand side
+// carry the same bits as the CSR the reference assembles; only the Krylov
+// sums are ordered differently.
+#include "internal.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace {
+
+using namespace cg_dev;
+
+// ------------------------------------------------------------ device side --
+struct RhsArgs {
+	const double* sx;      // cell sizes incl. ghosts (device)
+	const double* sy;
+	const double* fold;    // [ny | ny | nx | nx]: x-, x+, y-, y+
+	const double* src_a;   // SRC_FIELD: source field; SRC_DIV: x-face field
+	const double* src_b;   // SRC_DIV: y-face field
+	double* phi;           // field: x0 in, solution out (normal cells)
+	int mean;
+};
+
+struct MixedArgs {
+	StencilOp<float> op32;
+	Vecs<float> f;         // e (x), r, p, q
+	double inner_tol;
+	int inner_max;
+};
+
+// Row constant of StencilPoisson_::coe_row + ghost folds, then b = -constant
+// (trimmed to +0 when the constant is exactly zero, s_solver.hpp:110-127).
+// Exact IEEE operations in the reference's order (no contraction).
+template<int SRC>
+__device__ __forceinline__ double rhs_at(const GridSpace& sp, const RhsArgs& ra,
+		int i, int j, int a) {
+	const int gl = sp.gl;
+	double sxi = ra.sx[i + gl];
+	double f;
+	if (SRC == cg_host::SRC_FIELD) {
+		f = ra.src_a[a];
+	} else {
+		// Operation_::Div(VecF) (s_operation.hpp:100-120)
+		double d = 0.0;
+		d = __dadd_rn(d, __ddiv_rn(__dsub_rn(ra.src_a[a], ra.src_a[a - sp.P]), sxi));
+		d = __dadd_rn(d, __ddiv_rn(__dsub_rn(ra.src_b[a], ra.src_b[a - 1]), ra.sy[j + gl]));
+		f = d;
+	}
+	double val = __dmul_rn(__dmul_rn(1.0, sxi), sxi);
+	val = __dmul_rn(val, f);
+	const int nx = sp.nx, ny = sp.ny;
+	if (i == 0) val = __dadd_rn(val, ra.fold[j]);
+	if (j == 0) val = __dadd_rn(val, ra.fold[2 * ny + i]);
+	if (j == ny - 1) val = __dadd_rn(val, ra.fold[2 * ny + nx + i]);
+	if (i == nx - 1) val = __dadd_rn(val, ra.fold[ny + j]);
+	return val == 0.0 ? 0.0 : -val;
+}
+
+// FP32 CG on A32 e = r32 from e = 0 (one inner solve of the refinement).
+// Returns the number of iterations, or -1 on a barrier error.
+__device__ int inner_cg(const GridSpace& sp, const MixedArgs& m, int cap,
+		const GridCtl& gc, int& bank) {
+	const Vecs<float>& f = m.f;
+	const StencilOp<float>& op = m.op32;
+	float rr0[1] = { 0 };
+	KLOOP(sp) {
+		int a = sp.addr(k);
+		float r = f.r[a];
+		f.x[a] = 0.f;
+		f.p[a] = r;
+		rr0[0] = fmaf(r, r, rr0[0]);
+	}
+	if (!grid_allreduce<float, 1>(rr0, gc, bank)) return -1;
+	float rho = rr0[0];
+	const float stop = (float)(m.inner_tol * m.inner_tol) * rho;
+	int it = 0;
+	while (it < cap && rho > stop && rho > 0.f) {
+		float pq[1] = { 0 };
+		KLOOP(sp) {
+			int a = sp.addr(k);
+			float q = op.apply(f.p, k, a);
+			f.q[a] = q;
+			pq[0] = fmaf(f.p[a], q, pq[0]);
+		}
+		if (!grid_allreduce<float, 1>(pq, gc, bank)) return -1;
+		float alpha = rho / pq[0];
+		float rr[1] = { 0 };
+		KLOOP(sp) {
+			int a = sp.addr(k);
+			f.x[a] = fmaf(alpha, f.p[a], f.x[a]);
+			float r = fmaf(-alpha, f.q[a], f.r[a]);
+			f.r[a] = r;
+			rr[0] = fmaf(r, r, rr[0]);
+		}
+		if (!grid_allreduce<float, 1>(rr, gc, bank)) return -1;
+		float beta = rr[0] / rho;
+		rho = rr[0];
+		++it;
+		if (it < cap && rho > stop) {
+			KLOOP(sp) { int a = sp.addr(k); f.p[a] = fmaf(beta, f.p[a], f.r[a]); }
+			if (!grid_sync(gc)) return -1;
+		}
+	}
+	return it;
+}
+
+// FP32 inner CG inside FP64 iterative refinement: r = b - A x, the stopping
+// test and the update of x in FP64; the correction solve in FP32 with FP32
+// accumulation, on the residual scaled to unit norm.
+__device__ void mixed_run(const GridSpace& sp, const StencilOp<double>& op,
+		const Vecs<double>& v, const MixedArgs& m, const SolveCtl& sc,
+		bool mean, const GridCtl& gc, int& bank) {
+	const bool full = (sc.flags & CARPIO_GPU_FLAG_FULL_NRM2) || sp.count() == 1;
+	const int la = sp.last_addr();
+	const double n = (double)sp.count();
+	int hl = 0, total = 0, outer = 0;
+	double acc[1] = { 0 };
+	KLOOP(sp) {
+		int a = sp.addr(k);
+		double bb = v.b[a];
+		if (a != la || full) acc[0] = fma(bb, bb, acc[0]);
+	}
+	if (!grid_allreduce<double, 1>(acc, gc, bank)) return;
+	double normb = sqrt(acc[0]);
+	if (normb == 0.0) normb = 1;
+	double resid = 0;
+	for (;;) {
+		double rs[3] = { 0, 0, 0 };
+		KLOOP(sp) {
+			int a = sp.addr(k);
+			double r = v.b[a] - op.apply(v.x, k, a);
+			v.r[a] = r;
+			if (a != la || full) rs[0] = fma(r, r, rs[0]);
+			rs[1] += r;
+			rs[2] = fma(r, r, rs[2]);
+		}
+		if (!grid_allreduce<double, 3>(rs, gc, bank)) return;
+		resid = sqrt(rs[0]) / normb;
+		hist_push(sc, hl, resid);
+		if (resid <= sc.tol) {
+			if (blockIdx.x == 0 && threadIdx.x == 0) { sc.out->outer = outer; sc.out->inner = total; }
+			finish(sc, 0, total, resid, hl);
+			return;
+		}
+		if (total >= sc.max_iter) break;
+		double mr = mean ? rs[1] / n : 0.0;
+		double rn = sqrt(mean ? fmax(rs[2] - rs[1] * mr, 0.0) : rs[2]);
+		if (!(rn > 0.0)) break;
+		double sc_in = 1.0 / rn;
+		KLOOP(sp) { int a = sp.addr(k); m.f.r[a] = (float)((v.r[a] - mr) * sc_in); }
+		if (!grid_sync(gc)) return;
+		int it = inner_cg(sp, m, min(m.inner_max, sc.max_iter - total), gc, bank);
+		if (it < 0) return;
+		total += it;
+		++outer;
+		KLOOP(sp) { int a = sp.addr(k); v.x[a] = fma(rn, (double)m.f.x[a], v.x[a]); }
+		if (!grid_sync(gc)) return;
+		if (it == 0) break;
+	}
+	if (blockIdx.x == 0 && threadIdx.x == 0) { sc.out->outer = outer; sc.out->inner = total; }
+	finish(sc, 1, total, resid, hl);
+}
+
+template<int SRC, int KIND>
+__global__ void __launch_bounds__(kThreads) k_poisson(StencilOp<double> op,
+		Vecs<double> v, RhsArgs ra, MixedArgs mx, SolveCtl sc, GridCtl gc) {
+	gc.start();
+	int bank = 0;
+	const GridSpace& sp = op.sp;
+	// prologue: b (bit-exact row constants), x0 from phi
+	double s[1] = { 0 };
+	KLOOP(sp) {
+		int i, j;
+		sp.ij(k, i, j);
+		int a = sp.addr(k);
+		double bb = rhs_at<SRC>(sp, ra, i, j, a);
+		v.b[a] = bb;
+		v.x[a] = ra.phi[a];
+		s[0] += bb;
+	}
+	if (ra.mean) {
+		// null-space removal of b: b - mean(b)
+		if (!grid_allreduce<double, 1>(s, gc, bank)) return;
+		double m = s[0] / (double)sp.count();
+		KLOOP(sp) { int a = sp.addr(k); v.b[a] = v.b[a] - m; }
+	}
+	if (!grid_sync(gc)) return;
+	if (KIND == 4) mixed_run(sp, op, v, mx, sc, ra.mean != 0, gc, bank);
+	else krylov_run<double>(sp, op, v, sc, gc, bank);
+	if (read_err(gc)) {
+		if (blockIdx.x == 0 && threadIdx.x == 0) sc.out->code = read_err(gc);
+		return;
+	}
+	// epilogue: mean removal of x, x back into phi
+	double mx0 = 0.0;
+	if (ra.mean) {
+		double t[1] = { 0 };
+		KLOOP(sp) { int a = sp.addr(k); t[0] += v.x[a]; }
+		if (!grid_allreduce<double, 1>(t, gc, bank)) {
+			if (blockIdx.x == 0 && threadIdx.x == 0) sc.out->code = read_err(gc);
+			return;
+		}
+		mx0 = t[0] / (double)sp.count();
+	}
+	KLOOP(sp) { int a = sp.addr(k); ra.phi[a] = ra.mean ? v.x[a] - mx0 : v.x[a]; }
+}
+
+template<int SRC>
+const void* pick_kernel(int kind, int precision) {
+	if (precision == CARPIO_GPU_MIXED) return (const void*)k_poisson<SRC, 4>;
+	switch (kind) {
+	case CARPIO_GPU_CG: return (const void*)k_poisson<SRC, CARPIO_GPU_CG>;
+	case CARPIO_GPU_JACOBI: return (const void*)k_poisson<SRC, CARPIO_GPU_JACOBI>;
+	default: return (const void*)k_poisson<SRC, CARPIO_GPU_BICGSTAB>;
+	}
+}
+
+bool same_bc(const carpio_gpu_bc& a, const carpio_gpu_bc& b) {
+	return std::memcmp(&a, &b, sizeof a) == 0;
+}
+
+}  // namespace
+
+namespace cg_host {
+
+int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
+		StencilCoeffs& c, cudaStream_t s) {
+	if (c.valid && same_bc(c.bc, bc) && c.beta == beta) return 0;
+	const int nx = g->nx, ny = g->ny, gl = g->gl, P = g->P;
+	auto CX = [&](int i) { return g->cx[i + gl]; };
+	auto CY = [&](int j) { return g->cy[j + gl]; };
+	auto SX = [&](int i) { return g->sx[i + gl]; };
+	auto SY = [&](int j) { return g->sy[j + gl]; };
+	std::vector<double> D((size_t)g->NI * P, 0.0), ax(nx + 1, 0.0), ay(ny + 1, 0.0);
+	std::vector<double> fold(2 * (size_t)ny + 2 * (size_t)nx, 0.0);
+	// ghost substitution of one boundary face (Ghost_::_substitute_ghost,
+	// s_ghost.hpp:140-179): returns the centre increment, adds the constant
+	auto ghost = [&](int seg, int i, int j, double coe, double& dcen,
+			double& cst) {
+		int a = seg < 2 ? 0 : 1;
+		int gi = i, gj = j, oi = i, oj = j;
+		if (seg == 0) gi = -1;
+		if (seg == 1) gi = nx;
+		if (seg == 2) gj = -1;
+		if (seg == 3) gj = ny;
+		double c0 = a == 0 ? CX(gi) : CY(gj);
+		double c1 = a == 0 ? CX(oi) : CY(oj);
+		double hs = (a == 0 ? SX(oi) : SY(oj)) * 0.5;
+		double cf = (seg == 1 || seg == 3) ? c1 + hs : c1 - hs;
+		double dl = std::fabs(c1 - c0);
+		double d0 = std::fabs(cf - c0);
+		double d1 = std::fabs(c1 - cf);
+		double val = bc.value[seg];
+		if (coe == 0) return;
+		if (bc.type[seg] == 1) {
+			dcen = dcen + -coe * d0 / d1;
+			cst = cst + coe * dl * val / d1;
+		} else {
+			dcen = dcen + coe;
+			cst = cst + -val * dl * coe;
+		}
+	};
+	for (int j = 0; j < ny; ++j) {
+		for (int i = 0; i < nx; ++i) {
+			double axf = SY(j) * 1.0, ayf = 1.0 * SX(i);
+			double cxp = (-beta) * axf / std::fabs(CX(i) - CX(i + 1));
+			double cxm = (-beta) * axf / std::fabs(CX(i) - CX(i - 1));
+			double cyp = (-beta) * ayf / std::fabs(CY(j) - CY(j + 1));
+			double cym = (-beta) * ayf / std::fabs(CY(j) - CY(j - 1));
+			double coec = 0;
+			coec += -cxm;
+			coec += -cxp;
+			coec += -cym;
+			coec += -cyp;
+			// boundary constants accumulate per segment cell; for a corner
+			// cell the x- fold and the y- fold land in different arrays and
+			// are added in map order (x-, y-, y+, x+) on the device
+			double cW = 0, cS = 0, cN = 0, cE = 0;
+			if (i == 0) ghost(0, i, j, cxm, coec, cW);
+			if (j == 0) ghost(2, i, j, cym, coec, cS);
+			if (j == ny - 1) ghost(3, i, j, cyp, coec, cN);
+			if (i == nx - 1) ghost(1, i, j, cxp, coec, cE);
+			D[(size_t)(i + gl) * P + (j + gl)] = coec;
+			if (i == 0) fold[j] = cW;
+			if (i == nx - 1) fold[ny + j] = cE;
+			if (j == 0) fold[2 * ny + i] = cS;
+			if (j == ny - 1) fold[2 * ny + nx + i] = cN;
+			if (j == 0) ax[i] = i == 0 ? 0.0 : cxm;
+			if (j == 0 && i == nx - 1) ax[nx] = 0.0;
+			if (i == 0) ay[j] = j == 0 ? 0.0 : cym;
+			if (i == 0 && j == ny - 1) ay[ny] = 0.0;
+		}
+	}
+	std::vector<float> D32(D.size()), ax32(ax.size()), ay32(ay.size());
+	for (size_t k = 0; k < D.size(); ++k) D32[k] = (float)D[k];
+	for (size_t k = 0; k < ax.size(); ++k) ax32[k] = (float)ax[k];
+	for (size_t k = 0; k < ay.size(); ++k) ay32[k] = (float)ay[k];
+	int rc;
+	if ((rc = to_device(c.D, D.data(), sizeof(double) * D.size(), s))) return rc;
+	if ((rc = to_device(c.ax, ax.data(), sizeof(double) * ax.size(), s))) return rc;
+	if ((rc = to_device(c.ay, ay.data(), sizeof(double) * ay.size(), s))) return rc;
+	if ((rc = to_device(c.fold, fold.data(), sizeof(double) * fold.size(), s))) return rc;
+	if ((rc = to_device(c.D32, D32.data(), sizeof(float) * D32.size(), s))) return rc;
+	if ((rc = to_device(c.ax32, ax32.data(), sizeof(float) * ax32.size(), s))) return rc;
+	if ((rc = to_device(c.ay32, ay32.data(), sizeof(float) * ay32.size(), s))) return rc;
+	CG_CK(cudaStreamSynchronize(s));  // host vectors go out of scope
+	c.bc = bc;
+	c.beta = beta;
+	c.valid = true;
+	return 0;
+}
+
+int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
+		int src_mode, const double* src_a, const double* src_b, double* phi,
+		const carpio_gpu_solver_cfg& cfg, double* hist_dev, int hist_cap,
+		cg_dev::SolveOut* out_dev, cudaStream_t s) {
+	const size_t NF = (size_t)g->NI * g->P;
+	const bool mixed = cfg.precision == CARPIO_GPU_MIXED;
+	const int nv64 = 13, nv32 = 4;
+	int rc;
+	if (w.v64.bytes < sizeof(double) * NF * nv64) {
+		if ((rc = w.v64.ensure(sizeof(double) * NF * nv64))) return rc;
+		CG_CK(cudaMemsetAsync(w.v64.p, 0, w.v64.bytes, s));   // zero ghost rings
+	}
+	if (mixed && w.v32.bytes < sizeof(float) * NF * nv32) {
+		if ((rc = w.v32.ensure(sizeof(float) * NF * nv32))) return rc;
+		CG_CK(cudaMemsetAsync(w.v32.p, 0, w.v32.bytes, s));
+	}
+	const void* kern = src_mode == SRC_DIV ? pick_kernel<SRC_DIV>(cfg.kind, cfg.precision)
+	                                       : pick_kernel<SRC_FIELD>(cfg.kind, cfg.precision);
+	long n = (long)g->nx * g->ny;
+	int blocks = coop_blocks(kern, n, 2);
+	if ((rc = w.lw.ensure(blocks))) return rc;
+	StencilOp<double> op;
+	op.sp = GridSpace{ g->nx, g->ny, g->gl, g->P };
+	op.D = c.D.as<double>();
+	op.ax = c.ax.as<double>();
+	op.ay = c.ay.as<double>();
+	Vecs<double> v;
+	double* base = w.v64.as<double>();
+	double** slots[nv64] = { &v.x, &v.b, &v.r, &v.p, &v.q, &v.z, &v.rt, &v.ph,
+		&v.s, &v.sh, &v.t, &v.v, &v.d };
+	for (int i = 0; i < nv64; ++i) *slots[i] = base + (size_t)i * NF;
+	MixedArgs mx;
+	mx.op32.sp = op.sp;
+	mx.op32.D = c.D32.as<float>();
+	mx.op32.ax = c.ax32.as<float>();
+	mx.op32.ay = c.ay32.as<float>();
+	std::memset(&mx.f, 0, sizeof mx.f);
+	if (mixed) {
+		float* fb = w.v32.as<float>();
+		mx.f.x = fb;
+		mx.f.r = fb + NF;
+		mx.f.p = fb + 2 * NF;
+		mx.f.q = fb + 3 * NF;
+	}
+	mx.inner_tol = cfg.inner_tol > 0 ? cfg.inner_tol : 1e-4;
+	mx.inner_max = cfg.inner_max_iter > 0 ? cfg.inner_max_iter : 1 << 30;
+	RhsArgs ra;
+	ra.sx = g->d_sx;
+	ra.sy = g->d_sy;
+	ra.fold = c.fold.as<double>();
+	ra.src_a = src_a;
+	ra.src_b = src_b;
+	ra.phi = phi;
+	ra.mean = cfg.mean_removal ? 1 : 0;
+	SolveCtl sc;
+	sc.kind = cfg.kind;
+	sc.max_iter = cfg.max_iter;
+	sc.tol = cfg.tol;
+	sc.flags = cfg.flags;
+	sc.hist = hist_dev;
+	sc.hist_cap = hist_dev ? hist_cap : 0;
+	sc.out = out_dev;
+	GridCtl gc = make_gridctl(w.lw);
+	CG_CK(cudaMemsetAsync(w.lw.ctl.p, 0, sizeof(Ctl), s));
+	CG_CK(cudaMemsetAsync(out_dev, 0, sizeof(cg_dev::SolveOut), s));
+	void* args[] = { &op, &v, &ra, &mx, &sc, &gc };
+	CG_CK(cudaLaunchCooperativeKernel(kern, blocks, kThreads, args, 0, s));
+	return 0;
+}
+
+}  // namespace cg_host
+
+// ------------------------------------------------------------------ C ABI --
+extern "C" {
+
+int carpio_gpu_grid_create_uniform(int nx, int ny, int gl, double xmin,
+		double xmax, double ymin, double ymax, carpio_gpu_grid** out) {
+	using namespace cg_host;
+	if (!out || nx < 1 || ny < 1 || gl < 1 || gl > 8 || !(xmax > xmin)
+			|| !(ymax > ymin) || (long)nx * ny > (1L << 30))
+		return CARPIO_GPU_EINVAL;
+	*out = nullptr;
+	carpio_gpu_grid* g = new carpio_gpu_grid();
+	g->nx = nx;
+	g->ny = ny;
+	g->gl = gl;
+	g->NI = nx + 2 * gl;
+	g->NJ = ny + 2 * gl;
+	g->P = (g->NJ + 31) / 32 * 32;
+	// Grid_::_set_uniform_grid (s_grid.hpp:372-395)
+	auto build = [](int n, int gl, double lo, double hi, std::vector<double>& c,
+			std::vector<double>& s) {
+		int N = n + 2 * gl;
+		double ds = (hi - lo) / n;
+		s.assign(N, ds);
+		c.assign(N, 0.0);
+		double csum = 0.0, llg = 0.0;
+		for (int i = 0; i < N; ++i) {
+			c[i] = csum + 0.5 * s[i];
+			csum += s[i];
+		}
+		for (int i = 0; i < gl; ++i) llg += s[i];
+		double sh = lo - llg;
+		for (int i = 0; i < N; ++i) c[i] += sh;
+	};
+	build(nx, gl, xmin, xmax, g->cx, g->sx);
+	build(ny, gl, ymin, ymax, g->cy, g->sy);
+	cudaGetDevice(&g->device);
+	int rc = 0;
+	auto fail = [&](int code) {
+		carpio_gpu_grid_destroy(g);
+		return code;
+	};
+	if (cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking) != cudaSuccess) {
+		note_cuda_error(cudaGetLastError());
+		return fail(CARPIO_GPU_ECUDA);
+	}
+	double** dp[4] = { &g->d_cx, &g->d_sx, &g->d_cy, &g->d_sy };
+	std::vector<double>* hp[4] = { &g->cx, &g->sx, &g->cy, &g->sy };
+	for (int k = 0; k < 4; ++k) {
+		if (cudaMalloc((void**)dp[k], sizeof(double) * hp[k]->size()) != cudaSuccess) {
+			cudaGetLastError();
+			return fail(CARPIO_GPU_ENOMEM);
+		}
+		if (cudaMemcpy(*dp[k], hp[k]->data(), sizeof(double) * hp[k]->size(),
+				cudaMemcpyHostToDevice) != cudaSuccess) {
+			note_cuda_error(cudaGetLastError());
+			return fail(CARPIO_GPU_ECUDA);
+		}
+	}
+	(void)rc;
+	*out = g;
+	return 0;
+}
+
+int carpio_gpu_grid_destroy(carpio_gpu_grid* g) {
+	if (!g) return CARPIO_GPU_EINVAL;
+	if (g->stream) cudaStreamSynchronize(g->stream);
+	cudaFree(g->d_cx);
+	cudaFree(g->d_sx);
+	cudaFree(g->d_cy);
+	cudaFree(g->d_sy);
+	if (g->stream) cudaStreamDestroy(g->stream);
+	delete g;
+	return 0;
+}
+
+int carpio_gpu_grid_coords(const carpio_gpu_grid* g, double* cx, double* sx,
+		double* cy, double* sy) {
+	if (!g) return CARPIO_GPU_EINVAL;
+	if (cx) std::memcpy(cx, g->cx.data(), sizeof(double) * g->cx.size());
+	if (sx) std::memcpy(sx, g->sx.data(), sizeof(double) * g->sx.size());
+	if (cy) std::memcpy(cy, g->cy.data(), sizeof(double) * g->cy.size());
+	if (sy) std::memcpy(sy, g->sy.data(), sizeof(double) * g->sy.size());
+	return 0;
+}
+
+int carpio_gpu_poisson_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
+		double beta, const double* source, double* phi,
+		const carpio_gpu_solver_cfg* cfg, double* resid_hist, int hist_cap,
+		carpio_gpu_solver_stats* stats) {
+	using namespace cg_host;
+	if (!g || !bc || !source || !phi || !cfg || cfg->max_iter < 0
+			|| cfg->kind < 0 || cfg->kind > 3 || hist_cap < 0
+			|| (hist_cap > 0 && !resid_hist) || !(beta == beta))
+		return CARPIO_GPU_EINVAL;
+	if (cfg->precision == CARPIO_GPU_MIXED && cfg->kind != CARPIO_GPU_CG)
+		return CARPIO_GPU_EINVAL;
+	for (int k = 0; k < 4; ++k)
+		if (bc->type[k] != 1 && bc->type[k] != 2) return CARPIO_GPU_EINVAL;
+	std::lock_guard<std::mutex> lock(g->mu);
+	cudaStream_t s = g->stream;
+	int rc;
+	if ((rc = stencil_prepare(g, *bc, beta, g->coeffs, s))) return rc;
+	PoissonWs& w = g->pws;
+	const size_t NF = (size_t)g->NI * g->P;
+	if ((rc = w.src.ensure(sizeof(double) * NF))) return rc;
+	if ((rc = w.phi.ensure(sizeof(double) * NF))) return rc;
+	if ((rc = w.out.ensure(sizeof(cg_dev::SolveOut)))) return rc;
+	if ((rc = w.hist.ensure(sizeof(double) * (size_t)(hist_cap > 0 ? hist_cap : 1)))) return rc;
+	const size_t wb = sizeof(double) * g->NJ, pb = sizeof(double) * g->P;
+	CG_CK(cudaMemcpy2DAsync(w.src.p, pb, source, wb, wb, g->NI, cudaMemcpyDefault, s));
+	CG_CK(cudaMemcpy2DAsync(w.phi.p, pb, phi, wb, wb, g->NI, cudaMemcpyDefault, s));
+	cudaEvent_t e0, e1;
+	CG_CK(cudaEventCreate(&e0));
+	CG_CK(cudaEventCreate(&e1));
+	CG_CK(cudaEventRecord(e0, s));
+	rc = poisson_launch(g, g->coeffs, w, SRC_FIELD, w.src.as<double>(), nullptr,
+			w.phi.as<double>(), *cfg, hist_cap > 0 ? w.hist.as<double>() : nullptr,
+			hist_cap, w.out.as<cg_dev::SolveOut>(), s);
+	if (rc) {
+		cudaEventDestroy(e0);
+		cudaEventDestroy(e1);
+		return rc;
+	}
+	CG_CK(cudaEventRecord(e1, s));
+	cg_dev::SolveOut o;
+	CG_CK(cudaMemcpyAsync(&o, w.out.p, sizeof o, cudaMemcpyDeviceToHost, s));
+	Ctl ctl;
+	CG_CK(cudaMemcpyAsync(&ctl, w.lw.ctl.p, sizeof ctl, cudaMemcpyDeviceToHost, s));
+	CG_CK(cudaStreamSynchronize(s));
+	float ms = 0;
+	cudaEventElapsedTime(&ms, e0, e1);
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	int code = ctl.err ? ctl.err : o.code;
+	if (code >= 0) {
+		CG_CK(cudaMemcpy2DAsync(phi, wb, w.phi.p, pb, wb, g->NI, cudaMemcpyDefault, s));
+		int keep = std::min(o.hist_len, hist_cap);
+		if (keep > 0)
+			CG_CK(cudaMemcpyAsync(resid_hist, w.hist.p, sizeof(double) * keep,
+					cudaMemcpyDefault, s));
+		CG_CK(cudaStreamSynchronize(s));
+	}
+	if (stats) {
+		stats->code = code;
+		stats->iters = o.iters;
+		stats->tol_out = o.tol;
+		stats->outer_iters = o.outer;
+		stats->hist_len = o.hist_len;
+		stats->ms = ms;
+	}
+	return code;
+}
+
+}  // extern "C"

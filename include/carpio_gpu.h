@@ -1,0 +1,213 @@
+/*
+ * carpio_gpu.h -- C ABI of the GB300 (sm_103a) projection hot path.
+ *
+ * Drop-in for the CPU path of hyperpower/carpios. Two layers, as the reference
+ * has them:
+ *
+ *  1. Algebra level: the free-function Krylov solvers of
+ *     lib/algebra/solver_matrix.hpp on a CSR matrix (MatrixSCR_,
+ *     lib/algebra/matrix_SparCompRow.hpp:27-36), with the same in/out meaning
+ *     of x, max_iter, tol and the residual list, and the same return codes.
+ *  2. Structure level: the cell-centred 5-point Poisson solve behind
+ *     structure::Solver_<2>::solve (lib/structure/s_solver.hpp:77-171, the
+ *     seam Poisson_::solve calls, s_poisson.hpp:411-420) and the explicit
+ *     projection step NS_explicit_::run_one_step
+ *     (lib/structure/s_ns_explicit.hpp:118-229), matrix-free on the GPU.
+ *
+ * Only plain C types cross the boundary. Array arguments may be host or device
+ * (CUDA) pointers; the library detects which. Fields use the reference's
+ * SpaceT layout (lib/algebra/space.hpp:184-209): (nx+2gl) x (ny+2gl) doubles,
+ * row I = x index incl. ghosts, column J = y index incl. ghosts, J contiguous.
+ * Solver vectors (CSR layer) are plain length-n arrays.
+ *
+ * Errors are returned, never raised: no call exits or traps. Calls on one
+ * handle are not thread-safe; separate handles are independent.
+ */
+#ifndef CARPIO_GPU_H
+#define CARPIO_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----- return codes ------------------------------------------------------
+ * 0..3 are the reference's own solver codes (solver_matrix.hpp:264-745):
+ * 0 converged, 1 reached max_iter, 2 rho breakdown, 3 omega breakdown.
+ * Negative codes replace the reference's assert()/exit() paths. */
+#define CARPIO_GPU_OK 0
+#define CARPIO_GPU_MAXITER 1
+#define CARPIO_GPU_BREAKDOWN_RHO 2
+#define CARPIO_GPU_BREAKDOWN_OMEGA 3
+#define CARPIO_GPU_EINVAL (-1)      /* bad argument */
+#define CARPIO_GPU_ECUDA (-2)       /* CUDA runtime error */
+#define CARPIO_GPU_ENONFINITE (-3)  /* NaN/Inf in an input */
+#define CARPIO_GPU_EZERODIAG (-4)   /* DiaPre zero diagonal (preconditioner.hpp:223-227 exits) */
+#define CARPIO_GPU_ETIMEOUT (-5)    /* device watchdog expired */
+#define CARPIO_GPU_ENOMEM (-6)      /* device allocation failed */
+
+/* Krylov kinds, in the reference's order */
+#define CARPIO_GPU_CG 0            /* carpio::CG            solver_matrix.hpp:264-316 */
+#define CARPIO_GPU_JACOBI 1        /* carpio::Jacobi        solver_matrix.hpp:192-260 */
+#define CARPIO_GPU_DIA_BICGSTAB 2  /* carpio::Dia_BiCGSTAB  solver_matrix.hpp:599-672 */
+#define CARPIO_GPU_BICGSTAB 3      /* carpio::BiCGSTAB      solver_matrix.hpp:674-745 */
+
+/* flags (bitwise OR). 0 = the reference's exact semantics. */
+#define CARPIO_GPU_FLAG_FULL_NRM2 1u   /* use the full 2-norm instead of nrm2's
+                                          drop-last-element (BLAS_Level1.hpp:569) */
+
+/* ----- library ----------------------------------------------------------- */
+const char* carpio_gpu_version(void);
+const char* carpio_gpu_strerror(int code);
+/* Bound on every device-side wait and on a whole solve (milliseconds);
+ * on expiry the call returns CARPIO_GPU_ETIMEOUT. Defaults 2000 / 600000. */
+int carpio_gpu_set_watchdog(unsigned wait_ms, unsigned solve_ms);
+int carpio_gpu_device_count(void);
+
+/* ----- 1. algebra level: CSR drop-in ---------------------------------------
+ * Replaces   int CG(const MatrixSCR_<V>& A, ArrayListV<V>& x,
+ *                   const ArrayListV<V>& b, int& max_iter, Float& tol,
+ *                   std::list<Float>& lresid)
+ * and Jacobi / Dia_BiCGSTAB / BiCGSTAB of the same shape
+ * (lib/algebra/solver_matrix.hpp:193-198, 265-269, 600-606, 675-681).
+ * rowptr[n+1], col[nnz] (0-based, unsigned 32-bit like St), val[nnz]: the
+ * MatrixSCR_ arrays. x: in x0, out solution. max_iter, tol: in limits, out
+ * iterations and reached residual, exactly as the reference writes them
+ * (including its early exits that leave max_iter unchanged). resid_hist:
+ * the lresid list, up to hist_cap entries; *hist_len gets its full length
+ * (either may be NULL). Returns the reference's code or a negative error. */
+int carpio_gpu_krylov_csr(int kind, int n, int nnz, const uint32_t* rowptr,
+		const uint32_t* col, const double* val, const double* b, double* x,
+		int* max_iter, double* tol, double* resid_hist, int hist_cap,
+		int* hist_len, uint32_t flags);
+
+/* ----- 2. structure level ------------------------------------------------ */
+typedef struct carpio_gpu_grid carpio_gpu_grid;
+
+/* Grid_<2>(min, max, n, gl) with uniform cells (lib/structure/s_grid.hpp:25-34,
+ * 372-395). Centres are built by the same running sums, so they carry the
+ * same rounding. gl >= 1 (>= 2 for TVD advection). */
+int carpio_gpu_grid_create_uniform(int nx, int ny, int gl, double xmin,
+		double xmax, double ymin, double ymax, carpio_gpu_grid** out);
+int carpio_gpu_grid_destroy(carpio_gpu_grid* g);
+/* cell centres / sizes incl. ghosts: cx, sx [nx+2gl], cy, sy [ny+2gl] (host) */
+int carpio_gpu_grid_coords(const carpio_gpu_grid* g, double* cx, double* sx,
+		double* cy, double* sy);
+
+/* Boundary conditions of one field: BoundaryCondition type per segment
+ * (1 = Dirichlet _BC1_, 2 = Neumann _BC2_; lib/structure/s_boundary.hpp:10-36)
+ * and a constant value. Segments as GhostRegular_ numbers them
+ * (s_ghost.hpp:210-232): 0 x-, 1 x+, 2 y-, 3 y+. The reference's default
+ * (no BC registered) is Neumann 0. */
+typedef struct {
+	int type[4];
+	double value[4];
+} carpio_gpu_bc;
+
+#define CARPIO_GPU_FP64 0
+#define CARPIO_GPU_MIXED 1   /* FP32 inner CG inside FP64 iterative refinement */
+
+typedef struct {
+	int kind;          /* CARPIO_GPU_CG / JACOBI / DIA_BICGSTAB / BICGSTAB */
+	int precision;     /* CARPIO_GPU_FP64 or CARPIO_GPU_MIXED (CG only) */
+	int max_iter;      /* Solver_::set_max_iter */
+	double tol;        /* Solver_::set_tolerance (relative residual) */
+	int mean_removal;  /* remove the mean of b and x (all-Neumann null space) */
+	double inner_tol;  /* MIXED: relative residual reduction per inner solve */
+	int inner_max_iter;/* MIXED: cap on one inner solve */
+	uint32_t flags;    /* CARPIO_GPU_FLAG_* */
+} carpio_gpu_solver_cfg;
+
+typedef struct {
+	int code;          /* solver code (0..3) or negative error */
+	int iters;         /* the reference's max_iter out value (FP64); total
+	                      inner iterations (MIXED) */
+	double tol_out;    /* the reference's tol out value: relative residual */
+	int outer_iters;   /* MIXED: refinement cycles */
+	int hist_len;      /* length of the residual list */
+	double ms;         /* device time of the solve (CUDA events) */
+} carpio_gpu_solver_stats;
+
+/* Poisson_::run() for a set_depend'ed field (s_poisson.hpp:320-420, 513-533):
+ * assemble StencilPoisson_ (s_poisson.hpp:60-114) with GhostRegular_
+ * substitution (s_ghost.hpp:140-179, 334-357) for uniform beta, copy phi's
+ * normal cells to x (Solver_::_copy_to_x), solve, and write x back
+ * (_copy_to_cs). source and phi are full fields with ghosts; phi's normal
+ * cells are the initial guess and receive the solution, its ghosts are left
+ * as they were (the reference does not touch them either). */
+int carpio_gpu_poisson_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
+		double beta, const double* source, double* phi,
+		const carpio_gpu_solver_cfg* cfg, double* resid_hist, int hist_cap,
+		carpio_gpu_solver_stats* stats);
+
+/* Advection schemes of NS_::set_advection_scheme (s_ns.hpp:171-211), plus the
+ * minmod limiter of src/calculation/advection.hpp:1079-1081 in the same TVD
+ * framework (s_operation.hpp:549-596). */
+#define CARPIO_GPU_UPWIND1 0
+#define CARPIO_GPU_CENTER 1
+#define CARPIO_GPU_CENTER4 2
+#define CARPIO_GPU_UPWIND2 3
+#define CARPIO_GPU_VANLEER 4
+#define CARPIO_GPU_SUPERBEE 5
+#define CARPIO_GPU_WAHYD 6
+#define CARPIO_GPU_QUICK 7
+#define CARPIO_GPU_CUI 8
+#define CARPIO_GPU_MINMOD 9
+
+typedef struct {
+	double rho;          /* set_uniform_rho (NS_ s_ns.hpp:93-97) */
+	double mu;           /* set_uniform_mu (s_ns.hpp:106-110) */
+	double cfl;          /* set_CFL_number (s_ns.hpp:132-136) */
+	double diff_number;  /* set_diffusion_number: value (>= 100 disables) */
+	double diff_coef;    /*                         coefficient */
+	int scheme;          /* CARPIO_GPU_UPWIND1 .. MINMOD */
+	carpio_gpu_bc bc_u;  /* add_bc(0, seg, "u", ...) */
+	carpio_gpu_bc bc_v;  /* add_bc(0, seg, "v", ...) */
+	carpio_gpu_solver_cfg projection; /* set_projection_solver; mean removal
+	                                     is what makes the all-Neumann
+	                                     projection solvable */
+} carpio_gpu_ns_cfg;
+
+typedef struct carpio_gpu_ns carpio_gpu_ns;
+
+/* NS_explicit_<2>(grid) + initial(): all fields zero, dt = dt0
+ * (set_time(max_step, dt0), s_poisson.hpp/s_equation.hpp). */
+int carpio_gpu_ns_create(carpio_gpu_grid* g, const carpio_gpu_ns_cfg* cfg,
+		double dt0, carpio_gpu_ns** out);
+int carpio_gpu_ns_destroy(carpio_gpu_ns* ns);
+/* state: u, v (cell), uf, vf (face), phi, p (cell), all full fields with
+ * ghosts; NULL leaves a field unchanged (set) or skips it (get). */
+int carpio_gpu_ns_set_state(carpio_gpu_ns* ns, double dt, const double* u,
+		const double* v, const double* uf, const double* vf,
+		const double* phi, const double* p);
+int carpio_gpu_ns_get_state(carpio_gpu_ns* ns, double* dt, double* u,
+		double* v, double* uf, double* vf, double* phi, double* p);
+/* `steps` passes of Equation_::run's loop body (s_equation.hpp:154-171):
+ * run_one_step then Time_::advance. Per-step dt, projection iterations and
+ * residual go to the optional arrays (host or device, length steps).
+ * Returns 0 or the first non-zero projection code / error. */
+int carpio_gpu_ns_run(carpio_gpu_ns* ns, int steps, double* step_dt,
+		int* step_iters, double* step_resid);
+
+/* Single operators of Operation_ (s_operation.hpp) on full fields, for
+ * callers that drive their own loop and for per-kernel checks.
+ *   which: 0 Grad (:46-72)       in a        -> out1 (x faces), out2 (y faces)
+ *          1 Div(VecF) (:100-120) in a, b (faces) -> out1
+ *          2 InterpolateF2C (:141-164) in a, b -> out1, out2
+ *          3 InterpolateC2F (:166-187) in a, b -> out1, out2 (normal + low wall
+ *            faces written, the rest left as passed in)
+ *          4 VdotNabla (scheme, :313-628) faces a, b, field c -> out1
+ *          5 NablaMuNabla(mu) (:664-688) in c -> out1
+ *          6 apply_bc (s_equation.hpp:340-378) bc, in/out out1 (in place)
+ *          7 max_magnitude (s_vector.hpp:89-103) a, b -> *scalar
+ * Outputs of 0, 1, 2, 4, 5 are zero outside the cells the reference writes. */
+int carpio_gpu_operator(carpio_gpu_grid* g, int which, int scheme,
+		double coef, const carpio_gpu_bc* bc, const double* a,
+		const double* b, const double* c, double* out1, double* out2,
+		double* scalar);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

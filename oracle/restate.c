@@ -1,0 +1,856 @@
+/* Oracle: plain-C restatement of the reference algorithms on the projection
+ * hot path. TEST INFRASTRUCTURE ONLY (see restate.h): the product library
+ * never links it; tests, the smoke check and the benchmark's CPU-baseline
+ * leg use it as the checker. Every function names the reference lines it
+ * restates. Compiled with -ffp-contract=off so each a*b+c rounds twice, as
+ * the reference's x86 build does. */
+#include "restate.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define SMALL 1e-10 /* lib/type_define.hpp */
+
+/* ------------------------------------------------------------ BLAS-1 --- */
+/* BLAS_Level1.hpp:499-544: leading (n-1)%5+1 terms one by one, then the rest
+ * five at a time, each group added left to right onto the running sum. */
+double rs_dot(int n, const double* sx, const double* sy) {
+	double dot = 0.0;
+	if (n <= 0) return dot;
+	int m = (n - 1) % 5;
+	for (int i = 0; i <= m; ++i) dot = dot + sx[i] * sy[i];
+	if (n <= 5) return dot;
+	for (int i = m + 1; i < n; i += 5) {
+		dot = dot + sx[i] * sy[i] + sx[i + 1] * sy[i + 1]
+				+ sx[i + 2] * sy[i + 2] + sx[i + 3] * sy[i + 3]
+				+ sx[i + 4] * sy[i + 4];
+	}
+	return dot;
+}
+
+/* BLAS_Level1.hpp:556-577: sqrt of the sum of squares of x[0..n-2]; the last
+ * element is left out, zeros are skipped, n == 1 gives |x[0]|. */
+double rs_nrm2(int n, const double* x) {
+	double norm = 0.0;
+	if (n <= 0) return norm;
+	if (n == 1) return fabs(x[0]);
+	for (int i = 0; i < n - 1; ++i) {
+		if (x[i] != 0.0) norm += x[i] * x[i];
+	}
+	return sqrt(norm);
+}
+
+/* threaded variants for the CPU baseline: fixed static partition, partial sums
+ * combined in thread order (deterministic for a given thread count) */
+static double par_dot(int n, const double* x, const double* y, int th) {
+	if (th <= 1) return rs_dot(n, x, y);
+	double part[256];
+	if (th > 256) th = 256;
+	memset(part, 0, sizeof part);
+#pragma omp parallel num_threads(th)
+	{
+#ifdef _OPENMP
+		int t = omp_get_thread_num(), nt = omp_get_num_threads();
+#else
+		int t = 0, nt = 1;
+#endif
+		long lo = (long)n * t / nt, hi = (long)n * (t + 1) / nt;
+		double s = 0.0;
+		for (long i = lo; i < hi; ++i) s += x[i] * y[i];
+		part[t] = s;
+	}
+	double s = 0.0;
+	for (int t = 0; t < th; ++t) s += part[t];
+	return s;
+}
+static double par_nrm2(int n, const double* x, int th) {
+	if (th <= 1) return rs_nrm2(n, x);
+	if (n == 1) return fabs(x[0]);
+	return sqrt(par_dot(n - 1, x, x, th));
+}
+
+/* MatrixSCR_::operator* (matrix_SparCompRow.hpp:236-249): per row, from 0,
+ * res += x[col] * val in stored order. */
+static void spmv(int n, const unsigned* rp, const unsigned* ci,
+		const double* va, const double* x, double* y, int th) {
+#pragma omp parallel for num_threads(th) if (th > 1) schedule(static)
+	for (int i = 0; i < n; ++i) {
+		double s = 0.0;
+		for (unsigned k = rp[i]; k < rp[i + 1]; ++k) s += x[ci[k]] * va[k];
+		y[i] = s;
+	}
+}
+
+#define VLOOP(n, th) \
+	_Pragma("omp parallel for num_threads(th) if (th > 1) schedule(static)") \
+	for (int i = 0; i < (n); ++i)
+
+/* ----------------------------------------------------------- solvers --- */
+static int find_diag(int n, const unsigned* rp, const unsigned* ci,
+		const double* va, double* d, int inv) {
+	/* DiaPre (preconditioner.hpp:182-229): inv 1 -> 1/diag, inv 2 -> diag;
+	 * a zero or missing diagonal is a failure (the reference exits) */
+	for (int i = 0; i < n; ++i) {
+		d[i] = 0.0;
+		for (unsigned k = rp[i]; k < rp[i + 1]; ++k) {
+			if ((int)ci[k] == i) {
+				if (va[k] == 0.0) return RS_EZERODIAG;
+				d[i] = inv == 1 ? 1. / va[k] : va[k];
+				break;
+			}
+		}
+		if (d[i] == 0.0) return RS_EZERODIAG;
+	}
+	return 0;
+}
+
+static void hist_push(double* h, int cap, int* len, double v) {
+	if (*len < cap && h) h[*len] = v;
+	(*len)++;
+}
+
+/* solver_matrix.hpp:264-316 */
+static int cg(int n, const unsigned* rp, const unsigned* ci, const double* va,
+		const double* b, double* x, int* max_iter, double* tol, double* h,
+		int cap, int* hl, int th) {
+	double* r = malloc(sizeof(double) * n);
+	double* p = malloc(sizeof(double) * n);
+	double* q = malloc(sizeof(double) * n);
+	double* t = malloc(sizeof(double) * n);
+	double resid, alpha, beta, rho, rho_1 = 0.0;
+	int ret = 1;
+	double normb = par_nrm2(n, b, th);
+	spmv(n, rp, ci, va, x, t, th);
+	VLOOP(n, th) r[i] = b[i] - t[i];
+	if (normb == 0.0) normb = 1;
+	if ((resid = par_nrm2(n, r, th) / normb) <= *tol) {
+		*tol = resid;
+		*max_iter = 0;
+		ret = 0;
+		goto done;
+	}
+	for (int it = 1; it <= *max_iter; ++it) {
+		rho = par_dot(n, r, r, th); /* z = r */
+		if (it == 1) {
+			VLOOP(n, th) p[i] = r[i];
+		} else {
+			beta = rho / rho_1;
+			VLOOP(n, th) { double tt = beta * p[i]; p[i] = r[i] + tt; }
+		}
+		spmv(n, rp, ci, va, p, q, th);
+		alpha = rho / par_dot(n, p, q, th);
+		VLOOP(n, th) { double tt = alpha * p[i]; x[i] += tt; }
+		VLOOP(n, th) { double tt = alpha * q[i]; r[i] -= tt; }
+		resid = par_nrm2(n, r, th) / normb;
+		hist_push(h, cap, hl, resid);
+		if (resid <= *tol) {
+			*tol = resid;
+			*max_iter = it;
+			ret = 0;
+			goto done;
+		}
+		rho_1 = rho;
+	}
+	*tol = resid;
+done:
+	free(r); free(p); free(q); free(t);
+	return ret;
+}
+
+/* solver_matrix.hpp:192-260 */
+static int jacobi(int n, const unsigned* rp, const unsigned* ci,
+		const double* va, const double* b, double* x, int* max_iter,
+		double* tol, double* h, int cap, int* hl, int th) {
+	unsigned nz = rp[n];
+	double* T = malloc(sizeof(double) * (nz ? nz : 1));
+	double* C = malloc(sizeof(double) * n);
+	double* nx = malloc(sizeof(double) * n);
+	double* r = malloc(sizeof(double) * n);
+	double* t = malloc(sizeof(double) * n);
+	double resid;
+	int ret = 1;
+	memcpy(T, va, sizeof(double) * nz);
+	for (int i = 0; i < n; ++i) C[i] = 1.0 / SMALL;
+	double normb = par_nrm2(n, b, th);
+	spmv(n, rp, ci, va, x, t, th);
+	VLOOP(n, th) r[i] = b[i] - t[i];
+	if (normb == 0.0) normb = 1;
+	if ((resid = par_nrm2(n, r, th) / normb) <= *tol) {
+		*tol = resid;
+		*max_iter = 0;
+		ret = 0;
+		goto done;
+	}
+	for (int i = 0; i < n; ++i) {
+		double dv = 0.0;
+		long flag = -1;
+		for (unsigned k = rp[i]; k < rp[i + 1]; ++k) {
+			if ((int)ci[k] == i) { flag = k; dv = T[k]; T[k] = 0; break; }
+		}
+		if (flag < 0 || dv == 0.0) { ret = RS_EZERODIAG; goto done; }
+		for (unsigned k = rp[i]; k < rp[i + 1]; ++k) {
+			if ((long)k == flag) C[i] = b[ci[k]] / dv;
+			else T[k] = -T[k] / dv;
+		}
+	}
+	for (int it = 1; it <= *max_iter; ++it) {
+		spmv(n, rp, ci, T, x, t, th);
+		VLOOP(n, th) nx[i] = t[i] + C[i];
+		spmv(n, rp, ci, va, nx, t, th);
+		VLOOP(n, th) r[i] = b[i] - t[i];
+		resid = par_nrm2(n, r, th) / normb;
+		hist_push(h, cap, hl, resid);
+		if (resid <= *tol) {
+			*tol = resid;
+			*max_iter = it;
+			ret = 0;
+			goto done; /* x keeps the previous iterate, as in the reference */
+		}
+		memcpy(x, nx, sizeof(double) * n);
+	}
+	*tol = resid;
+done:
+	free(T); free(C); free(nx); free(r); free(t);
+	return ret;
+}
+
+/* solver_matrix.hpp:599-672 (inv = 1, Dia_BiCGSTAB) and 674-745 (inv = 2,
+ * BiCGSTAB). The two differ in the preconditioner and in whether the early
+ * exit on |s| and the initial check append to the residual list. */
+static int bicgstab(int inv, int n, const unsigned* rp, const unsigned* ci,
+		const double* va, const double* b, double* x, int* max_iter,
+		double* tol, double* h, int cap, int* hl, int th) {
+	double* d = malloc(sizeof(double) * n);
+	double* r = malloc(sizeof(double) * n);
+	double* rt = malloc(sizeof(double) * n);
+	double* p = malloc(sizeof(double) * n);
+	double* ph = malloc(sizeof(double) * n);
+	double* s = malloc(sizeof(double) * n);
+	double* sh = malloc(sizeof(double) * n);
+	double* t = malloc(sizeof(double) * n);
+	double* v = malloc(sizeof(double) * n);
+	double resid, rho_1, rho_2 = 0, alpha = 0, beta, omega = 0;
+	int ret = find_diag(n, rp, ci, va, d, inv);
+	if (ret) goto done;
+	ret = 1;
+	double normb = par_nrm2(n, b, th);
+	spmv(n, rp, ci, va, x, t, th);
+	VLOOP(n, th) r[i] = b[i] - t[i];
+	memcpy(rt, r, sizeof(double) * n);
+	if (normb == 0.0) normb = 1;
+	if ((resid = par_nrm2(n, r, th) / normb) <= *tol) {
+		*tol = resid;
+		*max_iter = 0;
+		if (inv == 1) hist_push(h, cap, hl, resid);
+		ret = 0;
+		goto done;
+	}
+	for (int it = 1; it <= *max_iter; ++it) {
+		rho_1 = par_dot(n, rt, r, th);
+		if (rho_1 == 0) {
+			*tol = par_nrm2(n, r, th) / normb;
+			ret = 2;
+			goto done;
+		}
+		if (it == 1) {
+			memcpy(p, r, sizeof(double) * n);
+		} else {
+			beta = (rho_1 / rho_2) * (alpha / omega);
+			VLOOP(n, th) {
+				double t1 = omega * v[i];
+				double t2 = p[i] - t1;
+				double t3 = beta * t2;
+				p[i] = r[i] + t3;
+			}
+		}
+		VLOOP(n, th) ph[i] = p[i] * d[i];
+		spmv(n, rp, ci, va, ph, v, th);
+		alpha = rho_1 / par_dot(n, rt, v, th);
+		VLOOP(n, th) { double t1 = alpha * v[i]; s[i] = r[i] - t1; }
+		if ((resid = par_nrm2(n, s, th) / normb) < *tol) {
+			VLOOP(n, th) { double t1 = alpha * ph[i]; x[i] += t1; }
+			*tol = resid;
+			if (inv == 1) hist_push(h, cap, hl, resid);
+			ret = 0; /* max_iter left unchanged, as in the reference */
+			goto done;
+		}
+		VLOOP(n, th) sh[i] = s[i] * d[i];
+		spmv(n, rp, ci, va, sh, t, th);
+		omega = par_dot(n, t, s, th) / par_dot(n, t, t, th);
+		VLOOP(n, th) {
+			double t1 = alpha * ph[i];
+			double t2 = omega * sh[i];
+			double t3 = t1 + t2;
+			x[i] += t3;
+		}
+		VLOOP(n, th) { double t1 = omega * t[i]; r[i] = s[i] - t1; }
+		rho_2 = rho_1;
+		resid = par_nrm2(n, r, th) / normb;
+		hist_push(h, cap, hl, resid);
+		if (resid < *tol) {
+			*tol = resid;
+			*max_iter = it;
+			ret = 0;
+			goto done;
+		}
+		if (omega == 0) {
+			*tol = par_nrm2(n, r, th) / normb;
+			ret = 3;
+			goto done;
+		}
+	}
+	*tol = resid;
+done:
+	free(d); free(r); free(rt); free(p); free(ph); free(s); free(sh);
+	free(t); free(v);
+	return ret;
+}
+
+int rs_krylov_csr(int kind, int n, const unsigned* rowptr, const unsigned* col,
+		const double* val, const double* b, double* x, int* max_iter,
+		double* tol, double* hist, int hist_cap, int* hist_len, int threads) {
+	int hl = 0, ret;
+	if (threads < 1) threads = 1;
+	switch (kind) {
+	case RS_CG:
+		ret = cg(n, rowptr, col, val, b, x, max_iter, tol, hist, hist_cap,
+				&hl, threads);
+		break;
+	case RS_JACOBI:
+		ret = jacobi(n, rowptr, col, val, b, x, max_iter, tol, hist, hist_cap,
+				&hl, threads);
+		break;
+	case RS_DIA_BICGSTAB:
+		ret = bicgstab(1, n, rowptr, col, val, b, x, max_iter, tol, hist,
+				hist_cap, &hl, threads);
+		break;
+	case RS_BICGSTAB:
+		ret = bicgstab(2, n, rowptr, col, val, b, x, max_iter, tol, hist,
+				hist_cap, &hl, threads);
+		break;
+	default:
+		return -1;
+	}
+	if (hist_len) *hist_len = hl;
+	return ret;
+}
+
+/* -------------------------------------------------------------- grid --- */
+void rs_grid_uniform(int n, int gl, double lo, double hi, double* c,
+		double* s) {
+	/* s_grid.hpp:372-395 */
+	int N = n + 2 * gl;
+	double ds = (hi - lo) / n;
+	double csum = 0.0, llg = 0.0;
+	for (int i = 0; i < N; ++i) s[i] = ds;
+	for (int i = 0; i < N; ++i) {
+		c[i] = csum + 0.5 * s[i];
+		csum += s[i];
+	}
+	for (int i = 0; i < gl; ++i) llg += s[i];
+	double sh = lo - llg;
+	for (int i = 0; i < N; ++i) c[i] += sh;
+}
+
+/* field accessors: cell (i, j) of a (nx+2gl) x (ny+2gl) array, i, j in
+ * normal-cell coordinates (ghosts negative / >= n) */
+#define AT(f, i, j) (f)[(size_t)((i) + gl) * NJ + (size_t)((j) + gl)]
+#define CX(i) cx[(i) + gl]
+#define CY(j) cy[(j) + gl]
+#define SX(i) sx[(i) + gl]
+#define SY(j) sy[(j) + gl]
+
+/* ---------------------------------------------------------- assembly --- */
+typedef struct {
+	int i, j;     /* term index */
+	int e;        /* exponent: 0 constant, 1 unknown */
+	double c;
+} term;
+
+/* Polynomial_ key order (polynomial.hpp:44-57 with Index_compare_,
+ * s_define.hpp:227-241): two constants are the same key; otherwise by index
+ * (x then y), then exponent. */
+static int key_cmp(const term* a, int i, int j, int e) {
+	if (a->e == 0 && e == 0) return 0;
+	if (a->i != i) return a->i < i ? -1 : 1;
+	if (a->j != j) return a->j < j ? -1 : 1;
+	if (a->e != e) return a->e < e ? -1 : 1;
+	return 0;
+}
+/* Polynomial_::insert (polynomial.hpp:199-219): add onto an existing key */
+static void poly_insert(term* row, int* len, double c, int i, int j, int e) {
+	int k = 0;
+	for (; k < *len; ++k) {
+		int r = key_cmp(&row[k], i, j, e);
+		if (r == 0) { row[k].c = row[k].c + c; return; }
+		if (r > 0) break;
+	}
+	memmove(&row[k + 1], &row[k], sizeof(term) * (*len - k));
+	row[k].i = i; row[k].j = j; row[k].e = e; row[k].c = c;
+	(*len)++;
+}
+
+int rs_assemble_poisson(int nx, int ny, int gl, const double* cx,
+		const double* sx, const double* cy, const double* sy, const rs_bc* bc,
+		double beta, const double* src, double src_value, unsigned* rowptr,
+		unsigned* col, double* val, double* b) {
+	const int NJ = ny + 2 * gl;
+	int nz = 0;
+	rowptr[0] = 0;
+	for (int j = 0; j < ny; ++j) {
+		for (int i = 0; i < nx; ++i) {
+			term row[16];
+			int len = 0;
+			/* StencilPoisson_::_coe_other (s_poisson.hpp:109-114):
+			 * -betaf * a / d, with a the face area (s_y for x faces, s_x for
+			 * y faces) and d the centre distance */
+			double ax = SY(j) * 1.0, ay = 1.0 * SX(i);
+			double cxp = (-beta) * ax / fabs(CX(i) - CX(i + 1));
+			double cxm = (-beta) * ax / fabs(CX(i) - CX(i - 1));
+			double cyp = (-beta) * ay / fabs(CY(j) - CY(j + 1));
+			double cym = (-beta) * ay / fabs(CY(j) - CY(j - 1));
+			/* coe_row (s_poisson.hpp:85-102) */
+			poly_insert(row, &len, cxp, i + 1, j, 1);
+			poly_insert(row, &len, cxm, i - 1, j, 1);
+			poly_insert(row, &len, cyp, i, j + 1, 1);
+			poly_insert(row, &len, cym, i, j - 1, 1);
+			double coec = 0;
+			coec += -cxm;
+			coec += -cxp;
+			coec += -cym;
+			coec += -cyp;
+			poly_insert(row, &len, coec, i, j, 1);
+			/* src (s_poisson.hpp:75-83): s_(0)^DIM * source */
+			double v = 1.0;
+			v *= SX(i);
+			v *= SX(i);
+			double f = src ? AT(src, i, j) : src_value;
+			poly_insert(row, &len, v * f, i, j, 0);
+			/* GhostRegular_::substitute (s_ghost.hpp:334-357), in key order */
+			for (int k = 0; k < len;) {
+				term tk = row[k];
+				int gx = tk.i < 0 || tk.i >= nx;
+				int gy = tk.j < 0 || tk.j >= ny;
+				if (tk.e == 1 && (gx || gy)) {
+					memmove(&row[k], &row[k + 1], sizeof(term) * (len - k - 1));
+					len--;
+					if (tk.c != 0) {
+						/* Ghost_::_substitute_ghost (s_ghost.hpp:140-179) */
+						int seg, a, oi = tk.i, oj = tk.j, ori;
+						if (gx) { a = 0; seg = tk.i < 0 ? 0 : 1; ori = tk.i < 0 ? 0 : 1; oi = tk.i < 0 ? 0 : nx - 1; }
+						else { a = 1; seg = tk.j < 0 ? 2 : 3; ori = tk.j < 0 ? 0 : 1; oj = tk.j < 0 ? 0 : ny - 1; }
+						double c0 = a == 0 ? CX(tk.i) : CY(tk.j);
+						double c1 = a == 0 ? CX(oi) : CY(oj);
+						double hs = (a == 0 ? SX(oi) : SY(oj)) * 0.5;
+						double cf = ori == 1 ? c1 + hs : c1 - hs;
+						double dl = fabs(c1 - c0);
+						double d0 = fabs(cf - c0);
+						double d1 = fabs(c1 - cf);
+						double bv = bc->value[seg];
+						if (bc->type[seg] == 1) {
+							poly_insert(row, &len, -tk.c * d0 / d1, oi, oj, 1);
+							poly_insert(row, &len, tk.c * dl * bv / d1, oi, oj, 0);
+						} else {
+							poly_insert(row, &len, tk.c, oi, oj, 1);
+							poly_insert(row, &len, -bv * dl * tk.c, oi, oj, 0);
+						}
+					}
+					/* the entry was erased; the next entry now sits at k,
+					 * unless an insert landed before it (never: inserts hit
+					 * the centre and constant, which sort after W and S) */
+					k = 0;
+					continue;
+				}
+				++k;
+			}
+			/* concise: trim_zero + merge_const (polynomial.hpp:288-330) */
+			int fconst = 0;
+			double bconst = 0.0;
+			for (int k = 0; k < len; ++k) {
+				if (row[k].c == 0) continue;
+				if (row[k].e == 0) {
+					fconst = 1;
+					bconst = -row[k].c; /* s_solver.hpp:122 */
+				} else {
+					col[nz] = (unsigned)(row[k].i + row[k].j * nx);
+					val[nz] = row[k].c;
+					nz++;
+				}
+			}
+			b[i + j * nx] = fconst ? bconst : 0.0;
+			rowptr[i + j * nx + 1] = (unsigned)nz;
+		}
+	}
+	return nz;
+}
+
+/* ------------------------------------------------------------ ghosts --- */
+void rs_apply_bc(int nx, int ny, int gl, const double* cx, const double* sx,
+		const double* cy, const double* sy, const rs_bc* bc, double* f) {
+	/* Equation_::apply_bc (s_equation.hpp:340-378): every ghost cell in the
+	 * IJK order of begin_IJK (x fastest), in place, so a corner reads the
+	 * neighbouring ghost row as it stands when the corner is visited. */
+	const int NI = nx + 2 * gl, NJ = ny + 2 * gl;
+	for (int J = 0; J < NJ; ++J) {
+		for (int I = 0; I < NI; ++I) {
+			int i = I - gl, j = J - gl;
+			int gx = i < 0 || i >= nx, gy = j < 0 || j >= ny;
+			if (!gx && !gy) continue;
+			int seg, a, oi = i, oj = j, ori;
+			if (gx) { a = 0; seg = i < 0 ? 0 : 1; ori = i < 0 ? 0 : 1; oi = i < 0 ? 0 : nx - 1; }
+			else { a = 1; seg = j < 0 ? 2 : 3; ori = j < 0 ? 0 : 1; oj = j < 0 ? 0 : ny - 1; }
+			double val = bc->value[seg];
+			double cg = a == 0 ? CX(i) : CY(j);
+			double co = a == 0 ? CX(oi) : CY(oj);
+			double dl = fabs(cg - co);
+			if (bc->type[seg] == 1) {
+				/* Interp_::Linear (arithmetic.hpp:427-430) through the face */
+				double hs = (a == 0 ? SX(oi) : SY(oj)) * 0.5;
+				double cf = ori == 1 ? co + hs : co - hs;
+				double u = (cg - cf) / (co - cf);
+				AT(f, i, j) = (val * (1.0 - u)) + (AT(f, oi, oj) * u);
+			} else {
+				double po = AT(f, oi, oj);
+				AT(f, i, j) = po - val * dl;
+			}
+		}
+	}
+}
+
+/* --------------------------------------------------------- operators --- */
+void rs_grad(int nx, int ny, int gl, const double* cx, const double* cy,
+		const double* phi, double* gx, double* gy) {
+	/* Operation_::Grad (s_operation.hpp:46-72) into zeroed face fields */
+	const int NJ = ny + 2 * gl;
+	size_t N = (size_t)(nx + 2 * gl) * NJ;
+	memset(gx, 0, sizeof(double) * N);
+	memset(gy, 0, sizeof(double) * N);
+	for (int j = 0; j < ny; ++j) {
+		for (int i = 0; i < nx; ++i) {
+			double vc = AT(phi, i, j);
+			AT(gx, i, j) = (AT(phi, i + 1, j) - vc) / (CX(i + 1) - CX(i));
+			if (i == 0) AT(gx, i - 1, j) = (AT(phi, i - 1, j) - vc) / (CX(i - 1) - CX(i));
+			AT(gy, i, j) = (AT(phi, i, j + 1) - vc) / (CY(j + 1) - CY(j));
+			if (j == 0) AT(gy, i, j - 1) = (AT(phi, i, j - 1) - vc) / (CY(j - 1) - CY(j));
+		}
+	}
+}
+
+void rs_div(int nx, int ny, int gl, const double* sx, const double* sy,
+		const double* fx, const double* fy, double* div) {
+	/* Operation_::Div(VecF) (s_operation.hpp:100-120) into a zeroed field */
+	const int NJ = ny + 2 * gl;
+	memset(div, 0, sizeof(double) * (size_t)(nx + 2 * gl) * NJ);
+	for (int j = 0; j < ny; ++j) {
+		for (int i = 0; i < nx; ++i) {
+			double d = 0;
+			d += (AT(fx, i, j) - AT(fx, i - 1, j)) / SX(i);
+			d += (AT(fy, i, j) - AT(fy, i, j - 1)) / SY(j);
+			AT(div, i, j) = d;
+		}
+	}
+}
+
+void rs_f2c(int nx, int ny, int gl, const double* fx, const double* fy,
+		double* cxo, double* cyo) {
+	/* Operation_::InterpolateF2C (s_operation.hpp:141-164) into zeroed fields */
+	const int NJ = ny + 2 * gl;
+	size_t N = (size_t)(nx + 2 * gl) * NJ;
+	memset(cxo, 0, sizeof(double) * N);
+	memset(cyo, 0, sizeof(double) * N);
+	for (int j = 0; j < ny; ++j) {
+		for (int i = 0; i < nx; ++i) {
+			AT(cxo, i, j) = (AT(fx, i, j) + AT(fx, i - 1, j)) * 0.5;
+			AT(cyo, i, j) = (AT(fy, i, j) + AT(fy, i, j - 1)) * 0.5;
+		}
+	}
+}
+
+void rs_c2f(int nx, int ny, int gl, const double* sx, const double* sy,
+		const double* u, const double* v, double* fx, double* fy) {
+	/* Operation_::InterpolateC2F(VecC, VecF) (s_operation.hpp:166-187):
+	 * writes the normal faces and the low wall face, leaves the rest */
+	const int NJ = ny + 2 * gl;
+	for (int j = 0; j < ny; ++j) {
+		for (int i = 0; i < nx; ++i) {
+			double vc = AT(u, i, j);
+			double hs = SX(i) * 0.5, hsp = SX(i + 1) * 0.5;
+			AT(fx, i, j) = (AT(u, i + 1, j) * hs + vc * hsp) / (hs + hsp);
+			if (i == 0) {
+				double hsm = SX(i - 1) * 0.5;
+				AT(fx, i - 1, j) = (AT(u, i - 1, j) * hs + vc * hsm) / (hs + hsm);
+			}
+			vc = AT(v, i, j);
+			hs = SY(j) * 0.5;
+			hsp = SY(j + 1) * 0.5;
+			AT(fy, i, j) = (AT(v, i, j + 1) * hs + vc * hsp) / (hs + hsp);
+			if (j == 0) {
+				double hsm = SY(j - 1) * 0.5;
+				AT(fy, i, j - 1) = (AT(v, i, j - 1) * hs + vc * hsm) / (hs + hsm);
+			}
+		}
+	}
+}
+
+/* NablaMuNabla(Vt mu, ...) (s_operation.hpp:664-688) at one cell */
+static double nmn(int nx, int ny, int gl, const double* cx, const double* sx,
+		const double* cy, const double* sy, double mu, const double* f, int i,
+		int j) {
+	const int NJ = ny + 2 * gl;
+	double t0, t1;
+	{
+		double dm = mu * (AT(f, i, j) - AT(f, i - 1, j)) / (CX(i) - CX(i - 1));
+		double dp = mu * (AT(f, i + 1, j) - AT(f, i, j)) / (CX(i + 1) - CX(i));
+		t0 = (dp - dm) / SX(i);
+	}
+	{
+		double dm = mu * (AT(f, i, j) - AT(f, i, j - 1)) / (CY(j) - CY(j - 1));
+		double dp = mu * (AT(f, i, j + 1) - AT(f, i, j)) / (CY(j + 1) - CY(j));
+		t1 = (dp - dm) / SY(j);
+	}
+	double res = 0.0;
+	res += t0;
+	res += t1;
+	return res;
+}
+
+void rs_diffusion(int nx, int ny, int gl, const double* cx, const double* sx,
+		const double* cy, const double* sy, double mu, const double* f,
+		double* out) {
+	const int NJ = ny + 2 * gl;
+	memset(out, 0, sizeof(double) * (size_t)(nx + 2 * gl) * NJ);
+	for (int j = 0; j < ny; ++j)
+		for (int i = 0; i < nx; ++i)
+			AT(out, i, j) = nmn(nx, ny, gl, cx, sx, cy, sy, mu, f, i, j);
+}
+
+/* std::min / std::max semantics ((b < a) ? b : a, (a < b) ? b : a) */
+static double smin(double a, double b) { return (b < a) ? b : a; }
+static double smax(double a, double b) { return (a < b) ? b : a; }
+
+/* limiters (s_operation.hpp:501-541, 598-600; minmod from
+ * src/calculation/advection.hpp:1079-1081) */
+static double limiter(int sch, double r, double R) {
+	switch (sch) {
+	case RS_VANLEER: return 0.5 * R * (r + fabs(r)) / (R - 1 + r);
+	case RS_SUPERBEE: return smax(smax(0.0, smin(R * r, 1.0)), smin(r, R));
+	case RS_WAHYD:
+		if (r <= 1.0) return 0.5 * R * (r + fabs(r)) / (R - 1 + r);
+		return smin((r + R * r * fabs(r)) / (R + r * r), R);
+	case RS_QUICK: return 0.75 * r + 0.25;
+	case RS_CUI: return 2.0 / 3.0 * r + 1.0 / 3.0;
+	case RS_UPWIND2: return r;
+	case RS_MINMOD: return smax(0.0, smin(1.0, r));
+	}
+	return 0.0;
+}
+
+/* one axis of the advection operators at cell (i, j); d = 0 x, 1 y.
+ * Cells along the axis are addressed with k relative offsets. */
+static double adv_axis(int sch, int d, int nx, int ny, int gl, const double* cx,
+		const double* sx, const double* cy, const double* sy, const double* uf,
+		const double* vf, const double* f, int i, int j) {
+	const int NJ = ny + 2 * gl;
+	const double* face = d == 0 ? uf : vf;
+#define F(k) (d == 0 ? AT(f, i + (k), j) : AT(f, i, j + (k)))
+#define C(k) (d == 0 ? CX(i + (k)) : CY(j + (k)))
+#define S(k) (d == 0 ? SX(i + (k)) : SY(j + (k)))
+#define FACE(k) (d == 0 ? AT(face, i + (k), j) : AT(face, i, j + (k)))
+	double veo = (FACE(0) + FACE(-1)) * 0.5;
+	switch (sch) {
+	case RS_UPWIND1: /* s_operation.hpp:400-422 */
+		if (veo > 0.0) return veo * (F(0) - F(-1)) / (C(0) - C(-1));
+		if (veo < 0.0) return veo * (F(1) - F(0)) / (C(1) - C(0));
+		return 0.0;
+	case RS_CENTER: /* :442-459 */
+		return veo * (F(1) - F(-1)) / (C(1) - C(-1));
+	case RS_CENTER4: { /* :461-482 (no velocity factor, as in the reference) */
+		double din = (F(1) - F(-1)) / (C(1) - C(-1));
+		double dout = (F(2) - F(-2)) / (C(2) - C(-2));
+		return (4.0 * din - dout) / 3.0;
+	}
+	default: { /* VdotNabla_TVD :549-596 */
+		int Cm, Um, Dm, Cp, Up, Dp;
+		if (veo >= 0.0) {
+			Dm = 0; Cm = -1; Um = -2;
+			Dp = 1; Cp = 0; Up = -1;
+		} else {
+			Dm = -1; Cm = 0; Um = 1;
+			Dp = 0; Cp = 1; Up = 2;
+		}
+		/* NaN veo takes neither branch in the reference and leaves the
+		 * indices as constructed (all zero) */
+		if (!(veo >= 0.0) && !(veo < 0.0)) { Dm = Cm = Um = Dp = Cp = Up = 0; }
+		double R, r, fp, fm;
+		R = (S(Dp) + S(Cp)) / S(Cp);
+		r = (F(Cp) - F(Up)) * (S(Dp) + S(Cp)) / (F(Dp) - F(Cp) + SMALL)
+				/ (S(Cp) + S(Up));
+		fp = F(Cp) + limiter(sch, r, R) / R * (F(Dp) - F(Cp));
+		R = (S(Dm) + S(Cm)) / S(Cm);
+		r = (F(Cm) - F(Um)) * (S(Dm) + S(Cm)) / (F(Dm) - F(Cm) + SMALL)
+				/ (S(Cm) + S(Um));
+		fm = F(Cm) + limiter(sch, r, R) / R * (F(Dm) - F(Cm));
+		return (FACE(0) * fp - FACE(-1) * fm) / S(0);
+	}
+	}
+#undef F
+#undef C
+#undef S
+#undef FACE
+}
+
+static double adv_cell(int sch, int nx, int ny, int gl, const double* cx,
+		const double* sx, const double* cy, const double* sy, const double* uf,
+		const double* vf, const double* f, int i, int j) {
+	double a0 = adv_axis(sch, 0, nx, ny, gl, cx, sx, cy, sy, uf, vf, f, i, j);
+	double a1 = adv_axis(sch, 1, nx, ny, gl, cx, sx, cy, sy, uf, vf, f, i, j);
+	double s = 0.0;
+	s += a0;
+	s += a1;
+	return s;
+}
+
+void rs_advection(int scheme, int nx, int ny, int gl, const double* cx,
+		const double* sx, const double* cy, const double* sy, const double* uf,
+		const double* vf, const double* f, double* out) {
+	const int NJ = ny + 2 * gl;
+	memset(out, 0, sizeof(double) * (size_t)(nx + 2 * gl) * NJ);
+	for (int j = 0; j < ny; ++j)
+		for (int i = 0; i < nx; ++i)
+			AT(out, i, j) = adv_cell(scheme, nx, ny, gl, cx, sx, cy, sy, uf, vf,
+					f, i, j);
+}
+
+double rs_max_magnitude(int nx, int ny, int gl, const double* u,
+		const double* v) {
+	/* VectorCenter_::max_magnitude (s_vector.hpp:89-103) */
+	const int NJ = ny + 2 * gl;
+	double mx = 0;
+	for (int j = 0; j < ny; ++j) {
+		for (int i = 0; i < nx; ++i) {
+			double s = 0;
+			s += AT(u, i, j) * AT(u, i, j);
+			s += AT(v, i, j) * AT(v, i, j);
+			mx = smax(mx, sqrt(s));
+		}
+	}
+	return mx;
+}
+
+/* ------------------------------------------------------------ NS run --- */
+int rs_ns_run(int nx, int ny, int gl, const double* cx, const double* sx,
+		const double* cy, const double* sy, const rs_bc* bc_u,
+		const rs_bc* bc_v, const rs_ns_cfg* cfg, int steps, double* dt,
+		double* u, double* v, double* uf, double* vf, double* phi, double* p,
+		double* step_dt, int* step_iters, double* step_resid) {
+	const int NI = nx + 2 * gl, NJ = ny + 2 * gl;
+	const size_t N = (size_t)NI * NJ;
+	const int n = nx * ny;
+	double* us = calloc(N, sizeof(double));
+	double* vs = calloc(N, sizeof(double));
+	double* usf = calloc(N, sizeof(double));
+	double* vsf = calloc(N, sizeof(double));
+	double* div = calloc(N, sizeof(double));
+	double* gx = calloc(N, sizeof(double));
+	double* gy = calloc(N, sizeof(double));
+	double* gcx = calloc(N, sizeof(double));
+	double* gcy = calloc(N, sizeof(double));
+	unsigned* rp = malloc(sizeof(unsigned) * (n + 1));
+	unsigned* ci = malloc(sizeof(unsigned) * 5 * n);
+	double* va = malloc(sizeof(double) * 5 * n);
+	double* b = malloc(sizeof(double) * n);
+	double* x = malloc(sizeof(double) * n);
+	rs_bc bc_phi;
+	for (int s = 0; s < 4; ++s) { bc_phi.type[s] = 2; bc_phi.value[s] = 0.0; }
+	int ret = 0;
+	double mins = 1.79769313486231570815e308;
+	for (int I = 0; I < NI; ++I) mins = smin(mins, sx[I]);
+	for (int J = 0; J < NJ; ++J) mins = smin(mins, sy[J]);
+	double minx = 1.79769313486231570815e308, miny = minx;
+	for (int I = 0; I < NI; ++I) minx = smin(minx, sx[I]);
+	for (int J = 0; J < NJ; ++J) miny = smin(miny, sy[J]);
+	for (int st = 0; st < steps; ++st) {
+		/* NS_::restrict_time (s_ns.hpp:146-169) */
+		double maxmag = rs_max_magnitude(nx, ny, gl, u, v);
+		double rdt = cfg->cfl * mins / maxmag;
+		double rdt2 = *dt;
+		if (cfg->diff_number < 100) {
+			double den = 0.0;
+			den += 1.0 / (minx * minx);
+			den += 1.0 / (miny * miny);
+			rdt2 = cfg->diff_number / cfg->diff_coef / den;
+		}
+		if (*dt > smin(rdt, rdt2)) *dt = smin(rdt, rdt2);
+		const double DT = *dt;
+		/* _veo_star_center (s_ns_explicit.hpp:173-229) */
+		rs_apply_bc(nx, ny, gl, cx, sx, cy, sy, bc_u, u);
+		rs_apply_bc(nx, ny, gl, cx, sx, cy, sy, bc_v, v);
+		for (int c = 0; c < 2; ++c) {
+			const double* s = c == 0 ? u : v;
+			double* ss = c == 0 ? us : vs;
+			for (int j = 0; j < ny; ++j) {
+				for (int i = 0; i < nx; ++i) {
+					double adv = adv_cell(cfg->scheme, nx, ny, gl, cx, sx, cy,
+							sy, uf, vf, s, i, j);
+					double dif = nmn(nx, ny, gl, cx, sx, cy, sy, cfg->mu, s, i, j);
+					double src = 0;
+					AT(ss, i, j) = (-adv + (dif + src) / cfg->rho) * DT + AT(s, i, j);
+				}
+			}
+		}
+		rs_apply_bc(nx, ny, gl, cx, sx, cy, sy, bc_u, us);
+		rs_apply_bc(nx, ny, gl, cx, sx, cy, sy, bc_v, vs);
+		/* run_one_step (s_ns_explicit.hpp:118-155) */
+		rs_c2f(nx, ny, gl, sx, sy, us, vs, usf, vsf);
+		rs_div(nx, ny, gl, sx, sy, usf, vsf, div);
+		/* projection: Poisson_::run with set_depend(phi, -, div), the
+		 * CG + mean-removal drop-in solver */
+		rs_assemble_poisson(nx, ny, gl, cx, sx, cy, sy, &bc_phi, 1.0, div, 0.0,
+				rp, ci, va, b);
+		for (int j = 0; j < ny; ++j)
+			for (int i = 0; i < nx; ++i) x[i + j * nx] = AT(phi, i, j);
+		double m = 0;
+		for (int k = 0; k < n; ++k) m += b[k];
+		m = m / (double)n;
+		for (int k = 0; k < n; ++k) b[k] = b[k] - m;
+		int mi = cfg->cg_max_iter;
+		double tol = cfg->cg_tol;
+		int r = rs_krylov_csr(RS_CG, n, rp, ci, va, b, x, &mi, &tol, NULL, 0,
+				NULL, cfg->threads);
+		if (r && !ret) ret = r;
+		m = 0;
+		for (int k = 0; k < n; ++k) m += x[k];
+		m = m / (double)n;
+		for (int k = 0; k < n; ++k) x[k] = x[k] - m;
+		for (int j = 0; j < ny; ++j)
+			for (int i = 0; i < nx; ++i) AT(phi, i, j) = x[i + j * nx];
+		rs_apply_bc(nx, ny, gl, cx, sx, cy, sy, &bc_phi, phi);
+		rs_grad(nx, ny, gl, cx, cy, phi, gx, gy);
+		/* p = phi (all cells), then p *= 1/dt on normal cells */
+		memcpy(p, phi, sizeof(double) * N);
+		{
+			double inv = 1.0 / DT;
+			for (int j = 0; j < ny; ++j)
+				for (int i = 0; i < nx; ++i) AT(p, i, j) = AT(p, i, j) * inv;
+		}
+		for (size_t k = 0; k < N; ++k) usf[k] = usf[k] - gx[k];
+		for (size_t k = 0; k < N; ++k) vsf[k] = vsf[k] - gy[k];
+		rs_f2c(nx, ny, gl, gx, gy, gcx, gcy);
+		for (size_t k = 0; k < N; ++k) us[k] = us[k] - gcx[k];
+		for (size_t k = 0; k < N; ++k) vs[k] = vs[k] - gcy[k];
+		memcpy(u, us, sizeof(double) * N);
+		memcpy(v, vs, sizeof(double) * N);
+		memcpy(uf, usf, sizeof(double) * N);
+		memcpy(vf, vsf, sizeof(double) * N);
+		if (step_dt) step_dt[st] = DT;
+		if (step_iters) step_iters[st] = mi;
+		if (step_resid) step_resid[st] = tol;
+	}
+	free(us); free(vs); free(usf); free(vsf); free(div); free(gx); free(gy);
+	free(gcx); free(gcy); free(rp); free(ci); free(va); free(b); free(x);
+	return ret;
+}

@@ -1,0 +1,55 @@
+"""Shared test helpers. Tests marked `gpu` need a CUDA device (GB300) and the
+built library; everything else runs on the CPU."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+# Parity bar of the plain FP64 path against the FP64 reference: relative L2.
+PLAIN_RTOL = 1e-10
+
+
+def pytest_configure(config):
+    config.addinivalue_line(
+        "markers", "gpu: needs a CUDA GPU (sm_103a) and libcarpio_gpu.so")
+
+
+def golden(name):
+    path = os.path.join(GOLDEN, name + ".npz")
+    with np.load(path) as d:
+        return {k: d[k] for k in d.files}
+
+
+def golden_names(prefix):
+    return sorted(f[:-4] for f in os.listdir(GOLDEN)
+                  if f.startswith(prefix) and f.endswith(".npz"))
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def bits_equal(a, b):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    b = np.ascontiguousarray(b, dtype=np.float64)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+@pytest.fixture(scope="session")
+def gpu_lib():
+    """The built library on a CUDA device; fails (does not skip) without one."""
+    from carpio_gb300 import _lib
+    L = _lib.load()
+    n = L.carpio_gpu_device_count()
+    if n < 1:
+        pytest.fail("no CUDA device visible: gpu tests need a GB300")
+    return L

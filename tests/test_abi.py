@@ -1,0 +1,91 @@
+"""CPU checks of the C-ABI boundary: the library loads, exports exactly the
+entry points include/carpio_gpu.h declares, the Python binding covers them,
+and argument validation runs before any device work."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def header_functions():
+    txt = open(os.path.join(ROOT, "include", "carpio_gpu.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(carpio_gpu_\w+)\s*\(", txt)))
+
+
+def test_header_symbols_exported():
+    from carpio_gb300 import _lib
+    L = _lib.load()
+    names = header_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(L, n), f"{n} declared in carpio_gpu.h but not exported"
+    assert set(names) == set(_lib.SIGNATURES), "binding out of sync with header"
+
+
+def test_exported_symbols_are_declared():
+    import subprocess
+    from carpio_gb300 import _lib
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH],
+                         capture_output=True, text=True, check=True).stdout
+    exported = sorted({l.split()[-1] for l in out.splitlines()
+                       if " T carpio_gpu_" in l})
+    assert exported == header_functions()
+
+
+def test_version_and_errors():
+    from carpio_gb300 import _lib
+    L = _lib.load()
+    assert b"sm_103a" in L.carpio_gpu_version()
+    for code in (0, 1, 2, 3, -1, -2, -3, -4, -5, -6):
+        assert L.carpio_gpu_strerror(code) != b"unknown code"
+    assert L.carpio_gpu_strerror(99) == b"unknown code"
+    assert L.carpio_gpu_set_watchdog(0, 10) == _lib.EINVAL
+    assert L.carpio_gpu_set_watchdog(2000, 600000) == 0
+
+
+def test_argument_validation_before_device_work():
+    from carpio_gb300 import _lib
+    L = _lib.load()
+    mi, tol = ctypes.c_int(10), ctypes.c_double(1e-8)
+    z = np.zeros(4)
+    # n <= 0, bad kind, missing pointers -> EINVAL without touching CUDA
+    assert L.carpio_gpu_krylov_csr(0, 0, 0, _lib.ptr(np.zeros(1, np.uint32)),
+                                   None, None, _lib.ptr(z), _lib.ptr(z),
+                                   ctypes.byref(mi), ctypes.byref(tol), None,
+                                   0, None, 0) == _lib.EINVAL
+    assert L.carpio_gpu_krylov_csr(9, 4, 0, _lib.ptr(np.zeros(5, np.uint32)),
+                                   None, None, _lib.ptr(z), _lib.ptr(z),
+                                   ctypes.byref(mi), ctypes.byref(tol), None,
+                                   0, None, 0) == _lib.EINVAL
+    h = ctypes.c_void_p()
+    assert L.carpio_gpu_grid_create_uniform(0, 4, 2, 0, 1, 0, 1,
+                                            ctypes.byref(h)) == _lib.EINVAL
+    assert L.carpio_gpu_grid_create_uniform(4, 4, 2, 1, 0, 0, 1,
+                                            ctypes.byref(h)) == _lib.EINVAL
+    assert L.carpio_gpu_grid_destroy(None) == _lib.EINVAL
+    assert L.carpio_gpu_ns_run(None, 1, None, None, None) == _lib.EINVAL
+    assert L.carpio_gpu_poisson_solve(None, None, 1.0, None, None, None, None,
+                                      0, None) == _lib.EINVAL
+
+
+def test_ctypes_structs_match_header_layout():
+    from carpio_gb300 import _lib
+    assert ctypes.sizeof(_lib.BC) == 4 * 4 + 4 * 8
+    # int kind, precision, max_iter; double tol; int mean; double inner_tol;
+    # int inner_max; uint32 flags  (natural alignment)
+    assert ctypes.sizeof(_lib.SolverCfg) == 48
+    assert ctypes.sizeof(_lib.SolverStats) == 32
+
+
+def test_product_does_not_import_the_oracle():
+    pkg = os.path.join(ROOT, "carpio_gb300")
+    for dirpath, _, files in os.walk(pkg):
+        for f in files:
+            if f.endswith((".py", ".cu", ".cuh", ".hpp", ".h", ".cpp")):
+                txt = open(os.path.join(dirpath, f)).read()
+                assert "oracle" not in re.sub(r"(#|//).*", "", txt) or f == "__init__.py", f

@@ -1,0 +1,126 @@
+"""GPU parity of the projection step (operators and NS_explicit_ stepping)
+against the reference's runs: operators bit for bit, stepped fields to the
+plain-path tolerance."""
+import numpy as np
+import pytest
+
+from conftest import PLAIN_RTOL, bits_equal, golden, golden_names, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+OPS_SCHEMES = ("upwind1", "center", "vanleer", "superbee", "minmod", "upwind2",
+               "quick", "cui", "wahyd", "center4")
+
+
+@pytest.mark.parametrize("name", golden_names("ops_"))
+def test_operators_bitwise(gpu_lib, name):
+    from carpio_gb300 import structure as S, _lib
+    d = golden(name)
+    nx, ny, gl = int(d["nx"]), int(d["ny"]), int(d["gl"])
+    g = S.Grid((0.0, 0.0), (1.0, 1.0), (nx, ny), gl)
+    assert bits_equal(g.cx, d["grid_cx"]) and bits_equal(g.cy, d["grid_cy"])
+    a, b, uf, vf = d["in_a"], d["in_b"], d["in_uf"], d["in_vf"]
+    gx, gy, _ = S.operator(g, 0, a=a)
+    assert bits_equal(gx, d["grad_x"]) and bits_equal(gy, d["grad_y"])
+    o, _, _ = S.operator(g, 1, a=uf, b=vf)
+    assert bits_equal(o, d["div"])
+    fx, fy, _ = S.operator(g, 2, a=uf, b=vf)
+    assert bits_equal(fx, d["f2c_x"]) and bits_equal(fy, d["f2c_y"])
+    fx, fy, _ = S.operator(g, 3, a=a, b=b)
+    assert bits_equal(fx, d["c2f_x"]) and bits_equal(fy, d["c2f_y"])
+    _, _, m = S.operator(g, 7, a=a, b=b)
+    assert m == float(d["max_magnitude"])
+    for s in OPS_SCHEMES:
+        if "adv_" + s in d:
+            o, _, _ = S.operator(g, 4, a=uf, b=vf, c=a, scheme=s)
+            assert bits_equal(o, d["adv_" + s]), s
+    o, _, _ = S.operator(g, 5, c=a, coef=0.37)
+    assert bits_equal(o, d["diffusion"])
+    bc = _lib.BC()
+    for k, (t, v) in enumerate(zip([1, 2, 2, 1], [0.5, -2.0, 1.5, 0.25])):
+        bc.type[k], bc.value[k] = t, v
+    o, _, _ = S.operator(g, 6, bc=bc, out1=b)
+    assert bits_equal(o, d["bc_filled"])
+
+
+def make_cavity(n, scheme, dt0, Re=1000.0, tol=1e-10, max_iter=100000,
+                precision="fp64", **kw):
+    from carpio_gb300 import structure as S
+    g = S.Grid((0.0, 0.0), (1.0, 1.0), (n, n), 2)
+    ns = S.NS_explicit(g)
+    ns.set_advection_scheme(scheme)
+    ns.set_time(0, dt0)
+    bc0, bc1 = S.BoundaryCondition(), S.BoundaryCondition()
+    bc0.set_default_1_bc(0.0)
+    bc1.set_default_1_bc(1.0)
+    for s in range(3):
+        ns.add_bc(0, s, "u", bc0)
+    ns.add_bc(0, 3, "u", bc1)
+    for s in range(4):
+        ns.add_bc(0, s, "v", bc0)
+    ns.set_uniform_rho(Re)
+    ns.set_diffusion_number(0.25, 1.0 / Re)
+    ns.set_projection_solver("CG", max_iter, tol, precision=precision, **kw)
+    return g, ns
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names("cavity_")
+                                  if not n.endswith("_2000")])
+def test_cavity_matches_reference(gpu_lib, name):
+    d = golden(name)
+    a = d["case_args"]
+    n, steps, scheme = int(a[1]), int(a[2]), str(a[3])
+    tol, max_iter, dt0, Re = float(a[4]), int(a[5]), float(a[6]), float(a[7])
+    g, ns = make_cavity(n, scheme, dt0, Re, tol, max_iter)
+    assert ns.run(steps) == 0
+    st = ns.state()
+    # dt: the diffusion limit is bitwise; the CFL limit follows max|u|
+    assert np.allclose(ns.step_dt, d["dt"], rtol=1e-12, atol=0)
+    its = np.asarray(ns.step_iters)
+    assert np.all(np.abs(its - d["cg_iters"]) <= np.maximum(2, d["cg_iters"] // 100))
+    for k in ("u", "v", "p", "phi", "uf", "vf"):
+        err = rel_l2(g.interior(st[k]), g.interior(d[k]))
+        assert err <= PLAIN_RTOL, (k, err)
+
+
+def test_cavity_first_step_fields(gpu_lib):
+    """One step of the 32^2 cavity against the reference's first-step dump:
+    velocities, faces, phi and p (ghosts and corners included)."""
+    d = golden("cavity_32_vanleer_20")
+    g, ns = make_cavity(32, "VanLeer", 0.015625)
+    assert ns.run(1) == 0
+    st = ns.state()
+    for k in ("u", "v", "uf", "vf", "phi", "p"):
+        err = rel_l2(st[k], d["s1_" + k])
+        assert err <= PLAIN_RTOL, (k, err)
+
+
+@pytest.mark.parametrize("n", [128, 256])
+def test_cavity_2000_steps(gpu_lib, n):
+    """BASELINE config: lid-driven cavity, Re 1000, van Leer, CG 1e-10 with
+    mean removal, 2000 steps from rest, field by field against the
+    reference's own run."""
+    name = f"cavity_{n}_vanleer_2000"
+    if name not in golden_names("cavity_"):
+        pytest.skip(f"fixture {name} not generated")
+    d = golden(name)
+    g, ns = make_cavity(n, "VanLeer", 0.5 / n)
+    assert ns.run(2000) == 0
+    st = ns.state()
+    assert np.allclose(ns.step_dt, d["dt"], rtol=1e-12, atol=0)
+    for k in ("u", "v", "p"):
+        err = rel_l2(g.interior(st[k]), d[k + "_interior"])
+        assert err <= 1e-8, (k, err)
+
+
+def test_cavity_mixed_precision_tracks_fp64(gpu_lib):
+    """FP32-inner projection against the FP64 projection, step by step."""
+    g, a = make_cavity(128, "VanLeer", 0.5 / 128, tol=1e-8)
+    _, b = make_cavity(128, "VanLeer", 0.5 / 128, tol=1e-8, precision="mixed",
+                       inner_tol=1e-3)
+    for _ in range(5):
+        assert a.run(10) == 0
+        assert b.run(10) == 0
+        sa, sb = a.state(), b.state()
+        for k in ("u", "v"):
+            assert rel_l2(g.interior(sb[k]), g.interior(sa[k])) < 1e-6

@@ -1,0 +1,149 @@
+"""GPU parity of the structure-level Poisson solve (matrix-free stencil,
+carpio_gpu_poisson_solve) against the reference's runs and the oracle."""
+import numpy as np
+import pytest
+
+from conftest import PLAIN_RTOL, golden, golden_names, rel_l2
+from oracle import restate as R
+
+pytestmark = pytest.mark.gpu
+
+BCS = {
+    "c1": ([1] * 4, [0.0] * 4),
+    "neumann": ([2] * 4, [0.0] * 4),
+    "mixed": ([1, 1, 2, 2], [1.0, -0.5, 0.75, -1.25]),
+}
+NAMES = {"cg": "CG", "jacobi": "Jacobi", "dia_bicgstab": "Dia_BiCGSTAB",
+         "bicgstab": "BiCGSTAB"}
+
+
+def make_poisson(n, case, kind, max_iter, tol, source, phi=None, nx=None,
+                 gl=2, **kw):
+    from carpio_gb300 import structure as S
+    g = S.Grid((0.0, 0.0), (1.0, 1.0), (nx or n, n), gl)
+    P = S.Poisson(g)
+    types, vals = BCS[case]
+    for seg in range(4):
+        bc = S.BoundaryCondition()
+        if types[seg] == 1:
+            bc.set_default_1_bc(vals[seg])
+        else:
+            bc.set_default_2_bc(vals[seg])
+        P.add_bc(0, seg, "phi", bc)
+    P.set_depend(g.zeros() if phi is None else phi.copy(), None, source)
+    P.set_solver(NAMES[kind], None, max_iter, tol,
+                 mean_removal=(case == "neumann"), **kw)
+    return g, P
+
+
+@pytest.mark.parametrize("name", golden_names("poisson_"))
+def test_poisson_matches_reference(gpu_lib, name):
+    d = golden(name)
+    case, n, kind = str(d["case_args"][1]), int(d["case_args"][2]), str(d["case_args"][3])
+    max_iter, tol = int(d["case_args"][4]), float(d["case_args"][5])
+    g, P = make_poisson(n, case, kind, max_iter, tol, d["source"])
+    rc = P.run()
+    st = P.stats
+    assert rc == int(d["ret"])
+    ref_it = int(d["max_iter_out"])
+    assert abs(st.iters - ref_it) <= max(2, ref_it // 1000), (st.iters, ref_it)
+    x = R.field_to_vec(R.Grid(n, n, 2), P.phi)
+    err = rel_l2(x, d["x"])
+    if kind in ("cg", "dia_bicgstab", "bicgstab") and tol <= 1e-10:
+        assert err <= max(PLAIN_RTOL, 10 * tol), err
+    else:
+        assert err <= 50 * tol, err
+    # ghosts of phi are untouched by the solve (the reference leaves them too)
+    assert np.all(P.phi[:2] == 0) and np.all(P.phi[-2:] == 0)
+
+
+def test_c1_exact_solution_error(gpu_lib):
+    """C1: 64^2, Dirichlet 0, f = -2 pi^2 sin sin: CG converges in one
+    iteration (the RHS is an eigenvector) with the reference's L2 error."""
+    d = golden("poisson_c1_64_cg")
+    for kind, its in (("cg", (1, 1)), ("jacobi", (19000, 19200))):
+        g, P = make_poisson(64, "c1", kind, 100000, 1e-10, d["source"])
+        assert P.run() == 0
+        assert its[0] <= P.stats.iters <= its[1]
+        X, Y = np.meshgrid(g.cx, g.cy, indexing="ij")
+        exact = np.sin(np.pi * X) * np.sin(np.pi * Y)
+        e = g.interior(P.phi) - g.interior(exact)
+        rms = np.sqrt(np.mean(e * e))
+        assert rms == pytest.approx(1.0041e-4, rel=1e-3)
+
+
+def test_ragged_grid_against_oracle(gpu_lib):
+    """non-square cell counts, gl = 1, mixed boundaries, random source"""
+    rng = np.random.default_rng(3)
+    for (nx, ny) in ((33, 17), (5, 3), (1, 7)):
+        from carpio_gb300 import structure as S
+        g = S.Grid((0.0, 0.0), (1.0, 1.0), (nx, ny), 1)
+        src = rng.uniform(-1, 1, g.N())
+        P = S.Poisson(g)
+        types, vals = BCS["mixed"]
+        for seg in range(4):
+            bc = S.BoundaryCondition()
+            (bc.set_default_1_bc if types[seg] == 1 else bc.set_default_2_bc)(vals[seg])
+            P.add_bc(0, seg, "phi", bc)
+        P.set_depend(g.zeros(), None, src)
+        P.set_solver("CG", None, 10000, 1e-13)
+        assert P.run() == 0
+        og = R.Grid(nx, ny, 1)
+        rp, ci, va, b = R.assemble_poisson(og, R.make_bc(types, vals), 1.0, src=src)
+        code, x, it, t, _ = R.krylov_csr("cg", rp, ci, va, b, np.zeros(nx * ny),
+                                         10000, 1e-13)
+        assert code == 0
+        assert rel_l2(R.field_to_vec(og, P.phi), x) < 1e-10
+
+
+def test_zero_rhs_and_initial_guess(gpu_lib):
+    # b = 0: normb is taken as 1 (solver_matrix.hpp:282-283); x0 = 0 is converged
+    g, P = make_poisson(16, "c1", "cg", 100, 1e-10, np.zeros((20, 20)))
+    assert P.run() == 0 and P.stats.iters == 0
+    assert np.all(P.phi == 0)
+
+
+def test_mixed_precision_matches_fp64(gpu_lib):
+    """FP32 inner CG in FP64 refinement reaches the same 1e-8 residual and
+    agrees with the FP64 solve to the accuracy the tolerance allows."""
+    rng = np.random.default_rng(5)
+    for case, n in (("neumann", 96), ("c1", 80)):
+        src = rng.uniform(-1, 1, (n + 4, n + 4))
+        g64, P64 = make_poisson(n, case, "cg", 20000, 1e-12, src)
+        assert P64.run() == 0
+        gm, Pm = make_poisson(n, case, "cg", 20000, 1e-8, src, precision="mixed",
+                              inner_tol=1e-3)
+        assert Pm.run() == 0
+        assert Pm.stats.tol_out <= 1e-8
+        assert Pm.stats.outer_iters >= 1
+        err = rel_l2(gm.interior(Pm.phi), g64.interior(P64.phi))
+        assert err < 1e-5, err
+
+
+def test_solver_is_repeatable(gpu_lib):
+    d = golden("poisson_neumann_48_cg")
+    outs = []
+    for _ in range(2):
+        g, P = make_poisson(48, "neumann", "cg", 5000, 1e-12, d["source"])
+        P.run()
+        outs.append(P.phi.copy())
+    assert np.array_equal(outs[0].view(np.uint64), outs[1].view(np.uint64))
+
+
+def test_watchdog_expiry_is_reported(gpu_lib):
+    """A solve that cannot finish inside the watchdog returns ETIMEOUT and
+    leaves the context usable (no trap, no hang)."""
+    from carpio_gb300 import _lib
+    L = gpu_lib
+    d = golden("poisson_c1_64_cg")
+    try:
+        assert L.carpio_gpu_set_watchdog(2000, 1) == 0   # 1 ms solve budget
+        g, P = make_poisson(256, "neumann", "jacobi", 10 ** 7, 1e-30,
+                            np.random.default_rng(0).uniform(-1, 1, (260, 260)))
+        with pytest.raises(_lib.CarpioGpuError) as e:
+            P.run()
+        assert e.value.code == _lib.ETIMEOUT
+    finally:
+        L.carpio_gpu_set_watchdog(2000, 600000)
+    g, P = make_poisson(64, "c1", "cg", 1000, 1e-10, d["source"])
+    assert P.run() == 0
