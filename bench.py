@@ -1,0 +1,414 @@
+"""Benchmark of the projection hot path: lid-driven cavity steps/s at 1024^2.
+
+Workload (the 1024^2 cavity configuration): uniform 1024x1024 cells on
+[0,1]^2, gl = 2, Re = 1000 (rho = 1000, mu = 1), lid u = 1 on the top wall,
+no-slip elsewhere, van Leer TVD advection, explicit diffusion, CFL 0.5 and
+diffusion number 0.25, dt0 = 0.5 h; all-Neumann pressure Poisson solved to
+1e-8 relative residual with mean removal, FP32 inner CG inside FP64
+iterative refinement. Synthetic state: the cavity started from rest; W
+warm-up steps, then K timed steps. One "step" = NS_explicit_::run_one_step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's CPU implementation of the same step
+(its restatement in oracle/, FP64 CG with mean removal, all host threads) on
+rank 0; the reference has no GPU path.
+
+Timing: CUDA events on the library's launching stream around each step
+(carpio_gpu_ns_profile), max over ranks. The per-step working set (10
+fields + the Krylov vectors, ~200 MB) is larger than the 129 MB L2, so no
+flush is inserted between steps. e2e: the same steps through the public API
+with host buffers, the full state copied host->device before and
+device->host after every step.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_DEFAULT = 1024
+TOL = 1e-8
+RE = 1000.0
+METRIC = "cavity_steps_per_s_1024"
+# kernels the library launches per projection step (restrict_time, 3 ghost
+# fills, predictor, C2F, the persistent projection solve, correction)
+LAUNCHES_PER_STEP = 8
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--inner-tol", type=float, default=1e-3)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the FP64 comparison, Poisson and CPU legs")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def config(n, precision, inner_tol):
+    return {"workload": f"lid-driven cavity {n}x{n}, Re 1000, van Leer, "
+                        f"CG to {TOL:g} with mean removal "
+                        f"({'FP32 inner / FP64 refinement' if precision == 'mixed' else 'FP64'})",
+            "n": n, "Re": RE, "scheme": "VanLeer", "tol": TOL,
+            "precision": precision, "inner_tol": inner_tol,
+            "cfl": 0.5, "diffusion_number": 0.25, "dt0": 0.5 / n,
+            "l2": "per-step working set ~200 MB > 129 MB L2; no flush",
+            "parallelism": "replicas"}
+
+
+def make_cavity(n, precision, inner_tol):
+    from carpio_gb300 import structure as S
+    g = S.Grid((0.0, 0.0), (1.0, 1.0), (n, n), 2)
+    ns = S.NS_explicit(g)
+    ns.set_advection_scheme("VanLeer")
+    ns.set_time(0, 0.5 / n)
+    bc0, bc1 = S.BoundaryCondition(), S.BoundaryCondition()
+    bc0.set_default_1_bc(0.0)
+    bc1.set_default_1_bc(1.0)
+    for s in range(3):
+        ns.add_bc(0, s, "u", bc0)
+    ns.add_bc(0, 3, "u", bc1)
+    for s in range(4):
+        ns.add_bc(0, s, "v", bc0)
+    ns.set_uniform_rho(RE)
+    ns.set_diffusion_number(0.25, 1.0 / RE)
+    ns.set_projection_solver("CG", 200000, TOL, precision=precision,
+                             inner_tol=inner_tol)
+    ns.initial()
+    return g, ns
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for line in self.lines:
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                smax.append(float(p[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[4:8]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def solve_bytes_per_cell(precision, inner, outer):
+    """Algorithmic bytes of one projection-solve launch per cell: prologue
+    (read 2 face fields + phi, write b and x: 40 B), per FP32 inner CG
+    iteration 40 B (read p, q, r, x, D; write p, q, x, r: 4 B each, the
+    operator's neighbours counted once), per FP64 refinement step 40 B
+    (read x, b, D; write r; write x), per FP64 CG iteration 80 B, epilogue
+    (mean removal + scatter: read x twice, write phi: 24 B)."""
+    if precision == "mixed":
+        return 40 + 40 * inner + 40 * (outer + 1) + 24
+    return 40 + 80 * inner + 24 + 24
+
+
+def traffic_per_launch(n, inner, outer):
+    """DRAM bytes per launch from the committed ncu capture, scaled by cells
+    and iterations, or None."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            t = json.load(f)
+        per_cell_iter = float(t["dram_bytes_per_cell_per_inner_iter"])
+        return per_cell_iter * n * n * max(inner, 1)
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def reference_iters(n):
+    """CG iterations per step of the reference algorithm (FP64 CG to 1e-8,
+    mean removal) on this workload, recorded by a full run of the oracle
+    restatement (oracle/record_cg_iters.py -> oracle/cavity_cg_iters_<n>.json)."""
+    path = os.path.join(ROOT, "oracle", f"cavity_cg_iters_{n}.json")
+    with open(path) as f:
+        return {r["step"]: r["cg_iters"] for r in json.load(f)["rows"]}
+
+
+def cpu_step_model(n, threads, caps=(20, 120)):
+    """Times the reference CPU step (oracle restatement of NS_explicit_ with
+    CSR assembly + carpio::CG, FP64) at size n on a bounded sample: step 1
+    from rest with the CG capped at each of `caps` iterations. Returns
+    (fixed seconds per step, seconds per CG iteration)."""
+    from oracle import restate as R
+    R.lib()
+    g = R.Grid(n, n, 2)
+    t = []
+    for m in caps:
+        st = R.new_state(g, 0.5 / n)
+        t0 = time.perf_counter()
+        R.ns_run(g, st, 1, scheme="vanleer", cg_tol=1e-300, cg_max_iter=m,
+                 threads=threads)
+        t.append(time.perf_counter() - t0)
+    per_it = max((t[1] - t[0]) / (caps[1] - caps[0]), 1e-9)
+    fixed = max(t[0] - caps[0] * per_it, 0.0)
+    return fixed, per_it
+
+
+def run_reference(a):
+    ws, rank, local = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    n = a.n
+    iters = reference_iters(n)
+    steps = list(range(a.warmup + 1, a.warmup + a.steps + 1))
+    fixed, per_it = cpu_step_model(n, threads)
+    # each timed step: the fixed part plus the step's own CG iteration count
+    per_step = [fixed + per_it * iters.get(s, iters[max(iters)]) for s in steps]
+    el = float(np.sum(per_step))
+    v = a.steps / el
+    sample = (f"{n}^2 cavity step sampled with CG capped at 20 and 120 "
+              f"iterations (fixed {fixed:.3f} s + {1e3 * per_it:.2f} ms/CG "
+              f"iteration on {threads} threads), scaled to the reference's "
+              f"{int(np.mean([iters.get(s, 0) for s in steps]))} CG iterations "
+              f"per step at steps {steps[0]}..{steps[-1]}")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s",
+        "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": 1e3 * el / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (cavity from rest)",
+        "config": config(n, "fp64", None),
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0}}), flush=True)
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+        return
+    ws, rank, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from carpio_gb300 import _lib
+    _lib.load()
+    n = a.n
+    g, ns = make_cavity(n, a.precision, a.inner_tol)
+    # warm-up (also builds the coefficient cache)
+    if a.warmup > 0:
+        rc = ns.run(a.warmup)
+        assert rc == 0, f"warm-up failed: {_lib.strerror(rc)}"
+    clocks = Clocks(local)
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    clocks.start()
+    t0 = time.perf_counter()
+    rc = ns.run(a.steps)
+    barrier()
+    wall = time.perf_counter() - t0
+    clk = clocks.stop()
+    assert rc == 0, f"timed steps failed: {_lib.strerror(rc)}"
+    prof = ns.profile()
+    dev_s = float(np.sum(prof["step_ms"])) / 1e3
+    elapsed = dev_s
+    if ws > 1:
+        import torch.distributed as dist
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    value = ws * a.steps / elapsed
+    inner = float(np.mean(prof["inner"]))
+    outer = float(np.mean(prof["outer"]))
+    solve_ms = float(np.mean(prof["solve_ms"]))
+    out = {
+        "metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws,
+        "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": 1e3 * elapsed / a.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if a.precision == "mixed" else "f64",
+        "data": "synthetic (cavity from rest)",
+        "config": config(n, a.precision, a.inner_tol),
+        "gpu_launches": LAUNCHES_PER_STEP * a.steps,
+        "clocks": clk,
+        "wall_ms_per_step": 1e3 * wall / a.steps,
+        "projection": {"solve_ms": solve_ms, "inner_iters": inner,
+                       "outer_iters": outer,
+                       "share_of_step": solve_ms / (1e3 * dev_s / a.steps)},
+    }
+    # roofline of the dominant kernel (the persistent projection solve)
+    peak, how = peaks()
+    bpc = solve_bytes_per_cell(a.precision, inner, outer)
+    achieved = bpc * n * n / (solve_ms / 1e3) / 1e9
+    out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak,
+                       "unit": "GB/s", "frac": achieved / peak,
+                       "peak_source": how,
+                       "traffic": traffic_per_launch(n, inner, outer),
+                       "algorithmic_bytes_per_launch": bpc * n * n,
+                       "kernel": "k_poisson (persistent projection solve)"}
+    # e2e through the public API with host buffers
+    if rank == 0 or True:
+        st = ns.state()
+        host = {k: np.ascontiguousarray(st[k]) for k in ("u", "v", "uf", "vf", "phi", "p")}
+        dt = st["dt"]
+        e2e_steps = max(1, min(a.steps, 5))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            ns.set_state(dt, **host)
+            rc = ns.run(1)
+            st = ns.state()
+            dt = st["dt"]
+            for k in host:
+                host[k] = st[k]
+        barrier()
+        e_el = time.perf_counter() - t0
+        nbytes = sum(v.nbytes for v in host.values())
+        out["e2e"] = {"value": ws * e2e_steps / e_el, "unit": "steps/s",
+                      "h2d_bytes_per_step": nbytes + 8,
+                      "d2h_bytes_per_step": nbytes + 8,
+                      "steps": e2e_steps}
+    if not a.no_extras and rank == 0:
+        # FP64-CG projection on the same workload, same GPU
+        other = "fp64" if a.precision == "mixed" else "mixed"
+        g2, ns2 = make_cavity(n, other, a.inner_tol)
+        ns2.run(a.warmup)
+        torch.cuda.synchronize()
+        ns2.run(a.steps)
+        p2 = ns2.profile()
+        out[f"{other}_projection"] = {
+            "steps_per_s": a.steps / (float(np.sum(p2["step_ms"])) / 1e3),
+            "solve_ms": float(np.mean(p2["solve_ms"])),
+            "iters": float(np.mean(p2["inner"]))}
+        del ns2
+        # Poisson ms to 1e-8 on the same divergence field: FP64 CG vs mixed
+        out["poisson_ms_to_1e-8"] = poisson_leg(n, a.inner_tol)
+        # CPU baseline: the reference's CPU step (restatement) on a bounded
+        # sample of the same workload, scaled to the timed steps' iterations
+        if ws == 1:
+            threads = os.cpu_count() or 1
+            fixed, per_it = cpu_step_model(n, threads)
+            iters = reference_iters(n)
+            steps = range(a.warmup + 1, a.warmup + a.steps + 1)
+            its = float(np.mean([iters.get(s, iters[max(iters)]) for s in steps]))
+            out["cpu_baseline"] = {
+                "value": 1.0 / (fixed + per_it * its), "unit": "steps/s",
+                "cores": threads, "kind": "port",
+                "sample": f"{n}^2 cavity step with CG capped at 20/120 "
+                          f"iterations (fixed {fixed:.3f} s, "
+                          f"{1e3 * per_it:.2f} ms per CG iteration), scaled to "
+                          f"the reference's {its:.0f} FP64 CG iterations per "
+                          f"step at the timed steps; oracle restatement, "
+                          f"{threads} threads"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def poisson_leg(n, inner_tol):
+    """Poisson time to 1e-8 relative residual on a synthetic smooth field
+    (sum of 8 seeded Gaussians, zero mean, all-Neumann): FP64 CG vs FP32
+    inner / FP64 refinement, device time of the solve."""
+    from carpio_gb300 import structure as S
+    rng = np.random.default_rng(1234)
+    g = S.Grid((0.0, 0.0), (1.0, 1.0), (n, n), 2)
+    X, Y = np.meshgrid(g.cx, g.cy, indexing="ij")
+    src = np.zeros(g.N())
+    for _ in range(8):
+        cx, cy = rng.uniform(0, 1, 2)
+        w = rng.uniform(0.02, 0.2)
+        src += rng.normal() * np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2 * w * w))
+    res = {}
+    for prec in ("fp64", "mixed"):
+        P = S.Poisson(g)
+        P.set_depend(g.zeros(), None, src)
+        P.set_solver("CG", None, 200000, TOL, mean_removal=True, precision=prec,
+                     inner_tol=inner_tol)
+        P.run()   # warm-up
+        P.set_depend(g.zeros(), None, src)
+        rc = P.run()
+        res[prec] = {"ms": P.stats.ms, "iters": P.stats.iters,
+                     "outer": P.stats.outer_iters, "resid": P.stats.tol_out,
+                     "code": rc}
+    res["speedup_mixed_over_fp64"] = res["fp64"]["ms"] / res["mixed"]["ms"]
+    return res
+
+
+if __name__ == "__main__":
+    main()

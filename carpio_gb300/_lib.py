@@ -78,6 +78,8 @@ SIGNATURES = {
     "carpio_gpu_ns_get_state": (ctypes.c_int, [
         _VP, _D, _VP, _VP, _VP, _VP, _VP, _VP]),
     "carpio_gpu_ns_run": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, _VP]),
+    "carpio_gpu_ns_profile": (ctypes.c_int, [
+        _VP, ctypes.c_int, _I, _VP, _VP, _VP, _VP]),
     "carpio_gpu_operator": (ctypes.c_int, [
         _VP, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.POINTER(BC),
         _VP, _VP, _VP, _VP, _VP, _D]),

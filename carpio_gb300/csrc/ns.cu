@@ -535,6 +535,13 @@ struct carpio_gpu_ns {
 	cudaStream_t s;
 	DtRule rule;
 	double t_host = 0;
+	// per-step events of the last run: [step start, solve start, solve end]
+	std::vector<cudaEvent_t> ev;
+	std::vector<cg_dev::SolveOut> last_rec;
+	int last_steps = 0;
+	~carpio_gpu_ns() {
+		for (cudaEvent_t e : ev) cudaEventDestroy(e);
+	}
 };
 
 extern "C" {
@@ -650,7 +657,14 @@ int carpio_gpu_ns_run(carpio_gpu_ns* ns, int steps, double* step_dt,
 	const int nbf = grid_blocks((long)g->NI * g->NJ);
 	const carpio_gpu_ns_cfg& c = ns->cfg;
 	cg_dev::SolveOut* rec = ns->rec.as<cg_dev::SolveOut>();
+	const size_t nev = 3 * (size_t)steps + 1;
+	while (ns->ev.size() < nev) {
+		cudaEvent_t e;
+		CG_CK(cudaEventCreate(&e));
+		ns->ev.push_back(e);
+	}
 	for (int st = 0; st < steps; ++st) {
+		CG_CK(cudaEventRecord(ns->ev[3 * st], s));
 		k_restrict_time<<<nb, kThreads, 0, s>>>(geo, u, v, ss, ns->rule,
 				ns->rec_dt.as<double>(), st);
 		CG_CK(cudaGetLastError());
@@ -659,14 +673,17 @@ int carpio_gpu_ns_run(carpio_gpu_ns* ns, int steps, double* step_dt,
 		CG_CK(launch_bc(geo, us, c.bc_u, vs, &c.bc_v, s));
 		k_c2f<<<nb, kThreads, 0, s>>>(geo, us, vs, usf, vsf);
 		CG_CK(cudaGetLastError());
+		CG_CK(cudaEventRecord(ns->ev[3 * st + 1], s));
 		if ((rc = poisson_launch(g, ns->coeffs, ns->pws, SRC_DIV, usf, vsf, phi,
 				c.projection, nullptr, 0, rec + st, s)))
 			return rc;
+		CG_CK(cudaEventRecord(ns->ev[3 * st + 2], s));
 		CG_CK(launch_bc(geo, phi, bc_phi, nullptr, nullptr, s));
 		k_correct<<<nbf, kThreads, 0, s>>>(geo, phi, us, vs, usf, vsf, u, v, uf,
 				vf, p, ss);
 		CG_CK(cudaGetLastError());
 	}
+	CG_CK(cudaEventRecord(ns->ev[3 * steps], s));
 	std::vector<cg_dev::SolveOut> h(steps);
 	std::vector<double> hdt(steps);
 	CG_CK(cudaMemcpyAsync(h.data(), rec, sizeof(cg_dev::SolveOut) * steps,
@@ -682,7 +699,28 @@ int carpio_gpu_ns_run(carpio_gpu_ns* ns, int steps, double* step_dt,
 		if (!first && h[st].code) first = h[st].code;
 		ns->t_host += hdt[st];
 	}
+	ns->last_rec = h;
+	ns->last_steps = steps;
 	return first;
+}
+
+int carpio_gpu_ns_profile(carpio_gpu_ns* ns, int cap, int* n,
+		double* solve_ms, double* step_ms, int* inner_iters, int* outer_iters) {
+	if (!ns || cap < 0) return CARPIO_GPU_EINVAL;
+	int m = ns->last_steps < cap ? ns->last_steps : cap;
+	if (n) *n = ns->last_steps;
+	for (int st = 0; st < m; ++st) {
+		float a = 0, b = 0;
+		CG_CK(cudaEventElapsedTime(&a, ns->ev[3 * st + 1], ns->ev[3 * st + 2]));
+		CG_CK(cudaEventElapsedTime(&b, ns->ev[3 * st], ns->ev[3 * st + 3]));
+		if (solve_ms) solve_ms[st] = a;
+		if (step_ms) step_ms[st] = b;
+		const cg_dev::SolveOut& o = ns->last_rec[st];
+		bool mixed = ns->cfg.projection.precision == CARPIO_GPU_MIXED;
+		if (inner_iters) inner_iters[st] = mixed ? o.inner : o.iters;
+		if (outer_iters) outer_iters[st] = mixed ? o.outer : 0;
+	}
+	return 0;
 }
 
 int carpio_gpu_operator(carpio_gpu_grid* g, int which, int scheme,

@@ -241,6 +241,23 @@ class NS_explicit:
         self.step_resid += res[:n].tolist()
         return rc
 
+    def profile(self):
+        """per-step device times of the last run (carpio_gpu_ns_profile)"""
+        n = ctypes.c_int(0)
+        _lib.load().carpio_gpu_ns_profile(self.handle, 0, ctypes.byref(n),
+                                          None, None, None, None)
+        m = n.value
+        solve, step = np.zeros(max(m, 1)), np.zeros(max(m, 1))
+        inner = np.zeros(max(m, 1), dtype=np.int32)
+        outer = np.zeros(max(m, 1), dtype=np.int32)
+        rc = _lib.load().carpio_gpu_ns_profile(
+            self.handle, m, ctypes.byref(n), _lib.ptr(solve), _lib.ptr(step),
+            _lib.ptr(inner), _lib.ptr(outer))
+        if rc:
+            raise _lib.CarpioGpuError(rc, "ns_profile")
+        return dict(solve_ms=solve[:m], step_ms=step[:m], inner=inner[:m],
+                    outer=outer[:m])
+
     def set_state(self, dt, **fields):
         args = [fields.get(k) for k in ("u", "v", "uf", "vf", "phi", "p")]
         rc = _lib.load().carpio_gpu_ns_set_state(

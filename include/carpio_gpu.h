@@ -190,6 +190,13 @@ int carpio_gpu_ns_get_state(carpio_gpu_ns* ns, double* dt, double* u,
 int carpio_gpu_ns_run(carpio_gpu_ns* ns, int steps, double* step_dt,
 		int* step_iters, double* step_resid);
 
+/* Timing of the last carpio_gpu_ns_run, per step (host arrays of length
+ * `cap`, any may be NULL): device time of the projection solve launch and of
+ * the whole step (CUDA events on the launching stream), inner (FP32) and
+ * outer iterations of the solve. *n gets the number of steps recorded. */
+int carpio_gpu_ns_profile(carpio_gpu_ns* ns, int cap, int* n,
+		double* solve_ms, double* step_ms, int* inner_iters, int* outer_iters);
+
 /* Single operators of Operation_ (s_operation.hpp) on full fields, for
  * callers that drive their own loop and for per-kernel checks.
  *   which: 0 Grad (:46-72)       in a        -> out1 (x faces), out2 (y faces)

@@ -53,3 +53,11 @@ def gpu_lib():
     if n < 1:
         pytest.fail("no CUDA device visible: gpu tests need a GB300")
     return L
+
+
+@pytest.fixture(scope="session", autouse=True)
+def _built_library():
+    """(Re)build libcarpio_gpu.so if its sources changed (no-op when fresh),
+    so the ABI tests always load the library the sources describe."""
+    from carpio_gb300 import compile as c
+    c.build()

@@ -15,6 +15,18 @@ def true_resid(A, x, b):
     return np.linalg.norm(r[:-1]) / (nb if nb else 1.0)
 
 
+def iter_band(kind, ref_it):
+    """Allowed |GPU - reference| iteration difference. Dot products are
+    summed in a different order on the GPU, so Krylov iteration counts move
+    by rounding: CG a few percent on ill-conditioned systems, BiCGSTAB (non-
+    monotone) more; Jacobi (a contraction) hardly at all."""
+    if kind.startswith("jacobi"):
+        return max(2, ref_it // 200)
+    if kind == "cg":
+        return max(3, ref_it // 20)
+    return max(3, ref_it // 5)
+
+
 @pytest.mark.parametrize("name", golden_names("csr_"))
 def test_csr_matches_reference(gpu_lib, name):
     from carpio_gb300 import algebra, _lib
@@ -33,17 +45,66 @@ def test_csr_matches_reference(gpu_lib, name):
     k = "jacobi" if kind == "jacobi_class" else kind
     code, it, t = algebra.krylov(k, A, x, b, max_iter, tol, lr)
     assert code == int(d["ret"])
-    # iteration counts: the parallel sums round differently; allow a few
-    # iterations either way on long runs, exact on short ones
-    ref_it = int(d["max_iter_out"])
-    assert abs(it - ref_it) <= max(2, ref_it // 1000), (it, ref_it)
-    assert len(lr) == pytest.approx(int(d["lresid_len"]), abs=max(2, ref_it // 1000))
+    # the residual list has one entry per iteration in both implementations
+    ref_len = int(d["lresid_len"])
+    assert abs(len(lr) - ref_len) <= iter_band(k, ref_len), (len(lr), ref_len)
     if code == 0:
-        stop = "<=" if k in ("cg", "jacobi") else "<"
-        assert (t <= tol) if stop == "<=" else (t < tol)
-    # solutions: both satisfy the same stopping test; the difference is
-    # bounded by the solver tolerance, not by rounding
-    assert rel_l2(x, d["x"]) <= max(1e-10, 50 * tol), rel_l2(x, d["x"])
+        assert (t <= tol) if k in ("cg", "jacobi") else (t < tol)
+        # the reported residual is the recursive one; the true residual of
+        # the returned x must agree with it
+        assert true_resid(A, x, b) <= 10 * tol
+        # BiCGSTAB's early exit on |s| (solver_matrix.hpp:642-647) leaves
+        # max_iter unchanged; which exit fires first is rounding-dependent
+        assert it == len(lr) - (1 if k == "dia_bicgstab" and it == max_iter else 0) \
+            or it == max_iter
+    assert rel_l2(x, d["x"]) <= 1e3 * tol, rel_l2(x, d["x"])
+
+
+@pytest.mark.parametrize("mtx,kind", [("csr_pde225_bicgstab", "bicgstab"),
+                                      ("csr_pde225_bicgstab", "dia_bicgstab"),
+                                      ("csr_pde225_bicgstab", "cg"),
+                                      ("csr_bus685_cg", "cg"),
+                                      ("csr_bus685_cg", "dia_bicgstab")])
+def test_csr_tight_tolerance_parity(gpu_lib, mtx, kind):
+    """Solved to 1e-13 both by the oracle (the reference's arithmetic,
+    bit-exact) and on the GPU: the solutions agree to the plain-path bar,
+    relative L2 <= 1e-10 (the 685_bus matrix, kappa ~ 4e5, to 1e-9)."""
+    from carpio_gb300 import algebra
+    d = golden(mtx)
+    if kind == "cg" and "pde225" in mtx:
+        pytest.skip("pde225 is not symmetric")
+    A = algebra.MatrixSCR(d["rowptr"], d["colind"], d["val"])
+    x = np.zeros(A.iLen())
+    code, it, t = algebra.krylov(kind, A, x, d["b"].copy(), 20000, 1e-13)
+    c2, x2, it2, t2, _ = R.krylov_csr(kind, A.rowptr, A.colind, A.val, d["b"],
+                                      np.zeros(A.iLen()), 20000, 1e-13)
+    assert code == c2 == 0
+    bar = 1e-9 if "bus685" in mtx else 1e-10
+    assert rel_l2(x, x2) <= bar, rel_l2(x, x2)
+
+
+def test_csr_early_exit_quirk(gpu_lib):
+    """On a diagonal matrix Dia_BiCGSTAB (M^-1 = 1/diag) finds s == 0 in the
+    first iteration and leaves through the early exit: max_iter stays as
+    passed and the residual is appended (solver_matrix.hpp:642-647).
+    BiCGSTAB's "M^-1" = diag (preconditioner.hpp:208-212) is no exact
+    inverse there, so it iterates; both match the oracle."""
+    from carpio_gb300 import algebra
+    n = 37
+    A = algebra.MatrixSCR(np.arange(n + 1), np.arange(n), np.linspace(1, 3, n))
+    b = np.linspace(-1, 1, n)
+    for solver, name in ((algebra.Dia_BiCGSTAB, "dia_bicgstab"),
+                         (algebra.BiCGSTAB, "bicgstab")):
+        x = np.zeros(n)
+        lr = []
+        code, it, t = solver(A, x, b.copy(), 50, 1e-12, lr)
+        c2, x2, it2, t2, h2 = R.krylov_csr(name, A.rowptr, A.colind, A.val, b,
+                                           np.zeros(n), 50, 1e-12)
+        assert code == c2 == 0
+        assert abs(len(lr) - len(h2)) <= 1
+        assert rel_l2(x, x2) < 1e-13
+        if name == "dia_bicgstab":
+            assert (it, len(lr)) == (it2, len(h2)) == (50, 1)
 
 
 def test_csr_zero_diagonal_is_an_error(gpu_lib):
