@@ -60,6 +60,9 @@ SIGNATURES = {
     "carpio_gpu_krylov_csr": (ctypes.c_int, [
         ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, _VP, _VP, _VP,
         _I, _D, _VP, ctypes.c_int, _I, ctypes.c_uint32]),
+    "carpio_gpu_krylov_csr_noalloc": (ctypes.c_int, [
+        ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, _VP, _VP, _VP,
+        _I, _D, _VP, ctypes.c_int, _I, ctypes.c_uint32, _VP]),
     "carpio_gpu_grid_create_uniform": (ctypes.c_int, [
         ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
         ctypes.c_double, ctypes.c_double, ctypes.c_double,

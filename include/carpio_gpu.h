@@ -82,6 +82,23 @@ int carpio_gpu_krylov_csr(int kind, int n, int nnz, const uint32_t* rowptr,
 		int* max_iter, double* tol, double* resid_hist, int hist_cap,
 		int* hist_len, uint32_t flags);
 
+/* The same solve for callers that cannot allocate device memory during a
+ * solve (a framework that owns all device memory through its own pool, or a
+ * time-stepping service that forbids cudaMalloc/cudaFree after start-up).
+ * No counterpart in the reference. All arrays must be device memory the
+ * caller owns; the solver's scratch is a fixed ~3 MiB array compiled into
+ * the library (held by every device that loads it) and n is limited to
+ * 32768 rows (larger n: CARPIO_GPU_EINVAL). The first call on a device sets
+ * up the array's address and should come before any stream capture. Calls
+ * share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller. `stream` is a cudaStream_t (NULL = default);
+ * the call returns when the solve has finished. */
+int carpio_gpu_krylov_csr_noalloc(int kind, int n, int nnz,
+		const uint32_t* rowptr, const uint32_t* col, const double* val,
+		const double* b, double* x, int* max_iter, double* tol,
+		double* resid_hist, int hist_cap, int* hist_len, uint32_t flags,
+		void* stream);
+
 /* ----- 2. structure level ------------------------------------------------ */
 typedef struct carpio_gpu_grid carpio_gpu_grid;
 
