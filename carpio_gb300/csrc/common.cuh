@@ -32,8 +32,8 @@ __device__ __forceinline__ unsigned long long globaltimer() {
 template<class T> __device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }
 
 struct GridCtl {
-	unsigned* count;          // arrivals at the current barrier
-	unsigned* gen;            // barrier generation
+	unsigned* count;          // barrier word (arrivals + release bit)
+	unsigned* gen;            // unused by the barrier; kept for layout
 	int* err;                 // first error code (0 = none)
 	double* partials;         // [2 banks][kMaxReduce][gridDim.x]
 	unsigned long long wait_ns;   // bound of one barrier wait
@@ -53,46 +53,59 @@ __device__ __forceinline__ void set_err(const GridCtl& c, int code) {
 
 // Returns false once any block has recorded an error (timeout included);
 // callers then leave the kernel. All threads of the block get the same answer.
+//
+// One counter word carries both arrival and release: every block adds 1,
+// block 0 adds 2^31 - (gridDim.x - 1), so the barrier's increments total
+// exactly 2^31 and the word's top bit flips when the last block arrives. A
+// block waits until the top bit differs from the value its own atomicAdd
+// returned. No reset is needed between barriers and the critical path is one
+// atomic plus one poll.
 __device__ __forceinline__ bool grid_sync(const GridCtl& c) {
 	__shared__ int s_ok;
 	__syncthreads();
 	if (threadIdx.x == 0) {
-		volatile unsigned* vgen = c.gen;
-		unsigned g = *vgen;
+		const unsigned inc = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1) : 1u;
 		__threadfence();
-		unsigned ticket = atomicAdd(c.count, 1u);
-		if (ticket == gridDim.x - 1) {
-			// the last arrival also enforces the solve deadline, so a launch
-			// whose blocks never wait (one block) is bounded as well
-			if (globaltimer() > c.deadline) set_err(c, CARPIO_GPU_ETIMEOUT);
-			atomicExch(c.count, 0u);
-			__threadfence();
-			atomicAdd(c.gen, 1u);
-		} else {
-			unsigned long long t0 = globaltimer();
-			while (*vgen == g) {
-				if (*(volatile int*)c.err) break;
+		const unsigned old = atomicAdd(c.count, inc);
+		volatile unsigned* vc = c.count;
+		unsigned long long t0 = 0;
+		unsigned polls = 0;
+		int ok = 1;
+		while (((*vc ^ old) & 0x80000000u) == 0) {
+			if ((++polls & 63u) == 0) {
+				// an error recorded by any block ends the wait; a block
+				// that gave up never arrives again, so the others see the
+				// error here within 64 polls
+				if (*(volatile int*)c.err) { ok = 0; break; }
 				unsigned long long t = globaltimer();
+				if (t0 == 0) t0 = t;
 				if (t - t0 > c.wait_ns || t > c.deadline) {
 					set_err(c, CARPIO_GPU_ETIMEOUT);
+					ok = 0;
 					break;
 				}
-				__nanosleep(32);
 			}
 		}
+		// the solve deadline also binds launches whose blocks never wait
+		if (ok && blockIdx.x == 0 && globaltimer() > c.deadline) {
+			set_err(c, CARPIO_GPU_ETIMEOUT);
+			ok = 0;
+		}
 		__threadfence();
-		s_ok = (read_err(c) == 0);
+		s_ok = ok;
 	}
 	__syncthreads();
 	return s_ok != 0;
 }
 
 // Sum of NV values over the block in a fixed tree; every thread gets it.
+// Any block size that is a multiple of 32, up to 1024.
 template<class R, int NV>
 __device__ __forceinline__ void block_sum(R (&v)[NV]) {
-	__shared__ R s_w[NV][kWarps];
+	__shared__ R s_w[NV][32];
 	__shared__ R s_out[NV];
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const int nwarps = blockDim.x >> 5;
 #pragma unroll
 	for (int m = 0; m < NV; ++m) {
 		R x = v[m];
@@ -104,7 +117,7 @@ __device__ __forceinline__ void block_sum(R (&v)[NV]) {
 	if (warp == 0) {
 #pragma unroll
 		for (int m = 0; m < NV; ++m) {
-			R x = lane < kWarps ? s_w[m][lane] : R(0);
+			R x = lane < nwarps ? s_w[m][lane] : R(0);
 #pragma unroll
 			for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
 			if (lane == 0) s_out[m] = x;
@@ -119,8 +132,9 @@ __device__ __forceinline__ void block_sum(R (&v)[NV]) {
 // Max of a non-negative value over the block (NaN never wins, matching
 // std::max(max, v) with max first).
 __device__ __forceinline__ double block_max(double v) {
-	__shared__ double s_w[kWarps];
+	__shared__ double s_w[32];
 	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const int nwarps = blockDim.x >> 5;
 #pragma unroll
 	for (int o = 16; o > 0; o >>= 1) {
 		double y = __shfl_down_sync(0xffffffffu, v, o);
@@ -129,7 +143,7 @@ __device__ __forceinline__ double block_max(double v) {
 	if (lane == 0) s_w[warp] = v;
 	__syncthreads();
 	if (warp == 0) {
-		v = lane < kWarps ? s_w[lane] : 0.0;
+		v = lane < nwarps ? s_w[lane] : 0.0;
 #pragma unroll
 		for (int o = 16; o > 0; o >>= 1) {
 			double y = __shfl_down_sync(0xffffffffu, v, o);
@@ -143,13 +157,39 @@ __device__ __forceinline__ double block_max(double v) {
 	return v;
 }
 
+// Block sum with one __syncthreads: warp trees, lane 0 of each warp writes
+// its value into buffer `buf`, then every thread adds the warp values in the
+// same fixed order. The caller guarantees that no thread still reads `buf`
+// from an earlier call (grid_allreduce alternates the buffers and a grid
+// barrier sits between two uses of the same one).
+template<class R, int NV>
+__device__ __forceinline__ void block_sum_light(R (&v)[NV], int buf) {
+	__shared__ R s_w[2][NV][32];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const int nwarps = blockDim.x >> 5;
+#pragma unroll
+	for (int m = 0; m < NV; ++m) {
+		R x = v[m];
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+		if (lane == 0) s_w[buf][m][warp] = x;
+	}
+	__syncthreads();
+#pragma unroll
+	for (int m = 0; m < NV; ++m) {
+		R x = 0;
+		for (int w = 0; w < nwarps; ++w) x += s_w[buf][m][w];
+		v[m] = x;
+	}
+}
+
 // Grid-wide sum of NV values (R = double or float). `bank` alternates 0/1 on
 // consecutive calls so a fast block never overwrites partials a slow block is
-// still reading. Returns false on error.
+// still reading. Every block ends with the same bits. Returns false on error.
 template<class R, int NV>
 __device__ __forceinline__ bool grid_allreduce(R (&v)[NV], const GridCtl& c,
 		int& bank) {
-	block_sum<R, NV>(v);
+	block_sum_light<R, NV>(v, 0);
 	double* part = c.partials + (size_t)bank * kMaxReduce * gridDim.x;
 	if (threadIdx.x == 0) {
 #pragma unroll
@@ -164,8 +204,16 @@ __device__ __forceinline__ bool grid_allreduce(R (&v)[NV], const GridCtl& c,
 			acc += (R)ldcg(&part[m * gridDim.x + b]);
 		v[m] = acc;
 	}
-	block_sum<R, NV>(v);
+	block_sum_light<R, NV>(v, 1);
 	return true;
 }
+
+// Scalars computed once per block by thread 0 and broadcast: FP64 division
+// and sqrt are long sequences on this GPU, not worth repeating per thread.
+struct Bcast {
+	double* s;   // shared scratch of at least 8 doubles
+	__device__ __forceinline__ bool lead() const { return threadIdx.x == 0; }
+	__device__ __forceinline__ void sync() const { __syncthreads(); }
+};
 
 }  // namespace cg_dev

@@ -24,9 +24,11 @@ struct CsrWs {
 	cg_host::DevBuf rp, ci, va, vec, hist;
 };
 
+// Never destroyed: freeing device memory from a static destructor can run
+// after the CUDA runtime has shut down at process exit.
 CsrWs& ws() {
-	static CsrWs w;
-	return w;
+	static CsrWs* w = new CsrWs();
+	return *w;
 }
 
 bool finite_all(const double* p, int n) {

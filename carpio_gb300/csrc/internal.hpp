@@ -5,6 +5,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -89,7 +90,7 @@ struct StencilCoeffs {
 
 struct PoissonWs {
 	LaunchWs lw;
-	DevBuf v64, v32, src, phi, hist, out;
+	DevBuf v64, v32, src, phi, hist, out, xbuf;
 };
 
 int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
@@ -122,5 +123,12 @@ struct carpio_gpu_grid {
 	std::mutex mu;
 	cg_host::StencilCoeffs coeffs;   // cache for carpio_gpu_poisson_solve
 	cg_host::PoissonWs pws;
+	// the caller's handle plus one per NS handle built on the grid; the grid
+	// is freed when the last of them is released
+	std::atomic<int> refs{ 1 };
 };
+
+namespace cg_host {
+void grid_release(carpio_gpu_grid* g);
+}
 

@@ -172,9 +172,13 @@ __device__ __forceinline__ bool norms2(const Sp& sp, const R* y, bool full,
 }
 
 // ------------------------------------------------------------------------ CG --
+// The scalar recurrences (divisions, sqrt, the stopping test) run in thread 0
+// of each block and reach the other threads through shared memory: every
+// block still derives them from the same all-reduced bits.
 template<class R, class Sp, class Op>
 __device__ void cg_run(const Sp& sp, const Op& op, const Vecs<R>& v,
 		const SolveCtl& sc, const GridCtl& gc, int& bank) {
+	__shared__ R s_sc[4];
 	const bool full = (sc.flags & CARPIO_GPU_FLAG_FULL_NRM2) || sp.count() == 1;
 	const int la = sp.last_addr();
 	int hl = 0;
@@ -188,17 +192,22 @@ __device__ void cg_run(const Sp& sp, const Op& op, const Vecs<R>& v,
 		if (a != la || full) { acc[0] = fma(bb, bb, acc[0]); acc[1] = fma(rr, rr, acc[1]); }
 	}
 	if (!grid_allreduce<R, 2>(acc, gc, bank)) return;
-	R rl = ldcg(v.r + la);
-	double normb = sqrt((double)acc[0]);
-	if (normb == 0.0) normb = 1;
-	double resid = sqrt((double)acc[1]) / normb;
-	if (resid <= sc.tol) { finish(sc, 0, 0, resid, hl); return; }
-	R rho = full ? acc[1] : acc[1] + rl * rl, rho_1 = 0;
+	double normb = 1, resid = 0;
+	if (threadIdx.x == 0) {
+		R rl = ldcg(v.r + la);
+		normb = sqrt((double)acc[0]);
+		if (normb == 0.0) normb = 1;
+		resid = sqrt((double)acc[1]) / normb;
+		s_sc[0] = resid <= sc.tol ? R(1) : R(0);
+		s_sc[1] = full ? acc[1] : acc[1] + rl * rl;   // rho = (r, r)
+	}
+	__syncthreads();
+	if (s_sc[0] != R(0)) { finish(sc, 0, 0, resid, hl); return; }
+	R rho = s_sc[1], beta = 0, alpha;
 	for (int it = 1; it <= sc.max_iter; ++it) {
 		if (it == 1) {
 			KLOOP(sp) { int a = sp.addr(k); v.p[a] = v.r[a]; }
 		} else {
-			R beta = rho / rho_1;
 			KLOOP(sp) { int a = sp.addr(k); v.p[a] = fma(beta, v.p[a], v.r[a]); }
 		}
 		if (!grid_sync(gc)) return;
@@ -210,7 +219,9 @@ __device__ void cg_run(const Sp& sp, const Op& op, const Vecs<R>& v,
 			pq[0] = fma(v.p[a], qq, pq[0]);
 		}
 		if (!grid_allreduce<R, 1>(pq, gc, bank)) return;
-		R alpha = rho / pq[0];
+		if (threadIdx.x == 0) s_sc[2] = rho / pq[0];
+		__syncthreads();
+		alpha = s_sc[2];
 		R rr[1] = { 0 };
 		KLOOP(sp) {
 			int a = sp.addr(k);
@@ -220,12 +231,19 @@ __device__ void cg_run(const Sp& sp, const Op& op, const Vecs<R>& v,
 			if (a != la || full) rr[0] = fma(r2, r2, rr[0]);
 		}
 		if (!grid_allreduce<R, 1>(rr, gc, bank)) return;
-		rl = ldcg(v.r + la);
-		resid = sqrt((double)rr[0]) / normb;
-		hist_push(sc, hl, resid);
-		if (resid <= sc.tol) { finish(sc, 0, it, resid, hl); return; }
-		rho_1 = rho;
-		rho = full ? rr[0] : rr[0] + rl * rl;
+		if (threadIdx.x == 0) {
+			R rl = ldcg(v.r + la);
+			resid = sqrt((double)rr[0]) / normb;
+			hist_push(sc, hl, resid);
+			R rho_new = full ? rr[0] : rr[0] + rl * rl;
+			s_sc[0] = resid <= sc.tol ? R(1) : R(0);
+			s_sc[1] = rho_new;
+			s_sc[3] = rho_new / rho;   // beta of the next iteration
+		}
+		__syncthreads();
+		if (s_sc[0] != R(0)) { finish(sc, 0, it, resid, hl); return; }
+		rho = s_sc[1];
+		beta = s_sc[3];
 	}
 	finish(sc, 1, sc.max_iter, resid, hl);
 }

@@ -556,11 +556,13 @@ int carpio_gpu_ns_create(carpio_gpu_grid* g, const carpio_gpu_ns_cfg* cfg,
 	*out = nullptr;
 	carpio_gpu_ns* ns = new carpio_gpu_ns();
 	ns->g = g;
+	g->refs.fetch_add(1);   // the grid outlives every NS handle built on it
 	ns->cfg = *cfg;
 	ns->s = g->stream;
 	const size_t NF = (size_t)g->NI * g->P;
 	if (ns->fields.ensure(sizeof(double) * NF * 10) || ns->scal.ensure(sizeof(StepScalars))) {
 		delete ns;
+		cg_host::grid_release(g);
 		return CARPIO_GPU_ENOMEM;
 	}
 	for (int k = 0; k < 10; ++k) ns->f[k] = ns->fields.as<double>() + k * NF;
@@ -572,6 +574,7 @@ int carpio_gpu_ns_create(carpio_gpu_grid* g, const carpio_gpu_ns_cfg* cfg,
 			|| cudaStreamSynchronize(ns->s) != cudaSuccess) {
 		note_cuda_error(cudaGetLastError());
 		delete ns;
+		cg_host::grid_release(g);
 		return CARPIO_GPU_ECUDA;
 	}
 	// Grid_::min_size (s_grid.hpp:173-185), cell sizes incl. ghosts
@@ -591,7 +594,9 @@ int carpio_gpu_ns_create(carpio_gpu_grid* g, const carpio_gpu_ns_cfg* cfg,
 int carpio_gpu_ns_destroy(carpio_gpu_ns* ns) {
 	if (!ns) return CARPIO_GPU_EINVAL;
 	cudaStreamSynchronize(ns->s);
+	carpio_gpu_grid* g = ns->g;
 	delete ns;
+	cg_host::grid_release(g);
 	return 0;
 }
 

@@ -213,6 +213,358 @@ __global__ void __launch_bounds__(kThreads) k_poisson(StencilOp<double> op,
 	KLOOP(sp) { int a = sp.addr(k); ra.phi[a] = ra.mean ? v.x[a] - mx0 : v.x[a]; }
 }
 
+// ------------------------------------------------ tile-resident FP32 CG --
+// The mixed solve with its Krylov state on chip: FP32 CG with reliable
+// updates. Whenever the FP32 residual has dropped by inner_tol since the last
+// update (or looks converged), the FP32 iterate is added into the FP64
+// solution, the true residual b - A x is recomputed in FP64 and replaces r,
+// and CG continues with its search direction (no restart). The stopping test
+// is always made on the FP64 residual. (Variants with one reduction per
+// iteration -- Chronopoulos-Gear, or |r - alpha q|^2 by recurrence -- lose
+// too much in FP32 at the condition numbers of these grids.)
+//
+// One CTA per SM owns a band of x-rows [r0, r1). Thread t owns the columns
+// t, t + T, ... (< ny) of every row of the band, so a cell's row and column
+// are loop indices and its x and q sit in registers; r and p live in shared
+// memory, p with one halo row above and below. p's halo rows are advanced
+// locally with the same FMA the neighbour band applies to the same inputs
+// (p = r + beta p with the neighbour's r), so the copies stay bit-identical;
+// the only data crossing CTAs per iteration is each band's first and last
+// row of r, published before the second reduction and read after it
+// (double-buffered by iteration parity).
+constexpr int kTileThreads = 512;
+
+struct TileArgs {
+	float* xbuf;           // [3][C][2][ny]: band edge rows of r (two iteration
+	                       // parities), then of r after a residual replacement
+	int rows_max;
+};
+
+__device__ __forceinline__ int band_lo(int c, int C, int nx) {
+	return (int)((long)c * nx / C);
+}
+
+struct TileOut {
+	int iters, updates, done;
+	double resid;
+};
+
+// NC columns per thread, RM rows per band at most.
+template<int NC, int RM>
+__device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
+		const Vecs<double>& v, const MixedArgs& m, const TileArgs& ta,
+		const SolveCtl& sc, bool mean, double normb, const GridCtl& gc,
+		int& bank, TileOut& to) {
+	extern __shared__ float smem[];
+	__shared__ double s_sc[4];
+	const int C = gridDim.x, c = blockIdx.x, T = blockDim.x, tid = threadIdx.x;
+	const int nx = sp.nx, ny = sp.ny, gl = sp.gl, P = sp.P;
+	const int r0 = band_lo(c, C, nx), r1 = band_lo(c + 1, C, nx);
+	const int rows = r1 - r0;
+	const int np = (ta.rows_max + 2) * ny + 2;
+	const bool full = (sc.flags & CARPIO_GPU_FLAG_FULL_NRM2) || sp.count() == 1;
+	const int la = sp.last_addr();
+	const double ncell = (double)sp.count();
+	float* p = smem;                // p[1 + (lr + 1) * ny + j], lr = -1 .. rows
+	float* rhal = p + np;           // halo rows of r: [0, ny) above, [ny, 2ny) below
+	float* rs = rhal + 2 * ny;      // the band's r, rs[lr * ny + j]
+	float* axs = rs + ta.rows_max * ny;   // x-face coefficients of faces r0 .. r1
+	float* ays = axs + ta.rows_max + 1;
+	float* dd = ays + ny + 1;       // the band's diagonal, dd[lr * ny + j]
+	const bool up = c > 0, down = c < C - 1;
+	const size_t edge = (size_t)2 * C * ny;   // one edge region
+	float* rbuf = ta.xbuf + 2 * edge;         // r edges
+	int par = 0;                              // q edges: xbuf + par * edge
+	for (int t = tid; t < np; t += T) p[t] = 0.f;
+	for (int t = tid; t < ny; t += T) { rhal[t] = 0.f; rhal[ny + t] = 0.f; }
+	for (int t = tid; t < rows * ny; t += T) {
+		const int lr = t / ny, j = t - lr * ny;
+		dd[t] = m.op32.D[(r0 + lr + gl) * P + j + gl];
+	}
+	for (int t = tid; t <= rows; t += T) axs[t] = m.op32.ax[r0 + t];
+	for (int t = tid; t <= ny; t += T) ays[t] = m.op32.ay[t];
+	float x[RM][NC], q[RM][NC];
+#pragma unroll
+	for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+		for (int k = 0; k < NC; ++k) x[lr][k] = q[lr][k] = 0.f;
+	__syncthreads();
+	// r (FP32) = (r64 - mean) * scale0 with scale0 fixed for the whole solve
+	double scale0 = 1.0, rn0 = 1.0;
+
+	auto publish_r = [&]() {
+		float* pub = rbuf + (size_t)(2 * c) * ny;
+#pragma unroll
+		for (int k = 0; k < NC; ++k) {
+			const int j = tid + k * T;
+			if (j < ny && rows > 0) {
+				pub[j] = rs[j];
+				pub[ny + j] = rs[(rows - 1) * ny + j];
+			}
+		}
+	};
+	// the neighbours' edge rows of region `src` into the halo rows of r.
+	// Thread t writes entries t and ny + t, the same mapping every reader of
+	// rhal uses, so no barrier is needed between the write and the reads.
+	auto read_rh = [&](const float* src) {
+		for (int t = tid; t < ny; t += T) {
+			if (up) rhal[t] = ldcg(src + (size_t)(2 * (c - 1) + 1) * ny + t);
+			if (down) rhal[ny + t] = ldcg(src + (size_t)(2 * (c + 1)) * ny + t);
+		}
+	};
+	// FP64 residual of the band (x64 complete on entry), into rs (FP32),
+	// edges exchanged; returns gamma = (r, r) of the new FP32 residual
+	auto true_residual = [&](bool first, float& gamma) -> bool {
+		double sums[3] = { 0, 0, 0 };
+		// the FP64 residual goes through v.r (each thread re-reads only
+		// its own cells) rather than registers
+#pragma unroll
+		for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+			for (int k = 0; k < NC; ++k) {
+				const int j = tid + k * T;
+				if (lr < rows && j < ny) {
+					const int kk = (r0 + lr) * ny + j;
+					const int a = (r0 + lr + gl) * P + j + gl;
+					const double rv = v.b[a] - op.apply(v.x, kk, a);
+					v.r[a] = rv;
+					if (a != la || full) sums[0] = fma(rv, rv, sums[0]);
+					sums[1] += rv;
+					sums[2] = fma(rv, rv, sums[2]);
+				}
+			}
+		if (!grid_allreduce<double, 3>(sums, gc, bank)) return false;
+		if (tid == 0) {
+			double mr = mean ? sums[1] / ncell : 0.0;
+			s_sc[0] = sqrt(sums[0]) / normb;
+			s_sc[1] = mr;
+			s_sc[2] = sqrt(mean ? fmax(sums[2] - sums[1] * mr, 0.0) : sums[2]);
+		}
+		__syncthreads();
+		to.resid = s_sc[0];
+		const double mr = s_sc[1];
+		if (first) {
+			rn0 = s_sc[2];
+			scale0 = rn0 > 0.0 ? 1.0 / rn0 : 1.0;
+		}
+		float g[1] = { 0.f };
+#pragma unroll
+		for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+			for (int k = 0; k < NC; ++k) {
+				const int j = tid + k * T;
+				if (lr < rows && j < ny) {
+					const int a = (r0 + lr + gl) * P + j + gl;
+					const float rv = (float)((v.r[a] - mr) * scale0);
+					rs[lr * ny + j] = rv;
+					g[0] = fmaf(rv, rv, g[0]);
+				}
+			}
+		publish_r();
+		if (!grid_allreduce<float, 1>(g, gc, bank)) return false;
+		read_rh(rbuf);
+		gamma = g[0];
+		return true;
+	};
+	// fold x (FP32, scaled) into x64 and clear it
+	auto fold_x = [&]() {
+#pragma unroll
+		for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+			for (int k = 0; k < NC; ++k) {
+				const int j = tid + k * T;
+				if (lr < rows && j < ny) {
+					const int a = (r0 + lr + gl) * P + j + gl;
+					v.x[a] = fma(rn0, (double)x[lr][k], v.x[a]);
+				}
+				x[lr][k] = 0.f;
+			}
+	};
+
+	to.iters = 0;
+	to.updates = 0;
+	to.done = 0;
+	float gamma = 0.f;
+	if (!true_residual(true, gamma)) return;
+	if (to.resid <= sc.tol) { to.done = 1; return; }
+	float gamma_ref = gamma, gamma_old = 1.f;
+	// an update when the FP32 residual has dropped by inner_tol, but at least
+	// every 1e-2 and every kStall iterations: FP32 CG cannot drive its
+	// recursive residual much further before it stops tracking the true one
+	const double it_tol = fmax(m.inner_tol, 1e-2);
+	const float drop = (float)(it_tol * it_tol);
+	constexpr int kStall = 1000;
+	int since = 0;
+	// iterated-residual level at which the FP64 residual is worth checking
+	const double tol_scaled = sc.tol * normb * scale0;
+	const float near = (float)(0.25 * tol_scaled * tol_scaled);
+	int it = 0;
+	bool first = true;
+	while (it < sc.max_iter && gamma > 0.f) {
+		const float beta = first ? 0.f : gamma / gamma_old;
+		first = false;
+		// p = r + beta p over the band and its halo rows
+#pragma unroll
+		for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+			for (int k = 0; k < NC; ++k) {
+				const int j = tid + k * T;
+				if (lr < rows && j < ny) {
+					const int pk = 1 + (lr + 1) * ny + j;
+					p[pk] = fmaf(beta, p[pk], rs[lr * ny + j]);
+				}
+			}
+		for (int t = tid; t < ny; t += T) {
+			if (up) p[1 + t] = fmaf(beta, p[1 + t], rhal[t]);
+			if (down) {
+				float* pp = p + 1 + (rows + 1) * ny + t;
+				*pp = fmaf(beta, *pp, rhal[ny + t]);
+			}
+		}
+		__syncthreads();
+		// q = A p, (p, q)
+		float pq[1] = { 0.f };
+#pragma unroll
+		for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+			for (int k = 0; k < NC; ++k) {
+				const int j = tid + k * T;
+				if (lr < rows && j < ny) {
+					const int pk = 1 + (lr + 1) * ny + j;
+					const float pc = p[pk];
+					float vv = dd[lr * ny + j] * pc;
+					vv = fmaf(axs[lr], p[pk - ny], vv);
+					vv = fmaf(axs[lr + 1], p[pk + ny], vv);
+					vv = fmaf(ays[j], p[pk - 1], vv);
+					vv = fmaf(ays[j + 1], p[pk + 1], vv);
+					q[lr][k] = vv;
+					pq[0] = fmaf(pc, vv, pq[0]);
+				}
+			}
+		if (!grid_allreduce<float, 1>(pq, gc, bank)) return;
+		const float alpha = gamma / pq[0];
+		// x += alpha p, r -= alpha q, (r, r); r's band edges published
+		float gn[1] = { 0.f };
+#pragma unroll
+		for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+			for (int k = 0; k < NC; ++k) {
+				const int j = tid + k * T;
+				if (lr < rows && j < ny) {
+					const int pk = 1 + (lr + 1) * ny + j;
+					x[lr][k] = fmaf(alpha, p[pk], x[lr][k]);
+					const float rv = fmaf(-alpha, q[lr][k], rs[lr * ny + j]);
+					rs[lr * ny + j] = rv;
+					gn[0] = fmaf(rv, rv, gn[0]);
+				}
+			}
+		float* ebuf = ta.xbuf + (size_t)par * edge;
+#pragma unroll
+		for (int k = 0; k < NC; ++k) {
+			const int j = tid + k * T;
+			if (j < ny && rows > 0) {
+				ebuf[(size_t)(2 * c) * ny + j] = rs[j];
+				ebuf[(size_t)(2 * c + 1) * ny + j] = rs[(rows - 1) * ny + j];
+			}
+		}
+		if (!grid_allreduce<float, 1>(gn, gc, bank)) return;
+		read_rh(ebuf);
+		par ^= 1;
+		++it;
+		++since;
+		float gnew = gn[0];
+		if (gnew < drop * gamma_ref || gnew <= near || since >= kStall) {
+			since = 0;
+			// reliable update: fold x, replace r by the FP64 residual
+			fold_x();
+			if (!grid_sync(gc)) return;
+			if (!true_residual(false, gnew)) return;
+			++to.updates;
+			if (to.resid <= sc.tol) { to.done = 1; break; }
+			gamma_ref = gnew;
+		}
+		gamma_old = gamma;
+		gamma = gnew;
+	}
+	to.iters = it;
+	if (!to.done) {
+		fold_x();
+		if (!grid_sync(gc)) return;
+	}
+}
+
+// mixed solve with the Krylov state on chip (tile_solve)
+template<int NC, int RM>
+__device__ void mixed_tile_run(const GridSpace& sp, const StencilOp<double>& op,
+		const Vecs<double>& v, const MixedArgs& m, const TileArgs& ta,
+		const SolveCtl& sc, bool mean, const GridCtl& gc, int& bank) {
+	const bool full = (sc.flags & CARPIO_GPU_FLAG_FULL_NRM2) || sp.count() == 1;
+	const int la = sp.last_addr();
+	__shared__ double s_nb;
+	double acc[1] = { 0 };
+	KLOOP(sp) {
+		int a = sp.addr(k);
+		double bb = v.b[a];
+		if (a != la || full) acc[0] = fma(bb, bb, acc[0]);
+	}
+	if (!grid_allreduce<double, 1>(acc, gc, bank)) return;
+	if (threadIdx.x == 0) {
+		double nb = sqrt(acc[0]);
+		s_nb = nb == 0.0 ? 1.0 : nb;
+	}
+	__syncthreads();
+	const double normb = s_nb;
+	TileOut to;
+	tile_solve<NC, RM>(sp, op, v, m, ta, sc, mean, normb, gc, bank, to);
+	if (read_err(gc)) return;
+	if (blockIdx.x == 0 && threadIdx.x == 0) {
+		sc.out->outer = to.updates;
+		sc.out->inner = to.iters;
+	}
+	finish(sc, to.done ? 0 : 1, to.iters, to.resid, to.updates + 1);
+}
+
+template<int SRC, int NC, int RM>
+__global__ void __launch_bounds__(kTileThreads, 1) k_poisson_mixed_tile(
+		StencilOp<double> op, Vecs<double> v, RhsArgs ra, MixedArgs mx,
+		TileArgs ta, SolveCtl sc, GridCtl gc) {
+	gc.start();
+	int bank = 0;
+	const GridSpace& sp = op.sp;
+	double s[1] = { 0 };
+	KLOOP(sp) {
+		int i, j;
+		sp.ij(k, i, j);
+		int a = sp.addr(k);
+		double bb = rhs_at<SRC>(sp, ra, i, j, a);
+		v.b[a] = bb;
+		v.x[a] = ra.phi[a];
+		s[0] += bb;
+	}
+	if (ra.mean) {
+		if (!grid_allreduce<double, 1>(s, gc, bank)) return;
+		double mm = s[0] / (double)sp.count();
+		KLOOP(sp) { int a = sp.addr(k); v.b[a] = v.b[a] - mm; }
+	}
+	if (!grid_sync(gc)) return;
+	mixed_tile_run<NC, RM>(sp, op, v, mx, ta, sc, ra.mean != 0, gc, bank);
+	if (read_err(gc)) {
+		if (blockIdx.x == 0 && threadIdx.x == 0) sc.out->code = read_err(gc);
+		return;
+	}
+	double mx0 = 0.0;
+	if (ra.mean) {
+		double t[1] = { 0 };
+		KLOOP(sp) { int a = sp.addr(k); t[0] += v.x[a]; }
+		if (!grid_allreduce<double, 1>(t, gc, bank)) {
+			if (blockIdx.x == 0 && threadIdx.x == 0) sc.out->code = read_err(gc);
+			return;
+		}
+		mx0 = t[0] / (double)sp.count();
+	}
+	KLOOP(sp) { int a = sp.addr(k); ra.phi[a] = ra.mean ? v.x[a] - mx0 : v.x[a]; }
+}
+
 template<int SRC>
 const void* pick_kernel(int kind, int precision) {
 	if (precision == CARPIO_GPU_MIXED) return (const void*)k_poisson<SRC, 4>;
@@ -230,6 +582,17 @@ bool same_bc(const carpio_gpu_bc& a, const carpio_gpu_bc& b) {
 }  // namespace
 
 namespace cg_host {
+
+void grid_release(carpio_gpu_grid* g) {
+	if (g->refs.fetch_sub(1) != 1) return;
+	if (g->stream) cudaStreamSynchronize(g->stream);
+	cudaFree(g->d_cx);
+	cudaFree(g->d_sx);
+	cudaFree(g->d_cy);
+	cudaFree(g->d_sy);
+	if (g->stream) cudaStreamDestroy(g->stream);
+	delete g;
+}
 
 int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
 		StencilCoeffs& c, cudaStream_t s) {
@@ -337,7 +700,9 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 	const void* kern = src_mode == SRC_DIV ? pick_kernel<SRC_DIV>(cfg.kind, cfg.precision)
 	                                       : pick_kernel<SRC_FIELD>(cfg.kind, cfg.precision);
 	long n = (long)g->nx * g->ny;
-	int blocks = coop_blocks(kern, n, 2);
+	// at most two 256-thread blocks per SM: enough warps for the FP64 pipe,
+	// few enough arrivals at each grid barrier
+	int blocks = std::min(coop_blocks(kern, n, 2), 2 * sm_count());
 	if ((rc = w.lw.ensure(blocks))) return rc;
 	StencilOp<double> op;
 	op.sp = GridSpace{ g->nx, g->ny, g->gl, g->P };
@@ -380,6 +745,41 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 	sc.hist = hist_dev;
 	sc.hist_cap = hist_dev ? hist_cap : 0;
 	sc.out = out_dev;
+	// mixed solves whose bands fit the tile kernel run on chip
+	if (mixed && !(cfg.flags & CARPIO_GPU_FLAG_NO_TILE)) {
+		const int C = std::min(sm_count(), g->nx);
+		const int rows_max = (g->nx + C - 1) / C;
+		const int nc = (g->ny + kTileThreads - 1) / kTileThreads;
+		const void* tk = nullptr;
+#define TILE_PICK(NC_, RM_)                                                         \
+		if (!tk && nc <= NC_ && rows_max <= RM_)                                    \
+			tk = src_mode == SRC_DIV ? (const void*)k_poisson_mixed_tile<SRC_DIV, NC_, RM_>      \
+			                         : (const void*)k_poisson_mixed_tile<SRC_FIELD, NC_, RM_>;
+		TILE_PICK(1, 4) TILE_PICK(1, 16) TILE_PICK(2, 8) TILE_PICK(4, 4)
+#undef TILE_PICK
+		const size_t smem = sizeof(float) * ((size_t)(rows_max + 2) * g->ny + 2
+				+ 2 * (size_t)g->ny + (size_t)rows_max * g->ny + rows_max + 1
+				+ g->ny + 1 + (size_t)rows_max * g->ny);
+		if (tk && smem <= 200 * 1024) {
+			CG_CK(cudaFuncSetAttribute(tk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+			int per_sm = 0;
+			CG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tk, kTileThreads, smem));
+			if (per_sm >= 1) {
+				if ((rc = w.lw.ensure(C))) return rc;
+				if ((rc = w.xbuf.ensure(sizeof(float) * 6 * (size_t)C * g->ny))) return rc;
+				TileArgs ta;
+				ta.xbuf = w.xbuf.as<float>();
+				ta.rows_max = rows_max;
+				mx.inner_tol = cfg.inner_tol > 0 ? cfg.inner_tol : 3e-2;
+				GridCtl gc = make_gridctl(w.lw);
+				CG_CK(cudaMemsetAsync(w.lw.ctl.p, 0, sizeof(Ctl), s));
+				CG_CK(cudaMemsetAsync(out_dev, 0, sizeof(cg_dev::SolveOut), s));
+				void* args[] = { &op, &v, &ra, &mx, &ta, &sc, &gc };
+				CG_CK(cudaLaunchCooperativeKernel(tk, C, kTileThreads, args, smem, s));
+				return 0;
+			}
+		}
+	}
 	GridCtl gc = make_gridctl(w.lw);
 	CG_CK(cudaMemsetAsync(w.lw.ctl.p, 0, sizeof(Ctl), s));
 	CG_CK(cudaMemsetAsync(out_dev, 0, sizeof(cg_dev::SolveOut), s));
@@ -455,13 +855,7 @@ int carpio_gpu_grid_create_uniform(int nx, int ny, int gl, double xmin,
 
 int carpio_gpu_grid_destroy(carpio_gpu_grid* g) {
 	if (!g) return CARPIO_GPU_EINVAL;
-	if (g->stream) cudaStreamSynchronize(g->stream);
-	cudaFree(g->d_cx);
-	cudaFree(g->d_sx);
-	cudaFree(g->d_cy);
-	cudaFree(g->d_sy);
-	if (g->stream) cudaStreamDestroy(g->stream);
-	delete g;
+	cg_host::grid_release(g);
 	return 0;
 }
 

@@ -5,6 +5,7 @@ Fields are numpy arrays (or CUDA tensors) of the reference's SpaceT shape
 (nx+2gl, ny+2gl), y contiguous, ghosts included.
 """
 import ctypes
+import sys
 
 import numpy as np
 
@@ -43,8 +44,10 @@ class Grid:
         return f[g:g + self.nx, g:g + self.ny]
 
     def __del__(self):
+        # no CUDA calls while the interpreter shuts down: the runtime may be
+        # gone already; the process exit releases the device memory
         h = getattr(self, "handle", None)
-        if h is not None and _lib._lib is not None:
+        if h is not None and _lib._lib is not None and not sys.is_finalizing():
             _lib._lib.carpio_gpu_grid_destroy(h)
             self.handle = None
 
@@ -283,7 +286,7 @@ class NS_explicit:
 
     def __del__(self):
         h = getattr(self, "handle", None)
-        if h is not None and _lib._lib is not None:
+        if h is not None and _lib._lib is not None and not sys.is_finalizing():
             _lib._lib.carpio_gpu_ns_destroy(h)
             self.handle = None
 

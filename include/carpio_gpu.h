@@ -56,6 +56,8 @@ extern "C" {
 /* flags (bitwise OR). 0 = the reference's exact semantics. */
 #define CARPIO_GPU_FLAG_FULL_NRM2 1u   /* use the full 2-norm instead of nrm2's
                                           drop-last-element (BLAS_Level1.hpp:569) */
+#define CARPIO_GPU_FLAG_NO_TILE 2u     /* MIXED: run the inner FP32 CG from global
+                                          memory instead of the on-chip tile kernel */
 
 /* ----- library ----------------------------------------------------------- */
 const char* carpio_gpu_version(void);
@@ -107,6 +109,8 @@ typedef struct carpio_gpu_grid carpio_gpu_grid;
  * same rounding. gl >= 1 (>= 2 for TVD advection). */
 int carpio_gpu_grid_create_uniform(int nx, int ny, int gl, double xmin,
 		double xmax, double ymin, double ymax, carpio_gpu_grid** out);
+/* Releases the caller's handle; the grid itself lives on while NS handles
+ * created on it exist. */
 int carpio_gpu_grid_destroy(carpio_gpu_grid* g);
 /* cell centres / sizes incl. ghosts: cx, sx [nx+2gl], cy, sy [ny+2gl] (host) */
 int carpio_gpu_grid_coords(const carpio_gpu_grid* g, double* cx, double* sx,
@@ -131,8 +135,10 @@ typedef struct {
 	int max_iter;      /* Solver_::set_max_iter */
 	double tol;        /* Solver_::set_tolerance (relative residual) */
 	int mean_removal;  /* remove the mean of b and x (all-Neumann null space) */
-	double inner_tol;  /* MIXED: relative residual reduction per inner solve */
-	int inner_max_iter;/* MIXED: cap on one inner solve */
+	double inner_tol;  /* MIXED: residual reduction between two FP64 residual
+	                      replacements (reliable updates; at most 1e-2 is used
+	                      on chip); 0 = 3e-2 */
+	int inner_max_iter;/* MIXED, global-memory path: cap on one inner solve */
 	uint32_t flags;    /* CARPIO_GPU_FLAG_* */
 } carpio_gpu_solver_cfg;
 

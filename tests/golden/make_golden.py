@@ -88,11 +88,15 @@ def main():
     ap.add_argument("--ref", default="/root/reference")
     ap.add_argument("--long", action="store_true")
     ap.add_argument("--long-dir", default=None)
+    ap.add_argument("--only-long", action="store_true",
+                    help="write only the 2000-step cavity fixtures")
     a = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref",
                     f"REF={a.ref}"], check=True)
+    if a.only_long:
+        a.long = True
     mtx = os.path.join(a.ref, "test", "input_files")
-    csr_cases = [
+    csr_cases = [] if a.only_long else [
         ("csr_bus685_cg", ["685_bus.mtx", "ones", "zeros", "cg", 10000, 1e-10]),
         ("csr_bus685_jacobi_class",
          ["685_bus.mtx", "ones", "ones", "jacobi_class", 100000, 1e-6]),
@@ -110,7 +114,7 @@ def main():
         args.append(c[1] if c[1] == "ones" else os.path.join(mtx, c[1]))
         args += c[2:]
         save(name, trim_hist(run(args, a.ref)))
-    poisson_cases = [
+    poisson_cases = [] if a.only_long else [
         ("poisson_c1_64_cg", ["c1", 64, "cg", 1000, 1e-10, 0]),
         ("poisson_c1_64_jacobi", ["c1", 64, "jacobi", 100000, 1e-10, 0]),
         ("poisson_c1_64_dia_bicgstab", ["c1", 64, "dia_bicgstab", 1000, 1e-10, 0]),
@@ -131,7 +135,7 @@ def main():
                 d.pop(k, None)
         save(name, d)
     # cavity: n steps scheme tol max_iter dt0 Re dump_every
-    cav = [
+    cav = [] if a.only_long else [
         ("cavity_32_vanleer_20", [32, 20, "VanLeer", 1e-10, 100000, 0.015625, 1000, 0]),
         ("cavity_16_superbee_10", [16, 10, "superbee", 1e-10, 100000, 0.03125, 1000, 0]),
         ("cavity_16_minmod_10", [16, 10, "minmod", 1e-10, 100000, 0.03125, 1000, 0]),
@@ -144,7 +148,8 @@ def main():
         if not name.startswith("cavity_32"):
             d = {k: v for k, v in d.items() if not k.startswith("s1_")}
         save(name, d)
-    for name, c in [("ops_13_gl2", [13, 5, 2]), ("ops_9_gl1", [9, 3, 1])]:
+    ops = [] if a.only_long else [("ops_13_gl2", [13, 5, 2]), ("ops_9_gl1", [9, 3, 1])]
+    for name, c in ops:
         save(name, run(["ops"] + c, a.ref))
     if a.long:
         for n, dt0 in [(128, 0.5 / 128), (256, 0.5 / 256)]:
