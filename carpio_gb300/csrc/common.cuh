@@ -183,29 +183,84 @@ __device__ __forceinline__ void block_sum_light(R (&v)[NV], int buf) {
 	}
 }
 
-// Grid-wide sum of NV values (R = double or float). `bank` alternates 0/1 on
-// consecutive calls so a fast block never overwrites partials a slow block is
-// still reading. Every block ends with the same bits. Returns false on error.
+__device__ __forceinline__ unsigned atom_add_release_gpu(unsigned* p, unsigned v) {
+	unsigned old;
+	asm volatile("atom.add.release.gpu.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+	return old;
+}
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+	unsigned v;
+	asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+
+// Grid-wide sum of NV values (R = double or float); every block ends with
+// the same bits. `bank` alternates 0/1 on consecutive calls so a fast block
+// never overwrites partials a slow block is still reading.
+//
+// One __syncthreads gathers the block's value; then warp 0 alone arrives at
+// the barrier (thread 0: release atomic on the flip-bit word, acquire polls
+// bounded by the watchdog), reads the blocks' partials in a fixed order and
+// reduces them; a second __syncthreads hands the result to the block. The
+// first __syncthreads also orders every thread's earlier global writes before
+// thread 0's release, so data published before the call is visible to every
+// block after it. Returns false on error.
 template<class R, int NV>
 __device__ __forceinline__ bool grid_allreduce(R (&v)[NV], const GridCtl& c,
 		int& bank) {
+	__shared__ R s_res[2][NV];
+	__shared__ int s_ok[2];
 	block_sum_light<R, NV>(v, 0);
 	double* part = c.partials + (size_t)bank * kMaxReduce * gridDim.x;
-	if (threadIdx.x == 0) {
+	const int lane = threadIdx.x & 31;
+	if (threadIdx.x < 32) {
+		int ok = 1;
+		if (lane == 0) {
 #pragma unroll
-		for (int m = 0; m < NV; ++m) part[m * gridDim.x + blockIdx.x] = (double)v[m];
+			for (int m = 0; m < NV; ++m) part[m * gridDim.x + blockIdx.x] = (double)v[m];
+			const unsigned inc = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1) : 1u;
+			const unsigned old = atom_add_release_gpu(c.count, inc);
+			unsigned long long t0 = 0;
+			unsigned polls = 0;
+			while (((ld_acquire_gpu(c.count) ^ old) & 0x80000000u) == 0) {
+				if ((++polls & 63u) == 0) {
+					if (*(volatile int*)c.err) { ok = 0; break; }
+					unsigned long long t = globaltimer();
+					if (t0 == 0) t0 = t;
+					if (t - t0 > c.wait_ns || t > c.deadline) {
+						set_err(c, CARPIO_GPU_ETIMEOUT);
+						ok = 0;
+						break;
+					}
+				}
+			}
+			if (ok && blockIdx.x == 0 && globaltimer() > c.deadline) {
+				set_err(c, CARPIO_GPU_ETIMEOUT);
+				ok = 0;
+			}
+		}
+		__syncwarp();
+		ok = __shfl_sync(0xffffffffu, ok, 0);
+		if (ok) {
+#pragma unroll
+			for (int m = 0; m < NV; ++m) {
+				R acc = 0;
+#pragma unroll 4
+				for (int b = lane; b < (int)gridDim.x; b += 32)
+					acc += (R)ldcg(&part[m * gridDim.x + b]);
+#pragma unroll
+				for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+				if (lane == 0) s_res[bank][m] = acc;
+			}
+		}
+		if (lane == 0) s_ok[bank] = ok;
 	}
+	__syncthreads();
+#pragma unroll
+	for (int m = 0; m < NV; ++m) v[m] = s_res[bank][m];
+	const bool ok = s_ok[bank] != 0;
 	bank ^= 1;
-	if (!grid_sync(c)) return false;
-#pragma unroll
-	for (int m = 0; m < NV; ++m) {
-		R acc = 0;
-		for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
-			acc += (R)ldcg(&part[m * gridDim.x + b]);
-		v[m] = acc;
-	}
-	block_sum_light<R, NV>(v, 1);
-	return true;
+	return ok;
 }
 
 // Scalars computed once per block by thread 0 and broadcast: FP64 division
