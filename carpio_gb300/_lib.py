@@ -46,6 +46,26 @@ class NSCfg(ctypes.Structure):
                 ("bc_u", BC), ("bc_v", BC), ("projection", SolverCfg)]
 
 
+class BatchProblem(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int),
+                ("xmin", ctypes.c_double), ("xmax", ctypes.c_double),
+                ("ymin", ctypes.c_double), ("ymax", ctypes.c_double),
+                ("bc", BC), ("mean_removal", ctypes.c_int),
+                ("beta", ctypes.c_double)]
+
+
+class BatchTiles(ctypes.Structure):
+    _fields_ = [("threads", ctypes.c_int), ("cluster", ctypes.c_int),
+                ("cells_per_cta", ctypes.c_int), ("use_graph", ctypes.c_int)]
+
+
+class BatchInfo(ctypes.Structure):
+    _fields_ = [("tiles", BatchTiles), ("clusters", ctypes.c_int),
+                ("ctas", ctypes.c_int), ("smem_bytes", ctypes.c_int),
+                ("teams", ctypes.c_int * 5), ("est_ms", ctypes.c_double),
+                ("candidates", ctypes.c_int), ("tuned_ms", ctypes.c_double)]
+
+
 _VP = ctypes.c_void_p
 _D = ctypes.POINTER(ctypes.c_double)
 _I = ctypes.POINTER(ctypes.c_int)
@@ -86,6 +106,24 @@ SIGNATURES = {
     "carpio_gpu_operator": (ctypes.c_int, [
         _VP, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.POINTER(BC),
         _VP, _VP, _VP, _VP, _VP, _D]),
+    "carpio_gpu_batch_create": (ctypes.c_int, [
+        ctypes.c_int, ctypes.POINTER(BatchProblem), ctypes.POINTER(SolverCfg),
+        ctypes.POINTER(BatchTiles), ctypes.POINTER(_VP)]),
+    "carpio_gpu_batch_destroy": (ctypes.c_int, [_VP]),
+    "carpio_gpu_batch_upload": (ctypes.c_int, [_VP, ctypes.c_int, _VP]),
+    "carpio_gpu_batch_download": (ctypes.c_int, [_VP, ctypes.c_int, _VP]),
+    "carpio_gpu_batch_field": (ctypes.c_int, [
+        _VP, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_VP)]),
+    "carpio_gpu_batch_zero": (ctypes.c_int, [_VP, ctypes.c_int]),
+    "carpio_gpu_batch_run": (ctypes.c_int, [
+        _VP, ctypes.POINTER(SolverStats), _D]),
+    "carpio_gpu_batch_autotune": (ctypes.c_int, [_VP, ctypes.c_int]),
+    "carpio_gpu_batch_get_info": (ctypes.c_int, [_VP, ctypes.POINTER(BatchInfo)]),
+    "carpio_gpu_batch_plan": (ctypes.c_int, [
+        ctypes.c_int, ctypes.POINTER(BatchProblem), ctypes.POINTER(BatchTiles),
+        ctypes.c_int, _I, _I, _D]),
+    "carpio_gpu_batch_shard": (ctypes.c_int, [
+        ctypes.c_int, ctypes.POINTER(BatchProblem), ctypes.c_int, _I]),
 }
 
 _lib = None

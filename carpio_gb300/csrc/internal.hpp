@@ -96,6 +96,18 @@ struct PoissonWs {
 int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
 		StencilCoeffs& c, cudaStream_t s);
 
+// Centres and sizes of the n + 2 gl cells of one uniform axis.
+void uniform_axis(int n, int gl, double lo, double hi, std::vector<double>& c,
+		std::vector<double>& s);
+
+// The coefficients above computed on the host from the axes (with ghosts):
+// D in a layout of nx + 2 gl rows of pitch P, ax[nx+1], ay[ny+1], fold.
+void stencil_host(int nx, int ny, int gl, int P, const std::vector<double>& cx,
+		const std::vector<double>& sx, const std::vector<double>& cy,
+		const std::vector<double>& sy, const carpio_gpu_bc& bc, double beta,
+		std::vector<double>& D, std::vector<double>& ax, std::vector<double>& ay,
+		std::vector<double>& fold);
+
 // Source of the right-hand side: a cell field, or the divergence of two face
 // fields (Operation_::Div(VecF), s_operation.hpp:100-120) as the NS projection
 // passes it.

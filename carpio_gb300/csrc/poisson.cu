@@ -8,6 +8,7 @@
 // carry the same bits as the CSR the reference assembles; only the Krylov
 // sums are ordered differently.
 #include "internal.hpp"
+#include "poisson_rhs.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -19,50 +20,12 @@ namespace {
 using namespace cg_dev;
 
 // ------------------------------------------------------------ device side --
-struct RhsArgs {
-	const double* sx;      // cell sizes incl. ghosts (device)
-	const double* sy;
-	const double* fold;    // [ny | ny | nx | nx]: x-, x+, y-, y+
-	const double* src_a;   // SRC_FIELD: source field; SRC_DIV: x-face field
-	const double* src_b;   // SRC_DIV: y-face field
-	double* phi;           // field: x0 in, solution out (normal cells)
-	int mean;
-};
-
 struct MixedArgs {
 	StencilOp<float> op32;
 	Vecs<float> f;         // e (x), r, p, q
 	double inner_tol;
 	int inner_max;
 };
-
-// Row constant of StencilPoisson_::coe_row + ghost folds, then b = -constant
-// (trimmed to +0 when the constant is exactly zero, s_solver.hpp:110-127).
-// Exact IEEE operations in the reference's order (no contraction).
-template<int SRC>
-__device__ __forceinline__ double rhs_at(const GridSpace& sp, const RhsArgs& ra,
-		int i, int j, int a) {
-	const int gl = sp.gl;
-	double sxi = ra.sx[i + gl];
-	double f;
-	if (SRC == cg_host::SRC_FIELD) {
-		f = ra.src_a[a];
-	} else {
-		// Operation_::Div(VecF) (s_operation.hpp:100-120)
-		double d = 0.0;
-		d = __dadd_rn(d, __ddiv_rn(__dsub_rn(ra.src_a[a], ra.src_a[a - sp.P]), sxi));
-		d = __dadd_rn(d, __ddiv_rn(__dsub_rn(ra.src_b[a], ra.src_b[a - 1]), ra.sy[j + gl]));
-		f = d;
-	}
-	double val = __dmul_rn(__dmul_rn(1.0, sxi), sxi);
-	val = __dmul_rn(val, f);
-	const int nx = sp.nx, ny = sp.ny;
-	if (i == 0) val = __dadd_rn(val, ra.fold[j]);
-	if (j == 0) val = __dadd_rn(val, ra.fold[2 * ny + i]);
-	if (j == ny - 1) val = __dadd_rn(val, ra.fold[2 * ny + nx + i]);
-	if (i == nx - 1) val = __dadd_rn(val, ra.fold[ny + j]);
-	return val == 0.0 ? 0.0 : -val;
-}
 
 // FP32 CG on A32 e = r32 from e = 0 (one inner solve of the refinement).
 // Returns the number of iterations, or -1 on a barrier error.
@@ -594,16 +557,37 @@ void grid_release(carpio_gpu_grid* g) {
 	delete g;
 }
 
-int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
-		StencilCoeffs& c, cudaStream_t s) {
-	if (c.valid && same_bc(c.bc, bc) && c.beta == beta) return 0;
-	const int nx = g->nx, ny = g->ny, gl = g->gl, P = g->P;
-	auto CX = [&](int i) { return g->cx[i + gl]; };
-	auto CY = [&](int j) { return g->cy[j + gl]; };
-	auto SX = [&](int i) { return g->sx[i + gl]; };
-	auto SY = [&](int j) { return g->sy[j + gl]; };
-	std::vector<double> D((size_t)g->NI * P, 0.0), ax(nx + 1, 0.0), ay(ny + 1, 0.0);
-	std::vector<double> fold(2 * (size_t)ny + 2 * (size_t)nx, 0.0);
+// Grid_::_set_uniform_grid (s_grid.hpp:372-395): centres and sizes of the
+// n + 2 gl cells of one axis, ghosts included
+void uniform_axis(int n, int gl, double lo, double hi, std::vector<double>& c,
+		std::vector<double>& s) {
+	int N = n + 2 * gl;
+	double ds = (hi - lo) / n;
+	s.assign(N, ds);
+	c.assign(N, 0.0);
+	double csum = 0.0, llg = 0.0;
+	for (int i = 0; i < N; ++i) {
+		c[i] = csum + 0.5 * s[i];
+		csum += s[i];
+	}
+	for (int i = 0; i < gl; ++i) llg += s[i];
+	double sh = lo - llg;
+	for (int i = 0; i < N; ++i) c[i] += sh;
+}
+
+void stencil_host(int nx, int ny, int gl, int P, const std::vector<double>& cx,
+		const std::vector<double>& sx, const std::vector<double>& cy,
+		const std::vector<double>& sy, const carpio_gpu_bc& bc, double beta,
+		std::vector<double>& D, std::vector<double>& ax, std::vector<double>& ay,
+		std::vector<double>& fold) {
+	auto CX = [&](int i) { return cx[i + gl]; };
+	auto CY = [&](int j) { return cy[j + gl]; };
+	auto SX = [&](int i) { return sx[i + gl]; };
+	auto SY = [&](int j) { return sy[j + gl]; };
+	D.assign((size_t)(nx + 2 * gl) * P, 0.0);
+	ax.assign(nx + 1, 0.0);
+	ay.assign(ny + 1, 0.0);
+	fold.assign(2 * (size_t)ny + 2 * (size_t)nx, 0.0);
 	// ghost substitution of one boundary face (Ghost_::_substitute_ghost,
 	// s_ghost.hpp:140-179): returns the centre increment, adds the constant
 	auto ghost = [&](int seg, int i, int j, double coe, double& dcen,
@@ -662,6 +646,14 @@ int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
 			if (i == 0 && j == ny - 1) ay[ny] = 0.0;
 		}
 	}
+}
+
+int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
+		StencilCoeffs& c, cudaStream_t s) {
+	if (c.valid && same_bc(c.bc, bc) && c.beta == beta) return 0;
+	std::vector<double> D, ax, ay, fold;
+	stencil_host(g->nx, g->ny, g->gl, g->P, g->cx, g->sx, g->cy, g->sy, bc, beta,
+			D, ax, ay, fold);
 	std::vector<float> D32(D.size()), ax32(ax.size()), ay32(ay.size());
 	for (size_t k = 0; k < D.size(); ++k) D32[k] = (float)D[k];
 	for (size_t k = 0; k < ax.size(); ++k) ax32[k] = (float)ax[k];
@@ -807,24 +799,8 @@ int carpio_gpu_grid_create_uniform(int nx, int ny, int gl, double xmin,
 	g->NI = nx + 2 * gl;
 	g->NJ = ny + 2 * gl;
 	g->P = (g->NJ + 31) / 32 * 32;
-	// Grid_::_set_uniform_grid (s_grid.hpp:372-395)
-	auto build = [](int n, int gl, double lo, double hi, std::vector<double>& c,
-			std::vector<double>& s) {
-		int N = n + 2 * gl;
-		double ds = (hi - lo) / n;
-		s.assign(N, ds);
-		c.assign(N, 0.0);
-		double csum = 0.0, llg = 0.0;
-		for (int i = 0; i < N; ++i) {
-			c[i] = csum + 0.5 * s[i];
-			csum += s[i];
-		}
-		for (int i = 0; i < gl; ++i) llg += s[i];
-		double sh = lo - llg;
-		for (int i = 0; i < N; ++i) c[i] += sh;
-	};
-	build(nx, gl, xmin, xmax, g->cx, g->sx);
-	build(ny, gl, ymin, ymax, g->cy, g->sy);
+	uniform_axis(nx, gl, xmin, xmax, g->cx, g->sx);
+	uniform_axis(ny, gl, ymin, ymax, g->cy, g->sy);
 	cudaGetDevice(&g->device);
 	int rc = 0;
 	auto fail = [&](int code) {

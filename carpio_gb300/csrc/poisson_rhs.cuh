@@ -1,0 +1,47 @@
+// Right-hand side of the structure-level Poisson solve, shared by the single
+// and the batched solvers.
+#pragma once
+
+#include "internal.hpp"
+
+namespace cg_dev {
+
+struct RhsArgs {
+	const double* sx;      // cell sizes incl. ghosts (device)
+	const double* sy;
+	const double* fold;    // [ny | ny | nx | nx]: x-, x+, y-, y+
+	const double* src_a;   // SRC_FIELD: source field; SRC_DIV: x-face field
+	const double* src_b;   // SRC_DIV: y-face field
+	double* phi;           // field: x0 in, solution out (normal cells)
+	int mean;
+};
+
+// Row constant of StencilPoisson_::coe_row + ghost folds, then b = -constant
+// (trimmed to +0 when the constant is exactly zero, s_solver.hpp:110-127).
+// Exact IEEE operations in the reference's order (no contraction).
+template<int SRC>
+__device__ __forceinline__ double rhs_at(const GridSpace& sp, const RhsArgs& ra,
+		int i, int j, int a) {
+	const int gl = sp.gl;
+	double sxi = ra.sx[i + gl];
+	double f;
+	if (SRC == cg_host::SRC_FIELD) {
+		f = ra.src_a[a];
+	} else {
+		// Operation_::Div(VecF) (s_operation.hpp:100-120)
+		double d = 0.0;
+		d = __dadd_rn(d, __ddiv_rn(__dsub_rn(ra.src_a[a], ra.src_a[a - sp.P]), sxi));
+		d = __dadd_rn(d, __ddiv_rn(__dsub_rn(ra.src_b[a], ra.src_b[a - 1]), ra.sy[j + gl]));
+		f = d;
+	}
+	double val = __dmul_rn(__dmul_rn(1.0, sxi), sxi);
+	val = __dmul_rn(val, f);
+	const int nx = sp.nx, ny = sp.ny;
+	if (i == 0) val = __dadd_rn(val, ra.fold[j]);
+	if (j == 0) val = __dadd_rn(val, ra.fold[2 * ny + i]);
+	if (j == ny - 1) val = __dadd_rn(val, ra.fold[2 * ny + nx + i]);
+	if (i == nx - 1) val = __dadd_rn(val, ra.fold[ny + j]);
+	return val == 0.0 ? 0.0 : -val;
+}
+
+}  // namespace cg_dev

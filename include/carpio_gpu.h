@@ -237,6 +237,88 @@ int carpio_gpu_operator(carpio_gpu_grid* g, int which, int scheme,
 		const double* b, const double* c, double* out1, double* out2,
 		double* scalar);
 
+/* ----- 3. batched Poisson solves -------------------------------------------
+ * No counterpart in the reference, which solves one Poisson_ at a time. Many
+ * independent Poisson_::run() solves on uniform grids of uneven sizes go into
+ * one persistent launch, replayed from a CUDA graph. Each problem is solved as
+ * carpio_gpu_poisson_solve solves one grid with the MIXED CG: FP32 inner
+ * iterations, FP64 residual, solution and mean removal, the same stopping
+ * test. The launch is made of thread-block clusters; a problem is owned by a
+ * team of 1..16 CTAs of one cluster (bands of x-rows), whose reductions and
+ * halo rows travel through distributed shared memory.
+ *
+ * The batch keeps its fields on the device in the layout of a grid with one
+ * ghost layer ((nx+2) x (ny+2) doubles, y contiguous, ghosts zero).
+ * carpio_gpu_batch_upload/download move plain interior arrays (nx*ny doubles,
+ * y contiguous; host or device memory) in and out of it. */
+typedef struct carpio_gpu_batch carpio_gpu_batch;
+
+typedef struct {
+	int nx, ny;                     /* cells */
+	double xmin, xmax, ymin, ymax;  /* the box (uniform Grid_) */
+	carpio_gpu_bc bc;               /* per segment, as for poisson_solve */
+	int mean_removal;               /* remove the means of b and x (all-Neumann) */
+	double beta;                    /* uniform beta (Poisson_::set_uniform_beta) */
+} carpio_gpu_batch_problem;
+
+/* Launch configuration ("tiles"); 0 in a field lets the library choose. */
+typedef struct {
+	int threads;        /* threads per CTA: 256 or 512 */
+	int cluster;        /* CTAs per cluster: 1, 2, 4, 8 or 16 */
+	int cells_per_cta;  /* target cells per CTA when sizing a problem's team */
+	int use_graph;      /* >= 0: replay a captured CUDA graph; < 0: plain launch */
+} carpio_gpu_batch_tiles;
+
+typedef struct {
+	carpio_gpu_batch_tiles tiles;  /* the configuration in use */
+	int clusters;       /* clusters launched (all resident) */
+	int ctas;           /* CTAs launched */
+	int smem_bytes;     /* dynamic shared memory per CTA */
+	int teams[5];       /* problems with team size 1, 2, 4, 8, 16 */
+	double est_ms;      /* the planner's makespan estimate */
+	int candidates;     /* configurations the autotuner timed (0: none) */
+	double tuned_ms;    /* the autotuner's time for the configuration in use */
+} carpio_gpu_batch_info;
+
+/* Plans the batch (teams, cluster slots, shared memory), uploads the
+ * coefficients and allocates the device fields (zero). cfg: kind CG,
+ * precision MIXED; tol, max_iter, inner_tol and flags apply to every problem.
+ * tiles may be NULL. Problems that fit no team are rejected (EINVAL). */
+int carpio_gpu_batch_create(int count, const carpio_gpu_batch_problem* probs,
+		const carpio_gpu_solver_cfg* cfg, const carpio_gpu_batch_tiles* tiles,
+		carpio_gpu_batch** out);
+int carpio_gpu_batch_destroy(carpio_gpu_batch* b);
+/* which: 0 source, 1 phi (initial guess in, solution out). fields[count]. */
+int carpio_gpu_batch_upload(carpio_gpu_batch* b, int which,
+		const double* const* fields);
+int carpio_gpu_batch_download(carpio_gpu_batch* b, int which,
+		double* const* fields);
+/* device address of problem i's field in the layout above */
+int carpio_gpu_batch_field(carpio_gpu_batch* b, int which, int i, double** dev);
+/* sets every problem's field `which` to zero (e.g. phi before a cold solve) */
+int carpio_gpu_batch_zero(carpio_gpu_batch* b, int which);
+/* Solves every problem on the device-resident fields. stats[count] may be
+ * NULL (per problem: code, inner iterations, residual, refinements, device
+ * ms); *ms (may be NULL) gets the device time of the whole launch. Returns 0
+ * when all converged, 1 if any reached max_iter, or a negative error. */
+int carpio_gpu_batch_run(carpio_gpu_batch* b, carpio_gpu_solver_stats* stats,
+		double* ms);
+/* Times up to max_candidates launch configurations on the fields now held
+ * (phi is restored after every trial) and keeps the fastest. */
+int carpio_gpu_batch_autotune(carpio_gpu_batch* b, int max_candidates);
+int carpio_gpu_batch_get_info(const carpio_gpu_batch* b,
+		carpio_gpu_batch_info* info);
+/* Host-only planning (no device call): the team size and cluster slot
+ * (cluster * 16 + slot) of every problem for the given tiles and number of
+ * clusters, and the estimated makespan. */
+int carpio_gpu_batch_plan(int count, const carpio_gpu_batch_problem* probs,
+		const carpio_gpu_batch_tiles* tiles, int clusters, int* team, int* slot,
+		double* est_ms);
+/* Host-only: split the problems across `world` processes by estimated work
+ * (largest first onto the least-loaded rank); rank_of[count]. */
+int carpio_gpu_batch_shard(int count, const carpio_gpu_batch_problem* probs,
+		int world, int* rank_of);
+
 #ifdef __cplusplus
 }
 #endif
