@@ -124,6 +124,10 @@ SIGNATURES = {
         ctypes.c_int, _I, _I, _D]),
     "carpio_gpu_batch_shard": (ctypes.c_int, [
         ctypes.c_int, ctypes.POINTER(BatchProblem), ctypes.c_int, _I]),
+    "carpio_gpu_nn_conv3x3": (ctypes.c_int, [
+        _VP, ctypes.c_int, _VP, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+        ctypes.c_int, _VP, ctypes.c_int, _VP, ctypes.c_int, _VP, _VP, _VP,
+        ctypes.c_int, _VP]),
 }
 
 _lib = None

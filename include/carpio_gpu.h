@@ -319,6 +319,23 @@ int carpio_gpu_batch_plan(int count, const carpio_gpu_batch_problem* probs,
 int carpio_gpu_batch_shard(int count, const carpio_gpu_batch_problem* probs,
 		int world, int* rank_of);
 
+/* ----- 4. learned preconditioner: tensor-core operators ---------------------
+ * No counterpart in the reference. One 3x3 convolution (stride 1, zero
+ * padding 1) of BF16 activations in NHWC layout ([n][h][w][c], c contiguous)
+ * with BF16 weights [9][cout][cin0 + cin1] (tap = 3 dy + dx), FP32
+ * accumulation on the tensor cores, BF16 output. in1 (may be NULL) is read
+ * as channels cin0.. of one concatenated input. Output channels [0, split)
+ * go to out0 (split channels per pixel), the rest to out1 (split = 0 means
+ * all to out0). relu: max(., 0); mask0/mask1 (may be NULL, layout of
+ * out0/out1): zero where the mask is not > 0. Device pointers only; channel
+ * counts multiples of 32, cout a multiple of 32 up to 256 or of 192/256
+ * above; n*h*w a multiple of 128 with 128-pixel tiles of whole rows or whole
+ * images. stream is a cudaStream_t (NULL = default); the call returns when
+ * the convolution has finished. */
+int carpio_gpu_nn_conv3x3(const void* in0, int cin0, const void* in1, int cin1,
+		int n, int h, int w, const void* wt, int cout, void* out0, int split,
+		void* out1, const void* mask0, const void* mask1, int relu, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
