@@ -124,6 +124,17 @@ SIGNATURES = {
         ctypes.c_int, _I, _I, _D]),
     "carpio_gpu_batch_shard": (ctypes.c_int, [
         ctypes.c_int, ctypes.POINTER(BatchProblem), ctypes.c_int, _I]),
+    "carpio_gpu_unet_num_params": (ctypes.c_long, []),
+    "carpio_gpu_unet_create": (ctypes.c_int, [ctypes.c_uint64, ctypes.POINTER(_VP)]),
+    "carpio_gpu_unet_destroy": (ctypes.c_int, [_VP]),
+    "carpio_gpu_unet_get_params": (ctypes.c_int, [_VP, _VP]),
+    "carpio_gpu_unet_set_params": (ctypes.c_int, [_VP, _VP]),
+    "carpio_gpu_unet_forward": (ctypes.c_int, [
+        _VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, _VP]),
+    "carpio_gpu_unet_grad": (ctypes.c_int, [
+        _VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, _VP, _D]),
+    "carpio_gpu_unet_train_step": (ctypes.c_int, [
+        _VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, ctypes.c_float, _D]),
     "carpio_gpu_nn_conv3x3": (ctypes.c_int, [
         _VP, ctypes.c_int, _VP, ctypes.c_int, ctypes.c_int, ctypes.c_int,
         ctypes.c_int, _VP, ctypes.c_int, _VP, ctypes.c_int, _VP, _VP, _VP,

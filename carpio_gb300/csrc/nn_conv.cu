@@ -332,6 +332,27 @@ int conv_launch(const ConvLaunch& L, cudaStream_t s) {
 	return 0;
 }
 
+// heap-held launches for the U-Net runner (nn.cu)
+int conv_prepare_ext(void** handle, const void* in0, int cin0, const void* in1, int cin1,
+		int n, int h, int w, const void* wt, int cout, int ntile, void* out0, int split,
+		void* out1, const void* mask0, const void* mask1, int relu, int* err) {
+	auto* L = new ConvLaunch();
+	int rc = conv_prepare(*L, in0, cin0, in1, cin1, n, h, w, wt, cout, ntile, out0, split,
+			out1, mask0, mask1, relu, err);
+	if (rc) {
+		delete L;
+		return rc;
+	}
+	*handle = L;
+	return 0;
+}
+
+int conv_launch_ext(const void* handle, cudaStream_t s) {
+	return conv_launch(*static_cast<const ConvLaunch*>(handle), s);
+}
+
+void conv_free_ext(void* handle) { delete static_cast<ConvLaunch*>(handle); }
+
 }  // namespace cg_host
 
 extern "C" int carpio_gpu_nn_conv3x3(const void* in0, int cin0, const void* in1, int cin1,

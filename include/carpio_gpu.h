@@ -336,6 +336,32 @@ int carpio_gpu_nn_conv3x3(const void* in0, int cin0, const void* in1, int cin1,
 		int n, int h, int w, const void* wt, int cout, void* out0, int split,
 		void* out1, const void* mask0, const void* mask1, int relu, void* stream);
 
+/* The learned preconditioner: a 4-level BF16 U-Net (32/64/128/256 channels,
+ * 3x3 convolutions, ReLU, average pooling, nearest upsampling, concatenating
+ * skips, no biases; carpio_gpu_unet_num_params() FP32 parameters) mapping a
+ * field x [n][h][w] (FP32) to z [n][h][w] (FP32); h, w multiples of 8 and at
+ * least 16. The convolutions run on the tensor cores; training is Adam on
+ * FP32 master weights with the relative squared error
+ * sum (z - t)^2 / sum t^2 as the loss. Field pointers are device memory. */
+typedef struct carpio_gpu_unet carpio_gpu_unet;
+long carpio_gpu_unet_num_params(void);
+/* deterministic He-normal initial weights from `seed` */
+int carpio_gpu_unet_create(uint64_t seed, carpio_gpu_unet** out);
+int carpio_gpu_unet_destroy(carpio_gpu_unet* u);
+/* all parameters as one FP32 vector (host or device memory): the input
+ * layer [9][32], the 13 3x3 layers [9][cout][cin] in network order, the
+ * output layer [32]; set also resets the optimiser state */
+int carpio_gpu_unet_get_params(carpio_gpu_unet* u, float* out);
+int carpio_gpu_unet_set_params(carpio_gpu_unet* u, const float* in);
+int carpio_gpu_unet_forward(carpio_gpu_unet* u, int n, int h, int w, const float* x,
+		float* z, void* stream);
+/* loss and gradient (FP32, layout of the parameters; host or device) */
+int carpio_gpu_unet_grad(carpio_gpu_unet* u, int n, int h, int w, const float* x,
+		const float* t, float* grad, double* loss);
+/* one Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on the batch */
+int carpio_gpu_unet_train_step(carpio_gpu_unet* u, int n, int h, int w, const float* x,
+		const float* t, float lr, double* loss);
+
 #ifdef __cplusplus
 }
 #endif
