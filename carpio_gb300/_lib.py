@@ -46,6 +46,12 @@ class NSCfg(ctypes.Structure):
                 ("bc_u", BC), ("bc_v", BC), ("projection", SolverCfg)]
 
 
+class LearnedCfg(ctypes.Structure):
+    _fields_ = [("use_net", ctypes.c_int), ("smooth", ctypes.c_int),
+                ("omega", ctypes.c_double), ("memory", ctypes.c_int),
+                ("stall", ctypes.c_int), ("fallback", ctypes.c_int)]
+
+
 class BatchProblem(ctypes.Structure):
     _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int),
                 ("xmin", ctypes.c_double), ("xmax", ctypes.c_double),
@@ -132,9 +138,15 @@ SIGNATURES = {
     "carpio_gpu_unet_forward": (ctypes.c_int, [
         _VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, _VP]),
     "carpio_gpu_unet_grad": (ctypes.c_int, [
-        _VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, _VP, _D]),
+        _VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, ctypes.c_int, _VP, _D]),
     "carpio_gpu_unet_train_step": (ctypes.c_int, [
-        _VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, ctypes.c_float, _D]),
+        _VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, ctypes.c_int,
+        ctypes.c_float, _D]),
+    "carpio_gpu_poisson_solve_learned": (ctypes.c_int, [
+        _VP, ctypes.POINTER(BC), ctypes.c_double, _VP, _VP,
+        ctypes.POINTER(SolverCfg), _VP, ctypes.POINTER(LearnedCfg), _VP, ctypes.c_int,
+        ctypes.POINTER(SolverStats)]),
+    "carpio_gpu_ns_set_learned": (ctypes.c_int, [_VP, _VP, ctypes.POINTER(LearnedCfg)]),
     "carpio_gpu_nn_conv3x3": (ctypes.c_int, [
         _VP, ctypes.c_int, _VP, ctypes.c_int, ctypes.c_int, ctypes.c_int,
         ctypes.c_int, _VP, ctypes.c_int, _VP, ctypes.c_int, _VP, _VP, _VP,

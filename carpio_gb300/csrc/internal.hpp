@@ -108,6 +108,13 @@ void stencil_host(int nx, int ny, int gl, int P, const std::vector<double>& cx,
 		std::vector<double>& D, std::vector<double>& ax, std::vector<double>& ay,
 		std::vector<double>& fold);
 
+// Workspace of the learned-preconditioner solve (learned.cu).
+struct LearnedWs {
+	DevBuf f64, f32, part, sc;
+	std::vector<double> hpart;
+	int nblk = 0;
+};
+
 // Source of the right-hand side: a cell field, or the divergence of two face
 // fields (Operation_::Div(VecF), s_operation.hpp:100-120) as the NS projection
 // passes it.
@@ -120,6 +127,16 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 		int src_mode, const double* src_a, const double* src_b, double* phi,
 		const carpio_gpu_solver_cfg& cfg, double* hist_dev, int hist_cap,
 		cg_dev::SolveOut* out_dev, cudaStream_t s);
+
+// FCG with the U-Net preconditioner (learned.cu): b from the source, x0 from
+// phi, the solve, x (mean removed) back into phi; a stall finishes with the
+// plain MIXED CG. All pointers are device pointers.
+bool learned_shape_ok(int nx, int ny);
+int learned_solve(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& pws, LearnedWs& w,
+		int src_mode, const double* src_a, const double* src_b, double* phi,
+		const carpio_gpu_solver_cfg& cfg, carpio_gpu_unet* net,
+		const carpio_gpu_learned_cfg& lc, cg_dev::SolveOut& out, cudaStream_t s,
+		std::vector<double>* hist = nullptr);
 
 }  // namespace cg_host
 
@@ -135,6 +152,7 @@ struct carpio_gpu_grid {
 	std::mutex mu;
 	cg_host::StencilCoeffs coeffs;   // cache for carpio_gpu_poisson_solve
 	cg_host::PoissonWs pws;
+	cg_host::LearnedWs lws;
 	// the caller's handle plus one per NS handle built on the grid; the grid
 	// is freed when the last of them is released
 	std::atomic<int> refs{ 1 };

@@ -365,6 +365,59 @@ __global__ void k_loss_parts(const float* __restrict__ z, const float* __restric
 	}
 }
 
+// (A f)[i][j] over one image: the all-Neumann 5-point operator with unit
+// face coefficients (sum over the existing neighbours of f - f_nb)
+__device__ __forceinline__ float neumann_apply(const float* __restrict__ f, long px, int h,
+		int wd) {
+	const int xx = (int)(px % wd), yy = (int)((px / wd) % h);
+	const float c = f[px];
+	float a = 0.f;
+	if (xx > 0) a += c - f[px - 1];
+	if (xx < wd - 1) a += c - f[px + 1];
+	if (yy > 0) a += c - f[px - wd];
+	if (yy < h - 1) a += c - f[px + wd];
+	return a;
+}
+
+// energy-norm loss parts: (e, A e) with e = z - t (e kept in `e`), (t, A t)
+__global__ void k_energy_parts(const float* __restrict__ e, const float* __restrict__ t,
+		int n, int h, int wd, double* __restrict__ part) {
+	__shared__ double s[2][kT];
+	const long npx = (long)n * h * wd;
+	double a = 0, b = 0;
+	for (long i = (long)blockIdx.x * kT + threadIdx.x; i < npx; i += (long)gridDim.x * kT) {
+		a += (double)e[i] * (double)neumann_apply(e, i, h, wd);
+		b += (double)t[i] * (double)neumann_apply(t, i, h, wd);
+	}
+	s[0][threadIdx.x] = a;
+	s[1][threadIdx.x] = b;
+	__syncthreads();
+	for (int o = kT / 2; o > 0; o >>= 1) {
+		if (threadIdx.x < o) {
+			s[0][threadIdx.x] += s[0][threadIdx.x + o];
+			s[1][threadIdx.x] += s[1][threadIdx.x + o];
+		}
+		__syncthreads();
+	}
+	if (threadIdx.x == 0) {
+		part[2 * blockIdx.x] = s[0][0];
+		part[2 * blockIdx.x + 1] = s[1][0];
+	}
+}
+
+__global__ void k_sub(const float* __restrict__ z, const float* __restrict__ t, long npx,
+		float* __restrict__ e) {
+	const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < npx) e[i] = z[i] - t[i];
+}
+
+// dz = scale * A e
+__global__ void k_dz_energy(const float* __restrict__ e, const float* __restrict__ scale,
+		int n, int h, int wd, float* __restrict__ dz) {
+	const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+	if (i < (long)n * h * wd) dz[i] = neumann_apply(e, i, h, wd) * *scale;
+}
+
 // loss = sum e / sum q, and the gradient scale 2 / sum q
 __global__ void k_loss_final(const double* __restrict__ part, int nb, double* __restrict__ loss,
 		float* __restrict__ scale) {
@@ -667,18 +720,27 @@ int dw_layer(carpio_gpu_unet* u, Shape& S, int layer, int lvl, const bf16* g,
 }
 
 // forward, loss, backward: gradient in u->g, loss in u->loss
-int grad(carpio_gpu_unet* u, Shape& S, const float* x, const float* t, cudaStream_t st) {
+int grad(carpio_gpu_unet* u, Shape& S, const float* x, const float* t, int loss_mode,
+		cudaStream_t st) {
 	const int n = S.n, h = S.h, w = S.w;
 	const int CH[4] = { C0, C1, C2, C3 };
 	const long np0 = (long)n * h * w;
 	float* z = S.z.as<float>();
 	NN_CK(forward(u, S, x, z, st));
 	const int nbl = 1024;
-	k_loss_parts<<<nbl, kT, 0, st>>>(z, t, np0, S.lpart.as<double>());
-	k_loss_final<<<1, 1, 0, st>>>(S.lpart.as<double>(), nbl, u->loss.as<double>(),
-			reinterpret_cast<float*>(S.lpart.as<double>() + 2 * nbl));
-	k_dz<<<nblk(np0), kT, 0, st>>>(z, t, reinterpret_cast<const float*>(S.lpart.as<double>() + 2 * nbl),
-			np0, S.dz.as<float>());
+	float* scale = reinterpret_cast<float*>(S.lpart.as<double>() + 2 * nbl);
+	if (loss_mode == 1) {
+		// energy norm: (e, A e) / (t, A t), dz = 2 A e / (t, A t)
+		float* e = S.gD[0].as<float>();   // scratch: gD[0] is written later
+		k_sub<<<nblk(np0), kT, 0, st>>>(z, t, np0, e);
+		k_energy_parts<<<nbl, kT, 0, st>>>(e, t, n, h, w, S.lpart.as<double>());
+		k_loss_final<<<1, 1, 0, st>>>(S.lpart.as<double>(), nbl, u->loss.as<double>(), scale);
+		k_dz_energy<<<nblk(np0), kT, 0, st>>>(e, scale, n, h, w, S.dz.as<float>());
+	} else {
+		k_loss_parts<<<nbl, kT, 0, st>>>(z, t, np0, S.lpart.as<double>());
+		k_loss_final<<<1, 1, 0, st>>>(S.lpart.as<double>(), nbl, u->loss.as<double>(), scale);
+		k_dz<<<nblk(np0), kT, 0, st>>>(z, t, scale, np0, S.dz.as<float>());
+	}
 	const float* W = u->w.as<float>();
 	float* G = u->g.as<float>();
 	// output layer
@@ -880,14 +942,15 @@ int carpio_gpu_unet_forward(carpio_gpu_unet* u, int n, int h, int w, const float
 }
 
 int carpio_gpu_unet_grad(carpio_gpu_unet* u, int n, int h, int w, const float* x,
-		const float* t, float* grad_out, double* loss) {
-	if (!u || !x || !t || !shape_ok(n, h, w)) return CARPIO_GPU_EINVAL;
+		const float* t, int loss_mode, float* grad_out, double* loss) {
+	if (!u || !x || !t || !shape_ok(n, h, w) || loss_mode < 0 || loss_mode > 1)
+		return CARPIO_GPU_EINVAL;
 	if (!cg_host::is_device_ptr(x) || !cg_host::is_device_ptr(t)) return CARPIO_GPU_EINVAL;
 	std::lock_guard<std::mutex> lk(u->mu);
 	int rc = 0;
 	Shape* S = get_shape(u, n, h, w, &rc);
 	if (!S) return rc;
-	if ((rc = grad(u, *S, x, t, u->s))) return rc;
+	if ((rc = grad(u, *S, x, t, loss_mode, u->s))) return rc;
 	if (grad_out)
 		CG_CK(cudaMemcpyAsync(grad_out, u->g.p, sizeof(float) * n_params(), cudaMemcpyDefault, u->s));
 	if (loss) CG_CK(cudaMemcpyAsync(loss, u->loss.p, sizeof(double), cudaMemcpyDefault, u->s));
@@ -896,15 +959,16 @@ int carpio_gpu_unet_grad(carpio_gpu_unet* u, int n, int h, int w, const float* x
 }
 
 int carpio_gpu_unet_train_step(carpio_gpu_unet* u, int n, int h, int w, const float* x,
-		const float* t, float lr, double* loss) {
-	if (!u || !x || !t || !shape_ok(n, h, w) || !(lr >= 0)) return CARPIO_GPU_EINVAL;
+		const float* t, int loss_mode, float lr, double* loss) {
+	if (!u || !x || !t || !shape_ok(n, h, w) || !(lr >= 0) || loss_mode < 0 || loss_mode > 1)
+		return CARPIO_GPU_EINVAL;
 	if (!cg_host::is_device_ptr(x) || !cg_host::is_device_ptr(t)) return CARPIO_GPU_EINVAL;
 	std::lock_guard<std::mutex> lk(u->mu);
 	int rc = 0;
 	Shape* S = get_shape(u, n, h, w, &rc);
 	if (!S) return rc;
 	cudaStream_t st = u->s;
-	if ((rc = grad(u, *S, x, t, st))) return rc;
+	if ((rc = grad(u, *S, x, t, loss_mode, st))) return rc;
 	++u->step;
 	const float b1 = 0.9f, b2 = 0.999f;
 	const float c1 = 1.f - std::pow(b1, (float)u->step), c2 = 1.f - std::pow(b2, (float)u->step);

@@ -539,6 +539,11 @@ struct carpio_gpu_ns {
 	std::vector<cudaEvent_t> ev;
 	std::vector<cg_dev::SolveOut> last_rec;
 	int last_steps = 0;
+	// the projection with the learned preconditioner (carpio_gpu_ns_set_learned)
+	carpio_gpu_unet* net = nullptr;
+	carpio_gpu_learned_cfg lcfg{};
+	bool learned = false;
+	cg_host::LearnedWs lws;
 	~carpio_gpu_ns() {
 		for (cudaEvent_t e : ev) cudaEventDestroy(e);
 	}
@@ -679,9 +684,16 @@ int carpio_gpu_ns_run(carpio_gpu_ns* ns, int steps, double* step_dt,
 		k_c2f<<<nb, kThreads, 0, s>>>(geo, us, vs, usf, vsf);
 		CG_CK(cudaGetLastError());
 		CG_CK(cudaEventRecord(ns->ev[3 * st + 1], s));
-		if ((rc = poisson_launch(g, ns->coeffs, ns->pws, SRC_DIV, usf, vsf, phi,
-				c.projection, nullptr, 0, rec + st, s)))
+		if (ns->learned) {
+			cg_dev::SolveOut o;
+			if ((rc = learned_solve(g, ns->coeffs, ns->pws, ns->lws, SRC_DIV, usf, vsf, phi,
+					c.projection, ns->net, ns->lcfg, o, s)))
+				return rc;
+			CG_CK(cudaMemcpyAsync(rec + st, &o, sizeof o, cudaMemcpyHostToDevice, s));
+		} else if ((rc = poisson_launch(g, ns->coeffs, ns->pws, SRC_DIV, usf, vsf, phi,
+				c.projection, nullptr, 0, rec + st, s))) {
 			return rc;
+		}
 		CG_CK(cudaEventRecord(ns->ev[3 * st + 2], s));
 		CG_CK(launch_bc(geo, phi, bc_phi, nullptr, nullptr, s));
 		k_correct<<<nbf, kThreads, 0, s>>>(geo, phi, us, vs, usf, vsf, u, v, uf,
@@ -707,6 +719,23 @@ int carpio_gpu_ns_run(carpio_gpu_ns* ns, int steps, double* step_dt,
 	ns->last_rec = h;
 	ns->last_steps = steps;
 	return first;
+}
+
+int carpio_gpu_ns_set_learned(carpio_gpu_ns* ns, carpio_gpu_unet* net,
+		const carpio_gpu_learned_cfg* lc) {
+	using namespace cg_host;
+	if (!ns) return CARPIO_GPU_EINVAL;
+	if (!net && (!lc || lc->use_net)) {
+		ns->learned = false;
+		ns->net = nullptr;
+		return 0;
+	}
+	if (!lc || (lc->use_net && (!net || !learned_shape_ok(ns->g->nx, ns->g->ny))))
+		return CARPIO_GPU_EINVAL;
+	ns->net = net;
+	ns->lcfg = *lc;
+	ns->learned = true;
+	return 0;
 }
 
 int carpio_gpu_ns_profile(carpio_gpu_ns* ns, int cap, int* n,

@@ -101,6 +101,13 @@ def solver_cfg(name="CG", max_iter=1000, tol=1e-3, mean_removal=False,
     return c
 
 
+def learned_cfg(use_net=True, smooth=4, omega=0.8, memory=2, stall=20, fallback=True):
+    c = _lib.LearnedCfg()
+    c.use_net, c.smooth, c.omega = int(bool(use_net)), int(smooth), float(omega)
+    c.memory, c.stall, c.fallback = int(memory), int(stall), int(bool(fallback))
+    return c
+
+
 class Poisson:
     """Poisson_<2> (s_poisson.hpp:265-594) with the GPU solver behind
     Solver_<2>::solve. set_solver accepts "CG", "Jacobi", "Dia_BiCGSTAB",
@@ -139,6 +146,13 @@ class Poisson:
     def set_solver(self, name, any_=None, max_iter=1000, tol=1e-3, **kw):
         self.cfg = solver_cfg(name, max_iter, tol, **kw)
 
+    def set_learned(self, net, use_net=True, smooth=4, omega=0.8, memory=2,
+                    stall=20, fallback=True):
+        """solve with flexible CG preconditioned by the U-Net `net`
+        (carpio_gb300.unet.UNet; None: back to the plain solver)"""
+        self.learned = None if net is None and use_net else (
+            net, learned_cfg(use_net, smooth, omega, memory, stall, fallback))
+
     def run(self):
         L = _lib.load()
         if self.phi is None:
@@ -146,6 +160,19 @@ class Poisson:
         if self.source is None:
             self.source = self.grid.zeros()
         bc = self._bi.to_c("phi")
+        if getattr(self, "learned", None) is not None:
+            net, lc = self.learned
+            cap = self.cfg.max_iter + 2
+            hist = np.zeros(max(cap, 1))
+            rc = L.carpio_gpu_poisson_solve_learned(
+                self.grid.handle, ctypes.byref(bc), self.beta, _lib.ptr(self.source),
+                _lib.ptr(self.phi), ctypes.byref(self.cfg),
+                net.handle if net is not None else None, ctypes.byref(lc),
+                _lib.ptr(hist), cap, ctypes.byref(self.stats))
+            if rc < 0:
+                raise _lib.CarpioGpuError(rc, "poisson_solve_learned")
+            self.lresid = hist[:min(self.stats.outer_iters + 1, cap)].tolist()
+            return rc
         cap = self.cfg.max_iter + 2
         hist = np.zeros(max(cap, 1))
         rc = L.carpio_gpu_poisson_solve(
@@ -204,6 +231,19 @@ class NS_explicit:
         if name not in _lib.SCHEMES:
             raise ValueError(f"unknown scheme {name}")
         self.scheme = name
+
+    def set_learned(self, net, use_net=True, smooth=4, omega=0.8, memory=2,
+                    stall=20, fallback=True):
+        """project with flexible CG preconditioned by the U-Net `net`
+        (None: back to the configured projection solver)"""
+        if self.handle is None:
+            self.initial()
+        self._learned = (net, learned_cfg(use_net, smooth, omega, memory, stall, fallback))
+        rc = _lib.load().carpio_gpu_ns_set_learned(
+            self.handle, net.handle if net is not None else None,
+            ctypes.byref(self._learned[1]))
+        if rc:
+            raise _lib.CarpioGpuError(rc, "ns_set_learned")
 
     def set_projection_solver(self, name="CG", max_iter=1000, tol=1e-3,
                               precision="fp64", **kw):

@@ -5,6 +5,7 @@ of 8 and at least 16; the network itself (weights, activations, optimiser
 state) lives behind the C ABI.
 """
 import ctypes
+import os
 import sys
 
 import numpy as np
@@ -20,6 +21,20 @@ def _check(rc, what):
 
 def num_params():
     return int(_lib.load().carpio_gpu_unet_num_params())
+
+
+# parameters trained by `python -m carpio_gb300.train --samples 20000 --epochs 4
+# --out carpio_gb300/weights/unet_poisson.f32` (256^2 pairs, energy-norm loss)
+TRAINED = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights",
+                       "unet_poisson.f32")
+
+
+def load_trained(path=TRAINED):
+    """a UNet with the shipped trained parameters (little-endian FP32)"""
+    net = UNet()
+    p = np.fromfile(path, dtype="<f4")
+    net.set_params(p)
+    return net
 
 
 class UNet:
@@ -60,25 +75,28 @@ class UNet:
                "carpio_gpu_unet_forward")
         return z
 
-    def grad(self, x, t):
+    LOSSES = {"mse": 0, "energy": 1}
+
+    def grad(self, x, t, loss="mse"):
         x, t = self._field(x), self._field(t)
         n, h, w = x.shape
         g = np.empty(self.n_params, dtype=np.float32)
-        loss = ctypes.c_double()
+        out = ctypes.c_double()
         _check(self._L.carpio_gpu_unet_grad(self._h, n, h, w, x.data_ptr(), t.data_ptr(),
-                                            g.ctypes.data, ctypes.byref(loss)),
+                                            self.LOSSES[loss], g.ctypes.data,
+                                            ctypes.byref(out)),
                "carpio_gpu_unet_grad")
-        return loss.value, g
+        return out.value, g
 
-    def train_step(self, x, t, lr):
+    def train_step(self, x, t, lr, loss="mse"):
         x, t = self._field(x), self._field(t)
         n, h, w = x.shape
-        loss = ctypes.c_double()
+        out = ctypes.c_double()
         _check(self._L.carpio_gpu_unet_train_step(self._h, n, h, w, x.data_ptr(),
-                                                  t.data_ptr(), float(lr),
-                                                  ctypes.byref(loss)),
+                                                  t.data_ptr(), self.LOSSES[loss],
+                                                  float(lr), ctypes.byref(out)),
                "carpio_gpu_unet_train_step")
-        return loss.value
+        return out.value
 
     @property
     def handle(self):

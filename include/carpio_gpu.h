@@ -341,8 +341,10 @@ int carpio_gpu_nn_conv3x3(const void* in0, int cin0, const void* in1, int cin1,
  * skips, no biases; carpio_gpu_unet_num_params() FP32 parameters) mapping a
  * field x [n][h][w] (FP32) to z [n][h][w] (FP32); h, w multiples of 8 and at
  * least 16. The convolutions run on the tensor cores; training is Adam on
- * FP32 master weights with the relative squared error
- * sum (z - t)^2 / sum t^2 as the loss. Field pointers are device memory. */
+ * FP32 master weights. loss_mode 0: relative squared error
+ * sum (z - t)^2 / sum t^2; 1: relative energy norm (e, A e) / (t, A t),
+ * e = z - t, A the all-Neumann 5-point operator with unit face coefficients
+ * (the norm conjugate gradients minimise). Field pointers are device memory. */
 typedef struct carpio_gpu_unet carpio_gpu_unet;
 long carpio_gpu_unet_num_params(void);
 /* deterministic He-normal initial weights from `seed` */
@@ -357,10 +359,40 @@ int carpio_gpu_unet_forward(carpio_gpu_unet* u, int n, int h, int w, const float
 		float* z, void* stream);
 /* loss and gradient (FP32, layout of the parameters; host or device) */
 int carpio_gpu_unet_grad(carpio_gpu_unet* u, int n, int h, int w, const float* x,
-		const float* t, float* grad, double* loss);
+		const float* t, int loss_mode, float* grad, double* loss);
 /* one Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on the batch */
 int carpio_gpu_unet_train_step(carpio_gpu_unet* u, int n, int h, int w, const float* x,
-		const float* t, float lr, double* loss);
+		const float* t, int loss_mode, float lr, double* loss);
+
+/* Poisson solve with the learned preconditioner: flexible CG (FCG(m),
+ * Notay) in FP64 whose preconditioner is the U-Net on the residual (scaled
+ * to unit RMS) followed by `smooth` damped Jacobi sweeps; the network's
+ * answer to the initial residual is also the warm start. The true FP64
+ * residual judges convergence (the reference's nrm2 test against cfg->tol);
+ * after `stall` iterations without a 10 % drop the solve finishes with the
+ * plain MIXED CG if `fallback` is set. use_net = 0 runs the same iteration
+ * without the network. The grid needs nx, ny multiples of 8 (>= 16) with the
+ * network's tiling. Arguments otherwise as carpio_gpu_poisson_solve
+ * (resid_hist: the FCG residuals, initial one first); stats: iters = FCG +
+ * fallback iterations, outer_iters = FCG iterations. */
+typedef struct {
+	int use_net;       /* 1: network + smoothing; 0: smoothing only */
+	int smooth;        /* Jacobi sweeps after the network */
+	double omega;      /* their damping (0 = 0.8) */
+	int memory;        /* FCG directions kept, 1..4 */
+	int stall;         /* iterations of the stall test (0 = 20) */
+	int fallback;      /* finish with the plain CG after a stall */
+} carpio_gpu_learned_cfg;
+
+int carpio_gpu_poisson_solve_learned(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
+		double beta, const double* source, double* phi,
+		const carpio_gpu_solver_cfg* cfg, carpio_gpu_unet* net,
+		const carpio_gpu_learned_cfg* lc, double* resid_hist, int hist_cap,
+		carpio_gpu_solver_stats* stats);
+/* The NS projection with the learned solve (net = NULL: back to the
+ * configured projection solver); lc is copied. */
+int carpio_gpu_ns_set_learned(carpio_gpu_ns* ns, carpio_gpu_unet* net,
+		const carpio_gpu_learned_cfg* lc);
 
 #ifdef __cplusplus
 }

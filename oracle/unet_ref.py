@@ -128,15 +128,40 @@ def forward(p, x, emulate_bf16=False):
     return z, A
 
 
-def loss_and_grad(p, x, t, emulate_bf16=False):
-    """(loss, gradient in the flat parameter layout)"""
+def neumann_apply(f):
+    """the all-Neumann 5-point operator with unit face coefficients, per
+    image of f [n, h, w]"""
+    a = np.zeros_like(f)
+    d = f[:, 1:, :] - f[:, :-1, :]
+    a[:, 1:, :] += d
+    a[:, :-1, :] -= d
+    d = f[:, :, 1:] - f[:, :, :-1]
+    a[:, :, 1:] += d
+    a[:, :, :-1] -= d
+    return a
+
+
+def loss_and_grad(p, x, t, emulate_bf16=False, loss="mse"):
+    """(loss, gradient in the flat parameter layout); loss "mse":
+    sum (z - t)^2 / sum t^2, "energy": (e, A e) / (t, A t) with e = z - t"""
     q = bf16_round if emulate_bf16 else (lambda a: a)
     w_in, ws, w_out = unpack(p, emulate_bf16)
     z, A = forward(p, x, emulate_bf16)
     t = np.asarray(t, dtype=np.float64)
-    qq = np.sum(t * t) or 1.0
-    loss = np.sum((z - t) ** 2) / qq
-    dz = np.float32(2.0 * (z - t) / qq).astype(np.float64) if emulate_bf16 else 2.0 * (z - t) / qq
+    if loss == "energy":
+        e = z - t
+        if emulate_bf16:
+            e = e.astype(np.float32).astype(np.float64)
+        qq = np.sum(t * neumann_apply(t)) or 1.0
+        value = np.sum(e * neumann_apply(e)) / qq
+        dz = 2.0 * neumann_apply(e) / qq
+    else:
+        qq = np.sum(t * t) or 1.0
+        value = np.sum((z - t) ** 2) / qq
+        dz = 2.0 * (z - t) / qq
+    if emulate_bf16:
+        dz = dz.astype(np.float32).astype(np.float64)
+    loss = value
     G = [None] * 13
     g_out = np.einsum("nhwc,nhw->c", A["d0"], dz)
     gpre = q(np.where(A["d0"] > 0, dz[..., None] * w_out, 0))       # d0

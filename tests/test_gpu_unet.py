@@ -36,13 +36,15 @@ def test_forward_matches_oracle(gpu_lib):
         assert rel_l2(z, zr) < 2e-2, rel_l2(z, zr)
 
 
-def test_gradient_matches_oracle(gpu_lib):
+@pytest.mark.parametrize("loss_kind", ["mse", "energy"])
+def test_gradient_matches_oracle(gpu_lib, loss_kind):
     from carpio_gb300.unet import UNet
     net = UNet(seed=2)
     p = net.params().astype(np.float64)
     x, t = fields(7, 2, 64, 64)
-    loss, g = net.grad(x, t)
-    lr_, gr = U.loss_and_grad(p, x.cpu().numpy(), t.cpu().numpy(), emulate_bf16=True)
+    loss, g = net.grad(x, t, loss=loss_kind)
+    lr_, gr = U.loss_and_grad(p, x.cpu().numpy(), t.cpu().numpy(), emulate_bf16=True,
+                              loss=loss_kind)
     assert abs(loss - lr_) <= 1e-2 * lr_
     g = g.astype(np.float64)
     cos = g @ gr / (np.linalg.norm(g) * np.linalg.norm(gr))

@@ -21,12 +21,16 @@ def test_parameter_count_matches_library():
     assert unet.num_params() == U.num_params() == 1944896
 
 
-def test_oracle_gradient_matches_finite_differences():
+import pytest
+
+
+@pytest.mark.parametrize("loss", ["mse", "energy"])
+def test_oracle_gradient_matches_finite_differences(loss):
     rng = np.random.default_rng(0)
     p = random_params(rng)
     x = rng.normal(size=(2, 16, 16))
     t = rng.normal(size=(2, 16, 16))
-    loss, g = U.loss_and_grad(p, x, t)
+    value, g = U.loss_and_grad(p, x, t, loss=loss)
     off = U.offsets()
     # a few parameters of every layer with a non-negligible gradient
     picks = []
@@ -42,7 +46,8 @@ def test_oracle_gradient_matches_finite_differences():
         pp, pm = p.copy(), p.copy()
         pp[i] += eps
         pm[i] -= eps
-        fd = (U.loss_and_grad(pp, x, t)[0] - U.loss_and_grad(pm, x, t)[0]) / (2 * eps)
+        fd = (U.loss_and_grad(pp, x, t, loss=loss)[0]
+              - U.loss_and_grad(pm, x, t, loss=loss)[0]) / (2 * eps)
         assert abs(fd - g[i]) <= 1e-5 * abs(g[i]) + 1e-9, (i, fd, g[i])
 
 
