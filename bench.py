@@ -54,7 +54,11 @@ def parse():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--inner-tol", type=float, default=3e-2)
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the FP64 comparison, Poisson and CPU legs")
+                    help="skip the FP64 comparison, Poisson, learned, batched and CPU legs")
+    ap.add_argument("--accuracy-steps", type=int, default=0,
+                    help="instead of the bench line: run the mixed and the FP64 "
+                         "projections side by side for this many steps and print "
+                         "their per-step relative L2 differences and solve times")
     return ap.parse_args()
 
 
@@ -253,6 +257,9 @@ def main():
     if a.impl == "reference":
         run_reference(a)
         return
+    if a.accuracy_steps > 0:
+        accuracy_run(a)
+        return
     ws, rank, local = dist_env()
     import torch
     torch.cuda.set_device(local)
@@ -356,7 +363,12 @@ def main():
             "iters": float(np.mean(p2["inner"]))}
         del ns2
         # Poisson ms to 1e-8 on the same divergence field: FP64 CG vs mixed
+        # vs the learned preconditioner, and on a held-out 512^2 field
         out["poisson_ms_to_1e-8"] = poisson_leg(n, a.inner_tol)
+        out["poisson_512_heldout"] = heldout_leg(512)
+        out["learned_cavity"] = learned_cavity_leg(n, a.inner_tol)
+        out["unet_forward"] = unet_leg(n)
+        out["batched_512"] = batched_leg()
         # CPU baseline: the reference's CPU step (restatement) on a bounded
         # sample of the same workload, scaled to the timed steps' iterations
         if ws == 1:
@@ -406,8 +418,204 @@ def poisson_leg(n, inner_tol):
         res[prec] = {"ms": P.stats.ms, "iters": P.stats.iters,
                      "outer": P.stats.outer_iters, "resid": P.stats.tol_out,
                      "code": rc}
+    if learned_ok(n):
+        from carpio_gb300.unet import load_trained
+        net = load_trained()
+        for label, use in (("learned", True), ("fcg_without_net", False)):
+            P = S.Poisson(g)
+            P.set_depend(g.zeros(), None, src)
+            P.set_solver("CG", None, 200000, TOL, mean_removal=True, precision="mixed",
+                         inner_tol=inner_tol)
+            P.set_learned(net if use else None, use_net=use, fallback=True)
+            P.run()   # warm-up
+            P.set_depend(g.zeros(), None, src)
+            rc = P.run()
+            res[label] = {"ms": P.stats.ms, "iters": P.stats.iters,
+                          "fcg_iters": P.stats.outer_iters,
+                          "fallback_iters": P.stats.iters - P.stats.outer_iters,
+                          "resid": P.stats.tol_out, "code": rc}
     res["speedup_mixed_over_fp64"] = res["fp64"]["ms"] / res["mixed"]["ms"]
+    if "learned" in res:
+        res["speedup_learned_over_fp64"] = res["fp64"]["ms"] / res["learned"]["ms"]
     return res
+
+
+def learned_ok(n):
+    h3 = n // 8
+    return n % 8 == 0 and n >= 16 and min(h3, 128) * min(h3, 128 // min(h3, 128)) == 128
+
+
+def heldout_leg(n):
+    """a held-out 512^2 random potential field (the training generator with
+    an unseen seed): iterations and device ms to 1e-8 of FP64 CG, the mixed
+    CG, flexible CG with the trained network and without it"""
+    from carpio_gb300 import structure as S, train as T
+    from carpio_gb300.unet import load_trained
+    net = load_trained()
+    phi = T.random_potentials(1, n, seed=20251203)[0]
+    b = T.neumann_laplacian(phi).cpu().numpy()
+    res = {}
+    for label in ("fp64", "mixed", "learned", "fcg_without_net"):
+        g = S.Grid((0.0, 0.0), (1.0, 1.0), (n, n), 1)
+        P = S.Poisson(g)
+        for seg in range(4):
+            bc = S.BoundaryCondition()
+            bc.set_default_2_bc(0.0)
+            P.add_bc(0, seg, "phi", bc)
+        src = g.zeros()
+        src[1:-1, 1:-1] = -b * n * n
+        P.set_solver("CG", None, 200000, TOL, mean_removal=True,
+                     precision="fp64" if label == "fp64" else "mixed")
+        if label in ("learned", "fcg_without_net"):
+            P.set_learned(net if label == "learned" else None,
+                          use_net=label == "learned", fallback=True)
+        for _ in range(2):   # warm-up, then the measured solve
+            P.set_depend(g.zeros(), None, src)
+            rc = P.run()
+        x = g.interior(P.phi)
+        err = float(np.linalg.norm(x - phi.cpu().numpy()) / np.linalg.norm(phi.cpu().numpy()))
+        res[label] = {"ms": P.stats.ms, "iters": P.stats.iters,
+                      "fcg_iters": P.stats.outer_iters if "learned" in label or "fcg" in label else None,
+                      "resid": P.stats.tol_out, "code": rc, "rel_l2_vs_exact": err}
+    res["iters_ratio_fp64_over_learned"] = res["fp64"]["iters"] / max(1, res["learned"]["iters"])
+    return res
+
+
+def learned_cavity_leg(n, inner_tol, steps=2, warmup=1):
+    """cavity steps/s with the learned projection (flexible CG + network,
+    fallback to the plain CG), same workload"""
+    if not learned_ok(n):
+        return None
+    from carpio_gb300.unet import load_trained
+    import torch
+    net = load_trained()
+    g, ns = make_cavity(n, "mixed", inner_tol)
+    ns.set_learned(net, fallback=True)
+    ns.run(warmup)
+    torch.cuda.synchronize()
+    ns.run(steps)
+    pr = ns.profile()
+    return {"steps_per_s": steps / (float(np.sum(pr["step_ms"])) / 1e3),
+            "solve_ms": float(np.mean(pr["solve_ms"])),
+            "iters": float(np.mean(pr["inner"])), "steps": steps}
+
+
+def unet_leg(n):
+    """device time of one U-Net application at n^2 and its tensor-core rate"""
+    import torch
+    from carpio_gb300.unet import load_trained
+    if not learned_ok(n):
+        return None
+    net = load_trained()
+    x = torch.randn(1, n, n, device="cuda")
+    z = torch.empty_like(x)
+    for _ in range(3):
+        net.forward(x, out=z)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 10
+    e0.record()
+    for _ in range(reps):
+        net.forward(x, out=z)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    # multiply-adds of the 13 tensor-core layers per pixel of their level
+    macs = 0
+    for (ci0, ci1, co), lvl in zip(
+            [(32, 0, 32), (32, 0, 64), (64, 0, 64), (64, 0, 128), (128, 0, 128),
+             (128, 0, 256), (256, 0, 256), (256, 128, 128), (128, 0, 128),
+             (128, 64, 64), (64, 0, 64), (64, 32, 32), (32, 0, 32)],
+            [0, 1, 1, 2, 2, 3, 3, 2, 2, 1, 1, 0, 0]):
+        macs += 9 * (ci0 + ci1) * co * (n >> lvl) ** 2
+    peak, how = bf16_peak()
+    tflops = 2.0 * macs / (ms / 1e3) / 1e12
+    return {"ms": ms, "tensor_gflop": 2.0 * macs / 1e9, "tflops": tflops,
+            "peak_tflops": peak, "frac": tflops / peak, "peak_source": how,
+            "note": "host-launched layers (stream-ordered), wall of 10 forwards / 10"}
+
+
+def bf16_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["bf16_tflops"]), "measured"
+    except Exception:
+        return 1900.0, "fallback"
+
+
+def batched_leg(count=512, reps=2):
+    """512 uneven Poisson problems (side N uniform in {32, 48, ..., 512}, 8
+    Gaussians, Dirichlet-0 or all-Neumann, FP32 inner / FP64 refinement to
+    1e-8): one persistent cluster launch replayed from a CUDA graph vs a loop
+    of single solves on the same device-resident inputs"""
+    import torch
+    from carpio_gb300 import batch, structure as S, workloads
+    probs, srcs = workloads.uneven_batch(count, seed=0)
+    bp = batch.BatchedPoisson(probs, tol=TOL)
+    bp.upload(0, srcs)
+    ms = []
+    for _ in range(reps + 1):
+        bp.zero(1)
+        rc = bp.run()
+        ms.append(bp.ms)
+    info = bp.info()
+    iters = sum(s["iters"] for s in bp.stats)
+    cells = sum(p.nx * p.ny for p in probs)
+    cell_iters = sum(s["iters"] * p.nx * p.ny for s, p in zip(bp.stats, probs))
+    t_batch = min(ms[1:])
+    # the same problems one at a time through carpio_gpu_poisson_solve
+    t0 = time.perf_counter()
+    dev_ms = 0.0
+    for i, p in enumerate(probs):
+        g = S.Grid(p.box[0], p.box[1], (p.nx, p.ny), 1)
+        P = S.Poisson(g)
+        for seg, (tt, v) in enumerate(p.bc):
+            bc = S.BoundaryCondition()
+            (bc.set_default_1_bc if tt == 1 else bc.set_default_2_bc)(v)
+            P.add_bc(0, seg, "phi", bc)
+        src = torch.zeros(p.nx + 2, p.ny + 2, dtype=torch.float64, device="cuda")
+        src[1:-1, 1:-1] = torch.from_numpy(srcs[i])
+        P.set_depend(torch.zeros_like(src), None, src)
+        P.set_solver("CG", None, 200000, TOL, mean_removal=p.mean_removal,
+                     precision="mixed")
+        P.run()
+        dev_ms += P.stats.ms
+    loop_wall = 1e3 * (time.perf_counter() - t0)
+    return {"problems": count, "cells": cells, "code": rc,
+            "persistent_graph_ms": t_batch, "loop_single_solves_ms": loop_wall,
+            "loop_device_ms": dev_ms, "speedup": loop_wall / t_batch,
+            "inner_iters": iters, "cell_iters_per_s": cell_iters / (t_batch / 1e3),
+            "max_resid": max(s["resid"] for s in bp.stats),
+            "tiles": {k: info[k] for k in ("threads", "cluster", "cells_per_cta",
+                                           "clusters", "ctas", "smem_bytes", "teams")}}
+
+
+def accuracy_run(a):
+    """the mixed projection against the FP64 projection on the same cavity,
+    step by step: relative L2 of u, v, p and the solve times"""
+    import torch
+    n, steps = a.n, a.accuracy_steps
+    gm, nm = make_cavity(n, "mixed", a.inner_tol)
+    gf, nf = make_cavity(n, "fp64", a.inner_tol)
+    rows = []
+    for st in range(steps):
+        nm.run(1)
+        nf.run(1)
+        pm, pf = nm.profile(), nf.profile()
+        sm, sf = nm.state(), nf.state()
+        row = {"step": st + 1,
+               "solve_ms_mixed": float(pm["solve_ms"][0]),
+               "solve_ms_fp64": float(pf["solve_ms"][0]),
+               "iters_mixed": int(pm["inner"][0]), "iters_fp64": int(pf["inner"][0])}
+        for k in ("u", "v", "p"):
+            d = gm.interior(sm[k]) - gf.interior(sf[k])
+            ref = np.linalg.norm(gf.interior(sf[k]))
+            row[f"rel_l2_{k}"] = float(np.linalg.norm(d) / ref) if ref > 0 else 0.0
+        rows.append(row)
+    print(json.dumps({"accuracy": f"mixed vs fp64 projection, {n}^2 cavity",
+                      "steps": steps, "rows": rows}), flush=True)
 
 
 if __name__ == "__main__":
