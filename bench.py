@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--inner-tol", type=float, default=3e-2)
+    ap.add_argument("--poly-degree", type=int, default=0,
+                    help="band-local Chebyshev degree of the FP32 CG (0 default, -1 none)")
+    ap.add_argument("--poly-ratio", type=float, default=0.0)
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP64 comparison, Poisson, learned, batched and CPU legs")
     ap.add_argument("--accuracy-steps", type=int, default=0,
@@ -75,9 +78,16 @@ def config(n, precision, inner_tol):
                         f"({'FP32 inner / FP64 refinement' if precision == 'mixed' else 'FP64'})",
             "n": n, "Re": RE, "scheme": "VanLeer", "tol": TOL,
             "precision": precision, "inner_tol": inner_tol,
+            "fp32_preconditioner": ("none" if POLY[0] < 0 else
+                                    f"band-local Chebyshev degree {POLY[0] or 3}, "
+                                    f"interval [2/{POLY[1] or 30:g}, 2] of D^-1 A"),
             "cfl": 0.5, "diffusion_number": 0.25, "dt0": 0.5 / n,
             "l2": "per-step working set ~200 MB > 129 MB L2; no flush",
             "parallelism": "replicas"}
+
+
+# band-local Chebyshev preconditioner of the FP32 CG: (degree, ratio), 0 = defaults
+POLY = [0, 0.0]
 
 
 def make_cavity(n, precision, inner_tol):
@@ -97,7 +107,7 @@ def make_cavity(n, precision, inner_tol):
     ns.set_uniform_rho(RE)
     ns.set_diffusion_number(0.25, 1.0 / RE)
     ns.set_projection_solver("CG", 200000, TOL, precision=precision,
-                             inner_tol=inner_tol)
+                             inner_tol=inner_tol, poly_degree=POLY[0], poly_ratio=POLY[1])
     ns.initial()
     return g, ns
 
@@ -257,6 +267,7 @@ def main():
     if a.impl == "reference":
         run_reference(a)
         return
+    POLY[0], POLY[1] = a.poly_degree, a.poly_ratio
     if a.accuracy_steps > 0:
         accuracy_run(a)
         return
@@ -411,7 +422,7 @@ def poisson_leg(n, inner_tol):
         P = S.Poisson(g)
         P.set_depend(g.zeros(), None, src)
         P.set_solver("CG", None, 200000, TOL, mean_removal=True, precision=prec,
-                     inner_tol=inner_tol)
+                     inner_tol=inner_tol, poly_degree=POLY[0], poly_ratio=POLY[1])
         P.run()   # warm-up
         P.set_depend(g.zeros(), None, src)
         rc = P.run()

@@ -30,7 +30,8 @@ class SolverCfg(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int), ("precision", ctypes.c_int),
                 ("max_iter", ctypes.c_int), ("tol", ctypes.c_double),
                 ("mean_removal", ctypes.c_int), ("inner_tol", ctypes.c_double),
-                ("inner_max_iter", ctypes.c_int), ("flags", ctypes.c_uint32)]
+                ("inner_max_iter", ctypes.c_int), ("flags", ctypes.c_uint32),
+                ("poly_degree", ctypes.c_int), ("poly_ratio", ctypes.c_double)]
 
 
 class SolverStats(ctypes.Structure):

@@ -25,6 +25,9 @@ struct MixedArgs {
 	Vecs<float> f;         // e (x), r, p, q
 	double inner_tol;
 	int inner_max;
+	int pdeg;              // on-chip path: degree of the band-local Chebyshev
+	                       // preconditioner (0 = none)
+	float pratio;          // its eigenvalue interval [2 / pratio, 2] of D^-1 A
 };
 
 // FP32 CG on A32 e = r32 from e = 0 (one inner solve of the refinement).
@@ -196,6 +199,9 @@ __global__ void __launch_bounds__(kThreads) k_poisson(StencilOp<double> op,
 // row of r, published before the second reduction and read after it
 // (double-buffered by iteration parity).
 constexpr int kTileThreads = 512;
+// default band-local Chebyshev preconditioner of the on-chip path
+constexpr int kPolyDegree = 3;
+constexpr double kPolyRatio = 30.0;
 
 struct TileArgs {
 	float* xbuf;           // [3][C][2][ny]: band edge rows of r (two iteration
@@ -234,11 +240,19 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	float* axs = rs + ta.rows_max * ny;   // x-face coefficients of faces r0 .. r1
 	float* ays = axs + ta.rows_max + 1;
 	float* dd = ays + ny + 1;       // the band's diagonal, dd[lr * ny + j]
+	// preconditioned: z = M r with its halo rows from the neighbours (in
+	// rhal), the Chebyshev direction with zero halo rows, the local residual
+	const int K = m.pdeg;
+	float* zs = K > 0 ? dd + ta.rows_max * ny : rs;
+	float* dsm = zs + ta.rows_max * ny;    // dsm[1 + (lr + 1) * ny + j]
+	float* rk = dsm + np;
 	const bool up = c > 0, down = c < C - 1;
 	const size_t edge = (size_t)2 * C * ny;   // one edge region
 	float* rbuf = ta.xbuf + 2 * edge;         // r edges
 	int par = 0;                              // q edges: xbuf + par * edge
 	for (int t = tid; t < np; t += T) p[t] = 0.f;
+	if (K > 0)
+		for (int t = tid; t < np; t += T) dsm[t] = 0.f;
 	for (int t = tid; t < ny; t += T) { rhal[t] = 0.f; rhal[ny + t] = 0.f; }
 	for (int t = tid; t < rows * ny; t += T) {
 		const int lr = t / ny, j = t - lr * ny;
@@ -254,6 +268,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	__syncthreads();
 	// r (FP32) = (r64 - mean) * scale0 with scale0 fixed for the whole solve
 	double scale0 = 1.0, rn0 = 1.0;
+	float rrn = 0.f;   // (r, r) of the current FP32 residual
 
 	auto publish_r = [&]() {
 		float* pub = rbuf + (size_t)(2 * c) * ny;
@@ -261,12 +276,101 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 		for (int k = 0; k < NC; ++k) {
 			const int j = tid + k * T;
 			if (j < ny && rows > 0) {
-				pub[j] = rs[j];
-				pub[ny + j] = rs[(rows - 1) * ny + j];
+				pub[j] = zs[j];
+				pub[ny + j] = zs[(rows - 1) * ny + j];
 			}
 		}
 	};
-	// the neighbours' edge rows of region `src` into the halo rows of r.
+	// z = M r: K steps of the Chebyshev iteration for A_band z = r from
+	// z = 0, A_band the band's operator with zero halo rows (a symmetric
+	// positive definite block-diagonal M with no exchange between CTAs).
+	// Returns (r, z) and (r, r) of the band in g. q's registers hold A d.
+	auto precond = [&](float (&g)[2]) {
+		g[0] = g[1] = 0.f;
+		if (K <= 0) {
+#pragma unroll
+			for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+				for (int k = 0; k < NC; ++k) {
+					const int j = tid + k * T;
+					if (lr < rows && j < ny) {
+						const float rv = rs[lr * ny + j];
+						g[0] = fmaf(rv, rv, g[0]);
+					}
+				}
+			g[1] = g[0];
+			return;
+		}
+		const float bmax = 2.f, amin = 2.f / m.pratio;
+		const float th = 0.5f * (bmax + amin), de = 0.5f * (bmax - amin);
+		const float sig = th / de;
+		float rho = 1.f / sig;
+		const float ith = 1.f / th;
+#pragma unroll
+		for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+			for (int k = 0; k < NC; ++k) {
+				const int j = tid + k * T;
+				if (lr < rows && j < ny) {
+					const int cc = lr * ny + j;
+					const float rv = rs[cc];
+					const float dv = __fdividef(rv * ith, dd[cc]);
+					dsm[1 + (lr + 1) * ny + j] = dv;
+					zs[cc] = dv;
+					rk[cc] = rv;
+				}
+			}
+		__syncthreads();
+		for (int step = 1; step < K; ++step) {
+#pragma unroll
+			for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+				for (int k = 0; k < NC; ++k) {
+					const int j = tid + k * T;
+					if (lr < rows && j < ny) {
+						const int pk = 1 + (lr + 1) * ny + j;
+						float vv = dd[lr * ny + j] * dsm[pk];
+						vv = fmaf(axs[lr], dsm[pk - ny], vv);
+						vv = fmaf(axs[lr + 1], dsm[pk + ny], vv);
+						vv = fmaf(ays[j], dsm[pk - 1], vv);
+						vv = fmaf(ays[j + 1], dsm[pk + 1], vv);
+						q[lr][k] = vv;
+					}
+				}
+			__syncthreads();
+			const float rn = 1.f / (2.f * sig - rho);
+			const float c1 = rn * rho, c2f = 2.f * rn / de;
+#pragma unroll
+			for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+				for (int k = 0; k < NC; ++k) {
+					const int j = tid + k * T;
+					if (lr < rows && j < ny) {
+						const int cc = lr * ny + j, pk = 1 + (lr + 1) * ny + j;
+						const float rkv = rk[cc] - q[lr][k];
+						const float dv = fmaf(c1, dsm[pk], __fdividef(c2f * rkv, dd[cc]));
+						rk[cc] = rkv;
+						dsm[pk] = dv;
+						zs[cc] += dv;
+					}
+				}
+			__syncthreads();
+			rho = rn;
+		}
+#pragma unroll
+		for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+			for (int k = 0; k < NC; ++k) {
+				const int j = tid + k * T;
+				if (lr < rows && j < ny) {
+					const int cc = lr * ny + j;
+					const float rv = rs[cc];
+					g[0] = fmaf(rv, zs[cc], g[0]);
+					g[1] = fmaf(rv, rv, g[1]);
+				}
+			}
+	};
+	// the neighbours' edge rows of region `src` into the halo rows of z.
 	// Thread t writes entries t and ny + t, the same mapping every reader of
 	// rhal uses, so no barrier is needed between the write and the reads.
 	auto read_rh = [&](const float* src) {
@@ -310,7 +414,6 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 			rn0 = s_sc[2];
 			scale0 = rn0 > 0.0 ? 1.0 / rn0 : 1.0;
 		}
-		float g[1] = { 0.f };
 #pragma unroll
 		for (int lr = 0; lr < RM; ++lr)
 #pragma unroll
@@ -318,15 +421,17 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				const int j = tid + k * T;
 				if (lr < rows && j < ny) {
 					const int a = (r0 + lr + gl) * P + j + gl;
-					const float rv = (float)((v.r[a] - mr) * scale0);
-					rs[lr * ny + j] = rv;
-					g[0] = fmaf(rv, rv, g[0]);
+					rs[lr * ny + j] = (float)((v.r[a] - mr) * scale0);
 				}
 			}
+		__syncthreads();
+		float g[2];
+		precond(g);
 		publish_r();
-		if (!grid_allreduce<float, 1>(g, gc, bank)) return false;
+		if (!grid_allreduce<float, 2>(g, gc, bank)) return false;
 		read_rh(rbuf);
 		gamma = g[0];
+		rrn = g[1];
 		return true;
 	};
 	// fold x (FP32, scaled) into x64 and clear it
@@ -347,10 +452,10 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	to.iters = 0;
 	to.updates = 0;
 	to.done = 0;
-	float gamma = 0.f;
+	float gamma = 0.f;   // (r, z)
 	if (!true_residual(true, gamma)) return;
 	if (to.resid <= sc.tol) { to.done = 1; return; }
-	float gamma_ref = gamma, gamma_old = 1.f;
+	float gamma_ref = rrn, gamma_old = 1.f;
 	// an update when the FP32 residual has dropped by inner_tol, but at least
 	// every 1e-2 and every kStall iterations: FP32 CG cannot drive its
 	// recursive residual much further before it stops tracking the true one
@@ -366,7 +471,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	while (it < sc.max_iter && gamma > 0.f) {
 		const float beta = first ? 0.f : gamma / gamma_old;
 		first = false;
-		// p = r + beta p over the band and its halo rows
+		// p = z + beta p over the band and its halo rows
 #pragma unroll
 		for (int lr = 0; lr < RM; ++lr)
 #pragma unroll
@@ -374,7 +479,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				const int j = tid + k * T;
 				if (lr < rows && j < ny) {
 					const int pk = 1 + (lr + 1) * ny + j;
-					p[pk] = fmaf(beta, p[pk], rs[lr * ny + j]);
+					p[pk] = fmaf(beta, p[pk], zs[lr * ny + j]);
 				}
 			}
 		for (int t = tid; t < ny; t += T) {
@@ -406,8 +511,8 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 			}
 		if (!grid_allreduce<float, 1>(pq, gc, bank)) return;
 		const float alpha = gamma / pq[0];
-		// x += alpha p, r -= alpha q, (r, r); r's band edges published
-		float gn[1] = { 0.f };
+		// x += alpha p, r -= alpha q; z = M r, (r, z), (r, r); z's band
+		// edges published
 #pragma unroll
 		for (int lr = 0; lr < RM; ++lr)
 #pragma unroll
@@ -416,27 +521,28 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				if (lr < rows && j < ny) {
 					const int pk = 1 + (lr + 1) * ny + j;
 					x[lr][k] = fmaf(alpha, p[pk], x[lr][k]);
-					const float rv = fmaf(-alpha, q[lr][k], rs[lr * ny + j]);
-					rs[lr * ny + j] = rv;
-					gn[0] = fmaf(rv, rv, gn[0]);
+					rs[lr * ny + j] = fmaf(-alpha, q[lr][k], rs[lr * ny + j]);
 				}
 			}
+		float gn[2];
+		precond(gn);
 		float* ebuf = ta.xbuf + (size_t)par * edge;
 #pragma unroll
 		for (int k = 0; k < NC; ++k) {
 			const int j = tid + k * T;
 			if (j < ny && rows > 0) {
-				ebuf[(size_t)(2 * c) * ny + j] = rs[j];
-				ebuf[(size_t)(2 * c + 1) * ny + j] = rs[(rows - 1) * ny + j];
+				ebuf[(size_t)(2 * c) * ny + j] = zs[j];
+				ebuf[(size_t)(2 * c + 1) * ny + j] = zs[(rows - 1) * ny + j];
 			}
 		}
-		if (!grid_allreduce<float, 1>(gn, gc, bank)) return;
+		if (!grid_allreduce<float, 2>(gn, gc, bank)) return;
 		read_rh(ebuf);
 		par ^= 1;
 		++it;
 		++since;
 		float gnew = gn[0];
-		if (gnew < drop * gamma_ref || gnew <= near || since >= kStall) {
+		rrn = gn[1];
+		if (rrn < drop * gamma_ref || rrn <= near || since >= kStall) {
 			since = 0;
 			// reliable update: fold x, replace r by the FP64 residual
 			fold_x();
@@ -444,7 +550,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 			if (!true_residual(false, gnew)) return;
 			++to.updates;
 			if (to.resid <= sc.tol) { to.done = 1; break; }
-			gamma_ref = gnew;
+			gamma_ref = rrn;
 		}
 		gamma_old = gamma;
 		gamma = gnew;
@@ -721,6 +827,8 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 	}
 	mx.inner_tol = cfg.inner_tol > 0 ? cfg.inner_tol : 1e-4;
 	mx.inner_max = cfg.inner_max_iter > 0 ? cfg.inner_max_iter : 1 << 30;
+	mx.pdeg = 0;
+	mx.pratio = 1.f;
 	RhsArgs ra;
 	ra.sx = g->d_sx;
 	ra.sy = g->d_sy;
@@ -749,10 +857,14 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 			                         : (const void*)k_poisson_mixed_tile<SRC_FIELD, NC_, RM_>;
 		TILE_PICK(1, 4) TILE_PICK(1, 16) TILE_PICK(2, 8) TILE_PICK(4, 4)
 #undef TILE_PICK
-		const size_t smem = sizeof(float) * ((size_t)(rows_max + 2) * g->ny + 2
-				+ 2 * (size_t)g->ny + (size_t)rows_max * g->ny + rows_max + 1
-				+ g->ny + 1 + (size_t)rows_max * g->ny);
-		if (tk && smem <= 200 * 1024) {
+		const int pdeg = cfg.poly_degree < 0 ? 0 : (cfg.poly_degree == 0 ? kPolyDegree : cfg.poly_degree);
+		const size_t np = (size_t)(rows_max + 2) * g->ny + 2;
+		size_t smem = sizeof(float) * (np + 2 * (size_t)g->ny + (size_t)rows_max * g->ny
+				+ rows_max + 1 + g->ny + 1 + (size_t)rows_max * g->ny);
+		if (pdeg > 0) smem += sizeof(float) * (2 * (size_t)rows_max * g->ny + np);
+		mx.pdeg = pdeg;
+		mx.pratio = (float)(cfg.poly_ratio > 1.0 ? cfg.poly_ratio : kPolyRatio);
+		if (tk && smem <= 220 * 1024) {
 			CG_CK(cudaFuncSetAttribute(tk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
 			int per_sm = 0;
 			CG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tk, kTileThreads, smem));

@@ -1,0 +1,55 @@
+"""Small fixed workloads of single kernels, for profilers and timing.
+
+    python -m carpio_gb300.profile_cases unet N
+        two forwards of the trained U-Net on one N x N field (the tcgen05
+        3x3 convolutions and the network's elementwise kernels)
+    python -m carpio_gb300.profile_cases batch COUNT N
+        one batched persistent solve of COUNT all-Neumann N x N problems with
+        Gaussian sources to 1e-8 (thread-block clusters of 16 CTAs)
+
+Each prints one line with its timing and exits 0 on success.
+"""
+import sys
+
+import numpy as np
+
+
+def unet(n):
+    import torch
+    from .unet import load_trained
+    net = load_trained()
+    x = torch.randn(1, n, n, device="cuda", generator=torch.Generator("cuda").manual_seed(0))
+    z = torch.empty_like(x)
+    for _ in range(2):
+        net.forward(x, out=z)
+    torch.cuda.synchronize()
+    print(f"unet {n}x{n}: mean |z| {float(z.abs().mean()):.4e}")
+
+
+def batch(count, n):
+    from . import workloads
+    from .batch import BatchedPoisson, Problem, NEUMANN
+    rng = np.random.default_rng(1)
+    probs = [Problem(n, n, bc=[(NEUMANN, 0.0)] * 4) for _ in range(count)]
+    srcs = [workloads.gaussian_source(n, n, rng) for _ in probs]
+    bp = BatchedPoisson(probs, tol=1e-8, tiles=dict(threads=512, cluster=16))
+    bp.upload(0, srcs)
+    bp.zero(1)
+    bp.run()
+    st = bp.stats[0]
+    print(f"batch {count} x {n}^2: {bp.ms:.2f} ms, {st['iters']} iterations, "
+          f"{1000 * st['ms'] / max(st['iters'], 1):.2f} us/iteration")
+
+
+def main(argv=None):
+    a = list(sys.argv[1:] if argv is None else argv)
+    if a[:1] == ["unet"] and len(a) == 2:
+        unet(int(a[1]))
+    elif a[:1] == ["batch"] and len(a) == 3:
+        batch(int(a[1]), int(a[2]))
+    else:
+        sys.exit(__doc__)
+
+
+if __name__ == "__main__":
+    main()

@@ -140,6 +140,12 @@ typedef struct {
 	                      on chip); 0 = 3e-2 */
 	int inner_max_iter;/* MIXED, global-memory path: cap on one inner solve */
 	uint32_t flags;    /* CARPIO_GPU_FLAG_* */
+	int poly_degree;   /* MIXED, on-chip path: degree of the band-local
+	                      Chebyshev preconditioner of the FP32 CG (each CTA's
+	                      band with zero halo, so no exchange); 0 = default 3,
+	                      < 0 = none (plain CG) */
+	double poly_ratio; /* its eigenvalue interval [2 / ratio, 2] of D^-1 A;
+	                      0 = 30 */
 } carpio_gpu_solver_cfg;
 
 typedef struct {
