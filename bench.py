@@ -177,15 +177,24 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def solve_bytes_per_cell(precision, inner, outer):
-    """Algorithmic bytes of one projection-solve launch per cell: prologue
-    (read 2 face fields + phi, write b and x: 40 B), per FP32 inner CG
-    iteration 40 B (read p, q, r, x, D; write p, q, x, r: 4 B each, the
-    operator's neighbours counted once), per FP64 refinement step 40 B
-    (read x, b, D; write r; write x), per FP64 CG iteration 80 B, epilogue
-    (mean removal + scatter: read x twice, write phi: 24 B)."""
+def poly_degree():
+    """degree of the FP32 CG's band-local Chebyshev preconditioner in use"""
+    return 0 if POLY[0] < 0 else (POLY[0] or 3)
+
+
+def solve_bytes_per_cell(precision, inner, outer, deg=0):
+    """Algorithmic bytes of one projection-solve launch per cell, i.e. what
+    the algorithm moves when its vectors live in memory: prologue (read 2
+    face fields + phi, write b and x: 40 B), per FP32 inner CG iteration
+    40 B (read p, q, r, x, D; write p, q, x, r: 4 B each, the operator's
+    neighbours counted once) plus the preconditioner's (first Chebyshev step:
+    read r, D, write d, z, r_k: 20 B; each further step: read d, r_k, z, D,
+    write d, r_k, z: 28 B; the (r, z) dot: 8 B), per FP64 refinement step
+    40 B (read x, b, D; write r; write x), per FP64 CG iteration 80 B,
+    epilogue (mean removal + scatter: read x twice, write phi: 24 B)."""
     if precision == "mixed":
-        return 40 + 40 * inner + 40 * (outer + 1) + 24
+        it = 40 + (20 + 28 * (deg - 1) + 8 if deg > 0 else 0)
+        return 40 + it * inner + 40 * (outer + 1) + 24
     return 40 + 80 * inner + 24 + 24
 
 
@@ -330,14 +339,16 @@ def main():
     }
     # roofline of the dominant kernel (the persistent projection solve)
     peak, how = peaks()
-    bpc = solve_bytes_per_cell(a.precision, inner, outer)
+    bpc = solve_bytes_per_cell(a.precision, inner, outer,
+                               poly_degree() if a.precision == "mixed" else 0)
     achieved = bpc * n * n / (solve_ms / 1e3) / 1e9
     out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak,
                        "unit": "GB/s", "frac": achieved / peak,
                        "peak_source": how,
                        "traffic": traffic_per_launch(n, inner, outer),
                        "algorithmic_bytes_per_launch": bpc * n * n,
-                       "kernel": "k_poisson (persistent projection solve)"}
+                       "kernel": ("k_poisson_mixed_tile" if a.precision == "mixed"
+                                  else "k_poisson") + " (persistent projection solve)"}
     # e2e through the public API with host buffers
     if rank == 0 or True:
         st = ns.state()

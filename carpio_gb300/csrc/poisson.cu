@@ -513,6 +513,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 		const float alpha = gamma / pq[0];
 		// x += alpha p, r -= alpha q; z = M r, (r, z), (r, r); z's band
 		// edges published
+		float rr = 0.f;
 #pragma unroll
 		for (int lr = 0; lr < RM; ++lr)
 #pragma unroll
@@ -521,11 +522,13 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				if (lr < rows && j < ny) {
 					const int pk = 1 + (lr + 1) * ny + j;
 					x[lr][k] = fmaf(alpha, p[pk], x[lr][k]);
-					rs[lr * ny + j] = fmaf(-alpha, q[lr][k], rs[lr * ny + j]);
+					const float rv = fmaf(-alpha, q[lr][k], rs[lr * ny + j]);
+					rs[lr * ny + j] = rv;
+					rr = fmaf(rv, rv, rr);
 				}
 			}
-		float gn[2];
-		precond(gn);
+		float gn[2] = { rr, rr };
+		if (K > 0) precond(gn);
 		float* ebuf = ta.xbuf + (size_t)par * edge;
 #pragma unroll
 		for (int k = 0; k < NC; ++k) {
