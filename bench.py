@@ -198,15 +198,16 @@ def solve_bytes_per_cell(precision, inner, outer, deg=0):
     return 40 + 80 * inner + 24 + 24
 
 
-def traffic_per_launch(n, inner, outer):
-    """DRAM bytes per launch from the committed ncu capture, scaled by cells
-    and iterations, or None."""
+def traffic_per_launch(n, precision):
+    """DRAM bytes of one projection-solve launch from the committed ncu
+    capture (a smaller case of the same kernel, scaled by cells), or None."""
+    if precision != "mixed":
+        return None
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
             t = json.load(f)
-        per_cell_iter = float(t["dram_bytes_per_cell_per_inner_iter"])
-        return per_cell_iter * n * n * max(inner, 1)
+        return float(t["dram_bytes_per_cell_per_launch"]) * n * n
     except (OSError, KeyError, ValueError):
         return None
 
@@ -345,7 +346,7 @@ def main():
     out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak,
                        "unit": "GB/s", "frac": achieved / peak,
                        "peak_source": how,
-                       "traffic": traffic_per_launch(n, inner, outer),
+                       "traffic": traffic_per_launch(n, a.precision),
                        "algorithmic_bytes_per_launch": bpc * n * n,
                        "kernel": ("k_poisson_mixed_tile" if a.precision == "mixed"
                                   else "k_poisson") + " (persistent projection solve)"}
