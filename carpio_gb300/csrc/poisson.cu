@@ -200,7 +200,7 @@ __global__ void __launch_bounds__(kThreads) k_poisson(StencilOp<double> op,
 // (double-buffered by iteration parity).
 constexpr int kTileThreads = 512;
 // default band-local Chebyshev preconditioner of the on-chip path
-constexpr int kPolyDegree = 3;
+constexpr int kPolyDegree = 5;
 constexpr double kPolyRatio = 30.0;
 
 struct TileArgs {
@@ -241,18 +241,19 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	float* ays = axs + ta.rows_max + 1;
 	float* dd = ays + ny + 1;       // the band's diagonal, dd[lr * ny + j]
 	// preconditioned: z = M r with its halo rows from the neighbours (in
-	// rhal), the Chebyshev direction with zero halo rows, the local residual
+	// rhal); the Chebyshev directions, two buffers in the layout of p with
+	// zero halo rows (one read, one written per step)
 	const int K = m.pdeg;
 	float* zs = K > 0 ? dd + ta.rows_max * ny : rs;
-	float* dsm = zs + ta.rows_max * ny;    // dsm[1 + (lr + 1) * ny + j]
-	float* rk = dsm + np;
+	float* dsa = zs + ta.rows_max * ny;    // dsa[1 + (lr + 1) * ny + j]
+	float* dsb = dsa + np;
 	const bool up = c > 0, down = c < C - 1;
 	const size_t edge = (size_t)2 * C * ny;   // one edge region
 	float* rbuf = ta.xbuf + 2 * edge;         // r edges
 	int par = 0;                              // q edges: xbuf + par * edge
 	for (int t = tid; t < np; t += T) p[t] = 0.f;
 	if (K > 0)
-		for (int t = tid; t < np; t += T) dsm[t] = 0.f;
+		for (int t = tid; t < 2 * np; t += T) dsa[t] = 0.f;
 	for (int t = tid; t < ny; t += T) { rhal[t] = 0.f; rhal[ny + t] = 0.f; }
 	for (int t = tid; t < rows * ny; t += T) {
 		const int lr = t / ny, j = t - lr * ny;
@@ -284,28 +285,19 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	// z = M r: K steps of the Chebyshev iteration for A_band z = r from
 	// z = 0, A_band the band's operator with zero halo rows (a symmetric
 	// positive definite block-diagonal M with no exchange between CTAs).
-	// Returns (r, z) and (r, r) of the band in g. q's registers hold A d.
+	// One pass per step: the stencil of the previous direction (read from
+	// one buffer) updates the local residual (registers, in q) and gives
+	// the next direction (written to the other buffer), so a step needs one
+	// block barrier. Returns (r, z) and (r, r) of the band in g.
 	auto precond = [&](float (&g)[2]) {
 		g[0] = g[1] = 0.f;
-		if (K <= 0) {
-#pragma unroll
-			for (int lr = 0; lr < RM; ++lr)
-#pragma unroll
-				for (int k = 0; k < NC; ++k) {
-					const int j = tid + k * T;
-					if (lr < rows && j < ny) {
-						const float rv = rs[lr * ny + j];
-						g[0] = fmaf(rv, rv, g[0]);
-					}
-				}
-			g[1] = g[0];
-			return;
-		}
 		const float bmax = 2.f, amin = 2.f / m.pratio;
 		const float th = 0.5f * (bmax + amin), de = 0.5f * (bmax - amin);
 		const float sig = th / de;
 		float rho = 1.f / sig;
 		const float ith = 1.f / th;
+		float* dcur = dsa;
+		float* dnxt = dsb;
 #pragma unroll
 		for (int lr = 0; lr < RM; ++lr)
 #pragma unroll
@@ -315,29 +307,13 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 					const int cc = lr * ny + j;
 					const float rv = rs[cc];
 					const float dv = __fdividef(rv * ith, dd[cc]);
-					dsm[1 + (lr + 1) * ny + j] = dv;
+					dcur[1 + (lr + 1) * ny + j] = dv;
 					zs[cc] = dv;
-					rk[cc] = rv;
+					q[lr][k] = rv;
 				}
 			}
 		__syncthreads();
 		for (int step = 1; step < K; ++step) {
-#pragma unroll
-			for (int lr = 0; lr < RM; ++lr)
-#pragma unroll
-				for (int k = 0; k < NC; ++k) {
-					const int j = tid + k * T;
-					if (lr < rows && j < ny) {
-						const int pk = 1 + (lr + 1) * ny + j;
-						float vv = dd[lr * ny + j] * dsm[pk];
-						vv = fmaf(axs[lr], dsm[pk - ny], vv);
-						vv = fmaf(axs[lr + 1], dsm[pk + ny], vv);
-						vv = fmaf(ays[j], dsm[pk - 1], vv);
-						vv = fmaf(ays[j + 1], dsm[pk + 1], vv);
-						q[lr][k] = vv;
-					}
-				}
-			__syncthreads();
 			const float rn = 1.f / (2.f * sig - rho);
 			const float c1 = rn * rho, c2f = 2.f * rn / de;
 #pragma unroll
@@ -347,14 +323,23 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 					const int j = tid + k * T;
 					if (lr < rows && j < ny) {
 						const int cc = lr * ny + j, pk = 1 + (lr + 1) * ny + j;
-						const float rkv = rk[cc] - q[lr][k];
-						const float dv = fmaf(c1, dsm[pk], __fdividef(c2f * rkv, dd[cc]));
-						rk[cc] = rkv;
-						dsm[pk] = dv;
+						const float dc = dcur[pk];
+						float vv = dd[cc] * dc;
+						vv = fmaf(axs[lr], dcur[pk - ny], vv);
+						vv = fmaf(axs[lr + 1], dcur[pk + ny], vv);
+						vv = fmaf(ays[j], dcur[pk - 1], vv);
+						vv = fmaf(ays[j + 1], dcur[pk + 1], vv);
+						const float rkv = q[lr][k] - vv;
+						q[lr][k] = rkv;
+						const float dv = fmaf(c1, dc, __fdividef(c2f * rkv, dd[cc]));
+						dnxt[pk] = dv;
 						zs[cc] += dv;
 					}
 				}
 			__syncthreads();
+			float* t = dcur;
+			dcur = dnxt;
+			dnxt = t;
 			rho = rn;
 		}
 #pragma unroll
@@ -414,6 +399,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 			rn0 = s_sc[2];
 			scale0 = rn0 > 0.0 ? 1.0 / rn0 : 1.0;
 		}
+		float rr = 0.f;
 #pragma unroll
 		for (int lr = 0; lr < RM; ++lr)
 #pragma unroll
@@ -421,12 +407,14 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				const int j = tid + k * T;
 				if (lr < rows && j < ny) {
 					const int a = (r0 + lr + gl) * P + j + gl;
-					rs[lr * ny + j] = (float)((v.r[a] - mr) * scale0);
+					const float rv = (float)((v.r[a] - mr) * scale0);
+					rs[lr * ny + j] = rv;
+					rr = fmaf(rv, rv, rr);
 				}
 			}
+		float g[2] = { rr, rr };
+		if (K > 0) precond(g);
 		__syncthreads();
-		float g[2];
-		precond(g);
 		publish_r();
 		if (!grid_allreduce<float, 2>(g, gc, bank)) return false;
 		read_rh(rbuf);
@@ -455,10 +443,12 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	float gamma = 0.f;   // (r, z)
 	if (!true_residual(true, gamma)) return;
 	if (to.resid <= sc.tol) { to.done = 1; return; }
-	float gamma_ref = rrn, gamma_old = 1.f;
-	// an update when the FP32 residual has dropped by inner_tol, but at least
-	// every 1e-2 and every kStall iterations: FP32 CG cannot drive its
-	// recursive residual much further before it stops tracking the true one
+	float gamma_ref = gamma, gamma_old = 1.f;
+	// an update when (r, z) (the residual's squared norm in the
+	// preconditioner's metric, (r, r) without one) has dropped by inner_tol^2
+	// (inner_tol capped at 1e-2 from below), and at least every kStall
+	// iterations: FP32 CG cannot drive its recursive residual much further
+	// before it stops tracking the true one
 	const double it_tol = fmax(m.inner_tol, 1e-2);
 	const float drop = (float)(it_tol * it_tol);
 	constexpr int kStall = 1000;
@@ -545,7 +535,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 		++since;
 		float gnew = gn[0];
 		rrn = gn[1];
-		if (rrn < drop * gamma_ref || rrn <= near || since >= kStall) {
+		if (gnew < drop * gamma_ref || rrn <= near || since >= kStall) {
 			since = 0;
 			// reliable update: fold x, replace r by the FP64 residual
 			fold_x();
@@ -553,7 +543,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 			if (!true_residual(false, gnew)) return;
 			++to.updates;
 			if (to.resid <= sc.tol) { to.done = 1; break; }
-			gamma_ref = rrn;
+			gamma_ref = gnew;
 		}
 		gamma_old = gamma;
 		gamma = gnew;
@@ -864,7 +854,7 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 		const size_t np = (size_t)(rows_max + 2) * g->ny + 2;
 		size_t smem = sizeof(float) * (np + 2 * (size_t)g->ny + (size_t)rows_max * g->ny
 				+ rows_max + 1 + g->ny + 1 + (size_t)rows_max * g->ny);
-		if (pdeg > 0) smem += sizeof(float) * (2 * (size_t)rows_max * g->ny + np);
+		if (pdeg > 0) smem += sizeof(float) * ((size_t)rows_max * g->ny + 2 * np);
 		mx.pdeg = pdeg;
 		mx.pratio = (float)(cfg.poly_ratio > 1.0 ? cfg.poly_ratio : kPolyRatio);
 		if (tk && smem <= 220 * 1024) {
@@ -877,7 +867,9 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 				TileArgs ta;
 				ta.xbuf = w.xbuf.as<float>();
 				ta.rows_max = rows_max;
-				mx.inner_tol = cfg.inner_tol > 0 ? cfg.inner_tol : 3e-2;
+				// the preconditioned FP32 CG stops tracking its residual
+				// sooner: replace it after a 1e-1 reduction
+				mx.inner_tol = cfg.inner_tol > 0 ? cfg.inner_tol : (pdeg > 0 ? 1e-1 : 3e-2);
 				GridCtl gc = make_gridctl(w.lw);
 				CG_CK(cudaMemsetAsync(w.lw.ctl.p, 0, sizeof(Ctl), s));
 				CG_CK(cudaMemsetAsync(out_dev, 0, sizeof(cg_dev::SolveOut), s));

@@ -88,7 +88,7 @@ class BoundaryIndex:
 
 
 def solver_cfg(name="CG", max_iter=1000, tol=1e-3, mean_removal=False,
-               precision="fp64", inner_tol=1e-4, inner_max_iter=0, flags=0,
+               precision="fp64", inner_tol=0.0, inner_max_iter=0, flags=0,
                poly_degree=0, poly_ratio=0.0):
     c = _lib.SolverCfg()
     c.poly_degree = int(poly_degree)

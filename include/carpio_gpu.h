@@ -137,12 +137,13 @@ typedef struct {
 	int mean_removal;  /* remove the mean of b and x (all-Neumann null space) */
 	double inner_tol;  /* MIXED: residual reduction between two FP64 residual
 	                      replacements (reliable updates; at most 1e-2 is used
-	                      on chip); 0 = 3e-2 */
+	                      on chip); 0 = 1e-1 on chip with the Chebyshev
+	                      preconditioner, else 3e-2 */
 	int inner_max_iter;/* MIXED, global-memory path: cap on one inner solve */
 	uint32_t flags;    /* CARPIO_GPU_FLAG_* */
 	int poly_degree;   /* MIXED, on-chip path: degree of the band-local
 	                      Chebyshev preconditioner of the FP32 CG (each CTA's
-	                      band with zero halo, so no exchange); 0 = default 3,
+	                      band with zero halo, so no exchange); 0 = default 5,
 	                      < 0 = none (plain CG) */
 	double poly_ratio; /* its eigenvalue interval [2 / ratio, 2] of D^-1 A;
 	                      0 = 30 */

@@ -97,7 +97,7 @@ def test_cavity_first_step_fields(gpu_lib):
 
 @pytest.mark.parametrize("n", [128, 256])
 def test_cavity_2000_steps(gpu_lib, n):
-    """BASELINE config: lid-driven cavity, Re 1000, van Leer, CG 1e-10 with
+    """The 2000-step workload: lid-driven cavity, Re 1000, van Leer, CG 1e-10 with
     mean removal, 2000 steps from rest, field by field against the
     reference's own run."""
     name = f"cavity_{n}_vanleer_2000"
