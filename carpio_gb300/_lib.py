@@ -10,7 +10,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libcarpio_gpu.so")
 
 OK, MAXITER, BREAKDOWN_RHO, BREAKDOWN_OMEGA = 0, 1, 2, 3
-EINVAL, ECUDA, ENONFINITE, EZERODIAG, ETIMEOUT, ENOMEM = -1, -2, -3, -4, -5, -6
+EINVAL, ECUDA, ENONFINITE, EZERODIAG, ETIMEOUT, ENOMEM, EIO = -1, -2, -3, -4, -5, -6, -7
 CG, JACOBI, DIA_BICGSTAB, BICGSTAB = 0, 1, 2, 3
 KINDS = {"cg": CG, "jacobi": JACOBI, "dia_bicgstab": DIA_BICGSTAB,
          "bicgstab": BICGSTAB, "CG": CG, "Jacobi": JACOBI,
@@ -95,6 +95,10 @@ SIGNATURES = {
         ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
         ctypes.c_double, ctypes.c_double, ctypes.c_double,
         ctypes.POINTER(_VP)]),
+    "carpio_gpu_grid_create": (ctypes.c_int, [
+        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double,
+        _VP, _VP, ctypes.POINTER(_VP)]),
+    "carpio_gpu_output_scalar": (ctypes.c_int, [_VP, ctypes.c_char_p, _VP]),
     "carpio_gpu_grid_destroy": (ctypes.c_int, [_VP]),
     "carpio_gpu_grid_coords": (ctypes.c_int, [_VP, _VP, _VP, _VP, _VP]),
     "carpio_gpu_poisson_solve": (ctypes.c_int, [

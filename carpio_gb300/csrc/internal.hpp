@@ -86,6 +86,8 @@ struct StencilCoeffs {
 	carpio_gpu_bc bc;
 	double beta = 0;
 	DevBuf D, ax, ay, fold, D32, ax32, ay32;
+	bool uniform = true;          // all weights 1: no wx/wy
+	DevBuf wx, wy, wx32, wy32;    // face-size weights of a non-uniform grid
 };
 
 struct PoissonWs {

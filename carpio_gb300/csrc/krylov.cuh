@@ -54,31 +54,53 @@ struct GridSpace {
 // + ax[i+1] pE + ay[j] pS + ay[j+1] pN. ax/ay are the reference's off-diagonal
 // coefficients (-beta*a/d) per face, 0 on boundary faces (their ghost entries
 // are folded into D by the ghost substitution). Vectors keep a zero ghost ring.
-template<class R>
+template<class R, bool NU = false>
 struct StencilOp {
 	GridSpace sp;
 	const R* D;
-	const R* ax;  // [nx+1]
-	const R* ay;  // [ny+1]
+	const R* ax;  // [nx+1]: x-face coefficients of row 0
+	const R* ay;  // [ny+1]: y-face coefficients of column 0
+	// non-uniform grids (NU): the x-face coefficient of cell row j is
+	// ax[i] wy[j] (face height sy_j / sy_0), the y-face one ay[j] wx[i];
+	// unused (null) on uniform grids, where the weights would all be 1
+	const R* wx = nullptr;  // [nx]
+	const R* wy = nullptr;  // [ny]
+	__device__ __forceinline__ void coeffs(int i, int j, R& xm, R& xp, R& ym, R& yp) const {
+		xm = ax[i];
+		xp = ax[i + 1];
+		ym = ay[j];
+		yp = ay[j + 1];
+		if constexpr (NU) {
+			const R w = wy[j], v = wx[i];
+			xm *= w;
+			xp *= w;
+			ym *= v;
+			yp *= v;
+		}
+	}
 	__device__ __forceinline__ R apply(const R* p, int k, int a) const {
 		int i, j;
 		sp.ij(k, i, j);
+		R xm, xp, ym, yp;
+		coeffs(i, j, xm, xp, ym, yp);
 		R c = D[a] * ldcg(p + a);
-		c = fma(ax[i], ldcg(p + a - sp.P), c);
-		c = fma(ax[i + 1], ldcg(p + a + sp.P), c);
-		c = fma(ay[j], ldcg(p + a - 1), c);
-		c = fma(ay[j + 1], ldcg(p + a + 1), c);
+		c = fma(xm, ldcg(p + a - sp.P), c);
+		c = fma(xp, ldcg(p + a + sp.P), c);
+		c = fma(ym, ldcg(p + a - 1), c);
+		c = fma(yp, ldcg(p + a + 1), c);
 		return c;
 	}
 	// sum of T x over the off-diagonal entries with T = -a / D (Jacobi)
 	__device__ __forceinline__ R jacobi_tx(const R* x, int k, int a) const {
 		int i, j;
 		sp.ij(k, i, j);
+		R xm, xp, ym, yp;
+		coeffs(i, j, xm, xp, ym, yp);
 		R d = D[a], s = 0;
-		s = fma(-ax[i] / d, ldcg(x + a - sp.P), s);
-		s = fma(-ay[j] / d, ldcg(x + a - 1), s);
-		s = fma(-ay[j + 1] / d, ldcg(x + a + 1), s);
-		s = fma(-ax[i + 1] / d, ldcg(x + a + sp.P), s);
+		s = fma(-xm / d, ldcg(x + a - sp.P), s);
+		s = fma(-ym / d, ldcg(x + a - 1), s);
+		s = fma(-yp / d, ldcg(x + a + 1), s);
+		s = fma(-xp / d, ldcg(x + a + sp.P), s);
 		return s;
 	}
 	__device__ __forceinline__ R diag(int k, int a) const { return D[a]; }

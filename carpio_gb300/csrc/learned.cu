@@ -312,6 +312,9 @@ int learned_solve(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& pws, LearnedW
 	op.D = c.D.as<double>();
 	op.ax = c.ax.as<double>();
 	op.ay = c.ay.as<double>();
+	// the network was trained on uniform grids and the kernels here apply
+	// the uniform operator
+	if (!c.uniform) return CARPIO_GPU_EINVAL;
 	const GridSpace sp = op.sp;
 	const bool mean = cfg.mean_removal != 0;
 	const int full = (cfg.flags & CARPIO_GPU_FLAG_FULL_NRM2) || n == 1 ? 1 : 0;

@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <vector>
 
@@ -20,8 +21,9 @@ namespace {
 using namespace cg_dev;
 
 // ------------------------------------------------------------ device side --
-struct MixedArgs {
-	StencilOp<float> op32;
+template<bool NU>
+struct MixedArgsT {
+	StencilOp<float, NU> op32;
 	Vecs<float> f;         // e (x), r, p, q
 	double inner_tol;
 	int inner_max;
@@ -29,13 +31,19 @@ struct MixedArgs {
 	                       // preconditioner (0 = none)
 	float pratio;          // its eigenvalue interval [2 / pratio, 2] of D^-1 A
 };
+using MixedArgs = MixedArgsT<false>;
+// the uniform and non-uniform specialisations differ in code only, so one
+// host-side argument block serves the kernels of either
+static_assert(sizeof(MixedArgsT<true>) == sizeof(MixedArgs), "layout");
+static_assert(sizeof(StencilOp<double, true>) == sizeof(StencilOp<double>), "layout");
 
 // FP32 CG on A32 e = r32 from e = 0 (one inner solve of the refinement).
 // Returns the number of iterations, or -1 on a barrier error.
-__device__ int inner_cg(const GridSpace& sp, const MixedArgs& m, int cap,
+template<bool NU>
+__device__ int inner_cg(const GridSpace& sp, const MixedArgsT<NU>& m, int cap,
 		const GridCtl& gc, int& bank) {
 	const Vecs<float>& f = m.f;
-	const StencilOp<float>& op = m.op32;
+	const StencilOp<float, NU>& op = m.op32;
 	float rr0[1] = { 0 };
 	KLOOP(sp) {
 		int a = sp.addr(k);
@@ -81,8 +89,9 @@ __device__ int inner_cg(const GridSpace& sp, const MixedArgs& m, int cap,
 // FP32 inner CG inside FP64 iterative refinement: r = b - A x, the stopping
 // test and the update of x in FP64; the correction solve in FP32 with FP32
 // accumulation, on the residual scaled to unit norm.
-__device__ void mixed_run(const GridSpace& sp, const StencilOp<double>& op,
-		const Vecs<double>& v, const MixedArgs& m, const SolveCtl& sc,
+template<bool NU>
+__device__ void mixed_run(const GridSpace& sp, const StencilOp<double, NU>& op,
+		const Vecs<double>& v, const MixedArgsT<NU>& m, const SolveCtl& sc,
 		bool mean, const GridCtl& gc, int& bank) {
 	const bool full = (sc.flags & CARPIO_GPU_FLAG_FULL_NRM2) || sp.count() == 1;
 	const int la = sp.last_addr();
@@ -135,9 +144,9 @@ __device__ void mixed_run(const GridSpace& sp, const StencilOp<double>& op,
 	finish(sc, 1, total, resid, hl);
 }
 
-template<int SRC, int KIND>
-__global__ void __launch_bounds__(kThreads) k_poisson(StencilOp<double> op,
-		Vecs<double> v, RhsArgs ra, MixedArgs mx, SolveCtl sc, GridCtl gc) {
+template<int SRC, int KIND, bool NU>
+__global__ void __launch_bounds__(kThreads) k_poisson(StencilOp<double, NU> op,
+		Vecs<double> v, RhsArgs ra, MixedArgsT<NU> mx, SolveCtl sc, GridCtl gc) {
 	gc.start();
 	int bank = 0;
 	const GridSpace& sp = op.sp;
@@ -628,12 +637,20 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_poisson_mixed_tile(
 }
 
 template<int SRC>
-const void* pick_kernel(int kind, int precision) {
-	if (precision == CARPIO_GPU_MIXED) return (const void*)k_poisson<SRC, 4>;
+const void* pick_kernel(int kind, int precision, bool nu) {
+	if (nu) {
+		if (precision == CARPIO_GPU_MIXED) return (const void*)k_poisson<SRC, 4, true>;
+		switch (kind) {
+		case CARPIO_GPU_CG: return (const void*)k_poisson<SRC, CARPIO_GPU_CG, true>;
+		case CARPIO_GPU_JACOBI: return (const void*)k_poisson<SRC, CARPIO_GPU_JACOBI, true>;
+		default: return (const void*)k_poisson<SRC, CARPIO_GPU_BICGSTAB, true>;
+		}
+	}
+	if (precision == CARPIO_GPU_MIXED) return (const void*)k_poisson<SRC, 4, false>;
 	switch (kind) {
-	case CARPIO_GPU_CG: return (const void*)k_poisson<SRC, CARPIO_GPU_CG>;
-	case CARPIO_GPU_JACOBI: return (const void*)k_poisson<SRC, CARPIO_GPU_JACOBI>;
-	default: return (const void*)k_poisson<SRC, CARPIO_GPU_BICGSTAB>;
+	case CARPIO_GPU_CG: return (const void*)k_poisson<SRC, CARPIO_GPU_CG, false>;
+	case CARPIO_GPU_JACOBI: return (const void*)k_poisson<SRC, CARPIO_GPU_JACOBI, false>;
+	default: return (const void*)k_poisson<SRC, CARPIO_GPU_BICGSTAB, false>;
 	}
 }
 
@@ -765,7 +782,28 @@ int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
 	if ((rc = to_device(c.D32, D32.data(), sizeof(float) * D32.size(), s))) return rc;
 	if ((rc = to_device(c.ax32, ax32.data(), sizeof(float) * ax32.size(), s))) return rc;
 	if ((rc = to_device(c.ay32, ay32.data(), sizeof(float) * ay32.size(), s))) return rc;
+	// a non-uniform grid: the face coefficients above belong to row /
+	// column 0; every other row and column scales them by its face size
+	const int gl = g->gl;
+	std::vector<double> wx(g->nx), wy(g->ny);
+	bool uniform = true;
+	for (int i = 0; i < g->nx; ++i) {
+		wx[i] = g->sx[i + gl] / g->sx[gl];
+		uniform = uniform && wx[i] == 1.0;
+	}
+	for (int j = 0; j < g->ny; ++j) {
+		wy[j] = g->sy[j + gl] / g->sy[gl];
+		uniform = uniform && wy[j] == 1.0;
+	}
+	std::vector<float> wx32(wx.begin(), wx.end()), wy32(wy.begin(), wy.end());
+	if (!uniform) {
+		if ((rc = to_device(c.wx, wx.data(), sizeof(double) * wx.size(), s))) return rc;
+		if ((rc = to_device(c.wy, wy.data(), sizeof(double) * wy.size(), s))) return rc;
+		if ((rc = to_device(c.wx32, wx32.data(), sizeof(float) * wx32.size(), s))) return rc;
+		if ((rc = to_device(c.wy32, wy32.data(), sizeof(float) * wy32.size(), s))) return rc;
+	}
 	CG_CK(cudaStreamSynchronize(s));  // host vectors go out of scope
+	c.uniform = uniform;
 	c.bc = bc;
 	c.beta = beta;
 	c.valid = true;
@@ -788,8 +826,8 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 		if ((rc = w.v32.ensure(sizeof(float) * NF * nv32))) return rc;
 		CG_CK(cudaMemsetAsync(w.v32.p, 0, w.v32.bytes, s));
 	}
-	const void* kern = src_mode == SRC_DIV ? pick_kernel<SRC_DIV>(cfg.kind, cfg.precision)
-	                                       : pick_kernel<SRC_FIELD>(cfg.kind, cfg.precision);
+	const void* kern = src_mode == SRC_DIV ? pick_kernel<SRC_DIV>(cfg.kind, cfg.precision, !c.uniform)
+	                                       : pick_kernel<SRC_FIELD>(cfg.kind, cfg.precision, !c.uniform);
 	long n = (long)g->nx * g->ny;
 	// at most two 256-thread blocks per SM: enough warps for the FP64 pipe,
 	// few enough arrivals at each grid barrier
@@ -800,6 +838,8 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 	op.D = c.D.as<double>();
 	op.ax = c.ax.as<double>();
 	op.ay = c.ay.as<double>();
+	op.wx = c.uniform ? nullptr : c.wx.as<double>();
+	op.wy = c.uniform ? nullptr : c.wy.as<double>();
 	Vecs<double> v;
 	double* base = w.v64.as<double>();
 	double** slots[nv64] = { &v.x, &v.b, &v.r, &v.p, &v.q, &v.z, &v.rt, &v.ph,
@@ -810,6 +850,8 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 	mx.op32.D = c.D32.as<float>();
 	mx.op32.ax = c.ax32.as<float>();
 	mx.op32.ay = c.ay32.as<float>();
+	mx.op32.wx = c.uniform ? nullptr : c.wx32.as<float>();
+	mx.op32.wy = c.uniform ? nullptr : c.wy32.as<float>();
 	std::memset(&mx.f, 0, sizeof mx.f);
 	if (mixed) {
 		float* fb = w.v32.as<float>();
@@ -839,7 +881,9 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 	sc.hist_cap = hist_dev ? hist_cap : 0;
 	sc.out = out_dev;
 	// mixed solves whose bands fit the tile kernel run on chip
-	if (mixed && !(cfg.flags & CARPIO_GPU_FLAG_NO_TILE)) {
+	// the on-chip kernel keeps one coefficient per face row / column: uniform
+	// grids only (non-uniform ones run the global-memory FP32 inner CG)
+	if (mixed && c.uniform && !(cfg.flags & CARPIO_GPU_FLAG_NO_TILE)) {
 		const int C = std::min(sm_count(), g->nx);
 		const int rows_max = (g->nx + C - 1) / C;
 		const int nc = (g->ny + kTileThreads - 1) / kTileThreads;
@@ -892,13 +936,34 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 // ------------------------------------------------------------------ C ABI --
 extern "C" {
 
-int carpio_gpu_grid_create_uniform(int nx, int ny, int gl, double xmin,
-		double xmax, double ymin, double ymax, carpio_gpu_grid** out) {
-	using namespace cg_host;
-	if (!out || nx < 1 || ny < 1 || gl < 1 || gl > 8 || !(xmax > xmin)
-			|| !(ymax > ymin) || (long)nx * ny > (1L << 30))
-		return CARPIO_GPU_EINVAL;
-	*out = nullptr;
+}  // extern "C"
+
+namespace cg_host {
+
+// Centres and sizes of the n + 2 gl cells of an axis given the normal cells'
+// sizes (Grid_::_set_non_uniform_grid, s_grid.hpp:397-434): ghosts take the
+// size of the nearest normal cell; centres are running sums shifted so the
+// first normal cell starts at lo.
+void sized_axis(int n, int gl, double lo, const double* cs, std::vector<double>& c,
+		std::vector<double>& s) {
+	const int N = n + 2 * gl;
+	s.assign(N, 0.0);
+	c.assign(N, 0.0);
+	for (int i = 0; i < N; ++i) s[i] = i < gl ? cs[0] : (i - gl >= n ? cs[n - 1] : cs[i - gl]);
+	double csum = 0.0, llg = 0.0;
+	for (int i = 0; i < N; ++i) {
+		c[i] = csum + 0.5 * s[i];
+		csum += s[i];
+	}
+	for (int i = 0; i < gl; ++i) llg += s[i];
+	const double sh = lo - llg;
+	for (int i = 0; i < N; ++i) c[i] += sh;
+}
+
+// A grid handle around host-built axes: stream and device copies.
+static int grid_from_axes(int nx, int ny, int gl, std::vector<double>&& cx,
+		std::vector<double>&& sx, std::vector<double>&& cy, std::vector<double>&& sy,
+		carpio_gpu_grid** out) {
 	carpio_gpu_grid* g = new carpio_gpu_grid();
 	g->nx = nx;
 	g->ny = ny;
@@ -906,8 +971,10 @@ int carpio_gpu_grid_create_uniform(int nx, int ny, int gl, double xmin,
 	g->NI = nx + 2 * gl;
 	g->NJ = ny + 2 * gl;
 	g->P = (g->NJ + 31) / 32 * 32;
-	uniform_axis(nx, gl, xmin, xmax, g->cx, g->sx);
-	uniform_axis(ny, gl, ymin, ymax, g->cy, g->sy);
+	g->cx = std::move(cx);
+	g->sx = std::move(sx);
+	g->cy = std::move(cy);
+	g->sy = std::move(sy);
 	cudaGetDevice(&g->device);
 	int rc = 0;
 	auto fail = [&](int code) {
@@ -934,6 +1001,71 @@ int carpio_gpu_grid_create_uniform(int nx, int ny, int gl, double xmin,
 	(void)rc;
 	*out = g;
 	return 0;
+}
+
+}  // namespace cg_host
+
+extern "C" {
+
+int carpio_gpu_grid_create_uniform(int nx, int ny, int gl, double xmin,
+		double xmax, double ymin, double ymax, carpio_gpu_grid** out) {
+	using namespace cg_host;
+	if (!out || nx < 1 || ny < 1 || gl < 1 || gl > 8 || !(xmax > xmin)
+			|| !(ymax > ymin) || (long)nx * ny > (1L << 30))
+		return CARPIO_GPU_EINVAL;
+	*out = nullptr;
+	std::vector<double> cx, sx, cy, sy;
+	uniform_axis(nx, gl, xmin, xmax, cx, sx);
+	uniform_axis(ny, gl, ymin, ymax, cy, sy);
+	return grid_from_axes(nx, ny, gl, std::move(cx), std::move(sx), std::move(cy),
+			std::move(sy), out);
+}
+
+int carpio_gpu_grid_create(int nx, int ny, int gl, double xmin, double ymin,
+		const double* csx, const double* csy, carpio_gpu_grid** out) {
+	using namespace cg_host;
+	if (!out || !csx || !csy || nx < 1 || ny < 1 || gl < 1 || gl > 8
+			|| (long)nx * ny > (1L << 30))
+		return CARPIO_GPU_EINVAL;
+	for (int i = 0; i < nx; ++i)
+		if (!(csx[i] > 0.0) || !std::isfinite(csx[i])) return CARPIO_GPU_EINVAL;
+	for (int j = 0; j < ny; ++j)
+		if (!(csy[j] > 0.0) || !std::isfinite(csy[j])) return CARPIO_GPU_EINVAL;
+	*out = nullptr;
+	std::vector<double> cx, sx, cy, sy;
+	sized_axis(nx, gl, xmin, csx, cx, sx);
+	sized_axis(ny, gl, ymin, csy, cy, sy);
+	return grid_from_axes(nx, ny, gl, std::move(cx), std::move(sx), std::move(cy),
+			std::move(sy), out);
+}
+
+int carpio_gpu_output_scalar(const carpio_gpu_grid* g, const char* filename,
+		const double* field) {
+	using namespace cg_host;
+	if (!g || !filename || !field) return CARPIO_GPU_EINVAL;
+	const size_t n = (size_t)g->NI * g->NJ;
+	std::vector<double> host;
+	const double* f = field;
+	if (is_device_ptr(field)) {
+		host.resize(n);
+		if (cudaMemcpy(host.data(), field, sizeof(double) * n, cudaMemcpyDeviceToHost)
+				!= cudaSuccess) {
+			note_cuda_error(cudaGetLastError());
+			return CARPIO_GPU_ECUDA;
+		}
+		f = host.data();
+	}
+	FILE* fp = std::fopen(filename, "w");
+	if (!fp) return CARPIO_GPU_EIO;
+	const int gl = g->gl;
+	bool ok = std::fprintf(fp, "## Size : %ld\n## Dim : 2\n## NX :  %d\n## NY :  %d\n",
+			(long)g->nx * g->ny, g->nx, g->ny) > 0;
+	for (int j = 0; j < g->ny && ok; ++j)
+		for (int i = 0; i < g->nx && ok; ++i)
+			ok = std::fprintf(fp, "%10.6e, %10.6e, %10.6e, %10.6e\n", g->cx[i + gl],
+					g->cy[j + gl], 0.0, f[(size_t)(i + gl) * g->NJ + (j + gl)]) > 0;
+	ok = (std::fclose(fp) == 0) && ok;
+	return ok ? 0 : CARPIO_GPU_EIO;
 }
 
 int carpio_gpu_grid_destroy(carpio_gpu_grid* g) {

@@ -134,6 +134,7 @@ const char* carpio_gpu_strerror(int code) {
 	case CARPIO_GPU_EZERODIAG: return "zero diagonal (diagonal preconditioner failure)";
 	case CARPIO_GPU_ETIMEOUT: return "device watchdog expired";
 	case CARPIO_GPU_ENOMEM: return "device allocation failed";
+	case CARPIO_GPU_EIO: return "file could not be written";
 	}
 	return "unknown code";
 }

@@ -5,6 +5,7 @@ Fields are numpy arrays (or CUDA tensors) of the reference's SpaceT shape
 (nx+2gl, ny+2gl), y contiguous, ghosts included.
 """
 import ctypes
+import os
 import sys
 
 import numpy as np
@@ -13,18 +14,26 @@ from . import _lib
 
 
 class Grid:
-    """Grid_<2>(pmin, pmax, n, gl) with uniform cells (s_grid.hpp:25-34)."""
+    """Grid_<2>(pmin, pmax, n, gl) with uniform cells (s_grid.hpp:25-34), or
+    Grid.from_sizes(pmin, gl, csx, csy) from the normal cells' sizes
+    (Grid_<2>(min, gl, csx, csy), s_grid.hpp:35-48, 397-434)."""
 
-    def __init__(self, pmin, pmax, n, gl):
+    def __init__(self, pmin, pmax, n, gl, _sizes=None):
         L = _lib.load()
         self.nx, self.ny = int(n[0]), int(n[1])
         self.gl = int(gl)
         h = ctypes.c_void_p()
-        rc = L.carpio_gpu_grid_create_uniform(
-            self.nx, self.ny, self.gl, float(pmin[0]), float(pmax[0]),
-            float(pmin[1]), float(pmax[1]), ctypes.byref(h))
+        if _sizes is None:
+            rc = L.carpio_gpu_grid_create_uniform(
+                self.nx, self.ny, self.gl, float(pmin[0]), float(pmax[0]),
+                float(pmin[1]), float(pmax[1]), ctypes.byref(h))
+        else:
+            csx, csy = _sizes
+            rc = L.carpio_gpu_grid_create(self.nx, self.ny, self.gl, float(pmin[0]),
+                                          float(pmin[1]), _lib.ptr(csx), _lib.ptr(csy),
+                                          ctypes.byref(h))
         if rc:
-            raise _lib.CarpioGpuError(rc, "grid_create_uniform")
+            raise _lib.CarpioGpuError(rc, "grid_create")
         self.handle = h
         self.cx = np.zeros(self.nx + 2 * self.gl)
         self.sx = np.zeros(self.nx + 2 * self.gl)
@@ -32,6 +41,12 @@ class Grid:
         self.sy = np.zeros(self.ny + 2 * self.gl)
         L.carpio_gpu_grid_coords(h, _lib.ptr(self.cx), _lib.ptr(self.sx),
                                  _lib.ptr(self.cy), _lib.ptr(self.sy))
+
+    @classmethod
+    def from_sizes(cls, pmin, gl, csx, csy):
+        csx = np.ascontiguousarray(csx, dtype=np.float64)
+        csy = np.ascontiguousarray(csy, dtype=np.float64)
+        return cls(pmin, None, (csx.size, csy.size), gl, _sizes=(csx, csy))
 
     def N(self):
         return (self.nx + 2 * self.gl, self.ny + 2 * self.gl)
@@ -50,6 +65,18 @@ class Grid:
         if h is not None and _lib._lib is not None and not sys.is_finalizing():
             _lib._lib.carpio_gpu_grid_destroy(h)
             self.handle = None
+
+
+def Output_Scalar(filename, grid, field):
+    """structure::Output_Scalar (s_io_file.hpp:43-71): writes the field (the
+    grid's layout with ghosts, host or device) in the reference's text
+    format"""
+    f = np.ascontiguousarray(field, dtype=np.float64)
+    if f.shape != grid.N():
+        raise ValueError(f"field shape {f.shape} != grid {grid.N()}")
+    rc = _lib.load().carpio_gpu_output_scalar(grid.handle, os.fsencode(filename), _lib.ptr(f))
+    if rc:
+        raise _lib.CarpioGpuError(rc, "output_scalar")
 
 
 class BoundaryCondition:

@@ -46,6 +46,7 @@ extern "C" {
 #define CARPIO_GPU_EZERODIAG (-4)   /* DiaPre zero diagonal (preconditioner.hpp:223-227 exits) */
 #define CARPIO_GPU_ETIMEOUT (-5)    /* device watchdog expired */
 #define CARPIO_GPU_ENOMEM (-6)      /* device allocation failed */
+#define CARPIO_GPU_EIO (-7)         /* file could not be written */
 
 /* Krylov kinds, in the reference's order */
 #define CARPIO_GPU_CG 0            /* carpio::CG            solver_matrix.hpp:264-316 */
@@ -113,6 +114,20 @@ int carpio_gpu_grid_create_uniform(int nx, int ny, int gl, double xmin,
  * created on it exist. */
 int carpio_gpu_grid_destroy(carpio_gpu_grid* g);
 /* cell centres / sizes incl. ghosts: cx, sx [nx+2gl], cy, sy [ny+2gl] (host) */
+/* Grid_<2>(min, gl, csx, csy) (s_grid.hpp:35-48, 397-434): nx, ny normal
+ * cells of the given sizes (host arrays of nx and ny positive values);
+ * ghost cells take the size of the nearest normal cell. Every operator and
+ * solver of the library works on it (coefficients from the axes); the
+ * learned and batched paths take uniform grids only. */
+int carpio_gpu_grid_create(int nx, int ny, int gl, double xmin, double ymin,
+		const double* csx, const double* csy, carpio_gpu_grid** out);
+/* structure::Output_Scalar (s_io_file.hpp:43-71): the text file the
+ * reference's output events write ("## Size : N", "## Dim : 2",
+ * "## NX :  nx", "## NY :  ny", then per normal cell, x fastest,
+ * "x, y, z, value" in %10.6e with z = 0). field: the SpaceT layout with
+ * ghosts ((nx+2gl) x (ny+2gl) doubles, y contiguous), host or device. */
+int carpio_gpu_output_scalar(const carpio_gpu_grid* g, const char* filename,
+		const double* field);
 int carpio_gpu_grid_coords(const carpio_gpu_grid* g, double* cx, double* sx,
 		double* cy, double* sy);
 

@@ -12,18 +12,21 @@
 //           carpio::CG / Jacobi / Dia_BiCGSTAB / BiCGSTAB on a MatrixMarket
 //           matrix read with lib/io/mmio.h:220 (as test/algebra/_test_solver.hpp
 //           does), CSR built by MatrixSCR_(MatrixSCO_).
-//   poisson <case> <n> <solver> <max_iter> <tol> <seed>
+//   poisson <case> <n> <solver> <max_iter> <tol> <seed> [stretch]
 //           case: c1 | neumann | mixed ; solver: cg | jacobi | dia_bicgstab |
 //           bicgstab. Poisson_ (s_poisson.hpp) with the solver replaced by a
 //           drop-in structure::Solver_ that assembles the CSR with the
 //           reference's _build_exp/_build_matrix and calls the carpio:: free
 //           function (mean removal of b and x for the all-Neumann case).
-//   cavity  <n> <steps> <scheme> <tol> <max_iter> <dt0> <Re> <dump_every>
+//   cavity  <n> <steps> <scheme> <tol> <max_iter> <dt0> <Re> <dump_every> [stretch]
 //           NS_explicit_ (s_ns_explicit.hpp) lid-driven cavity on [0,1]^2,
 //           gl = 2, projection by the CG + mean-removal drop-in.
-//   ops     <n> <seed> <gl>
+//   ops     <n> <seed> <gl> [stretch]
 //           single operators of Operation_ (s_operation.hpp) and
-//           Equation_::apply_bc (s_equation.hpp:340-378) on seeded fields.
+//           Equation_::apply_bc (s_equation.hpp:340-378) on seeded fields;
+//           `stretch` (here and for poisson / cavity) builds the grid from
+//           cell sizes (make_grid). Also writes the
+//           field in_a with Output_Scalar (s_io_file.hpp:43-71) to dump.txt.
 
 #include "structure/s_grid.hpp"
 #include "structure/s_poisson.hpp"
@@ -49,6 +52,9 @@ typedef Poi_<2> Poi;
 typedef Scalar_<2> Scalar;
 typedef std::shared_ptr<Scalar> spScalar;
 typedef Operation_<2> Op;
+
+// structure::Output_Scalar, instantiated in dump_scalar.cpp
+void harness_output_scalar(const std::string& filename, const Scalar& s);
 
 // ---------------------------------------------------------------- output ---
 static std::string g_out;
@@ -116,6 +122,24 @@ static void put_csr(const Mat& m) {
 	put_array("colind", "u32", ci.data(), ci.size(), ci.size());
 	put_array("val", "f64", va.data(), va.size(), va.size());
 }
+// [0,1]^2 with nx x ny cells: uniform (Grid_(min, max, n, gl)), or from
+// cell sizes (Grid_(min, gl, csx, csy), s_grid.hpp:35-48, 397-434):
+// geometric growth along x, a wave along y, both scaled to length 1
+static spGrid make_grid(int nx, int ny, int gl, bool stretch) {
+	Poi pmin(0.0, 0.0), pmax(1.0, 1.0);
+	if (!stretch) return spGrid(new Grid(pmin, pmax, Index(nx, ny), gl));
+	Arr csx(nx), csy(ny);
+	double lx = 0, ly = 0;
+	for (int i = 0; i < nx; ++i) { csx[i] = std::pow(1.07, double(i)); lx += csx[i]; }
+	for (int j = 0; j < ny; ++j) { csy[j] = 1.0 + 0.6 * std::sin(0.9 * j); ly += csy[j]; }
+	for (int i = 0; i < nx; ++i) csx[i] /= lx;
+	for (int j = 0; j < ny; ++j) csy[j] /= ly;
+	return spGrid(new Grid(pmin, gl, csx, csy));
+}
+static bool stretch_arg(int argc, char** argv, int k) {
+	return argc > k + 1 && std::string(argv[k]) == "stretch";
+}
+
 static void put_grid(const Grid& g) {
 	for (St d = 0; d < 2; ++d) {
 		int N = g.N(d);
@@ -285,10 +309,10 @@ static int cmd_poisson(int argc, char** argv) {
 	int max_iter = std::atoi(argv[5]);
 	double tol = std::atof(argv[6]);
 	unsigned seed = unsigned(std::atoi(argv[7]));
-	out_open(argv[8]);
-	Poi pmin(0.0, 0.0), pmax(1.0, 1.0);
-	Index mn(n, n);
-	spGrid g(new Grid(pmin, pmax, mn, 2));
+	out_open(argv[argc - 1]);
+	const bool stretch = stretch_arg(argc, argv, 8);
+	spGrid g = make_grid(n, n, 2, stretch);
+	put_scalar("stretch", stretch ? 1.0 : 0.0);
 	put_grid(*g);
 	std::vector<SolveRecord> rec;
 	bool mean = (cs == "neumann");
@@ -383,10 +407,10 @@ static int cmd_cavity(int argc, char** argv) {
 	double dt0 = std::atof(argv[7]);
 	double Re = std::atof(argv[8]);
 	int dump_every = std::atoi(argv[9]);
-	out_open(argv[10]);
-	Poi pmin(0.0, 0.0), pmax(1.0, 1.0);
-	Index mn(n, n);
-	spGrid g(new Grid(pmin, pmax, mn, 2));
+	out_open(argv[argc - 1]);
+	const bool stretch = stretch_arg(argc, argv, 10);
+	spGrid g = make_grid(n, n, 2, stretch);
+	put_scalar("stretch", stretch ? 1.0 : 0.0);
 	put_grid(*g);
 	std::vector<SolveRecord> rec;
 	NSAlg_ ns(g, max_iter, tol, &rec);
@@ -455,11 +479,11 @@ static int cmd_ops(int argc, char** argv) {
 	int n = std::atoi(argv[2]);
 	unsigned seed = unsigned(std::atoi(argv[3]));
 	int gl = std::atoi(argv[4]);
-	out_open(argv[5]);
+	out_open(argv[argc - 1]);
 	int nx = n, ny = n + 3;  // non-square cell counts on a square box
-	Poi pmin(0.0, 0.0), pmax(1.0, 1.0);
-	Index mn(nx, ny);
-	spGrid g(new Grid(pmin, pmax, mn, gl));
+	const bool stretch = stretch_arg(argc, argv, 5);
+	spGrid g = make_grid(nx, ny, gl, stretch);
+	put_scalar("stretch", stretch ? 1.0 : 0.0);
 	put_grid(*g);
 	put_scalar("nx", nx);
 	put_scalar("ny", ny);
@@ -475,6 +499,7 @@ static int cmd_ops(int argc, char** argv) {
 	};
 	spScalar a = rnd("in_a"), b = rnd("in_b"), uf = rnd("in_uf"),
 			vf = rnd("in_vf");
+	harness_output_scalar(g_out + "/dump.txt", *a);
 	VectorFace_<2> VF(uf, vf, nullptr);
 	std::shared_ptr<VectorFace_<2> > spVF(new VectorFace_<2>(uf, vf, nullptr));
 	// Grad / Div / interpolations

@@ -356,6 +356,23 @@ void rs_grid_uniform(int n, int gl, double lo, double hi, double* c,
 	for (int i = 0; i < N; ++i) c[i] += sh;
 }
 
+void rs_grid_sizes(int n, int gl, double lo, const double* cs, double* c,
+		double* s) {
+	/* s_grid.hpp:397-434: ghost cells take the size of the nearest normal
+	 * cell; centres are running sums, shifted so the first normal cell
+	 * starts at lo */
+	int N = n + 2 * gl;
+	double csum = 0.0, llg = 0.0;
+	for (int i = 0; i < N; ++i) s[i] = i < gl ? cs[0] : (i - gl >= n ? cs[n - 1] : cs[i - gl]);
+	for (int i = 0; i < N; ++i) {
+		c[i] = csum + 0.5 * s[i];
+		csum += s[i];
+	}
+	for (int i = 0; i < gl; ++i) llg += s[i];
+	double sh = lo - llg;
+	for (int i = 0; i < N; ++i) c[i] += sh;
+}
+
 /* field accessors: cell (i, j) of a (nx+2gl) x (ny+2gl) array, i, j in
  * normal-cell coordinates (ghosts negative / >= n) */
 #define AT(f, i, j) (f)[(size_t)((i) + gl) * NJ + (size_t)((j) + gl)]

@@ -44,6 +44,7 @@ double rs_nrm2(int n, const double* x);
 /* Grid_::_set_uniform_grid (lib/structure/s_grid.hpp:372-395): cell sizes
  * s[0..n+2gl) and centres c[0..n+2gl), ghosts included. */
 void rs_grid_uniform(int n, int gl, double lo, double hi, double* c, double* s);
+void rs_grid_sizes(int n, int gl, double lo, const double* cs, double* c, double* s);
 
 /* Boundary description of one field: type per segment (1 Dirichlet,
  * 2 Neumann; segments 0 x-, 1 x+, 2 y-, 3 y+) and a constant value. */

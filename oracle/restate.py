@@ -62,6 +62,8 @@ def lib():
         L.rs_nrm2.restype = ctypes.c_double
         L.rs_grid_uniform.argtypes = [ctypes.c_int, ctypes.c_int,
                                       ctypes.c_double, ctypes.c_double, _d, _d]
+        L.rs_grid_sizes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                    _d, _d, _d]
         L.rs_assemble_poisson.argtypes = [
             ctypes.c_int, ctypes.c_int, ctypes.c_int, _d, _d, _d, _d,
             ctypes.POINTER(BC), ctypes.c_double, _d, ctypes.c_double, _u, _u,
@@ -105,18 +107,28 @@ def make_bc(types, values):
 
 
 class Grid:
-    """Uniform grid arrays as Grid_::_set_uniform_grid builds them
-    (lib/structure/s_grid.hpp:372-395), ghosts included."""
+    """Grid arrays with ghosts as Grid_ builds them: uniform
+    (_set_uniform_grid, lib/structure/s_grid.hpp:372-395) or, given the
+    normal cells' sizes csx, csy, non-uniform (_set_non_uniform_grid,
+    s_grid.hpp:397-434; nx, ny are then their lengths)."""
 
-    def __init__(self, nx, ny, gl, x0=0.0, x1=1.0, y0=0.0, y1=1.0):
+    def __init__(self, nx, ny, gl, x0=0.0, x1=1.0, y0=0.0, y1=1.0, csx=None, csy=None):
+        if csx is not None:
+            csx = np.ascontiguousarray(csx, dtype=np.float64)
+            csy = np.ascontiguousarray(csy, dtype=np.float64)
+            nx, ny = csx.size, csy.size
         self.nx, self.ny, self.gl = nx, ny, gl
         L = lib()
         self.cx = np.zeros(nx + 2 * gl)
         self.sx = np.zeros(nx + 2 * gl)
         self.cy = np.zeros(ny + 2 * gl)
         self.sy = np.zeros(ny + 2 * gl)
-        L.rs_grid_uniform(nx, gl, x0, x1, _p(self.cx), _p(self.sx))
-        L.rs_grid_uniform(ny, gl, y0, y1, _p(self.cy), _p(self.sy))
+        if csx is not None:
+            L.rs_grid_sizes(nx, gl, x0, _p(csx), _p(self.cx), _p(self.sx))
+            L.rs_grid_sizes(ny, gl, y0, _p(csy), _p(self.cy), _p(self.sy))
+        else:
+            L.rs_grid_uniform(nx, gl, x0, x1, _p(self.cx), _p(self.sx))
+            L.rs_grid_uniform(ny, gl, y0, y1, _p(self.cy), _p(self.sy))
 
     @property
     def shape(self):

@@ -31,6 +31,31 @@ def golden_names(prefix):
                   if f.startswith(prefix) and f.endswith(".npz"))
 
 
+def fixture_sizes(d, nx, ny, gl):
+    """the normal cells' sizes of a fixture's stretched grid, or None"""
+    if "stretch" in d and float(d["stretch"]):
+        return d["grid_sx"][gl:gl + nx], d["grid_sy"][gl:gl + ny]
+    return None
+
+
+def gpu_grid(d, nx, ny, gl):
+    """the library grid of a fixture: uniform on [0,1]^2 or from sizes"""
+    from carpio_gb300 import structure as S
+    sz = fixture_sizes(d, nx, ny, gl)
+    if sz is None:
+        return S.Grid((0.0, 0.0), (1.0, 1.0), (nx, ny), gl)
+    return S.Grid.from_sizes((0.0, 0.0), gl, sz[0], sz[1])
+
+
+def oracle_grid(d, nx, ny, gl):
+    """the oracle grid of a fixture"""
+    from oracle import restate as R
+    sz = fixture_sizes(d, nx, ny, gl)
+    if sz is None:
+        return R.Grid(nx, ny, gl)
+    return R.Grid(nx, ny, gl, csx=sz[0], csy=sz[1])
+
+
 def rel_l2(a, b):
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)

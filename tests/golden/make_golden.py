@@ -72,7 +72,13 @@ def _run(args, ref):
                     "exit_code": np.int64(r.returncode)}
         if r.returncode != 0:
             raise RuntimeError(" ".join(cmd) + "\n" + r.stderr)
-        return load_dir(out)
+        d = load_dir(out)
+        dump = os.path.join(out, "dump.txt")
+        if os.path.exists(dump):
+            # Output_Scalar's text file, byte for byte
+            with open(dump, "rb") as f:
+                d["dump_text"] = np.frombuffer(f.read(), dtype=np.uint8).copy()
+        return d
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
 
@@ -126,6 +132,8 @@ def main():
         ("poisson_mixed_24_dia_bicgstab", ["mixed", 24, "dia_bicgstab", 5000, 1e-10, 0]),
         ("poisson_mixed_24_bicgstab", ["mixed", 24, "bicgstab", 5000, 1e-10, 0]),
         ("poisson_mixed_16_jacobi", ["mixed", 16, "jacobi", 20000, 1e-8, 0]),
+        ("poisson_mixed_24_cg_stretch", ["mixed", 24, "cg", 5000, 1e-10, 0, "stretch"]),
+        ("poisson_neumann_32_cg_stretch", ["neumann", 32, "cg", 5000, 1e-10, 7, "stretch"]),
     ]
     csr_kept = {"poisson_c1_64_cg", "poisson_neumann_32_cg", "poisson_mixed_24_cg"}
     for name, c in poisson_cases:
@@ -142,13 +150,16 @@ def main():
         ("cavity_16_upwind1_10", [16, 10, "upwind1", 1e-10, 100000, 0.03125, 1000, 0]),
         ("cavity_20_quick_8", [20, 8, "QUICK", 1e-10, 100000, 0.025, 100, 0]),
         ("cavity_64_vanleer_200", [64, 200, "VanLeer", 1e-10, 100000, 0.0078125, 1000, 0]),
+        ("cavity_24_vanleer_10_stretch", [24, 10, "VanLeer", 1e-10, 100000, 0.01, 1000, 0,
+                                          "stretch"]),
     ]
     for name, c in cav:
         d = run(["cavity"] + c, a.ref)
         if not name.startswith("cavity_32"):
             d = {k: v for k, v in d.items() if not k.startswith("s1_")}
         save(name, d)
-    ops = [] if a.only_long else [("ops_13_gl2", [13, 5, 2]), ("ops_9_gl1", [9, 3, 1])]
+    ops = [] if a.only_long else [("ops_13_gl2", [13, 5, 2]), ("ops_9_gl1", [9, 3, 1]),
+                                  ("ops_12_gl2_stretch", [12, 7, 2, "stretch"])]
     for name, c in ops:
         save(name, run(["ops"] + c, a.ref))
     if a.long:

@@ -4,7 +4,7 @@ plain-path tolerance."""
 import numpy as np
 import pytest
 
-from conftest import PLAIN_RTOL, bits_equal, golden, golden_names, rel_l2
+from conftest import PLAIN_RTOL, bits_equal, golden, golden_names, gpu_grid, rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -17,8 +17,9 @@ def test_operators_bitwise(gpu_lib, name):
     from carpio_gb300 import structure as S, _lib
     d = golden(name)
     nx, ny, gl = int(d["nx"]), int(d["ny"]), int(d["gl"])
-    g = S.Grid((0.0, 0.0), (1.0, 1.0), (nx, ny), gl)
+    g = gpu_grid(d, nx, ny, gl)
     assert bits_equal(g.cx, d["grid_cx"]) and bits_equal(g.cy, d["grid_cy"])
+    assert bits_equal(g.sx, d["grid_sx"]) and bits_equal(g.sy, d["grid_sy"])
     a, b, uf, vf = d["in_a"], d["in_b"], d["in_uf"], d["in_vf"]
     gx, gy, _ = S.operator(g, 0, a=a)
     assert bits_equal(gx, d["grad_x"]) and bits_equal(gy, d["grad_y"])
@@ -44,9 +45,9 @@ def test_operators_bitwise(gpu_lib, name):
 
 
 def make_cavity(n, scheme, dt0, Re=1000.0, tol=1e-10, max_iter=100000,
-                precision="fp64", **kw):
+                precision="fp64", fixture=None, **kw):
     from carpio_gb300 import structure as S
-    g = S.Grid((0.0, 0.0), (1.0, 1.0), (n, n), 2)
+    g = gpu_grid(fixture or {}, n, n, 2)
     ns = S.NS_explicit(g)
     ns.set_advection_scheme(scheme)
     ns.set_time(0, dt0)
@@ -71,7 +72,8 @@ def test_cavity_matches_reference(gpu_lib, name):
     a = d["case_args"]
     n, steps, scheme = int(a[1]), int(a[2]), str(a[3])
     tol, max_iter, dt0, Re = float(a[4]), int(a[5]), float(a[6]), float(a[7])
-    g, ns = make_cavity(n, scheme, dt0, Re, tol, max_iter)
+    g, ns = make_cavity(n, scheme, dt0, Re, tol, max_iter, fixture=d)
+    assert bits_equal(g.cx, d["grid_cx"]) and bits_equal(g.sy, d["grid_sy"])
     assert ns.run(steps) == 0
     st = ns.state()
     # dt: the diffusion limit is bitwise; the CFL limit follows max|u|
@@ -124,3 +126,23 @@ def test_cavity_mixed_precision_tracks_fp64(gpu_lib):
         sa, sb = a.state(), b.state()
         for k in ("u", "v"):
             assert rel_l2(g.interior(sb[k]), g.interior(sa[k])) < 1e-6
+
+
+@pytest.mark.parametrize("name", golden_names("ops_"))
+def test_output_scalar_matches_reference(gpu_lib, name, tmp_path):
+    """structure::Output_Scalar's text file, byte for byte, from a host and
+    from a device copy of the field"""
+    import torch
+    from carpio_gb300 import structure as S
+    d = golden(name)
+    if "dump_text" not in d:
+        pytest.skip("fixture without a dump")
+    nx, ny, gl = int(d["nx"]), int(d["ny"]), int(d["gl"])
+    g = gpu_grid(d, nx, ny, gl)
+    ref = d["dump_text"].tobytes()
+    f = tmp_path / "a.txt"
+    S.Output_Scalar(str(f), g, d["in_a"])
+    assert f.read_bytes() == ref
+    dev = torch.from_numpy(np.ascontiguousarray(d["in_a"])).cuda()
+    rc = gpu_lib.carpio_gpu_output_scalar(g.handle, str(f).encode(), dev.data_ptr())
+    assert rc == 0 and f.read_bytes() == ref

@@ -3,7 +3,7 @@ carpio_gpu_poisson_solve) against the reference's runs and the oracle."""
 import numpy as np
 import pytest
 
-from conftest import PLAIN_RTOL, golden, golden_names, rel_l2
+from conftest import PLAIN_RTOL, golden, golden_names, gpu_grid, oracle_grid, rel_l2
 from oracle import restate as R
 
 pytestmark = pytest.mark.gpu
@@ -18,9 +18,9 @@ NAMES = {"cg": "CG", "jacobi": "Jacobi", "dia_bicgstab": "Dia_BiCGSTAB",
 
 
 def make_poisson(n, case, kind, max_iter, tol, source, phi=None, nx=None,
-                 gl=2, **kw):
+                 gl=2, fixture=None, **kw):
     from carpio_gb300 import structure as S
-    g = S.Grid((0.0, 0.0), (1.0, 1.0), (nx or n, n), gl)
+    g = gpu_grid(fixture or {}, nx or n, n, gl)
     P = S.Poisson(g)
     types, vals = BCS[case]
     for seg in range(4):
@@ -49,13 +49,14 @@ def test_poisson_matches_reference(gpu_lib, name):
     d = golden(name)
     case, n, kind = str(d["case_args"][1]), int(d["case_args"][2]), str(d["case_args"][3])
     max_iter, tol = int(d["case_args"][4]), float(d["case_args"][5])
-    g, P = make_poisson(n, case, kind, max_iter, tol, d["source"])
+    g, P = make_poisson(n, case, kind, max_iter, tol, d["source"], fixture=d)
+    assert np.array_equal(g.cx, d["grid_cx"]) and np.array_equal(g.sy, d["grid_sy"])
     rc = P.run()
     st = P.stats
     assert rc == int(d["ret"])
     ref_len = int(d["lresid_len"])
     assert abs(st.hist_len - ref_len) <= iter_band(kind, ref_len), (st.hist_len, ref_len)
-    x = R.field_to_vec(R.Grid(n, n, 2), P.phi)
+    x = R.field_to_vec(oracle_grid(d, n, n, 2), P.phi)
     err = rel_l2(x, d["x"])
     # at the reference's own tolerance both stop near tol; the difference
     # is bounded by the tolerance (the tight test below holds the 1e-10 bar)
@@ -64,19 +65,22 @@ def test_poisson_matches_reference(gpu_lib, name):
     assert np.all(P.phi[:2] == 0) and np.all(P.phi[-2:] == 0)
 
 
-@pytest.mark.parametrize("case,n,kind", [("c1", 64, "cg"), ("c1", 64, "bicgstab"),
-                                         ("c1", 64, "dia_bicgstab"),
-                                         ("neumann", 48, "cg"), ("mixed", 24, "cg"),
-                                         ("mixed", 24, "dia_bicgstab"),
-                                         ("mixed", 24, "bicgstab")])
-def test_poisson_tight_tolerance_parity(gpu_lib, case, n, kind):
+@pytest.mark.parametrize("case,n,kind,sfx", [("c1", 64, "cg", ""), ("c1", 64, "bicgstab", ""),
+                                             ("c1", 64, "dia_bicgstab", ""),
+                                             ("neumann", 48, "cg", ""), ("mixed", 24, "cg", ""),
+                                             ("mixed", 24, "dia_bicgstab", ""),
+                                             ("mixed", 24, "bicgstab", ""),
+                                             ("mixed", 24, "cg", "_stretch"),
+                                             ("neumann", 32, "cg", "_stretch")])
+def test_poisson_tight_tolerance_parity(gpu_lib, case, n, kind, sfx):
     """Matrix-free GPU solve and the oracle (assembled CSR, reference
-    arithmetic) both to 1e-13: relative L2 <= 1e-10 (the plain-path bar)."""
-    d = golden(f"poisson_{case}_{n}_cg" if case != "mixed" else "poisson_mixed_24_cg")
+    arithmetic) both to 1e-13: relative L2 <= 1e-10 (the plain-path bar);
+    `_stretch`: on the fixture's non-uniform grid."""
+    d = golden((f"poisson_{case}_{n}_cg" if case != "mixed" else "poisson_mixed_24_cg") + sfx)
     src = d["source"]
-    g, P = make_poisson(n, case, kind, 50000, 1e-13, src)
+    g, P = make_poisson(n, case, kind, 50000, 1e-13, src, fixture=d)
     assert P.run() == 0
-    og = R.Grid(n, n, 2)
+    og = oracle_grid(d, n, n, 2)
     rp, ci, va, b = R.assemble_poisson(og, R.make_bc(*BCS[case]), 1.0, src=src)
     if case == "neumann":
         b = b - b.mean()

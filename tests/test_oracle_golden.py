@@ -52,9 +52,18 @@ def test_csr_solvers_bitwise(name):
     check_hist(d, hist)
 
 
+def oracle_grid(d, nx, ny, gl):
+    """the fixture's grid: uniform on [0,1]^2, or (stretch) from the normal
+    cells' sizes the reference used"""
+    if "stretch" in d and float(d["stretch"]):
+        sx, sy = d["grid_sx"], d["grid_sy"]
+        return R.Grid(nx, ny, gl, csx=sx[gl:gl + nx], csy=sy[gl:gl + ny])
+    return R.Grid(nx, ny, gl)
+
+
 def poisson_inputs(d):
     case, n = str(d["case_args"][1]), int(d["case_args"][2])
-    g = R.Grid(n, n, 2)
+    g = oracle_grid(d, n, n, 2)
     assert bits_equal(g.cx, d["grid_cx"]) and bits_equal(g.sy, d["grid_sy"])
     rp, ci, va, b = R.assemble_poisson(g, BC_CASES[case], 1.0, src=d["source"])
     return case, g, rp, ci, va, b
@@ -96,7 +105,7 @@ def cavity_case(d):
 def test_cavity_steps_bitwise(name):
     d = golden(name)
     n, steps, scheme, tol, max_iter, dt0, Re = cavity_case(d)
-    g = R.Grid(n, n, 2)
+    g = oracle_grid(d, n, n, 2)
     st = R.new_state(g, dt0)
     code, sdt, sit, sres = R.ns_run(g, st, steps, Re=Re, scheme=scheme,
                                     cg_tol=tol, cg_max_iter=max_iter)
@@ -144,8 +153,9 @@ def test_cavity_first_step_intermediates_bitwise():
 def test_operators_bitwise(name):
     d = golden(name)
     nx, ny, gl = int(d["nx"]), int(d["ny"]), int(d["gl"])
-    g = R.Grid(nx, ny, gl)
+    g = oracle_grid(d, nx, ny, gl)
     assert bits_equal(g.cx, d["grid_cx"]) and bits_equal(g.cy, d["grid_cy"])
+    assert bits_equal(g.sx, d["grid_sx"]) and bits_equal(g.sy, d["grid_sy"])
     a, b, uf, vf = d["in_a"], d["in_b"], d["in_uf"], d["in_vf"]
     gx, gy = R.grad(g, a)
     assert bits_equal(gx, d["grad_x"]) and bits_equal(gy, d["grad_y"])
