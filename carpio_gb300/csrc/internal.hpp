@@ -85,6 +85,8 @@ struct StencilCoeffs {
 	bool valid = false;
 	carpio_gpu_bc bc;
 	double beta = 0;
+	bool helm = false;            // StencilHelmholtz_: diagonal + sx sy alpha
+	double alpha = 0;
 	DevBuf D, ax, ay, fold, D32, ax32, ay32;
 	bool uniform = true;          // all weights 1: no wx/wy
 	DevBuf wx, wy, wx32, wy32;    // face-size weights of a non-uniform grid
@@ -96,7 +98,7 @@ struct PoissonWs {
 };
 
 int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
-		StencilCoeffs& c, cudaStream_t s);
+		StencilCoeffs& c, cudaStream_t s, bool helm = false, double alpha = 0.0);
 
 // Centres and sizes of the n + 2 gl cells of one uniform axis.
 void uniform_axis(int n, int gl, double lo, double hi, std::vector<double>& c,
@@ -108,7 +110,7 @@ void stencil_host(int nx, int ny, int gl, int P, const std::vector<double>& cx,
 		const std::vector<double>& sx, const std::vector<double>& cy,
 		const std::vector<double>& sy, const carpio_gpu_bc& bc, double beta,
 		std::vector<double>& D, std::vector<double>& ax, std::vector<double>& ay,
-		std::vector<double>& fold);
+		std::vector<double>& fold, bool helm = false, double alpha = 0.0);
 
 // Workspace of the learned-preconditioner solve (learned.cu).
 struct LearnedWs {

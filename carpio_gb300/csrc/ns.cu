@@ -404,6 +404,89 @@ __global__ void __launch_bounds__(kThreads) k_correct(Geo g, const double* phi,
 	}
 }
 
+// ------------------------------------------------------------- NS_kim_ --
+// NS_kim_::_veo_star_center (s_ns_kim.hpp:188-242): the right-hand side of
+// each component's Helmholtz predictor, over the normal cells,
+//   adv = 1.5 adv(uf, u) - 0.5 adv(umf, um)   (adv(uf, u) alone on step 0)
+//   scr = (adv - (0.5 NablaMuNabla(mu, u) + 0) / rho) dt - u
+// um, umf: the velocities copied at the start of the step (before the
+// ghost fill of u), as run_one_step does.
+template<int SCH>
+__global__ void __launch_bounds__(kThreads) k_kim_source(Geo g, const double* u,
+		const double* v, const double* uf, const double* vf, const double* um,
+		const double* vm, const double* umf, const double* vmf, double* xs,
+		double* ys, const StepScalars* ss, double rho, double mu, int first) {
+	const double dt = ss->dt;
+	const long n = (long)g.nx * g.ny;
+	for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n;
+			k += (long)gridDim.x * blockDim.x) {
+		int i = (int)(k / g.ny), j = (int)(k - (long)i * g.ny);
+		int a = g.at(i, j);
+#pragma unroll
+		for (int d = 0; d < 2; ++d) {
+			const double* s = d == 0 ? u : v;
+			const double* sm = d == 0 ? um : vm;
+			double advn = adv_cell<SCH>(g, uf, vf, s, i, j);
+			double dif = diffusion(g, mu, s, i, j);
+			double src = 0.0;
+			double veos;
+			if (first) {
+				veos = (advn - (0.5 * dif + src) / rho) * dt - s[a];
+			} else {
+				double advnm1 = adv_cell<SCH>(g, umf, vmf, sm, i, j);
+				double adv = 1.5 * advn - 0.5 * advnm1;
+				veos = (adv - (0.5 * dif + src) / rho) * dt - s[a];
+			}
+			(d == 0 ? xs : ys)[a] = veos;
+		}
+	}
+}
+
+// The end of NS_kim_::run_one_step (s_ns_kim.hpp:160-187) over every array
+// element: as k_correct, with p = phi / dt - NablaMuNabla(mu, phi) 0.5 / rho
+// on the normal cells, and the corrected velocities also written back into
+// the star fields (the reference corrects them in place and copies).
+__global__ void __launch_bounds__(kThreads) k_kim_correct(Geo g, const double* phi,
+		double* us, double* vs, double* usf, double* vsf, double* u, double* v,
+		double* uf, double* vf, double* p, const StepScalars* ss, double rho,
+		double mu) {
+	const double inv = 1.0 / ss->dt;
+	const double c = 0.5 / rho;
+	const long n = (long)g.NI * g.NJ;
+	for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n;
+			k += (long)gridDim.x * blockDim.x) {
+		int I = (int)(k / g.NJ), J = (int)(k - (long)I * g.NJ);
+		int i = I - g.gl, j = J - g.gl;
+		int a = I * g.P + J;
+		bool jin = j >= 0 && j < g.ny, iin = i >= 0 && i < g.nx;
+		double gx = (jin && i >= -1 && i < g.nx) ? gx_at(g, phi, i, j) : 0.0;
+		double gy = (iin && j >= -1 && j < g.ny) ? gy_at(g, phi, i, j) : 0.0;
+		double pv = phi[a];
+		if (iin && jin) {
+			pv = pv * inv;
+			double lap = diffusion(g, mu, phi, i, j);
+			lap = lap * c;
+			pv = pv - lap;
+		}
+		p[a] = pv;
+		double ufn = usf[a] - gx, vfn = vsf[a] - gy;
+		double gcx = 0.0, gcy = 0.0;
+		if (iin && jin) {
+			gcx = (gx + gx_at(g, phi, i - 1, j)) * 0.5;
+			gcy = (gy + gy_at(g, phi, i, j - 1)) * 0.5;
+		}
+		double un = us[a] - gcx, vn = vs[a] - gcy;
+		usf[a] = ufn;
+		vsf[a] = vfn;
+		uf[a] = ufn;
+		vf[a] = vfn;
+		us[a] = un;
+		vs[a] = vn;
+		u[a] = un;
+		v[a] = vn;
+	}
+}
+
 // ----------------------------------------------------- single operators --
 __global__ void k_op(Geo g, int which, int sch, double coef, const double* a,
 		const double* b, const double* c, double* o1, double* o2) {
@@ -515,6 +598,32 @@ cudaError_t launch_predictor(int sch, const Geo& geo, int blocks, cudaStream_t s
 	return cudaErrorInvalidValue;
 }
 
+template<int SCH>
+cudaError_t launch_kim_src(const Geo& geo, int blocks, cudaStream_t s, const double* u,
+		const double* v, const double* uf, const double* vf, const double* um,
+		const double* vm, const double* umf, const double* vmf, double* xs,
+		double* ys, const StepScalars* ss, double rho, double mu, int first) {
+	k_kim_source<SCH><<<blocks, kThreads, 0, s>>>(geo, u, v, uf, vf, um, vm, umf, vmf,
+			xs, ys, ss, rho, mu, first);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_kim_source(int sch, const Geo& geo, int blocks, cudaStream_t s,
+		const double* u, const double* v, const double* uf, const double* vf,
+		const double* um, const double* vm, const double* umf, const double* vmf,
+		double* xs, double* ys, const StepScalars* ss, double rho, double mu, int first) {
+	switch (sch) {
+#define CASE(S) case S: return launch_kim_src<S>(geo, blocks, s, u, v, uf, vf, um, vm, \
+		umf, vmf, xs, ys, ss, rho, mu, first);
+	CASE(CARPIO_GPU_UPWIND1) CASE(CARPIO_GPU_CENTER) CASE(CARPIO_GPU_CENTER4)
+	CASE(CARPIO_GPU_UPWIND2) CASE(CARPIO_GPU_VANLEER) CASE(CARPIO_GPU_SUPERBEE)
+	CASE(CARPIO_GPU_WAHYD) CASE(CARPIO_GPU_QUICK) CASE(CARPIO_GPU_CUI)
+	CASE(CARPIO_GPU_MINMOD)
+#undef CASE
+	}
+	return cudaErrorInvalidValue;
+}
+
 bool valid_bc(const carpio_gpu_bc& b) {
 	for (int k = 0; k < 4; ++k)
 		if (b.type[k] != 1 && b.type[k] != 2) return false;
@@ -544,6 +653,13 @@ struct carpio_gpu_ns {
 	carpio_gpu_learned_cfg lcfg{};
 	bool learned = false;
 	cg_host::LearnedWs lws;
+	// NS_kim_ stepping (carpio_gpu_ns_set_stepper)
+	int stepper = CARPIO_GPU_STEPPER_EXPLICIT;
+	cg_host::DevBuf kim_fields;   // um vm umf vmf xscr yscr
+	double* k[6] = {};
+	cg_host::StencilCoeffs kim_coeffs;   // the predictor's Helmholtz rows
+	cg_host::DevBuf kim_out;      // SolveOut of the predictor solves
+	long steps_done = 0;          // Time_::current_step
 	~carpio_gpu_ns() {
 		for (cudaEvent_t e : ev) cudaEventDestroy(e);
 	}
@@ -673,8 +789,69 @@ int carpio_gpu_ns_run(carpio_gpu_ns* ns, int steps, double* step_dt,
 		CG_CK(cudaEventCreate(&e));
 		ns->ev.push_back(e);
 	}
+	const bool kim = ns->stepper == CARPIO_GPU_STEPPER_KIM;
+	carpio_gpu_solver_cfg jcfg{};
+	cg_dev::SolveOut* kout = nullptr;
+	if (kim) {
+		// the predictor's Poisson_ (s_ns_kim.hpp:104, 232-235): Helmholtz rows
+		// with alpha 1 and uniform beta dt 0.5 / rho, its own (default,
+		// Neumann 0) boundary conditions for "phi", the default solver
+		// Solver_Jacobi_ with max_iter 1000 and tolerance 1e-4 (s_solver.hpp:73-74)
+		double dt;
+		CG_CK(cudaMemcpyAsync(&dt, &ss->dt, sizeof dt, cudaMemcpyDeviceToHost, s));
+		CG_CK(cudaStreamSynchronize(s));
+		const double smu = dt * 0.5 / c.rho;
+		carpio_gpu_bc bc_n;
+		for (int k = 0; k < 4; ++k) { bc_n.type[k] = 2; bc_n.value[k] = 0.0; }
+		if ((rc = stencil_prepare(g, bc_n, smu, ns->kim_coeffs, s, true, 1.0))) return rc;
+		if ((rc = ns->kim_out.ensure(2 * sizeof(cg_dev::SolveOut)))) return rc;
+		kout = ns->kim_out.as<cg_dev::SolveOut>();
+		jcfg.kind = CARPIO_GPU_JACOBI;
+		jcfg.precision = CARPIO_GPU_FP64;
+		jcfg.max_iter = 1000;
+		jcfg.tol = 1e-4;
+	}
+	const size_t fbytes = sizeof(double) * (size_t)g->NI * g->P;
 	for (int st = 0; st < steps; ++st) {
 		CG_CK(cudaEventRecord(ns->ev[3 * st], s));
+		if (kim) {
+			// NS_kim_::run_one_step (s_ns_kim.hpp:125-187): no restrict_time
+			double* um = ns->k[0];
+			double* vm = ns->k[1];
+			double* umf = ns->k[2];
+			double* vmf = ns->k[3];
+			double* xs = ns->k[4];
+			double* ys = ns->k[5];
+			CG_CK(cudaMemcpyAsync(ns->rec_dt.as<double>() + st, &ss->dt, sizeof(double),
+					cudaMemcpyDeviceToDevice, s));
+			CG_CK(cudaMemcpyAsync(um, u, fbytes, cudaMemcpyDeviceToDevice, s));
+			CG_CK(cudaMemcpyAsync(vm, v, fbytes, cudaMemcpyDeviceToDevice, s));
+			CG_CK(cudaMemcpyAsync(umf, uf, fbytes, cudaMemcpyDeviceToDevice, s));
+			CG_CK(cudaMemcpyAsync(vmf, vf, fbytes, cudaMemcpyDeviceToDevice, s));
+			CG_CK(launch_bc(geo, u, c.bc_u, v, &c.bc_v, s));
+			CG_CK(launch_kim_source(c.scheme, geo, nb, s, u, v, uf, vf, um, vm, umf, vmf,
+					xs, ys, ss, c.rho, c.mu, ns->steps_done == 0 ? 1 : 0));
+			if ((rc = poisson_launch(g, ns->kim_coeffs, ns->pws, SRC_FIELD, xs, nullptr, us,
+					jcfg, nullptr, 0, kout, s)))
+				return rc;
+			if ((rc = poisson_launch(g, ns->kim_coeffs, ns->pws, SRC_FIELD, ys, nullptr, vs,
+					jcfg, nullptr, 0, kout + 1, s)))
+				return rc;
+			CG_CK(launch_bc(geo, us, c.bc_u, vs, &c.bc_v, s));
+			k_c2f<<<nb, kThreads, 0, s>>>(geo, us, vs, usf, vsf);
+			CG_CK(cudaGetLastError());
+			CG_CK(cudaEventRecord(ns->ev[3 * st + 1], s));
+			if ((rc = poisson_launch(g, ns->coeffs, ns->pws, SRC_DIV, usf, vsf, phi,
+					c.projection, nullptr, 0, rec + st, s)))
+				return rc;
+			CG_CK(cudaEventRecord(ns->ev[3 * st + 2], s));
+			CG_CK(launch_bc(geo, phi, bc_phi, nullptr, nullptr, s));
+			k_kim_correct<<<nbf, kThreads, 0, s>>>(geo, phi, us, vs, usf, vsf, u, v, uf,
+					vf, p, ss, c.rho, c.mu);
+			CG_CK(cudaGetLastError());
+			++ns->steps_done;
+			continue;
+		}
 		k_restrict_time<<<nb, kThreads, 0, s>>>(geo, u, v, ss, ns->rule,
 				ns->rec_dt.as<double>(), st);
 		CG_CK(cudaGetLastError());
@@ -699,6 +876,7 @@ int carpio_gpu_ns_run(carpio_gpu_ns* ns, int steps, double* step_dt,
 		k_correct<<<nbf, kThreads, 0, s>>>(geo, phi, us, vs, usf, vsf, u, v, uf,
 				vf, p, ss);
 		CG_CK(cudaGetLastError());
+		++ns->steps_done;
 	}
 	CG_CK(cudaEventRecord(ns->ev[3 * steps], s));
 	std::vector<cg_dev::SolveOut> h(steps);
@@ -709,6 +887,14 @@ int carpio_gpu_ns_run(carpio_gpu_ns* ns, int steps, double* step_dt,
 			cudaMemcpyDeviceToHost, s));
 	CG_CK(cudaStreamSynchronize(s));
 	int first = 0;
+	if (kim) {
+		// the predictor's own result codes are not checked by the reference
+		// (a Jacobi that reaches max_iter is kept); device errors are
+		cg_dev::SolveOut ko[2];
+		CG_CK(cudaMemcpy(ko, kout, sizeof ko, cudaMemcpyDeviceToHost));
+		for (const cg_dev::SolveOut& o : ko)
+			if (o.code < 0) return o.code;
+	}
 	for (int st = 0; st < steps; ++st) {
 		if (step_dt) step_dt[st] = hdt[st];
 		if (step_iters) step_iters[st] = h[st].iters;
@@ -719,6 +905,26 @@ int carpio_gpu_ns_run(carpio_gpu_ns* ns, int steps, double* step_dt,
 	ns->last_rec = h;
 	ns->last_steps = steps;
 	return first;
+}
+
+int carpio_gpu_ns_set_stepper(carpio_gpu_ns* ns, int stepper) {
+	using namespace cg_host;
+	if (!ns || (stepper != CARPIO_GPU_STEPPER_EXPLICIT && stepper != CARPIO_GPU_STEPPER_KIM))
+		return CARPIO_GPU_EINVAL;
+	if (stepper == CARPIO_GPU_STEPPER_KIM) {
+		if (ns->learned) return CARPIO_GPU_EINVAL;
+		carpio_gpu_grid* g = ns->g;
+		const size_t fn = (size_t)g->NI * g->P;
+		if (!ns->kim_fields.p) {
+			int rc = ns->kim_fields.ensure(sizeof(double) * 6 * fn);
+			if (rc) return rc;
+			CG_CK(cudaMemsetAsync(ns->kim_fields.p, 0, ns->kim_fields.bytes, ns->s));
+			CG_CK(cudaStreamSynchronize(ns->s));
+		}
+		for (int k = 0; k < 6; ++k) ns->k[k] = ns->kim_fields.as<double>() + k * fn;
+	}
+	ns->stepper = stepper;
+	return 0;
 }
 
 int carpio_gpu_ns_set_learned(carpio_gpu_ns* ns, carpio_gpu_unet* net,

@@ -695,7 +695,7 @@ void stencil_host(int nx, int ny, int gl, int P, const std::vector<double>& cx,
 		const std::vector<double>& sx, const std::vector<double>& cy,
 		const std::vector<double>& sy, const carpio_gpu_bc& bc, double beta,
 		std::vector<double>& D, std::vector<double>& ax, std::vector<double>& ay,
-		std::vector<double>& fold) {
+		std::vector<double>& fold, bool helm, double alpha) {
 	auto CX = [&](int i) { return cx[i + gl]; };
 	auto CY = [&](int j) { return cy[j + gl]; };
 	auto SX = [&](int i) { return sx[i + gl]; };
@@ -743,6 +743,13 @@ void stencil_host(int nx, int ny, int gl, int P, const std::vector<double>& cx,
 			coec += -cxp;
 			coec += -cym;
 			coec += -cyp;
+			if (helm) {
+				// StencilHelmholtz_::coe_row: coec + (1 * sx * sy) alpha
+				double v = 1.0;
+				v *= SX(i);
+				v *= SY(j);
+				coec = coec + v * alpha;
+			}
 			// boundary constants accumulate per segment cell; for a corner
 			// cell the x- fold and the y- fold land in different arrays and
 			// are added in map order (x-, y-, y+, x+) on the device
@@ -765,11 +772,13 @@ void stencil_host(int nx, int ny, int gl, int P, const std::vector<double>& cx,
 }
 
 int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
-		StencilCoeffs& c, cudaStream_t s) {
-	if (c.valid && same_bc(c.bc, bc) && c.beta == beta) return 0;
+		StencilCoeffs& c, cudaStream_t s, bool helm, double alpha) {
+	if (c.valid && same_bc(c.bc, bc) && c.beta == beta && c.helm == helm
+			&& (!helm || c.alpha == alpha))
+		return 0;
 	std::vector<double> D, ax, ay, fold;
 	stencil_host(g->nx, g->ny, g->gl, g->P, g->cx, g->sx, g->cy, g->sy, bc, beta,
-			D, ax, ay, fold);
+			D, ax, ay, fold, helm, alpha);
 	std::vector<float> D32(D.size()), ax32(ax.size()), ay32(ay.size());
 	for (size_t k = 0; k < D.size(); ++k) D32[k] = (float)D[k];
 	for (size_t k = 0; k < ax.size(); ++k) ax32[k] = (float)ax[k];
@@ -806,6 +815,8 @@ int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
 	c.uniform = uniform;
 	c.bc = bc;
 	c.beta = beta;
+	c.helm = helm;
+	c.alpha = alpha;
 	c.valid = true;
 	return 0;
 }
@@ -872,6 +883,7 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 	ra.src_b = src_b;
 	ra.phi = phi;
 	ra.mean = cfg.mean_removal ? 1 : 0;
+	ra.helm = c.helm ? 1 : 0;
 	SolveCtl sc;
 	sc.kind = cfg.kind;
 	sc.max_iter = cfg.max_iter;
@@ -1084,14 +1096,18 @@ int carpio_gpu_grid_coords(const carpio_gpu_grid* g, double* cx, double* sx,
 	return 0;
 }
 
-int carpio_gpu_poisson_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
-		double beta, const double* source, double* phi,
+}  // extern "C"
+
+// Poisson_::run for a set_depend'ed field; helm: the StencilHelmholtz_
+// variant (Poisson_ with an alpha term, s_poisson.hpp:343-347, 577-590)
+static int structured_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
+		bool helm, double alpha, double beta, const double* source, double* phi,
 		const carpio_gpu_solver_cfg* cfg, double* resid_hist, int hist_cap,
 		carpio_gpu_solver_stats* stats) {
 	using namespace cg_host;
 	if (!g || !bc || !source || !phi || !cfg || cfg->max_iter < 0
 			|| cfg->kind < 0 || cfg->kind > 3 || hist_cap < 0
-			|| (hist_cap > 0 && !resid_hist) || !(beta == beta))
+			|| (hist_cap > 0 && !resid_hist) || !(beta == beta) || !(alpha == alpha))
 		return CARPIO_GPU_EINVAL;
 	if (cfg->precision == CARPIO_GPU_MIXED && cfg->kind != CARPIO_GPU_CG)
 		return CARPIO_GPU_EINVAL;
@@ -1100,7 +1116,7 @@ int carpio_gpu_poisson_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
 	std::lock_guard<std::mutex> lock(g->mu);
 	cudaStream_t s = g->stream;
 	int rc;
-	if ((rc = stencil_prepare(g, *bc, beta, g->coeffs, s))) return rc;
+	if ((rc = stencil_prepare(g, *bc, beta, g->coeffs, s, helm, alpha))) return rc;
 	PoissonWs& w = g->pws;
 	const size_t NF = (size_t)g->NI * g->P;
 	if ((rc = w.src.ensure(sizeof(double) * NF))) return rc;
@@ -1150,6 +1166,24 @@ int carpio_gpu_poisson_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
 		stats->ms = ms;
 	}
 	return code;
+}
+
+extern "C" {
+
+int carpio_gpu_poisson_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
+		double beta, const double* source, double* phi,
+		const carpio_gpu_solver_cfg* cfg, double* resid_hist, int hist_cap,
+		carpio_gpu_solver_stats* stats) {
+	return structured_solve(g, bc, false, 0.0, beta, source, phi, cfg, resid_hist,
+			hist_cap, stats);
+}
+
+int carpio_gpu_helmholtz_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
+		double alpha, double beta, const double* source, double* phi,
+		const carpio_gpu_solver_cfg* cfg, double* resid_hist, int hist_cap,
+		carpio_gpu_solver_stats* stats) {
+	return structured_solve(g, bc, true, alpha, beta, source, phi, cfg, resid_hist,
+			hist_cap, stats);
 }
 
 }  // extern "C"

@@ -14,6 +14,10 @@ struct RhsArgs {
 	const double* src_b;   // SRC_DIV: y-face field
 	double* phi;           // field: x0 in, solution out (normal cells)
 	int mean;
+	// Helmholtz stencil (StencilHelmholtz_::coe_row, s_poisson.hpp:240-258):
+	// the source scales by the cell volume sx sy; StencilPoisson_::src
+	// (:75-83) multiplies sx by itself (it indexes the size by `dim`)
+	int helm = 0;
 };
 
 // Row constant of StencilPoisson_::coe_row + ghost folds, then b = -constant
@@ -34,7 +38,7 @@ __device__ __forceinline__ double rhs_at(const GridSpace& sp, const RhsArgs& ra,
 		d = __dadd_rn(d, __ddiv_rn(__dsub_rn(ra.src_b[a], ra.src_b[a - 1]), ra.sy[j + gl]));
 		f = d;
 	}
-	double val = __dmul_rn(__dmul_rn(1.0, sxi), sxi);
+	double val = __dmul_rn(__dmul_rn(1.0, sxi), ra.helm ? ra.sy[j + gl] : sxi);
 	val = __dmul_rn(val, f);
 	const int nx = sp.nx, ny = sp.ny;
 	if (i == 0) val = __dadd_rn(val, ra.fold[j]);

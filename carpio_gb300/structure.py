@@ -176,6 +176,14 @@ class Poisson:
     def set_solver(self, name, any_=None, max_iter=1000, tol=1e-3, **kw):
         self.cfg = solver_cfg(name, max_iter, tol, **kw)
 
+    def set_uniform_alpha(self, a=1.0):
+        """Poisson_::set_uniform_alpha (s_poisson.hpp:461-471): the
+        StencilHelmholtz_ rows with a uniform alpha"""
+        self.alpha = float(a)
+
+    def unset_uniform_alpha(self):
+        self.alpha = None
+
     def set_learned(self, net, use_net=True, smooth=4, omega=0.8, memory=2,
                     stall=20, fallback=True):
         """solve with flexible CG preconditioned by the U-Net `net`
@@ -205,10 +213,16 @@ class Poisson:
             return rc
         cap = self.cfg.max_iter + 2
         hist = np.zeros(max(cap, 1))
-        rc = L.carpio_gpu_poisson_solve(
-            self.grid.handle, ctypes.byref(bc), self.beta,
-            _lib.ptr(self.source), _lib.ptr(self.phi), ctypes.byref(self.cfg),
-            _lib.ptr(hist), cap, ctypes.byref(self.stats))
+        if getattr(self, "alpha", None) is not None:
+            rc = L.carpio_gpu_helmholtz_solve(
+                self.grid.handle, ctypes.byref(bc), self.alpha, self.beta,
+                _lib.ptr(self.source), _lib.ptr(self.phi), ctypes.byref(self.cfg),
+                _lib.ptr(hist), cap, ctypes.byref(self.stats))
+        else:
+            rc = L.carpio_gpu_poisson_solve(
+                self.grid.handle, ctypes.byref(bc), self.beta,
+                _lib.ptr(self.source), _lib.ptr(self.phi), ctypes.byref(self.cfg),
+                _lib.ptr(hist), cap, ctypes.byref(self.stats))
         if rc < 0:
             raise _lib.CarpioGpuError(rc, "poisson_solve")
         self.lresid = hist[:min(self.stats.hist_len, cap)].tolist()
@@ -339,9 +353,12 @@ class NS_explicit:
         if rc:
             raise _lib.CarpioGpuError(rc, "ns_set_state")
 
-    def state(self):
+    def state(self, out=None):
+        """the fields (and dt) as host arrays; `out`: a dict of arrays to
+        fill instead (e.g. pinned torch tensors)"""
         g = self.grid
-        out = {k: g.zeros() for k in ("u", "v", "uf", "vf", "phi", "p")}
+        if out is None:
+            out = {k: g.zeros() for k in ("u", "v", "uf", "vf", "phi", "p")}
         dt = ctypes.c_double()
         rc = _lib.load().carpio_gpu_ns_get_state(
             self.handle, ctypes.byref(dt),
@@ -359,6 +376,18 @@ class NS_explicit:
         if h is not None and _lib._lib is not None and not sys.is_finalizing():
             _lib._lib.carpio_gpu_ns_destroy(h)
             self.handle = None
+
+
+class NS_kim(NS_explicit):
+    """NS_kim_<2> (s_ns_kim.hpp, Kim and Moin 1985) stepping on the GPU:
+    configured like NS_explicit; the time-step restriction settings are
+    ignored, as the reference's stepper does not call restrict_time."""
+
+    def initial(self):
+        super().initial()
+        rc = _lib.load().carpio_gpu_ns_set_stepper(self.handle, 1)
+        if rc:
+            raise _lib.CarpioGpuError(rc, "ns_set_stepper")
 
 
 def operator(grid, which, a=None, b=None, c=None, scheme=0, coef=0.0,

@@ -185,6 +185,14 @@ int carpio_gpu_poisson_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
 		double beta, const double* source, double* phi,
 		const carpio_gpu_solver_cfg* cfg, double* resid_hist, int hist_cap,
 		carpio_gpu_solver_stats* stats);
+/* Poisson_ with an alpha term (set_uniform_alpha, s_poisson.hpp:461-471):
+ * the StencilHelmholtz_ rows (s_poisson.hpp:185-258), diagonal plus
+ * sx sy alpha and the source scaled by sx sy; otherwise as
+ * carpio_gpu_poisson_solve. */
+int carpio_gpu_helmholtz_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
+		double alpha, double beta, const double* source, double* phi,
+		const carpio_gpu_solver_cfg* cfg, double* resid_hist, int hist_cap,
+		carpio_gpu_solver_stats* stats);
 
 /* Advection schemes of NS_::set_advection_scheme (s_ns.hpp:171-211), plus the
  * minmod limiter of src/calculation/advection.hpp:1079-1081 in the same TVD
@@ -234,6 +242,13 @@ int carpio_gpu_ns_get_state(carpio_gpu_ns* ns, double* dt, double* u,
  * Returns 0 or the first non-zero projection code / error. */
 int carpio_gpu_ns_run(carpio_gpu_ns* ns, int steps, double* step_dt,
 		int* step_iters, double* step_resid);
+/* The time stepper of the handle: NS_explicit_ (s_ns_explicit.hpp, default)
+ * or NS_kim_ (s_ns_kim.hpp: Adams-Bashforth advection, per-component
+ * Helmholtz predictor solved by the reference's default Jacobi, projection,
+ * p = phi / dt - NablaMuNabla(mu, phi) / (2 rho); no time-step restriction). */
+#define CARPIO_GPU_STEPPER_EXPLICIT 0
+#define CARPIO_GPU_STEPPER_KIM 1
+int carpio_gpu_ns_set_stepper(carpio_gpu_ns* ns, int stepper);
 
 /* Timing of the last carpio_gpu_ns_run, per step (host arrays of length
  * `cap`, any may be NULL): device time of the projection solve launch and of

@@ -21,6 +21,9 @@
 //   cavity  <n> <steps> <scheme> <tol> <max_iter> <dt0> <Re> <dump_every> [stretch]
 //           NS_explicit_ (s_ns_explicit.hpp) lid-driven cavity on [0,1]^2,
 //           gl = 2, projection by the CG + mean-removal drop-in.
+//   kim     <n> <steps> <scheme> <tol> <max_iter> <dt0> <Re>
+//           NS_kim_ (s_ns_kim.hpp) lid-driven cavity, gl = 2, projection by
+//           the CG + mean-removal drop-in.
 //   ops     <n> <seed> <gl> [stretch]
 //           single operators of Operation_ (s_operation.hpp) and
 //           Equation_::apply_bc (s_equation.hpp:340-378) on seeded fields;
@@ -31,6 +34,7 @@
 #include "structure/s_grid.hpp"
 #include "structure/s_poisson.hpp"
 #include "structure/s_ns_explicit.hpp"
+#include "structure/s_ns_kim.hpp"
 #include "structure/s_operation.hpp"
 #include "io/mmio.h"
 
@@ -464,6 +468,76 @@ static int cmd_cavity(int argc, char** argv) {
 	return 0;
 }
 
+// ------------------------------------------------------------ kim cmd ---
+// NS_kim_ (s_ns_kim.hpp) lid-driven cavity: the predictor's Helmholtz solves
+// keep the reference's default Jacobi solver (Poisson_::_init_solver), the
+// projection is the CG + mean-removal drop-in as for NS_explicit_.
+class NSKimAlg_: public NS_kim_<2> {
+public:
+	NSKimAlg_(spGrid g, int max_iter, double tol, std::vector<SolveRecord>* rec)
+		: NS_kim_<2>(g) {
+		this->_projection = spPoisson(
+				new PoissonAlg_(g, "cg", true, max_iter, tol, rec, false));
+	}
+	void set_scheme(const std::string& s) {
+		if (s == "minmod") this->fun_v_dot_nabla = &VdotNabla_TVD_minmod;
+		else this->set_advection_scheme(s);
+	}
+	void step_once() {
+		this->run_one_step(this->_time->current_step());
+		this->_time->advance();
+	}
+	spScalar cs(const std::string& n) { return this->_css[n]; }
+	spScalar scr(int d) { return this->_sscr->get_spdata(d); }
+};
+
+static int cmd_kim(int argc, char** argv) {
+	if (argc < 9) return 2;
+	int n = std::atoi(argv[2]);
+	int steps = std::atoi(argv[3]);
+	std::string scheme = argv[4];
+	double tol = std::atof(argv[5]);
+	int max_iter = std::atoi(argv[6]);
+	double dt0 = std::atof(argv[7]);
+	double Re = std::atof(argv[8]);
+	out_open(argv[argc - 1]);
+	spGrid g = make_grid(n, n, 2, false);
+	put_grid(*g);
+	std::vector<SolveRecord> rec;
+	NSKimAlg_ ns(g, max_iter, tol, &rec);
+	ns.set_scheme(scheme);
+	ns.set_time(steps > 0 ? steps - 1 : 0, dt0);
+	NS_<2>::spBC bc0(new NS_<2>::BC()), bc1(new NS_<2>::BC());
+	bc0->set_default_1_bc(0);
+	bc1->set_default_1_bc(1);
+	for (int s = 0; s < 3; ++s) ns.add_bc(0, s, "u", bc0);
+	ns.add_bc(0, 3, "u", bc1);
+	for (int s = 0; s < 4; ++s) ns.add_bc(0, s, "v", bc0);
+	ns.set_uniform_rho(Re);
+	ns.initial();
+	std::vector<double> its, res;
+	for (int s = 0; s < steps; ++s) {
+		ns.step_once();
+		its.push_back(rec.back().iters);
+		res.push_back(rec.back().tol_out);
+		if (s == 0) {
+			put_field("s1_xscr", *ns.scr(0));
+			put_field("s1_yscr", *ns.scr(1));
+			put_field("s1_phi", *ns.cs("phi"));
+			put_field("s1_p", *ns.cs("p"));
+			put_field("s1_u", *ns.cs("u"));
+			put_field("s1_v", *ns.cs("v"));
+			put_field("s1_uf", *ns.cs("uf"));
+			put_field("s1_vf", *ns.cs("vf"));
+		}
+	}
+	const char* names[] = { "u", "v", "p", "phi", "uf", "vf", "us", "vs" };
+	for (const char* nm : names) put_field(nm, *ns.cs(nm));
+	put_vec("cg_iters", its);
+	put_vec("cg_resid", res);
+	return 0;
+}
+
 // ------------------------------------------------------------ ops cmd ---
 class EqProbe_: public Equation_<2> {
 public:
@@ -579,6 +653,7 @@ int main(int argc, char** argv) {
 	else if (c == "poisson") rc = cmd_poisson(argc, argv);
 	else if (c == "cavity") rc = cmd_cavity(argc, argv);
 	else if (c == "ops") rc = cmd_ops(argc, argv);
+	else if (c == "kim") rc = cmd_kim(argc, argv);
 	if (rc == 2) std::fprintf(stderr, "bad arguments for %s\n", c.c_str());
 	g_meta.close();
 	return rc;

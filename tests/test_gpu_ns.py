@@ -146,3 +146,43 @@ def test_output_scalar_matches_reference(gpu_lib, name, tmp_path):
     dev = torch.from_numpy(np.ascontiguousarray(d["in_a"])).cuda()
     rc = gpu_lib.carpio_gpu_output_scalar(g.handle, str(f).encode(), dev.data_ptr())
     assert rc == 0 and f.read_bytes() == ref
+
+
+def make_kim(n, scheme, dt0, Re, tol, max_iter):
+    from carpio_gb300 import structure as S
+    g = S.Grid((0.0, 0.0), (1.0, 1.0), (n, n), 2)
+    ns = S.NS_kim(g)
+    ns.set_advection_scheme(scheme)
+    ns.set_time(0, dt0)
+    bc0, bc1 = S.BoundaryCondition(), S.BoundaryCondition()
+    bc0.set_default_1_bc(0.0)
+    bc1.set_default_1_bc(1.0)
+    for s in range(3):
+        ns.add_bc(0, s, "u", bc0)
+    ns.add_bc(0, 3, "u", bc1)
+    for s in range(4):
+        ns.add_bc(0, s, "v", bc0)
+    ns.set_uniform_rho(Re)
+    ns.set_projection_solver("CG", max_iter, tol)
+    return g, ns
+
+
+@pytest.mark.parametrize("name", golden_names("kim_"))
+def test_kim_matches_reference(gpu_lib, name):
+    """NS_kim_ stepping (Helmholtz predictor by Jacobi, CG projection)
+    against the reference's run: the first step's fields, then all steps"""
+    d = golden(name)
+    a = d["case_args"]
+    n, steps, scheme = int(a[1]), int(a[2]), str(a[3])
+    tol, max_iter, dt0, Re = float(a[4]), int(a[5]), float(a[6]), float(a[7])
+    g, ns = make_kim(n, scheme, dt0, Re, tol, max_iter)
+    assert ns.run(1) == 0
+    st = ns.state()
+    for k in ("u", "v", "uf", "vf", "phi", "p"):
+        err = rel_l2(st[k], d["s1_" + k])
+        assert err <= PLAIN_RTOL, (k, err)
+    assert ns.run(steps - 1) == 0
+    st = ns.state()
+    for k in ("u", "v", "p", "phi", "uf", "vf"):
+        err = rel_l2(st[k], d[k])
+        assert err <= PLAIN_RTOL, (k, err)
