@@ -11,10 +11,11 @@ LIB_PATH = os.path.join(HERE, "libcarpio_gpu.so")
 
 OK, MAXITER, BREAKDOWN_RHO, BREAKDOWN_OMEGA = 0, 1, 2, 3
 EINVAL, ECUDA, ENONFINITE, EZERODIAG, ETIMEOUT, ENOMEM, EIO = -1, -2, -3, -4, -5, -6, -7
-CG, JACOBI, DIA_BICGSTAB, BICGSTAB = 0, 1, 2, 3
+CG, JACOBI, DIA_BICGSTAB, BICGSTAB, IC_CGS, IC_CG = 0, 1, 2, 3, 4, 5
 KINDS = {"cg": CG, "jacobi": JACOBI, "dia_bicgstab": DIA_BICGSTAB,
          "bicgstab": BICGSTAB, "CG": CG, "Jacobi": JACOBI,
-         "Dia_BiCGSTAB": DIA_BICGSTAB, "BiCGSTAB": BICGSTAB}
+         "Dia_BiCGSTAB": DIA_BICGSTAB, "BiCGSTAB": BICGSTAB,
+         "ic_cgs": IC_CGS, "IC_CGS": IC_CGS, "ic_cg": IC_CG, "IC_CG": IC_CG}
 FP64, MIXED = 0, 1
 FLAG_FULL_NRM2 = 1
 FLAG_NO_TILE = 2

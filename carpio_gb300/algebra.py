@@ -122,3 +122,14 @@ class Solver_Jacobi_:
 
     def get_residual_array(self):
         return np.asarray(self._lresid)
+
+
+def IC_CGS(A, x, b, max_iter, tol, lresid=None, flags=0):
+    """carpio::IC_CGS (solver_matrix.hpp:376-438) with ICPre
+    (preconditioner.hpp:97-177)"""
+    return krylov(_lib.IC_CGS, A, x, b, max_iter, tol, lresid, flags)
+
+
+def IC_CG(A, x, b, max_iter, tol, lresid=None, flags=0):
+    """carpio::IC_CG (solver_matrix.hpp:318-374) with ICPre"""
+    return krylov(_lib.IC_CG, A, x, b, max_iter, tol, lresid, flags)

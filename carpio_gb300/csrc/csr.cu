@@ -1,10 +1,14 @@
-// Algebra-level drop-in: carpio::CG / Jacobi / Dia_BiCGSTAB / BiCGSTAB
-// (lib/algebra/solver_matrix.hpp) on a MatrixSCR_ CSR matrix, one persistent
-// cooperative launch per solve.
+// Algebra-level drop-in: carpio::CG / Jacobi / Dia_BiCGSTAB / BiCGSTAB and
+// IC_CGS / IC_CG (lib/algebra/solver_matrix.hpp) on a MatrixSCR_ CSR
+// matrix, one persistent cooperative launch per solve.
 #include "internal.hpp"
+#include "ic.cuh"
 
+#include <algorithm>
 #include <cmath>
 #include <mutex>
+#include <numeric>
+#include <vector>
 
 namespace {
 
@@ -17,12 +21,81 @@ __global__ void __launch_bounds__(kThreads) k_csr_solve(CsrOp op, FlatSpace sp,
 	krylov_run<double>(sp, op, v, sc, gc, bank);
 }
 
+__global__ void __launch_bounds__(kThreads) k_csr_solve_ic(CsrOp op, IcOp ic,
+		Vecs<double> v, SolveCtl sc, GridCtl gc) {
+	gc.start();
+	int bank = 0;
+	if (sc.kind == CARPIO_GPU_IC_CGS) ic_cgs_run(ic.n, op, ic, v, sc, gc, bank);
+	else ic_cg_run(ic.n, op, ic, v, sc, gc, bank);
+}
+
 struct CsrWs {
 	std::mutex mu;
 	cudaStream_t s = nullptr;
 	cg_host::LaunchWs lw;
 	cg_host::DevBuf rp, ci, va, vec, hist;
+	cg_host::DevBuf icd, icu[3], icl[3], icf[2], icb[2];   // IC factor, levels
 };
+
+// ICPre (preconditioner.hpp:97-136): the upper triangle with its diagonal,
+// columns ascending per row, factored by ICFactor (:20-48) in its order.
+// Returns false when a row has no diagonal (the reference exits).
+struct IcHost {
+	std::vector<uint32_t> pntr, indx;
+	std::vector<double> val;
+};
+
+bool ic_factor(int n, const uint32_t* rp, const uint32_t* ci, const double* va, IcHost& f) {
+	f.pntr.assign(n + 1, 0);
+	f.indx.clear();
+	f.val.clear();
+	for (int k = 0; k < n; ++k) {
+		std::vector<std::pair<uint32_t, double> > row;
+		for (uint32_t j = rp[k]; j < rp[k + 1]; ++j)
+			if (ci[j] >= (uint32_t)k) row.push_back({ ci[j], va[j] });
+		std::sort(row.begin(), row.end(),
+				[](const std::pair<uint32_t, double>& a, const std::pair<uint32_t, double>& b) {
+					return a.first < b.first;
+				});
+		for (auto& e : row) { f.indx.push_back(e.first); f.val.push_back(e.second); }
+		f.pntr[k + 1] = (uint32_t)f.indx.size();
+		if (row.empty() || row[0].first != (uint32_t)k) return false;
+	}
+	std::vector<uint32_t>& pntr = f.pntr;
+	std::vector<uint32_t>& indx = f.indx;
+	std::vector<double>& val = f.val;
+	// the factorisation, step for step as ICFactor; indx is read one entry
+	// past a row's end there, so keep a sentinel past the last entry
+	indx.push_back(0);
+	for (int k = 0; k < n - 1; ++k) {
+		const uint32_t d = pntr[k];
+		double z = val[d] = std::sqrt(val[d]);
+		for (uint32_t i = d + 1; i < pntr[k + 1]; ++i) val[i] /= z;
+		for (uint32_t i = d + 1; i < pntr[k + 1]; ++i) {
+			z = val[i];
+			const uint32_t h = indx[i];
+			uint32_t g = i;
+			for (uint32_t j = pntr[h]; j < pntr[h + 1]; ++j)
+				for (; g < pntr[k + 1] && indx[g + 1] <= indx[j]; ++g)
+					if (indx[g] == indx[j]) val[j] -= z * val[g];
+		}
+	}
+	val[pntr[n - 1]] = std::sqrt(val[pntr[n - 1]]);
+	indx.pop_back();
+	return true;
+}
+
+// rows grouped by level: level[i] ascending, rows ascending within a level
+void by_level(const std::vector<int>& level, std::vector<uint32_t>& ptr,
+		std::vector<uint32_t>& rows) {
+	const int nl = level.empty() ? 0 : *std::max_element(level.begin(), level.end()) + 1;
+	ptr.assign(nl + 1, 0);
+	for (int l : level) ++ptr[l + 1];
+	for (int l = 0; l < nl; ++l) ptr[l + 1] += ptr[l];
+	rows.assign(level.size(), 0);
+	std::vector<uint32_t> pos(ptr.begin(), ptr.end() - 1);
+	for (size_t i = 0; i < level.size(); ++i) rows[pos[level[i]]++] = (uint32_t)i;
+}
 
 // Never destroyed: freeing device memory from a static destructor can run
 // after the CUDA runtime has shut down at process exit.
@@ -45,7 +118,7 @@ extern "C" int carpio_gpu_krylov_csr(int kind, int n, int nnz,
 		double* resid_hist, int hist_cap, int* hist_len, uint32_t flags) {
 	using namespace cg_host;
 	if (n <= 0 || nnz < 0 || !rowptr || (!col && nnz) || (!val && nnz) || !b
-			|| !x || !max_iter || !tol || kind < 0 || kind > 3)
+			|| !x || !max_iter || !tol || kind < 0 || kind > CARPIO_GPU_IC_CG)
 		return CARPIO_GPU_EINVAL;
 	if (hist_cap < 0 || (hist_cap > 0 && !resid_hist)) return CARPIO_GPU_EINVAL;
 	CsrWs& w = ws();
@@ -70,12 +143,86 @@ extern "C" int carpio_gpu_krylov_csr(int kind, int n, int nnz,
 	for (int i = 0; i < nvec; ++i) *slots[i] = base + (size_t)i * n;
 	CG_CK(cudaMemcpyAsync(v.x, x, sizeof(double) * n, cudaMemcpyDefault, s));
 	CG_CK(cudaMemcpyAsync(v.b, b, sizeof(double) * n, cudaMemcpyDefault, s));
-	int blocks = coop_blocks((const void*)k_csr_solve, n, 2);
+	const bool ic = kind == CARPIO_GPU_IC_CGS || kind == CARPIO_GPU_IC_CG;
+	int blocks = coop_blocks(ic ? (const void*)k_csr_solve_ic : (const void*)k_csr_solve, n, 2);
 	if ((rc = w.lw.ensure(blocks))) return rc;
 	if ((rc = w.hist.ensure(sizeof(double) * (size_t)(hist_cap > 0 ? hist_cap : 1)))) return rc;
 	CG_CK(cudaMemsetAsync(w.lw.ctl.p, 0, sizeof(Ctl), s));
 	CsrOp op{ w.rp.as<uint32_t>(), w.ci.as<uint32_t>(), w.va.as<double>() };
 	FlatSpace sp{ n };
+	IcOp icop{};
+	if (ic) {
+		// the factor on the host (from host copies of the matrix)
+		std::vector<uint32_t> hrp(n + 1), hci(nnz);
+		std::vector<double> hva(nnz);
+		CG_CK(cudaMemcpy(hrp.data(), rowptr, sizeof(uint32_t) * (n + 1), cudaMemcpyDefault));
+		if (nnz) {
+			CG_CK(cudaMemcpy(hci.data(), col, sizeof(uint32_t) * nnz, cudaMemcpyDefault));
+			CG_CK(cudaMemcpy(hva.data(), val, sizeof(double) * nnz, cudaMemcpyDefault));
+		}
+		IcHost f;
+		if (!ic_factor(n, hrp.data(), hci.data(), hva.data(), f)) return CARPIO_GPU_EZERODIAG;
+		std::vector<double> dg(n);
+		std::vector<uint32_t> up(n + 1, 0), ui, lcount(n + 1, 0);
+		std::vector<double> uv;
+		for (int i = 0; i < n; ++i) {
+			dg[i] = f.val[f.pntr[i]];
+			for (uint32_t e = f.pntr[i] + 1; e < f.pntr[i + 1]; ++e) {
+				ui.push_back(f.indx[e]);
+				uv.push_back(f.val[e]);
+				++lcount[f.indx[e] + 1];
+			}
+			up[i + 1] = (uint32_t)ui.size();
+		}
+		// forward: the rows updating row k, ascending (transpose of the factor)
+		std::vector<uint32_t> lp(n + 1, 0);
+		for (int k = 0; k < n; ++k) lp[k + 1] = lp[k] + lcount[k + 1];
+		std::vector<uint32_t> li(lp[n]), fill(lp.begin(), lp.end() - 1);
+		std::vector<double> lv(lp[n]);
+		for (int i = 0; i < n; ++i)
+			for (uint32_t e = up[i]; e < up[i + 1]; ++e) {
+				const uint32_t k = ui[e];
+				li[fill[k]] = (uint32_t)i;
+				lv[fill[k]++] = uv[e];
+			}
+		std::vector<int> lf(n, 0), lb(n, 0);
+		for (int k = 0; k < n; ++k)
+			for (uint32_t e = lp[k]; e < lp[k + 1]; ++e) lf[k] = std::max(lf[k], lf[li[e]] + 1);
+		for (int i = n - 1; i >= 0; --i)
+			for (uint32_t e = up[i]; e < up[i + 1]; ++e) lb[i] = std::max(lb[i], lb[ui[e]] + 1);
+		std::vector<uint32_t> fptr, frows, bptr, brows;
+		by_level(lf, fptr, frows);
+		by_level(lb, bptr, brows);
+		auto put = [&](DevBuf& d, const void* p, size_t bytes) {
+			return to_device(d, p, bytes ? bytes : 8, s);
+		};
+		if ((rc = put(w.icd, dg.data(), sizeof(double) * n))) return rc;
+		if ((rc = put(w.icu[0], up.data(), sizeof(uint32_t) * up.size()))) return rc;
+		if ((rc = put(w.icu[1], ui.data(), sizeof(uint32_t) * ui.size()))) return rc;
+		if ((rc = put(w.icu[2], uv.data(), sizeof(double) * uv.size()))) return rc;
+		if ((rc = put(w.icl[0], lp.data(), sizeof(uint32_t) * lp.size()))) return rc;
+		if ((rc = put(w.icl[1], li.data(), sizeof(uint32_t) * li.size()))) return rc;
+		if ((rc = put(w.icl[2], lv.data(), sizeof(double) * lv.size()))) return rc;
+		if ((rc = put(w.icf[0], fptr.data(), sizeof(uint32_t) * fptr.size()))) return rc;
+		if ((rc = put(w.icf[1], frows.data(), sizeof(uint32_t) * frows.size()))) return rc;
+		if ((rc = put(w.icb[0], bptr.data(), sizeof(uint32_t) * bptr.size()))) return rc;
+		if ((rc = put(w.icb[1], brows.data(), sizeof(uint32_t) * brows.size()))) return rc;
+		CG_CK(cudaStreamSynchronize(s));   // host vectors go out of scope
+		icop.n = n;
+		icop.d = w.icd.as<double>();
+		icop.up = w.icu[0].as<uint32_t>();
+		icop.ui = w.icu[1].as<uint32_t>();
+		icop.uv = w.icu[2].as<double>();
+		icop.lp = w.icl[0].as<uint32_t>();
+		icop.li = w.icl[1].as<uint32_t>();
+		icop.lv = w.icl[2].as<double>();
+		icop.fptr = w.icf[0].as<uint32_t>();
+		icop.frows = w.icf[1].as<uint32_t>();
+		icop.nfl = (int)fptr.size() - 1;
+		icop.bptr = w.icb[0].as<uint32_t>();
+		icop.brows = w.icb[1].as<uint32_t>();
+		icop.nbl = (int)bptr.size() - 1;
+	}
 	SolveCtl sc;
 	sc.kind = kind;
 	sc.max_iter = *max_iter;
@@ -85,9 +232,15 @@ extern "C" int carpio_gpu_krylov_csr(int kind, int n, int nnz,
 	sc.hist_cap = hist_cap;
 	sc.out = &w.lw.ctl.as<Ctl>()->out;
 	GridCtl gc = make_gridctl(w.lw);
-	void* args[] = { &op, &sp, &v, &sc, &gc };
-	CG_CK(cudaLaunchCooperativeKernel((const void*)k_csr_solve, blocks,
-			kThreads, args, 0, s));
+	if (ic) {
+		void* args[] = { &op, &icop, &v, &sc, &gc };
+		CG_CK(cudaLaunchCooperativeKernel((const void*)k_csr_solve_ic, blocks,
+				kThreads, args, 0, s));
+	} else {
+		void* args[] = { &op, &sp, &v, &sc, &gc };
+		CG_CK(cudaLaunchCooperativeKernel((const void*)k_csr_solve, blocks,
+				kThreads, args, 0, s));
+	}
 	CG_CK(cudaMemcpyAsync(w.lw.host_ctl, w.lw.ctl.p, sizeof(Ctl),
 			cudaMemcpyDeviceToHost, s));
 	CG_CK(cudaStreamSynchronize(s));

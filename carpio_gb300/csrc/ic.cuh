@@ -1,0 +1,228 @@
+// IC(0)-preconditioned Krylov solvers of the reference: carpio::IC_CG and
+// carpio::IC_CGS (lib/algebra/solver_matrix.hpp:318-438) with ICPre
+// (lib/algebra/preconditioner.hpp:20-177). The incomplete Cholesky factor is
+// computed on the host in the reference's order (csr.cu); here it is applied
+// by level-scheduled triangular solves inside the persistent solver launch:
+// the rows of one level depend only on rows of earlier levels, so a level is
+// one parallel pass and levels are separated by grid barriers.
+#pragma once
+
+#include "krylov.cuh"
+
+namespace cg_dev {
+
+// ICPre's factor, rearranged for level scheduling. Forward solve (the
+// reference's column sweep, y[indx] -= z val) gathered per row k: the rows
+// i < k that update k (lp/li/lv, i ascending, i.e. the reference's order of
+// updates); backward solve per row i: its off-diagonal entries (up/ui/uv,
+// columns ascending).
+struct IcOp {
+	int n;
+	const double* d;                                  // val_[pntr_[i]]
+	const uint32_t *lp, *li; const double* lv;
+	const uint32_t *up, *ui; const double* uv;
+	const uint32_t *fptr, *frows; int nfl;            // forward levels
+	const uint32_t *bptr, *brows; int nbl;            // backward levels
+};
+
+#define GLOOP(cnt)                                                             \
+	for (int t = blockIdx.x * blockDim.x + threadIdx.x, _c = (cnt); t < _c;  \
+			t += gridDim.x * blockDim.x)
+
+// out = M^-1 in (ICPre::solve); exact IEEE operations in the reference's
+// order, so the result does not depend on the level split
+__device__ bool ic_apply(const IcOp& ic, const double* in, double* out,
+		const GridCtl& gc) {
+	GLOOP(ic.n) out[t] = in[t];
+	if (!grid_sync(gc)) return false;
+	for (int l = 0; l < ic.nfl; ++l) {
+		const uint32_t b0 = ic.fptr[l];
+		GLOOP((int)(ic.fptr[l + 1] - b0)) {
+			const uint32_t k = ic.frows[b0 + t];
+			double y = ldcg(out + k);
+			for (uint32_t e = ic.lp[k]; e < ic.lp[k + 1]; ++e)
+				y = __dsub_rn(y, __dmul_rn(ldcg(out + ic.li[e]), ic.lv[e]));
+			out[k] = __ddiv_rn(y, ic.d[k]);
+		}
+		if (!grid_sync(gc)) return false;
+	}
+	for (int l = 0; l < ic.nbl; ++l) {
+		const uint32_t b0 = ic.bptr[l];
+		GLOOP((int)(ic.bptr[l + 1] - b0)) {
+			const uint32_t i = ic.brows[b0 + t];
+			double z = 0.0;
+			for (uint32_t e = ic.up[i]; e < ic.up[i + 1]; ++e)
+				z = __dadd_rn(z, __dmul_rn(ldcg(out + ic.ui[e]), ic.uv[e]));
+			out[i] = __ddiv_rn(__dsub_rn(ldcg(out + i), z), ic.d[i]);
+		}
+		if (!grid_sync(gc)) return false;
+	}
+	return true;
+}
+
+// grid sums of NV products (full dot products, dot() of BLAS_Level1)
+template<int NV>
+__device__ __forceinline__ bool dots(const double* const (&a)[NV], const double* const (&b)[NV],
+		int n, const GridCtl& gc, int& bank, double (&res)[NV]) {
+	double acc[NV];
+#pragma unroll
+	for (int m = 0; m < NV; ++m) acc[m] = 0.0;
+	GLOOP(n) {
+#pragma unroll
+		for (int m = 0; m < NV; ++m) acc[m] = fma(ldcg(a[m] + t), ldcg(b[m] + t), acc[m]);
+	}
+	if (!grid_allreduce<double, NV>(acc, gc, bank)) return false;
+#pragma unroll
+	for (int m = 0; m < NV; ++m) res[m] = acc[m];
+	return true;
+}
+
+// nrm2 with the reference's quirk (the last element left out unless FULL_NRM2
+// or n == 1), as a relative residual
+__device__ __forceinline__ bool nrm2_rel(const double* r, int n, bool full, double normb,
+		const GridCtl& gc, int& bank, double& resid) {
+	double acc[1] = { 0.0 };
+	GLOOP(n) {
+		if (t != n - 1 || full) { const double x = ldcg(r + t); acc[0] = fma(x, x, acc[0]); }
+	}
+	if (!grid_allreduce<double, 1>(acc, gc, bank)) return false;
+	resid = sqrt(acc[0]) / normb;
+	return true;
+}
+
+// r = b - A x; normb = nrm2(b) (1 when zero); resid = nrm2(r) / normb
+template<class Op>
+__device__ bool ic_start(const Op& op, const Vecs<double>& v, int n, bool full,
+		const GridCtl& gc, int& bank, double& normb, double& resid) {
+	double acc[2] = { 0.0, 0.0 };
+	GLOOP(n) {
+		const double bb = v.b[t];
+		const double rr = bb - op.apply(v.x, t, t);
+		v.r[t] = rr;
+		if (t != n - 1 || full) { acc[0] = fma(bb, bb, acc[0]); acc[1] = fma(rr, rr, acc[1]); }
+	}
+	if (!grid_allreduce<double, 2>(acc, gc, bank)) return false;
+	normb = sqrt(acc[0]);
+	if (normb == 0.0) normb = 1;
+	resid = sqrt(acc[1]) / normb;
+	return true;
+}
+
+// carpio::IC_CG (solver_matrix.hpp:318-374)
+template<class Op>
+__device__ void ic_cg_run(int n, const Op& op, const IcOp& ic, const Vecs<double>& v,
+		const SolveCtl& sc, const GridCtl& gc, int& bank) {
+	const bool full = (sc.flags & CARPIO_GPU_FLAG_FULL_NRM2) || n == 1;
+	int hl = 0;
+	double normb, resid;
+	if (!ic_start(op, v, n, full, gc, bank, normb, resid)) return;
+	if (resid <= sc.tol) { finish(sc, 0, 0, resid, hl); return; }
+	double rho_1 = 0.0;
+	for (int it = 1; it <= sc.max_iter; ++it) {
+		if (!grid_sync(gc)) return;
+		if (!ic_apply(ic, v.r, v.z, gc)) return;           // z = M^-1 r
+		double rz[1];
+		{
+			const double* a[1] = { v.r };
+			const double* b[1] = { v.z };
+			if (!dots<1>(a, b, n, gc, bank, rz)) return;
+		}
+		const double rho = rz[0];
+		const double beta = it == 1 ? 0.0 : rho / rho_1;
+		GLOOP(n) v.p[t] = it == 1 ? v.z[t] : fma(beta, v.p[t], v.z[t]);
+		if (!grid_sync(gc)) return;
+		GLOOP(n) v.q[t] = op.apply(v.p, t, t);
+		if (!grid_sync(gc)) return;
+		double pq[1];
+		{
+			const double* a[1] = { v.p };
+			const double* b[1] = { v.q };
+			if (!dots<1>(a, b, n, gc, bank, pq)) return;
+		}
+		const double alpha = rho / pq[0];
+		GLOOP(n) {
+			v.x[t] = fma(alpha, v.p[t], v.x[t]);
+			v.r[t] = fma(-alpha, v.q[t], v.r[t]);
+		}
+		if (!grid_sync(gc)) return;
+		if (!nrm2_rel(v.r, n, full, normb, gc, bank, resid)) return;
+		hist_push(sc, hl, resid);
+		if (resid <= sc.tol) { finish(sc, 0, it, resid, hl); return; }
+		rho_1 = rho;
+	}
+	finish(sc, 1, sc.max_iter, resid, hl);
+}
+
+// carpio::IC_CGS (solver_matrix.hpp:376-438); rtilde = rt, u = s, phat = ph,
+// vhat = v, uhat = sh, qhat = t, u + q = d
+template<class Op>
+__device__ void ic_cgs_run(int n, const Op& op, const IcOp& ic, const Vecs<double>& v,
+		const SolveCtl& sc, const GridCtl& gc, int& bank) {
+	const bool full = (sc.flags & CARPIO_GPU_FLAG_FULL_NRM2) || n == 1;
+	int hl = 0;
+	double normb, resid;
+	if (!ic_start(op, v, n, full, gc, bank, normb, resid)) return;
+	GLOOP(n) v.rt[t] = v.r[t];
+	if (resid <= sc.tol) { finish(sc, 0, 0, resid, hl); return; }
+	double rho_2 = 0.0;
+	for (int it = 1; it <= sc.max_iter; ++it) {
+		if (!grid_sync(gc)) return;
+		double r1[1];
+		{
+			const double* a[1] = { v.rt };
+			const double* b[1] = { v.r };
+			if (!dots<1>(a, b, n, gc, bank, r1)) return;
+		}
+		const double rho_1 = r1[0];
+		if (rho_1 == 0.0) {
+			// the reference returns with max_iter unchanged
+			if (!nrm2_rel(v.r, n, full, normb, gc, bank, resid)) return;
+			finish(sc, 2, sc.max_iter, resid, hl);
+			return;
+		}
+		if (it == 1) {
+			GLOOP(n) { const double r = v.r[t]; v.s[t] = r; v.p[t] = r; }
+		} else {
+			const double beta = rho_1 / rho_2;
+			GLOOP(n) {
+				const double u = fma(beta, v.q[t], v.r[t]);
+				v.s[t] = u;
+				v.p[t] = fma(beta, fma(beta, v.p[t], v.q[t]), u);
+			}
+		}
+		if (!grid_sync(gc)) return;
+		if (!ic_apply(ic, v.p, v.ph, gc)) return;          // phat = M^-1 p
+		GLOOP(n) v.v[t] = op.apply(v.ph, t, t);            // vhat = A phat
+		if (!grid_sync(gc)) return;
+		double rv[1];
+		{
+			const double* a[1] = { v.rt };
+			const double* b[1] = { v.v };
+			if (!dots<1>(a, b, n, gc, bank, rv)) return;
+		}
+		const double alpha = rho_1 / rv[0];
+		GLOOP(n) {
+			const double q = fma(-alpha, v.v[t], v.s[t]);
+			v.q[t] = q;
+			v.d[t] = v.s[t] + q;                           // u + q
+		}
+		if (!grid_sync(gc)) return;
+		if (!ic_apply(ic, v.d, v.sh, gc)) return;          // uhat = M^-1 (u + q)
+		GLOOP(n) {
+			v.x[t] = fma(alpha, v.sh[t], v.x[t]);
+			v.t[t] = op.apply(v.sh, t, t);                 // qhat = A uhat
+		}
+		if (!grid_sync(gc)) return;
+		GLOOP(n) v.r[t] = fma(-alpha, v.t[t], v.r[t]);
+		if (!grid_sync(gc)) return;
+		rho_2 = rho_1;
+		if (!nrm2_rel(v.r, n, full, normb, gc, bank, resid)) return;
+		hist_push(sc, hl, resid);
+		if (resid < sc.tol) { finish(sc, 0, it, resid, hl); return; }
+	}
+	finish(sc, 1, sc.max_iter, resid, hl);
+}
+
+#undef GLOOP
+
+}  // namespace cg_dev

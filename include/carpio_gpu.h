@@ -53,6 +53,8 @@ extern "C" {
 #define CARPIO_GPU_JACOBI 1        /* carpio::Jacobi        solver_matrix.hpp:192-260 */
 #define CARPIO_GPU_DIA_BICGSTAB 2  /* carpio::Dia_BiCGSTAB  solver_matrix.hpp:599-672 */
 #define CARPIO_GPU_BICGSTAB 3      /* carpio::BiCGSTAB      solver_matrix.hpp:674-745 */
+#define CARPIO_GPU_IC_CGS 4        /* carpio::IC_CGS        solver_matrix.hpp:376-438 (CSR only) */
+#define CARPIO_GPU_IC_CG 5         /* carpio::IC_CG         solver_matrix.hpp:318-374 (CSR only) */
 
 /* flags (bitwise OR). 0 = the reference's exact semantics. */
 #define CARPIO_GPU_FLAG_FULL_NRM2 1u   /* use the full 2-norm instead of nrm2's
@@ -79,7 +81,12 @@ int carpio_gpu_device_count(void);
  * iterations and reached residual, exactly as the reference writes them
  * (including its early exits that leave max_iter unchanged). resid_hist:
  * the lresid list, up to hist_cap entries; *hist_len gets its full length
- * (either may be NULL). Returns the reference's code or a negative error. */
+ * (either may be NULL). Returns the reference's code or a negative error.
+ * kind IC_CGS / IC_CG: ICPre's incomplete Cholesky factor of the upper
+ * triangle (preconditioner.hpp:97-177) is built on the host in the
+ * reference's order, the triangular solves run level by level on the GPU;
+ * a row without a diagonal returns CARPIO_GPU_EZERODIAG (the reference
+ * exits). */
 int carpio_gpu_krylov_csr(int kind, int n, int nnz, const uint32_t* rowptr,
 		const uint32_t* col, const double* val, const double* b, double* x,
 		int* max_iter, double* tol, double* resid_hist, int hist_cap,

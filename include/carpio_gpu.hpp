@@ -77,6 +77,18 @@ int BiCGSTAB(const MAT& A, ARR& x, const ARR& b, int& max_iter, double& tol,
 		std::list<double>& lresid) {
 	return krylov(CARPIO_GPU_BICGSTAB, A, x, b, max_iter, tol, lresid);
 }
+// IC(0)-preconditioned solvers (solver_matrix.hpp:318-438): the factor is
+// computed on the host in ICPre's order, the triangular solves run on the GPU
+template<class MAT, class ARR>
+int IC_CGS(const MAT& A, ARR& x, const ARR& b, int& max_iter, double& tol,
+		std::list<double>& lresid) {
+	return krylov(CARPIO_GPU_IC_CGS, A, x, b, max_iter, tol, lresid);
+}
+template<class MAT, class ARR>
+int IC_CG(const MAT& A, ARR& x, const ARR& b, int& max_iter, double& tol,
+		std::list<double>& lresid) {
+	return krylov(CARPIO_GPU_IC_CG, A, x, b, max_iter, tol, lresid);
+}
 
 // RAII handles for the structure level.
 class Grid {

@@ -162,6 +162,8 @@ static int run_carpio(const std::string& kind, const Mat& A, Arr& x,
 	if (kind == "dia_bicgstab")
 		return carpio::Dia_BiCGSTAB(A, x, b, max_iter, tol, lr);
 	if (kind == "bicgstab") return carpio::BiCGSTAB(A, x, b, max_iter, tol, lr);
+	if (kind == "ic_cgs") return carpio::IC_CGS(A, x, b, max_iter, tol, lr);
+	if (kind == "ic_cg") return carpio::IC_CG(A, x, b, max_iter, tol, lr);
 	std::fprintf(stderr, "unknown solver kind %s\n", kind.c_str());
 	std::exit(2);
 }

@@ -310,6 +310,150 @@ done:
 	return ret;
 }
 
+/* ICPre (preconditioner.hpp:97-177): the upper triangle with the diagonal,
+ * columns ascending per row, factored as ICFactor (:20-48) does */
+typedef struct { unsigned* pntr; unsigned* indx; double* val; } IcF;
+
+typedef struct { unsigned c; double v; } ColVal;
+static int colval_cmp(const void* a, const void* b) {
+	unsigned x = ((const ColVal*)a)->c, y = ((const ColVal*)b)->c;
+	return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+static int ic_build(int n, const unsigned* rp, const unsigned* ci, const double* va, IcF* f) {
+	unsigned nz = 0;
+	for (int k = 0; k < n; ++k)
+		for (unsigned j = rp[k]; j < rp[k + 1]; ++j)
+			if (ci[j] >= (unsigned)k) ++nz;
+	f->pntr = malloc(sizeof(unsigned) * (n + 1));
+	f->indx = malloc(sizeof(unsigned) * (nz + 1));   /* + a sentinel */
+	f->val = malloc(sizeof(double) * (nz ? nz : 1));
+	ColVal* tmp = malloc(sizeof(ColVal) * (n + 1));   /* a row has at most n entries */
+	f->pntr[0] = 0;
+	for (int k = 0; k < n; ++k) {
+		unsigned m = 0, base = f->pntr[k];
+		for (unsigned j = rp[k]; j < rp[k + 1]; ++j)
+			if (ci[j] >= (unsigned)k) { tmp[m].c = ci[j]; tmp[m].v = va[j]; ++m; }
+		qsort(tmp, m, sizeof(ColVal), colval_cmp);
+		for (unsigned e = 0; e < m; ++e) { f->indx[base + e] = tmp[e].c; f->val[base + e] = tmp[e].v; }
+		f->pntr[k + 1] = base + m;
+		if (m == 0 || tmp[0].c != (unsigned)k) { free(tmp); return RS_EZERODIAG; }
+	}
+	free(tmp);
+	f->indx[nz] = 0;
+	unsigned* pntr = f->pntr;
+	unsigned* indx = f->indx;
+	double* val = f->val;
+	for (int k = 0; k < n - 1; ++k) {
+		unsigned d = pntr[k];
+		double z = val[d] = sqrt(val[d]);
+		for (unsigned i = d + 1; i < pntr[k + 1]; ++i) val[i] /= z;
+		for (unsigned i = d + 1; i < pntr[k + 1]; ++i) {
+			z = val[i];
+			unsigned h = indx[i], g = i;
+			for (unsigned j = pntr[h]; j < pntr[h + 1]; ++j)
+				for (; g < pntr[k + 1] && indx[g + 1] <= indx[j]; ++g)
+					if (indx[g] == indx[j]) val[j] -= z * val[g];
+		}
+	}
+	val[pntr[n - 1]] = sqrt(val[pntr[n - 1]]);
+	return 0;
+}
+
+/* ICPre::solve: forward column sweep, then backward sweep */
+static void ic_solve(int n, const IcF* f, const double* x, double* y) {
+	for (int i = 0; i < n; ++i) y[i] = x[i];
+	for (int i = 0; i < n; ++i) {
+		double z = y[i] / f->val[f->pntr[i]];
+		y[i] = z;
+		for (unsigned j = f->pntr[i] + 1; j < f->pntr[i + 1]; ++j) y[f->indx[j]] -= z * f->val[j];
+	}
+	for (int i = n - 1; i >= 0; --i) {
+		double z = 0;
+		for (unsigned j = f->pntr[i] + 1; j < f->pntr[i + 1]; ++j) z += y[f->indx[j]] * f->val[j];
+		y[i] = (y[i] - z) / f->val[f->pntr[i]];
+	}
+}
+
+/* solver_matrix.hpp:318-374 (cgs = 0) and 376-438 (cgs = 1) */
+static int ic_krylov(int cgs, int n, const unsigned* rp, const unsigned* ci,
+		const double* va, const double* b, double* x, int* max_iter, double* tol,
+		double* h, int cap, int* hl) {
+	IcF f;
+	int rc = ic_build(n, rp, ci, va, &f);
+	if (rc) { free(f.pntr); free(f.indx); free(f.val); return rc; }
+	double* w[12];
+	for (int k = 0; k < 12; ++k) w[k] = malloc(sizeof(double) * n);
+	double *r = w[0], *rt = w[1], *p = w[2], *ph = w[3], *q = w[4], *qh = w[5],
+		   *vh = w[6], *u = w[7], *uh = w[8], *z = w[9], *t = w[10], *s = w[11];
+	double resid, alpha, beta, rho_1 = 0.0, rho_2 = 0.0;
+	int ret = 1;
+	double normb = rs_nrm2(n, b);
+	spmv(n, rp, ci, va, x, t, 1);
+	for (int i = 0; i < n; ++i) r[i] = b[i] - t[i];
+	for (int i = 0; i < n; ++i) rt[i] = r[i];
+	if (normb == 0.0) normb = 1;
+	if ((resid = rs_nrm2(n, r) / normb) <= *tol) {
+		*tol = resid;
+		*max_iter = 0;
+		ret = 0;
+		goto done;
+	}
+	for (int it = 1; it <= *max_iter; ++it) {
+		if (!cgs) {
+			ic_solve(n, &f, r, z);
+			double rho = rs_dot(n, r, z);
+			if (it == 1) {
+				for (int i = 0; i < n; ++i) p[i] = z[i];
+			} else {
+				beta = rho / rho_1;
+				for (int i = 0; i < n; ++i) { double tt = beta * p[i]; p[i] = z[i] + tt; }
+			}
+			spmv(n, rp, ci, va, p, q, 1);
+			alpha = rho / rs_dot(n, p, q);
+			for (int i = 0; i < n; ++i) { double tt = alpha * p[i]; x[i] += tt; }
+			for (int i = 0; i < n; ++i) { double tt = alpha * q[i]; r[i] -= tt; }
+			resid = rs_nrm2(n, r) / normb;
+			hist_push(h, cap, hl, resid);
+			if (resid <= *tol) { *tol = resid; *max_iter = it; ret = 0; goto done; }
+			rho_1 = rho;
+			continue;
+		}
+		rho_1 = rs_dot(n, rt, r);
+		if (rho_1 == 0) { *tol = rs_nrm2(n, r) / normb; ret = 2; goto done; }
+		if (it == 1) {
+			for (int i = 0; i < n; ++i) { u[i] = r[i]; p[i] = u[i]; }
+		} else {
+			beta = rho_1 / rho_2;
+			for (int i = 0; i < n; ++i) { double tt = beta * q[i]; u[i] = r[i] + tt; }
+			for (int i = 0; i < n; ++i) {
+				double t1 = beta * p[i];
+				double t2 = q[i] + t1;
+				double t3 = beta * t2;
+				p[i] = u[i] + t3;
+			}
+		}
+		ic_solve(n, &f, p, ph);
+		spmv(n, rp, ci, va, ph, vh, 1);
+		alpha = rho_1 / rs_dot(n, rt, vh);
+		for (int i = 0; i < n; ++i) { double tt = alpha * vh[i]; q[i] = u[i] - tt; }
+		for (int i = 0; i < n; ++i) s[i] = u[i] + q[i];
+		ic_solve(n, &f, s, uh);
+		for (int i = 0; i < n; ++i) { double tt = alpha * uh[i]; x[i] += tt; }
+		spmv(n, rp, ci, va, uh, qh, 1);
+		for (int i = 0; i < n; ++i) { double tt = alpha * qh[i]; r[i] -= tt; }
+		rho_2 = rho_1;
+		resid = rs_nrm2(n, r) / normb;
+		hist_push(h, cap, hl, resid);
+		if (resid < *tol) { *tol = resid; *max_iter = it; ret = 0; goto done; }
+	}
+	*tol = resid;
+done:
+	for (int k = 0; k < 12; ++k) free(w[k]);
+	free(f.pntr); free(f.indx); free(f.val);
+	return ret;
+}
+
 int rs_krylov_csr(int kind, int n, const unsigned* rowptr, const unsigned* col,
 		const double* val, const double* b, double* x, int* max_iter,
 		double* tol, double* hist, int hist_cap, int* hist_len, int threads) {
@@ -331,6 +475,11 @@ int rs_krylov_csr(int kind, int n, const unsigned* rowptr, const unsigned* col,
 	case RS_BICGSTAB:
 		ret = bicgstab(2, n, rowptr, col, val, b, x, max_iter, tol, hist,
 				hist_cap, &hl, threads);
+		break;
+	case RS_IC_CGS:
+	case RS_IC_CG:
+		ret = ic_krylov(kind == RS_IC_CGS, n, rowptr, col, val, b, x, max_iter, tol,
+				hist, hist_cap, &hl);
 		break;
 	default:
 		return -1;

@@ -23,7 +23,8 @@ extern "C" {
 #endif
 
 /* Krylov kinds, in the order of the carpio:: free functions */
-enum { RS_CG = 0, RS_JACOBI = 1, RS_DIA_BICGSTAB = 2, RS_BICGSTAB = 3 };
+enum { RS_CG = 0, RS_JACOBI = 1, RS_DIA_BICGSTAB = 2, RS_BICGSTAB = 3,
+	RS_IC_CGS = 4, RS_IC_CG = 5 };
 #define RS_EZERODIAG (-4)
 
 /* lib/algebra/solver_matrix.hpp:192-260 (Jacobi), 264-316 (CG),

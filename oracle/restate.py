@@ -14,9 +14,9 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _SO = os.path.join(_HERE, "_build", "librestate.so")
 _lib = None
 
-CG, JACOBI, DIA_BICGSTAB, BICGSTAB = 0, 1, 2, 3
+CG, JACOBI, DIA_BICGSTAB, BICGSTAB, IC_CGS, IC_CG = 0, 1, 2, 3, 4, 5
 KINDS = {"cg": CG, "jacobi": JACOBI, "dia_bicgstab": DIA_BICGSTAB,
-         "bicgstab": BICGSTAB}
+         "bicgstab": BICGSTAB, "ic_cgs": IC_CGS, "ic_cg": IC_CG}
 SCHEMES = {"upwind1": 0, "center": 1, "center4": 2, "upwind2": 3,
            "vanleer": 4, "superbee": 5, "wahyd": 6, "quick": 7, "cui": 8,
            "minmod": 9}

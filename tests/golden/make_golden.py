@@ -119,6 +119,9 @@ def main():
         ("csr_pde225_jacobi", ["pde225.mtx", "ones", "zeros", "jacobi", 5000, 1e-8]),
         ("csr_e05r0100_dia_bicgstab",
          ["e05r0100.mtx", "e05r0100_rhs1.mtx", "zeros", "dia_bicgstab", 1000, 1e-8]),
+        ("csr_bus685_ic_cg", ["685_bus.mtx", "ones", "zeros", "ic_cg", 10000, 1e-10]),
+        ("csr_bus685_ic_cgs", ["685_bus.mtx", "ones", "zeros", "ic_cgs", 10000, 1e-10]),
+        ("csr_pde225_ic_cgs", ["pde225.mtx", "ones", "zeros", "ic_cgs", 1000, 1e-10]),
     ]
     for name, c in csr_cases:
         args = ["csr", os.path.join(mtx, c[0])]

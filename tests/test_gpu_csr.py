@@ -22,7 +22,7 @@ def iter_band(kind, ref_it):
     monotone) more; Jacobi (a contraction) hardly at all."""
     if kind.startswith("jacobi"):
         return max(2, ref_it // 200)
-    if kind == "cg":
+    if kind in ("cg", "ic_cg"):
         return max(3, ref_it // 20)
     return max(3, ref_it // 5)
 
@@ -48,19 +48,28 @@ def test_csr_matches_reference(gpu_lib, name):
     # the residual list has one entry per iteration in both implementations
     ref_len = int(d["lresid_len"])
     assert abs(len(lr) - ref_len) <= iter_band(k, ref_len), (len(lr), ref_len)
+    # IC_CGS's recursive residual drifts away from the true one (in the
+    # reference too: 7.2e-6 true against 9e-11 recursive on 685_bus), so its
+    # solutions agree to that attainable accuracy, not to tol
+    ref_true = true_resid(A, d["x"], b) if k == "ic_cgs" else 0.0
     if code == 0:
-        assert (t <= tol) if k in ("cg", "jacobi") else (t < tol)
+        assert (t <= tol) if k in ("cg", "jacobi", "ic_cg") else (t < tol)
         # the reported residual is the recursive one; the true residual of
         # the returned x must agree with it
-        assert true_resid(A, x, b) <= 10 * tol
+        assert true_resid(A, x, b) <= 10 * max(tol, ref_true)
         # BiCGSTAB's early exit on |s| (solver_matrix.hpp:642-647) leaves
         # max_iter unchanged; which exit fires first is rounding-dependent
         assert it == len(lr) - (1 if k == "dia_bicgstab" and it == max_iter else 0) \
             or it == max_iter
-    assert rel_l2(x, d["x"]) <= 1e3 * tol, rel_l2(x, d["x"])
+    if np.isnan(d["x"]).any():
+        # IC_CGS on pde225: a negative pivot in the factor, NaN throughout
+        assert np.isnan(t) and np.isnan(x).all() == np.isnan(d["x"]).all()
+        return
+    assert rel_l2(x, d["x"]) <= max(1e3 * tol, ref_true), rel_l2(x, d["x"])
 
 
-@pytest.mark.parametrize("mtx,kind", [("csr_pde225_bicgstab", "bicgstab"),
+@pytest.mark.parametrize("mtx,kind", [("csr_bus685_ic_cg", "ic_cg"),
+                                      ("csr_bus685_ic_cgs", "ic_cgs"),("csr_pde225_bicgstab", "bicgstab"),
                                       ("csr_pde225_bicgstab", "dia_bicgstab"),
                                       ("csr_pde225_bicgstab", "cg"),
                                       ("csr_bus685_cg", "cg"),
@@ -80,6 +89,9 @@ def test_csr_tight_tolerance_parity(gpu_lib, mtx, kind):
                                       np.zeros(A.iLen()), 20000, 1e-13)
     assert code == c2 == 0
     bar = 1e-9 if "bus685" in mtx else 1e-10
+    if kind == "ic_cgs":
+        # the attainable accuracy: the oracle's own true residual
+        bar = max(bar, true_resid(A, x2, d["b"]))
     assert rel_l2(x, x2) <= bar, rel_l2(x, x2)
 
 

@@ -47,7 +47,9 @@ def test_csr_solvers_bitwise(name):
                                         d["b"], d["x0"], max_iter, tol)
     assert code == int(d["ret"])
     assert it == int(d["max_iter_out"])
-    assert t == float(d["tol_out"])
+    # (IC_CGS on pde225: the factor takes the square root of a negative
+    # pivot and everything after is NaN, in the reference too)
+    assert bits_equal(t, float(d["tol_out"]))
     assert bits_equal(x, d["x"])
     check_hist(d, hist)
 
