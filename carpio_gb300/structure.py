@@ -355,7 +355,8 @@ class NS_explicit:
 
     def state(self, out=None):
         """the fields (and dt) as host arrays; `out`: a dict of arrays to
-        fill instead (e.g. pinned torch tensors)"""
+        fill instead (e.g. pinned torch tensors; the returned dict holds
+        them plus dt, `out` itself is not changed)"""
         g = self.grid
         if out is None:
             out = {k: g.zeros() for k in ("u", "v", "uf", "vf", "phi", "p")}
@@ -365,8 +366,9 @@ class NS_explicit:
             *[_lib.ptr(out[k]) for k in ("u", "v", "uf", "vf", "phi", "p")])
         if rc:
             raise _lib.CarpioGpuError(rc, "ns_get_state")
-        out["dt"] = dt.value
-        return out
+        res = dict(out)
+        res["dt"] = dt.value
+        return res
 
     def get_CS(self, name):
         return self.state()[name]
