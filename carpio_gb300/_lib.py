@@ -115,6 +115,10 @@ SIGNATURES = {
         _VP, _D, _VP, _VP, _VP, _VP, _VP, _VP]),
     "carpio_gpu_ns_run": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, _VP]),
     "carpio_gpu_ns_set_stepper": (ctypes.c_int, [_VP, ctypes.c_int]),
+    "carpio_gpu_poisson_solve_beta": (ctypes.c_int, [
+        _VP, ctypes.POINTER(BC), _VP, _VP, _VP,
+        ctypes.POINTER(SolverCfg), _VP, ctypes.c_int,
+        ctypes.POINTER(SolverStats)]),
     "carpio_gpu_helmholtz_solve": (ctypes.c_int, [
         _VP, ctypes.POINTER(BC), ctypes.c_double, ctypes.c_double, _VP, _VP,
         ctypes.POINTER(SolverCfg), _VP, ctypes.c_int,

@@ -88,8 +88,9 @@ struct StencilCoeffs {
 	bool helm = false;            // StencilHelmholtz_: diagonal + sx sy alpha
 	double alpha = 0;
 	DevBuf D, ax, ay, fold, D32, ax32, ay32;
-	bool uniform = true;          // all weights 1: no wx/wy
-	DevBuf wx, wy, wx32, wy32;    // face-size weights of a non-uniform grid
+	bool uniform = true;          // rows described by ax / ay
+	bool bfield_free = true;      // built without a beta field
+	DevBuf cf, cf32;              // otherwise: per-cell coefficients x-, x+, y-, y+
 };
 
 struct PoissonWs {
@@ -97,8 +98,12 @@ struct PoissonWs {
 	DevBuf v64, v32, src, phi, hist, out, xbuf;
 };
 
+// bfield: a variable beta (StencilPoisson_ with a beta field, face values
+// by _build_default_beta, s_poisson.hpp:144-164), host or device, in the
+// host field layout (nx + 2 gl) x (ny + 2 gl); null: the uniform beta
 int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
-		StencilCoeffs& c, cudaStream_t s, bool helm = false, double alpha = 0.0);
+		StencilCoeffs& c, cudaStream_t s, bool helm = false, double alpha = 0.0,
+		const double* bfield = nullptr);
 
 // Centres and sizes of the n + 2 gl cells of one uniform axis.
 void uniform_axis(int n, int gl, double lo, double hi, std::vector<double>& c,
@@ -110,7 +115,8 @@ void stencil_host(int nx, int ny, int gl, int P, const std::vector<double>& cx,
 		const std::vector<double>& sx, const std::vector<double>& cy,
 		const std::vector<double>& sy, const carpio_gpu_bc& bc, double beta,
 		std::vector<double>& D, std::vector<double>& ax, std::vector<double>& ay,
-		std::vector<double>& fold, bool helm = false, double alpha = 0.0);
+		std::vector<double>& fold, bool helm = false, double alpha = 0.0,
+		std::vector<double>* cf = nullptr, const double* bfield = nullptr);
 
 // Workspace of the learned-preconditioner solve (learned.cu).
 struct LearnedWs {

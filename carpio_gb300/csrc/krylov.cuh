@@ -60,29 +60,29 @@ struct StencilOp {
 	const R* D;
 	const R* ax;  // [nx+1]: x-face coefficients of row 0
 	const R* ay;  // [ny+1]: y-face coefficients of column 0
-	// non-uniform grids (NU): the x-face coefficient of cell row j is
-	// ax[i] wy[j] (face height sy_j / sy_0), the y-face one ay[j] wx[i];
-	// unused (null) on uniform grids, where the weights would all be 1
-	const R* wx = nullptr;  // [nx]
-	const R* wy = nullptr;  // [ny]
-	__device__ __forceinline__ void coeffs(int i, int j, R& xm, R& xp, R& ym, R& yp) const {
-		xm = ax[i];
-		xp = ax[i + 1];
-		ym = ay[j];
-		yp = ay[j + 1];
+	// general rows (NU: non-uniform grids, variable beta): each cell's own
+	// four off-diagonal coefficients, arrays in the field layout (x-, x+,
+	// y-, y+ one field apart); unused (null) when ax / ay describe the rows
+	const R* cf = nullptr;
+	size_t cfs = 0;                // distance between the four arrays
+	__device__ __forceinline__ void coeffs(int i, int j, int a, R& xm, R& xp, R& ym, R& yp) const {
 		if constexpr (NU) {
-			const R w = wy[j], v = wx[i];
-			xm *= w;
-			xp *= w;
-			ym *= v;
-			yp *= v;
+			xm = cf[a];
+			xp = cf[cfs + a];
+			ym = cf[2 * cfs + a];
+			yp = cf[3 * cfs + a];
+		} else {
+			xm = ax[i];
+			xp = ax[i + 1];
+			ym = ay[j];
+			yp = ay[j + 1];
 		}
 	}
 	__device__ __forceinline__ R apply(const R* p, int k, int a) const {
 		int i, j;
 		sp.ij(k, i, j);
 		R xm, xp, ym, yp;
-		coeffs(i, j, xm, xp, ym, yp);
+		coeffs(i, j, a, xm, xp, ym, yp);
 		R c = D[a] * ldcg(p + a);
 		c = fma(xm, ldcg(p + a - sp.P), c);
 		c = fma(xp, ldcg(p + a + sp.P), c);
@@ -95,7 +95,7 @@ struct StencilOp {
 		int i, j;
 		sp.ij(k, i, j);
 		R xm, xp, ym, yp;
-		coeffs(i, j, xm, xp, ym, yp);
+		coeffs(i, j, a, xm, xp, ym, yp);
 		R d = D[a], s = 0;
 		s = fma(-xm / d, ldcg(x + a - sp.P), s);
 		s = fma(-ym / d, ldcg(x + a - 1), s);

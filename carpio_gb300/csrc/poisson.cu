@@ -695,11 +695,32 @@ void stencil_host(int nx, int ny, int gl, int P, const std::vector<double>& cx,
 		const std::vector<double>& sx, const std::vector<double>& cy,
 		const std::vector<double>& sy, const carpio_gpu_bc& bc, double beta,
 		std::vector<double>& D, std::vector<double>& ax, std::vector<double>& ay,
-		std::vector<double>& fold, bool helm, double alpha) {
+		std::vector<double>& fold, bool helm, double alpha, std::vector<double>* cf,
+		const double* bfield) {
 	auto CX = [&](int i) { return cx[i + gl]; };
 	auto CY = [&](int j) { return cy[j + gl]; };
 	auto SX = [&](int i) { return sx[i + gl]; };
 	auto SY = [&](int j) { return sy[j + gl]; };
+	const size_t NF = (size_t)(nx + 2 * gl) * P;
+	if (cf) cf->assign(4 * NF, 0.0);
+	// face value of a beta field (StencilPoisson_::_build_default_beta,
+	// s_poisson.hpp:144-164): weights df_ = |half size - centre|
+	// (Grid_::df_, s_grid.hpp:226-230) of the cell and of its neighbour on
+	// the face's side, values of the cell and of its + neighbour (the
+	// reference takes index.p(dim) for both faces)
+	const int NJ = ny + 2 * gl;
+	auto BF = [&](int i, int j) { return bfield[(size_t)(i + gl) * NJ + (j + gl)]; };
+	auto DFX = [&](int i) { return std::fabs(SX(i) * 0.5 - CX(i)); };
+	auto DFY = [&](int j) { return std::fabs(SY(j) * 0.5 - CY(j)); };
+	auto betaf = [&](int i, int j, int dim, int ori) {
+		if (!bfield) return beta;
+		const double v = BF(i, j);
+		const double df = dim == 0 ? DFX(i) : DFY(j);
+		const double vo = dim == 0 ? BF(i + 1, j) : BF(i, j + 1);
+		const int o = ori == 0 ? -1 : 1;
+		const double dfo = dim == 0 ? DFX(i + o) : DFY(j + o);
+		return (df * v + dfo * vo) / (df + dfo);
+	};
 	D.assign((size_t)(nx + 2 * gl) * P, 0.0);
 	ax.assign(nx + 1, 0.0);
 	ay.assign(ny + 1, 0.0);
@@ -734,10 +755,10 @@ void stencil_host(int nx, int ny, int gl, int P, const std::vector<double>& cx,
 	for (int j = 0; j < ny; ++j) {
 		for (int i = 0; i < nx; ++i) {
 			double axf = SY(j) * 1.0, ayf = 1.0 * SX(i);
-			double cxp = (-beta) * axf / std::fabs(CX(i) - CX(i + 1));
-			double cxm = (-beta) * axf / std::fabs(CX(i) - CX(i - 1));
-			double cyp = (-beta) * ayf / std::fabs(CY(j) - CY(j + 1));
-			double cym = (-beta) * ayf / std::fabs(CY(j) - CY(j - 1));
+			double cxp = (-betaf(i, j, 0, 1)) * axf / std::fabs(CX(i) - CX(i + 1));
+			double cxm = (-betaf(i, j, 0, 0)) * axf / std::fabs(CX(i) - CX(i - 1));
+			double cyp = (-betaf(i, j, 1, 1)) * ayf / std::fabs(CY(j) - CY(j + 1));
+			double cym = (-betaf(i, j, 1, 0)) * ayf / std::fabs(CY(j) - CY(j - 1));
 			double coec = 0;
 			coec += -cxm;
 			coec += -cxp;
@@ -767,18 +788,39 @@ void stencil_host(int nx, int ny, int gl, int P, const std::vector<double>& cx,
 			if (j == 0 && i == nx - 1) ax[nx] = 0.0;
 			if (i == 0) ay[j] = j == 0 ? 0.0 : cym;
 			if (i == 0 && j == ny - 1) ay[ny] = 0.0;
+			if (cf) {
+				// the row's own coefficients; boundary faces are folded
+				const size_t a = (size_t)(i + gl) * P + (j + gl);
+				(*cf)[a] = i == 0 ? 0.0 : cxm;
+				(*cf)[NF + a] = i == nx - 1 ? 0.0 : cxp;
+				(*cf)[2 * NF + a] = j == 0 ? 0.0 : cym;
+				(*cf)[3 * NF + a] = j == ny - 1 ? 0.0 : cyp;
+			}
 		}
 	}
 }
 
 int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
-		StencilCoeffs& c, cudaStream_t s, bool helm, double alpha) {
-	if (c.valid && same_bc(c.bc, bc) && c.beta == beta && c.helm == helm
-			&& (!helm || c.alpha == alpha))
+		StencilCoeffs& c, cudaStream_t s, bool helm, double alpha,
+		const double* bfield) {
+	// a beta field is read afresh every time (its contents are not tracked)
+	if (!bfield && c.valid && c.bfield_free && same_bc(c.bc, bc) && c.beta == beta
+			&& c.helm == helm && (!helm || c.alpha == alpha))
 		return 0;
-	std::vector<double> D, ax, ay, fold;
-	stencil_host(g->nx, g->ny, g->gl, g->P, g->cx, g->sx, g->cy, g->sy, bc, beta,
-			D, ax, ay, fold, helm, alpha);
+	const int gl = g->gl;
+	bool uniform = !bfield;
+	for (int i = 1; i < g->nx && uniform; ++i) uniform = g->sx[i + gl] == g->sx[gl];
+	for (int j = 1; j < g->ny && uniform; ++j) uniform = g->sy[j + gl] == g->sy[gl];
+	std::vector<double> bhost;
+	if (bfield && is_device_ptr(bfield)) {
+		bhost.resize((size_t)g->NI * g->NJ);
+		CG_CK(cudaMemcpy(bhost.data(), bfield, sizeof(double) * bhost.size(),
+				cudaMemcpyDeviceToHost));
+		bfield = bhost.data();
+	}
+	std::vector<double> D, ax, ay, fold, cf;
+	stencil_host(g->nx, g->ny, gl, g->P, g->cx, g->sx, g->cy, g->sy, bc, beta,
+			D, ax, ay, fold, helm, alpha, uniform ? nullptr : &cf, bfield);
 	std::vector<float> D32(D.size()), ax32(ax.size()), ay32(ay.size());
 	for (size_t k = 0; k < D.size(); ++k) D32[k] = (float)D[k];
 	for (size_t k = 0; k < ax.size(); ++k) ax32[k] = (float)ax[k];
@@ -791,28 +833,15 @@ int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
 	if ((rc = to_device(c.D32, D32.data(), sizeof(float) * D32.size(), s))) return rc;
 	if ((rc = to_device(c.ax32, ax32.data(), sizeof(float) * ax32.size(), s))) return rc;
 	if ((rc = to_device(c.ay32, ay32.data(), sizeof(float) * ay32.size(), s))) return rc;
-	// a non-uniform grid: the face coefficients above belong to row /
-	// column 0; every other row and column scales them by its face size
-	const int gl = g->gl;
-	std::vector<double> wx(g->nx), wy(g->ny);
-	bool uniform = true;
-	for (int i = 0; i < g->nx; ++i) {
-		wx[i] = g->sx[i + gl] / g->sx[gl];
-		uniform = uniform && wx[i] == 1.0;
-	}
-	for (int j = 0; j < g->ny; ++j) {
-		wy[j] = g->sy[j + gl] / g->sy[gl];
-		uniform = uniform && wy[j] == 1.0;
-	}
-	std::vector<float> wx32(wx.begin(), wx.end()), wy32(wy.begin(), wy.end());
+	// a non-uniform grid or a beta field: every row's own four coefficients
+	std::vector<float> cf32(cf.begin(), cf.end());
 	if (!uniform) {
-		if ((rc = to_device(c.wx, wx.data(), sizeof(double) * wx.size(), s))) return rc;
-		if ((rc = to_device(c.wy, wy.data(), sizeof(double) * wy.size(), s))) return rc;
-		if ((rc = to_device(c.wx32, wx32.data(), sizeof(float) * wx32.size(), s))) return rc;
-		if ((rc = to_device(c.wy32, wy32.data(), sizeof(float) * wy32.size(), s))) return rc;
+		if ((rc = to_device(c.cf, cf.data(), sizeof(double) * cf.size(), s))) return rc;
+		if ((rc = to_device(c.cf32, cf32.data(), sizeof(float) * cf32.size(), s))) return rc;
 	}
 	CG_CK(cudaStreamSynchronize(s));  // host vectors go out of scope
 	c.uniform = uniform;
+	c.bfield_free = !bfield;
 	c.bc = bc;
 	c.beta = beta;
 	c.helm = helm;
@@ -849,8 +878,8 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 	op.D = c.D.as<double>();
 	op.ax = c.ax.as<double>();
 	op.ay = c.ay.as<double>();
-	op.wx = c.uniform ? nullptr : c.wx.as<double>();
-	op.wy = c.uniform ? nullptr : c.wy.as<double>();
+	op.cf = c.uniform ? nullptr : c.cf.as<double>();
+	op.cfs = (size_t)g->NI * g->P;
 	Vecs<double> v;
 	double* base = w.v64.as<double>();
 	double** slots[nv64] = { &v.x, &v.b, &v.r, &v.p, &v.q, &v.z, &v.rt, &v.ph,
@@ -861,8 +890,8 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 	mx.op32.D = c.D32.as<float>();
 	mx.op32.ax = c.ax32.as<float>();
 	mx.op32.ay = c.ay32.as<float>();
-	mx.op32.wx = c.uniform ? nullptr : c.wx32.as<float>();
-	mx.op32.wy = c.uniform ? nullptr : c.wy32.as<float>();
+	mx.op32.cf = c.uniform ? nullptr : c.cf32.as<float>();
+	mx.op32.cfs = (size_t)g->NI * g->P;
 	std::memset(&mx.f, 0, sizeof mx.f);
 	if (mixed) {
 		float* fb = w.v32.as<float>();
@@ -1101,8 +1130,8 @@ int carpio_gpu_grid_coords(const carpio_gpu_grid* g, double* cx, double* sx,
 // Poisson_::run for a set_depend'ed field; helm: the StencilHelmholtz_
 // variant (Poisson_ with an alpha term, s_poisson.hpp:343-347, 577-590)
 static int structured_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
-		bool helm, double alpha, double beta, const double* source, double* phi,
-		const carpio_gpu_solver_cfg* cfg, double* resid_hist, int hist_cap,
+		bool helm, double alpha, double beta, const double* bfield, const double* source,
+		double* phi, const carpio_gpu_solver_cfg* cfg, double* resid_hist, int hist_cap,
 		carpio_gpu_solver_stats* stats) {
 	using namespace cg_host;
 	if (!g || !bc || !source || !phi || !cfg || cfg->max_iter < 0
@@ -1116,7 +1145,7 @@ static int structured_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
 	std::lock_guard<std::mutex> lock(g->mu);
 	cudaStream_t s = g->stream;
 	int rc;
-	if ((rc = stencil_prepare(g, *bc, beta, g->coeffs, s, helm, alpha))) return rc;
+	if ((rc = stencil_prepare(g, *bc, beta, g->coeffs, s, helm, alpha, bfield))) return rc;
 	PoissonWs& w = g->pws;
 	const size_t NF = (size_t)g->NI * g->P;
 	if ((rc = w.src.ensure(sizeof(double) * NF))) return rc;
@@ -1174,15 +1203,24 @@ int carpio_gpu_poisson_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
 		double beta, const double* source, double* phi,
 		const carpio_gpu_solver_cfg* cfg, double* resid_hist, int hist_cap,
 		carpio_gpu_solver_stats* stats) {
-	return structured_solve(g, bc, false, 0.0, beta, source, phi, cfg, resid_hist,
+	return structured_solve(g, bc, false, 0.0, beta, nullptr, source, phi, cfg, resid_hist,
 			hist_cap, stats);
+}
+
+int carpio_gpu_poisson_solve_beta(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
+		const double* beta_field, const double* source, double* phi,
+		const carpio_gpu_solver_cfg* cfg, double* resid_hist, int hist_cap,
+		carpio_gpu_solver_stats* stats) {
+	if (!beta_field) return CARPIO_GPU_EINVAL;
+	return structured_solve(g, bc, false, 0.0, 1.0, beta_field, source, phi, cfg,
+			resid_hist, hist_cap, stats);
 }
 
 int carpio_gpu_helmholtz_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
 		double alpha, double beta, const double* source, double* phi,
 		const carpio_gpu_solver_cfg* cfg, double* resid_hist, int hist_cap,
 		carpio_gpu_solver_stats* stats) {
-	return structured_solve(g, bc, true, alpha, beta, source, phi, cfg, resid_hist,
+	return structured_solve(g, bc, true, alpha, beta, nullptr, source, phi, cfg, resid_hist,
 			hist_cap, stats);
 }
 

@@ -176,6 +176,12 @@ class Poisson:
     def set_solver(self, name, any_=None, max_iter=1000, tol=1e-3, **kw):
         self.cfg = solver_cfg(name, max_iter, tol, **kw)
 
+    def set_beta(self, field):
+        """a beta field (full field with ghosts), as set_depend(phi, spbeta,
+        source) gives the reference's Poisson_; None: back to the uniform
+        beta"""
+        self.beta_field = field
+
     def set_uniform_alpha(self, a=1.0):
         """Poisson_::set_uniform_alpha (s_poisson.hpp:461-471): the
         StencilHelmholtz_ rows with a uniform alpha"""
@@ -213,7 +219,13 @@ class Poisson:
             return rc
         cap = self.cfg.max_iter + 2
         hist = np.zeros(max(cap, 1))
-        if getattr(self, "alpha", None) is not None:
+        if getattr(self, "beta_field", None) is not None:
+            bf = np.ascontiguousarray(self.beta_field, dtype=np.float64)
+            rc = L.carpio_gpu_poisson_solve_beta(
+                self.grid.handle, ctypes.byref(bc), _lib.ptr(bf),
+                _lib.ptr(self.source), _lib.ptr(self.phi), ctypes.byref(self.cfg),
+                _lib.ptr(hist), cap, ctypes.byref(self.stats))
+        elif getattr(self, "alpha", None) is not None:
             rc = L.carpio_gpu_helmholtz_solve(
                 self.grid.handle, ctypes.byref(bc), self.alpha, self.beta,
                 _lib.ptr(self.source), _lib.ptr(self.phi), ctypes.byref(self.cfg),

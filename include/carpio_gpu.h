@@ -196,6 +196,17 @@ int carpio_gpu_poisson_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
  * the StencilHelmholtz_ rows (s_poisson.hpp:185-258), diagonal plus
  * sx sy alpha and the source scaled by sx sy; otherwise as
  * carpio_gpu_poisson_solve. */
+/* Poisson_ with a beta field (set_depend with spbeta, s_poisson.hpp:513-533):
+ * face values by StencilPoisson_::_build_default_beta (s_poisson.hpp:
+ * 144-164), as the reference computes them (weights |half size - centre| of
+ * the cell and its face-side neighbour, values of the cell and its +
+ * neighbour), so the rows are not symmetric in general (use BiCGSTAB or
+ * Jacobi). beta_field: full field with ghosts, host or device; the mixed
+ * on-chip path is not used. Otherwise as carpio_gpu_poisson_solve. */
+int carpio_gpu_poisson_solve_beta(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
+		const double* beta_field, const double* source, double* phi,
+		const carpio_gpu_solver_cfg* cfg, double* resid_hist, int hist_cap,
+		carpio_gpu_solver_stats* stats);
 int carpio_gpu_helmholtz_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
 		double alpha, double beta, const double* source, double* phi,
 		const carpio_gpu_solver_cfg* cfg, double* resid_hist, int hist_cap,

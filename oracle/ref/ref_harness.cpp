@@ -307,6 +307,7 @@ static int cmd_csr(int argc, char** argv) {
 //          mean removed from b and x
 //  mixed   [0,1]^2, seg0 Dirichlet 1, seg1 Dirichlet -0.5, seg2 Neumann 0.75,
 //          seg3 Neumann -1.25, f = 20 cos(3 pi x) sin(2 pi y)
+//  vbeta   as mixed with beta = 1.2 + 0.5 sin(2 pi x) cos(pi y) as a field
 static int cmd_poisson(int argc, char** argv) {
 	if (argc < 9) return 2;
 	std::string cs = argv[2];
@@ -342,7 +343,7 @@ static int cmd_poisson(int argc, char** argv) {
 		spScalar phi(new Scalar(g));
 		put_field("source_field", *src);
 		P.set_depend(phi, nullptr, src);
-	} else if (cs == "mixed") {
+	} else if (cs == "mixed" || cs == "vbeta") {
 		double vals[4] = { 1.0, -0.5, 0.75, -1.25 };
 		for (int d = 0; d < 4; ++d) {
 			Poisson_<2>::spBC bc(new Poisson_<2>::BC());
@@ -354,10 +355,15 @@ static int cmd_poisson(int argc, char** argv) {
 			return 20.0 * std::cos(3 * carpio::PI * x)
 					* std::sin(2 * carpio::PI * y);
 		});
+		if (cs == "vbeta")
+			P.set_beta([](Vt t, Vt x, Vt y, Vt z) {
+				return 1.2 + 0.5 * std::sin(2 * carpio::PI * x) * std::cos(carpio::PI * y);
+			});
 	} else {
 		return 2;
 	}
 	P.run();
+	if (cs == "vbeta") put_field("beta_field", *P.get_CS("beta"));
 	put_field("phi", *P.get_CS("phi"));
 	put_field("source", *P.get_CS("source"));
 	const SolveRecord& r = rec.back();

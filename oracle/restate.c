@@ -563,7 +563,7 @@ static void poly_insert(term* row, int* len, double c, int i, int j, int e) {
 int rs_assemble_poisson(int nx, int ny, int gl, const double* cx,
 		const double* sx, const double* cy, const double* sy, const rs_bc* bc,
 		double beta, const double* src, double src_value, unsigned* rowptr,
-		unsigned* col, double* val, double* b) {
+		unsigned* col, double* val, double* b, const double* bfield) {
 	const int NJ = ny + 2 * gl;
 	int nz = 0;
 	rowptr[0] = 0;
@@ -575,10 +575,26 @@ int rs_assemble_poisson(int nx, int ny, int gl, const double* cx,
 			 * -betaf * a / d, with a the face area (s_y for x faces, s_x for
 			 * y faces) and d the centre distance */
 			double ax = SY(j) * 1.0, ay = 1.0 * SX(i);
-			double cxp = (-beta) * ax / fabs(CX(i) - CX(i + 1));
-			double cxm = (-beta) * ax / fabs(CX(i) - CX(i - 1));
-			double cyp = (-beta) * ay / fabs(CY(j) - CY(j + 1));
-			double cym = (-beta) * ay / fabs(CY(j) - CY(j - 1));
+			/* a beta field: _build_default_beta (s_poisson.hpp:144-164), the
+			 * face value from the cell and its + neighbour, weighted by
+			 * Grid_::df_ = |half size - centre| of the cell and of its
+			 * neighbour on the face's side */
+			double bxp = beta, bxm = beta, byp = beta, bym = beta;
+			if (bfield) {
+#define DFX(k) fabs(SX(k) * 0.5 - CX(k))
+#define DFY(k) fabs(SY(k) * 0.5 - CY(k))
+				double v = AT(bfield, i, j), vx = AT(bfield, i + 1, j), vy = AT(bfield, i, j + 1);
+				bxp = (DFX(i) * v + DFX(i + 1) * vx) / (DFX(i) + DFX(i + 1));
+				bxm = (DFX(i) * v + DFX(i - 1) * vx) / (DFX(i) + DFX(i - 1));
+				byp = (DFY(j) * v + DFY(j + 1) * vy) / (DFY(j) + DFY(j + 1));
+				bym = (DFY(j) * v + DFY(j - 1) * vy) / (DFY(j) + DFY(j - 1));
+#undef DFX
+#undef DFY
+			}
+			double cxp = (-bxp) * ax / fabs(CX(i) - CX(i + 1));
+			double cxm = (-bxm) * ax / fabs(CX(i) - CX(i - 1));
+			double cyp = (-byp) * ay / fabs(CY(j) - CY(j + 1));
+			double cym = (-bym) * ay / fabs(CY(j) - CY(j - 1));
 			/* coe_row (s_poisson.hpp:85-102) */
 			poly_insert(row, &len, cxp, i + 1, j, 1);
 			poly_insert(row, &len, cxm, i - 1, j, 1);
@@ -976,7 +992,7 @@ int rs_ns_run(int nx, int ny, int gl, const double* cx, const double* sx,
 		/* projection: Poisson_::run with set_depend(phi, -, div), the
 		 * CG + mean-removal drop-in solver */
 		rs_assemble_poisson(nx, ny, gl, cx, sx, cy, sy, &bc_phi, 1.0, div, 0.0,
-				rp, ci, va, b);
+				rp, ci, va, b, NULL);
 		for (int j = 0; j < ny; ++j)
 			for (int i = 0; i < nx; ++i) x[i + j * nx] = AT(phi, i, j);
 		double m = 0;

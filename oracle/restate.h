@@ -63,7 +63,7 @@ typedef struct {
 int rs_assemble_poisson(int nx, int ny, int gl, const double* cx,
 		const double* sx, const double* cy, const double* sy, const rs_bc* bc,
 		double beta, const double* src, double src_value, unsigned* rowptr,
-		unsigned* col, double* val, double* b);
+		unsigned* col, double* val, double* b, const double* bfield);
 
 /* Equation_::apply_bc (s_equation.hpp:340-378) on a cell field. */
 void rs_apply_bc(int nx, int ny, int gl, const double* cx, const double* sx,

@@ -67,7 +67,7 @@ def lib():
         L.rs_assemble_poisson.argtypes = [
             ctypes.c_int, ctypes.c_int, ctypes.c_int, _d, _d, _d, _d,
             ctypes.POINTER(BC), ctypes.c_double, _d, ctypes.c_double, _u, _u,
-            _d, _d]
+            _d, _d, _d]
         L.rs_assemble_poisson.restype = ctypes.c_int
         L.rs_apply_bc.argtypes = [ctypes.c_int] * 3 + [_d] * 4 + [
             ctypes.POINTER(BC), _d]
@@ -171,7 +171,9 @@ def krylov_csr(kind, rowptr, colind, val, b, x0, max_iter, tol,
     return code, x, mi.value, t.value, hist[:min(hl.value, cap)]
 
 
-def assemble_poisson(grid, bc, beta=1.0, src=None, src_value=0.0):
+def assemble_poisson(grid, bc, beta=1.0, src=None, src_value=0.0, bfield=None):
+    """StencilPoisson_ + GhostRegular_ assembled as Solver_::_build_matrix;
+    bfield: a beta field (full field with ghosts) instead of the uniform beta"""
     L = lib()
     n = grid.nx * grid.ny
     rp = np.zeros(n + 1, dtype=np.uint32)
@@ -183,7 +185,8 @@ def assemble_poisson(grid, bc, beta=1.0, src=None, src_value=0.0):
                                float(beta),
                                _p(s) if s is not None else None,
                                float(src_value), _p(rp, _u), _p(ci, _u),
-                               _p(va), _p(b))
+                               _p(va), _p(b),
+                               _p(_f64(bfield)) if bfield is not None else None)
     return rp, ci[:nz].copy(), va[:nz].copy(), b
 
 

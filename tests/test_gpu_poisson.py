@@ -12,6 +12,7 @@ BCS = {
     "c1": ([1] * 4, [0.0] * 4),
     "neumann": ([2] * 4, [0.0] * 4),
     "mixed": ([1, 1, 2, 2], [1.0, -0.5, 0.75, -1.25]),
+    "vbeta": ([1, 1, 2, 2], [1.0, -0.5, 0.75, -1.25]),
 }
 NAMES = {"cg": "CG", "jacobi": "Jacobi", "dia_bicgstab": "Dia_BiCGSTAB",
          "bicgstab": "BiCGSTAB"}
@@ -31,6 +32,8 @@ def make_poisson(n, case, kind, max_iter, tol, source, phi=None, nx=None,
             bc.set_default_2_bc(vals[seg])
         P.add_bc(0, seg, "phi", bc)
     P.set_depend(g.zeros() if phi is None else phi.copy(), None, source)
+    if fixture is not None and "beta_field" in fixture:
+        P.set_beta(fixture["beta_field"])
     P.set_solver(NAMES[kind], None, max_iter, tol,
                  mean_removal=(case == "neumann"), **kw)
     return g, P
@@ -71,17 +74,23 @@ def test_poisson_matches_reference(gpu_lib, name):
                                              ("mixed", 24, "dia_bicgstab", ""),
                                              ("mixed", 24, "bicgstab", ""),
                                              ("mixed", 24, "cg", "_stretch"),
-                                             ("neumann", 32, "cg", "_stretch")])
+                                             ("neumann", 32, "cg", "_stretch"),
+                                             ("vbeta", 24, "bicgstab", ""),
+                                             ("vbeta", 20, "jacobi", "")])
 def test_poisson_tight_tolerance_parity(gpu_lib, case, n, kind, sfx):
     """Matrix-free GPU solve and the oracle (assembled CSR, reference
     arithmetic) both to 1e-13: relative L2 <= 1e-10 (the plain-path bar);
     `_stretch`: on the fixture's non-uniform grid."""
-    d = golden((f"poisson_{case}_{n}_cg" if case != "mixed" else "poisson_mixed_24_cg") + sfx)
+    if case == "vbeta":
+        d = golden(f"poisson_vbeta_{n}_{kind}")
+    else:
+        d = golden((f"poisson_{case}_{n}_cg" if case != "mixed" else "poisson_mixed_24_cg") + sfx)
     src = d["source"]
     g, P = make_poisson(n, case, kind, 50000, 1e-13, src, fixture=d)
     assert P.run() == 0
     og = oracle_grid(d, n, n, 2)
-    rp, ci, va, b = R.assemble_poisson(og, R.make_bc(*BCS[case]), 1.0, src=src)
+    rp, ci, va, b = R.assemble_poisson(og, R.make_bc(*BCS[case]), 1.0, src=src,
+                                       bfield=d.get("beta_field"))
     if case == "neumann":
         b = b - b.mean()
     code, x, it, t, _ = R.krylov_csr(kind, rp, ci, va, b, np.zeros(n * n), 50000, 1e-13)

@@ -11,6 +11,7 @@ BC_CASES = {
     "c1": R.make_bc([1] * 4, [0.0] * 4),
     "neumann": R.make_bc([2] * 4, [0.0] * 4),
     "mixed": R.make_bc([1, 1, 2, 2], [1.0, -0.5, 0.75, -1.25]),
+    "vbeta": R.make_bc([1, 1, 2, 2], [1.0, -0.5, 0.75, -1.25]),
 }
 
 
@@ -67,7 +68,8 @@ def poisson_inputs(d):
     case, n = str(d["case_args"][1]), int(d["case_args"][2])
     g = oracle_grid(d, n, n, 2)
     assert bits_equal(g.cx, d["grid_cx"]) and bits_equal(g.sy, d["grid_sy"])
-    rp, ci, va, b = R.assemble_poisson(g, BC_CASES[case], 1.0, src=d["source"])
+    rp, ci, va, b = R.assemble_poisson(g, BC_CASES[case], 1.0, src=d["source"],
+                                       bfield=d.get("beta_field"))
     return case, g, rp, ci, va, b
 
 
