@@ -234,6 +234,33 @@ __device__ __forceinline__ double diffusion(const Geo& g, double mu,
 	return res;
 }
 
+// NablaMuNabla(const Scalar& mu, ...) (s_operation.hpp:630-662): face mu
+// from the cell and its neighbour weighted by the half sizes
+__device__ __forceinline__ double diffusion_var(const Geo& g, const double* mu,
+		const double* f, int i, int j) {
+	const int a = g.at(i, j);
+	double t[2];
+#pragma unroll
+	for (int d = 0; d < 2; ++d) {
+		const int st = d == 0 ? g.P : 1;
+		const double hs = (d == 0 ? g.SX(i) : g.SY(j)) * 0.5;
+		const double hsp = (d == 0 ? g.SX(i + 1) : g.SY(j + 1)) * 0.5;
+		const double hsm = (d == 0 ? g.SX(i - 1) : g.SY(j - 1)) * 0.5;
+		const double c = d == 0 ? g.CX(i) : g.CY(j);
+		const double cp = d == 0 ? g.CX(i + 1) : g.CY(j + 1);
+		const double cm = d == 0 ? g.CX(i - 1) : g.CY(j - 1);
+		const double mufp = (hs * mu[a + st] + hsp * mu[a]) / (hsp + hs);
+		const double mufm = (hs * mu[a - st] + hsm * mu[a]) / (hsm + hs);
+		const double dp = mufp * (f[a + st] - f[a]) / (cp - c);
+		const double dm = mufm * (f[a] - f[a - st]) / (c - cm);
+		t[d] = (dp - dm) / (d == 0 ? g.SX(i) : g.SY(j));
+	}
+	double res = 0.0;
+	res += t[0];
+	res += t[1];
+	return res;
+}
+
 // ------------------------------------------------------------- NS kernels --
 struct StepScalars {
 	double dt;                // current time step (Time_::_dt)
@@ -528,6 +555,9 @@ __global__ void k_op(Geo g, int which, int sch, double coef, const double* a,
 		}
 		case 5:
 			o1[x] = diffusion(g, coef, c, i, j);
+			break;
+		case 8:
+			o1[x] = diffusion_var(g, a, c, i, j);
 			break;
 		}
 	}
@@ -968,7 +998,8 @@ int carpio_gpu_operator(carpio_gpu_grid* g, int which, int scheme,
 		const double* b, const double* c, double* out1, double* out2,
 		double* scalar) {
 	using namespace cg_host;
-	if (!g || which < 0 || which > 7) return CARPIO_GPU_EINVAL;
+	if (!g || which < 0 || which > 8) return CARPIO_GPU_EINVAL;
+	if (which == 8 && (!a || !c)) return CARPIO_GPU_EINVAL;
 	if (which == 4 && (scheme < 0 || scheme > 9 || g->gl < (scheme >= 2 ? 2 : 1)))
 		return CARPIO_GPU_EINVAL;
 	if (which == 6 && (!bc || !valid_bc(*bc) || !out1)) return CARPIO_GPU_EINVAL;
@@ -1013,7 +1044,7 @@ int carpio_gpu_operator(carpio_gpu_grid* g, int which, int scheme,
 	}
 	CG_CK(cudaGetLastError());
 	if (out1 && (rc = copy_field(g, out1, d[3], false, s))) return rc;
-	if (out2 && which != 1 && which != 4 && which != 5 && which != 6
+	if (out2 && which != 1 && which != 4 && which != 5 && which != 6 && which != 8
 			&& (rc = copy_field(g, out2, d[4], false, s)))
 		return rc;
 	CG_CK(cudaStreamSynchronize(s));

@@ -631,6 +631,17 @@ static int cmd_ops(int argc, char** argv) {
 			out(ijk.current()) = Op::NablaMuNabla(0.37, *a, ijk.current());
 		put_field("diffusion", out);
 	}
+	{
+		// NablaMuNabla with a mu field (s_operation.hpp:630-662), mu > 0
+		spScalar mu(new Scalar(g));
+		for (int I = 0; I < g->N(0); ++I)
+			for (int J = 0; J < g->N(1); ++J) mu->VAL(I, J) = 1.5 + U(rng);
+		put_field("in_mu", *mu);
+		Scalar out(g);
+		for (typename Grid::Ijk ijk = g->begin_ijk(); !ijk.is_end(); ++ijk)
+			out(ijk.current()) = Op::NablaMuNabla(*mu, *a, ijk.current());
+		put_field("diffusion_var", out);
+	}
 	// ghost fill (Equation_::apply_bc) for Dirichlet and Neumann segments
 	{
 		EqProbe_ eq(g);

@@ -810,6 +810,38 @@ void rs_diffusion(int nx, int ny, int gl, const double* cx, const double* sx,
 			AT(out, i, j) = nmn(nx, ny, gl, cx, sx, cy, sy, mu, f, i, j);
 }
 
+/* NablaMuNabla(const Scalar& mu, ...) (s_operation.hpp:630-662): face mu
+ * from the cell and its neighbour weighted by the half sizes */
+void rs_diffusion_var(int nx, int ny, int gl, const double* cx, const double* sx,
+		const double* cy, const double* sy, const double* mu, const double* f,
+		double* out) {
+	const int NJ = ny + 2 * gl;
+	memset(out, 0, sizeof(double) * (size_t)(nx + 2 * gl) * NJ);
+	for (int j = 0; j < ny; ++j)
+		for (int i = 0; i < nx; ++i) {
+			double t[2];
+			for (int d = 0; d < 2; ++d) {
+				int ip = d == 0 ? i + 1 : i, jp = d == 0 ? j : j + 1;
+				int im = d == 0 ? i - 1 : i, jm = d == 0 ? j : j - 1;
+				double hs = (d == 0 ? SX(i) : SY(j)) * 0.5;
+				double hsp = (d == 0 ? SX(ip) : SY(jp)) * 0.5;
+				double hsm = (d == 0 ? SX(im) : SY(jm)) * 0.5;
+				double c = d == 0 ? CX(i) : CY(j);
+				double cp = d == 0 ? CX(ip) : CY(jp);
+				double cm = d == 0 ? CX(im) : CY(jm);
+				double mufp = (hs * AT(mu, ip, jp) + hsp * AT(mu, i, j)) / (hsp + hs);
+				double mufm = (hs * AT(mu, im, jm) + hsm * AT(mu, i, j)) / (hsm + hs);
+				double dp = mufp * (AT(f, ip, jp) - AT(f, i, j)) / (cp - c);
+				double dm = mufm * (AT(f, i, j) - AT(f, im, jm)) / (c - cm);
+				t[d] = (dp - dm) / (d == 0 ? SX(i) : SY(j));
+			}
+			double res = 0.0;
+			res += t[0];
+			res += t[1];
+			AT(out, i, j) = res;
+		}
+}
+
 /* std::min / std::max semantics ((b < a) ? b : a, (a < b) ? b : a) */
 static double smin(double a, double b) { return (b < a) ? b : a; }
 static double smax(double a, double b) { return (a < b) ? b : a; }

@@ -82,6 +82,9 @@ void rs_c2f(int nx, int ny, int gl, const double* sx, const double* sy,
 void rs_diffusion(int nx, int ny, int gl, const double* cx, const double* sx,
 		const double* cy, const double* sy, double mu, const double* f,
 		double* out);
+void rs_diffusion_var(int nx, int ny, int gl, const double* cx, const double* sx,
+		const double* cy, const double* sy, const double* mu, const double* f,
+		double* out);
 
 /* Advection schemes of NS_::set_advection_scheme (s_ns.hpp:171-211) plus the
  * minmod limiter of src/calculation/advection.hpp:1079-1081. */

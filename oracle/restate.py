@@ -77,6 +77,7 @@ def lib():
         L.rs_c2f.argtypes = [ctypes.c_int] * 3 + [_d] * 6
         L.rs_diffusion.argtypes = [ctypes.c_int] * 3 + [_d] * 4 + [
             ctypes.c_double, _d, _d]
+        L.rs_diffusion_var.argtypes = [ctypes.c_int] * 3 + [_d] * 7
         L.rs_advection.argtypes = [ctypes.c_int] * 4 + [_d] * 8
         L.rs_max_magnitude.argtypes = [ctypes.c_int] * 3 + [_d] * 2
         L.rs_max_magnitude.restype = ctypes.c_double
@@ -240,6 +241,14 @@ def diffusion(grid, mu, f):
     out = grid.zeros()
     lib().rs_diffusion(*grid.args(), *grid.geo(), float(mu), _p(_f64(f)),
                        _p(out))
+    return out
+
+
+def diffusion_var(grid, mu, f):
+    """NablaMuNabla with a mu field (s_operation.hpp:630-662)"""
+    out = grid.zeros()
+    lib().rs_diffusion_var(*grid.args(), *grid.geo(), _p(_f64(mu)), _p(_f64(f)),
+                           _p(out))
     return out
 
 

@@ -37,6 +37,9 @@ def test_operators_bitwise(gpu_lib, name):
             assert bits_equal(o, d["adv_" + s]), s
     o, _, _ = S.operator(g, 5, c=a, coef=0.37)
     assert bits_equal(o, d["diffusion"])
+    if "diffusion_var" in d:
+        o, _, _ = S.operator(g, 8, a=d["in_mu"], c=a)
+        assert bits_equal(o, d["diffusion_var"])
     bc = _lib.BC()
     for k, (t, v) in enumerate(zip([1, 2, 2, 1], [0.5, -2.0, 1.5, 0.25])):
         bc.type[k], bc.value[k] = t, v

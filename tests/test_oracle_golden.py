@@ -174,5 +174,7 @@ def test_operators_bitwise(name):
         if "adv_" + s in d:
             assert bits_equal(R.advection(g, s, uf, vf, a), d["adv_" + s]), s
     assert bits_equal(R.diffusion(g, 0.37, a), d["diffusion"])
+    if "diffusion_var" in d:
+        assert bits_equal(R.diffusion_var(g, d["in_mu"], a), d["diffusion_var"])
     bc = R.make_bc([1, 2, 2, 1], [0.5, -2.0, 1.5, 0.25])
     assert bits_equal(R.apply_bc(g, bc, b), d["bc_filled"])
