@@ -276,6 +276,14 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 #pragma unroll
 		for (int k = 0; k < NC; ++k) x[lr][k] = q[lr][k] = 0.f;
 	__syncthreads();
+	// the y-face coefficients of the thread's columns, for the whole solve
+	float ayl[NC], ayr[NC];
+#pragma unroll
+	for (int k = 0; k < NC; ++k) {
+		const int j = tid + k * T;
+		ayl[k] = j < ny ? ays[j] : 0.f;
+		ayr[k] = j < ny ? ays[j + 1] : 0.f;
+	}
 	// r (FP32) = (r64 - mean) * scale0 with scale0 fixed for the whole solve
 	double scale0 = 1.0, rn0 = 1.0;
 	float rrn = 0.f;   // (r, r) of the current FP32 residual
@@ -326,7 +334,8 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 			const float rn = 1.f / (2.f * sig - rho);
 			const float c1 = rn * rho, c2f = 2.f * rn / de;
 #pragma unroll
-			for (int lr = 0; lr < RM; ++lr)
+			for (int lr = 0; lr < RM; ++lr) {
+				const float ax0 = axs[lr], ax1 = axs[lr + 1];
 #pragma unroll
 				for (int k = 0; k < NC; ++k) {
 					const int j = tid + k * T;
@@ -334,10 +343,10 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 						const int cc = lr * ny + j, pk = 1 + (lr + 1) * ny + j;
 						const float dc = dcur[pk];
 						float vv = dd[cc] * dc;
-						vv = fmaf(axs[lr], dcur[pk - ny], vv);
-						vv = fmaf(axs[lr + 1], dcur[pk + ny], vv);
-						vv = fmaf(ays[j], dcur[pk - 1], vv);
-						vv = fmaf(ays[j + 1], dcur[pk + 1], vv);
+						vv = fmaf(ax0, dcur[pk - ny], vv);
+						vv = fmaf(ax1, dcur[pk + ny], vv);
+						vv = fmaf(ayl[k], dcur[pk - 1], vv);
+						vv = fmaf(ayr[k], dcur[pk + 1], vv);
 						const float rkv = q[lr][k] - vv;
 						q[lr][k] = rkv;
 						const float dv = fmaf(c1, dc, __fdividef(c2f * rkv, dd[cc]));
@@ -345,6 +354,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 						zs[cc] += dv;
 					}
 				}
+			}
 			__syncthreads();
 			float* t = dcur;
 			dcur = dnxt;
@@ -492,7 +502,8 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 		// q = A p, (p, q)
 		float pq[1] = { 0.f };
 #pragma unroll
-		for (int lr = 0; lr < RM; ++lr)
+		for (int lr = 0; lr < RM; ++lr) {
+			const float ax0 = axs[lr], ax1 = axs[lr + 1];
 #pragma unroll
 			for (int k = 0; k < NC; ++k) {
 				const int j = tid + k * T;
@@ -500,14 +511,15 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 					const int pk = 1 + (lr + 1) * ny + j;
 					const float pc = p[pk];
 					float vv = dd[lr * ny + j] * pc;
-					vv = fmaf(axs[lr], p[pk - ny], vv);
-					vv = fmaf(axs[lr + 1], p[pk + ny], vv);
-					vv = fmaf(ays[j], p[pk - 1], vv);
-					vv = fmaf(ays[j + 1], p[pk + 1], vv);
+					vv = fmaf(ax0, p[pk - ny], vv);
+					vv = fmaf(ax1, p[pk + ny], vv);
+					vv = fmaf(ayl[k], p[pk - 1], vv);
+					vv = fmaf(ayr[k], p[pk + 1], vv);
 					q[lr][k] = vv;
 					pq[0] = fmaf(pc, vv, pq[0]);
 				}
 			}
+		}
 		if (!grid_allreduce<float, 1>(pq, gc, bank)) return;
 		const float alpha = gamma / pq[0];
 		// x += alpha p, r -= alpha q; z = M r, (r, z), (r, r); z's band
