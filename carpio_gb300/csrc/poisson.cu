@@ -648,6 +648,21 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_poisson_mixed_tile(
 	KLOOP(sp) { int a = sp.addr(k); ra.phi[a] = ra.mean ? v.x[a] - mx0 : v.x[a]; }
 }
 
+// b and x0 as vectors in the reference's numbering (x fastest: i + j nx),
+// for the solvers that run on an assembled CSR matrix
+template<int SRC>
+__global__ void __launch_bounds__(kThreads) k_rhs_vec(GridSpace sp, RhsArgs ra,
+		double* b, double* x) {
+	KLOOP(sp) {
+		int i, j;
+		sp.ij(k, i, j);
+		const int a = sp.addr(k);
+		const int r = i + j * sp.nx;
+		b[r] = rhs_at<SRC>(sp, ra, i, j, a);
+		x[r] = ra.phi[a];
+	}
+}
+
 template<int SRC>
 const void* pick_kernel(int kind, int precision, bool nu) {
 	if (nu) {
@@ -862,10 +877,101 @@ int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
 	return 0;
 }
 
+// IC_CGS / IC_CG at the structure level (Solver_IC_CGS_, s_solver.hpp:
+// 329-352, with the drop-in's mean removal): the CSR matrix assembled on the
+// host from the stencil rows (x-fastest numbering, columns ascending), b
+// from the device right-hand side, the algebra-level IC solver, x back into
+// phi's normal cells. Synchronous (small systems: the IC solves are level
+// scheduled).
+static int ic_structured(carpio_gpu_grid* g, StencilCoeffs& c, int src_mode,
+		const double* src_a, const double* src_b, double* phi,
+		const carpio_gpu_solver_cfg& cfg, double* hist_dev, int hist_cap,
+		cg_dev::SolveOut* out_dev, cudaStream_t s) {
+	const int nx = g->nx, ny = g->ny, gl = g->gl, P = g->P;
+	const int n = nx * ny;
+	std::vector<double> D, ax, ay, fold, cf;
+	stencil_host(nx, ny, gl, P, g->cx, g->sx, g->cy, g->sy, c.bc, c.beta, D, ax, ay,
+			fold, c.helm, c.alpha, &cf, nullptr);
+	const size_t NF = (size_t)g->NI * P;
+	std::vector<uint32_t> rp(n + 1, 0), ci;
+	std::vector<double> va;
+	ci.reserve(5 * (size_t)n);
+	va.reserve(5 * (size_t)n);
+	for (int j = 0; j < ny; ++j)
+		for (int i = 0; i < nx; ++i) {
+			const int r = i + j * nx;
+			const size_t a = (size_t)(i + gl) * P + (j + gl);
+			auto put = [&](int col, double v) { ci.push_back((uint32_t)col); va.push_back(v); };
+			if (j > 0) put(r - nx, cf[2 * NF + a]);
+			if (i > 0) put(r - 1, cf[a]);
+			put(r, D[a]);
+			if (i < nx - 1) put(r + 1, cf[NF + a]);
+			if (j < ny - 1) put(r + nx, cf[3 * NF + a]);
+			rp[r + 1] = (uint32_t)ci.size();
+		}
+	DevBuf bx;
+	int rc;
+	if ((rc = bx.ensure(sizeof(double) * 2 * (size_t)n))) return rc;
+	RhsArgs ra;
+	ra.sx = g->d_sx;
+	ra.sy = g->d_sy;
+	ra.fold = c.fold.as<double>();
+	ra.src_a = src_a;
+	ra.src_b = src_b;
+	ra.phi = phi;
+	ra.mean = 0;
+	ra.helm = c.helm ? 1 : 0;
+	const GridSpace sp{ nx, ny, gl, P };
+	const int nb = (int)std::min<long>(((long)n + kThreads - 1) / kThreads, 8L * sm_count());
+	if (src_mode == SRC_DIV)
+		k_rhs_vec<SRC_DIV><<<nb, kThreads, 0, s>>>(sp, ra, bx.as<double>(), bx.as<double>() + n);
+	else
+		k_rhs_vec<SRC_FIELD><<<nb, kThreads, 0, s>>>(sp, ra, bx.as<double>(), bx.as<double>() + n);
+	CG_CK(cudaGetLastError());
+	std::vector<double> b(n), x(n);
+	CG_CK(cudaMemcpyAsync(b.data(), bx.p, sizeof(double) * n, cudaMemcpyDeviceToHost, s));
+	CG_CK(cudaMemcpyAsync(x.data(), bx.as<double>() + n, sizeof(double) * n,
+			cudaMemcpyDeviceToHost, s));
+	CG_CK(cudaStreamSynchronize(s));
+	// the drop-in's null-space removal: the mean in sequence, then a - m
+	auto remove_mean = [&](std::vector<double>& v) {
+		double m = 0;
+		for (double e : v) m += e;
+		m = m / double(v.size());
+		for (double& e : v) e = e - m;
+	};
+	if (cfg.mean_removal) remove_mean(b);
+	int it = cfg.max_iter;
+	double tol = cfg.tol;
+	int hl = 0;
+	const int code = carpio_gpu_krylov_csr(cfg.kind, n, (int)ci.size(), rp.data(), ci.data(),
+			va.data(), b.data(), x.data(), &it, &tol, hist_dev, hist_cap, &hl, cfg.flags);
+	cg_dev::SolveOut o{};
+	o.code = code;
+	o.iters = it;
+	o.tol = tol;
+	o.hist_len = hl;
+	if (code >= 0) {
+		if (cfg.mean_removal) remove_mean(x);
+		std::vector<double> f(NF);
+		CG_CK(cudaMemcpy(f.data(), phi, sizeof(double) * NF, cudaMemcpyDeviceToHost));
+		for (int j = 0; j < ny; ++j)
+			for (int i = 0; i < nx; ++i) f[(size_t)(i + gl) * P + (j + gl)] = x[i + j * nx];
+		CG_CK(cudaMemcpy(phi, f.data(), sizeof(double) * NF, cudaMemcpyHostToDevice));
+	}
+	CG_CK(cudaMemcpy(out_dev, &o, sizeof o, cudaMemcpyHostToDevice));
+	return 0;
+}
+
 int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 		int src_mode, const double* src_a, const double* src_b, double* phi,
 		const carpio_gpu_solver_cfg& cfg, double* hist_dev, int hist_cap,
 		cg_dev::SolveOut* out_dev, cudaStream_t s) {
+	if (cfg.kind == CARPIO_GPU_IC_CGS || cfg.kind == CARPIO_GPU_IC_CG) {
+		if (cfg.precision != CARPIO_GPU_FP64 || !c.bfield_free) return CARPIO_GPU_EINVAL;
+		return ic_structured(g, c, src_mode, src_a, src_b, phi, cfg, hist_dev, hist_cap,
+				out_dev, s);
+	}
 	const size_t NF = (size_t)g->NI * g->P;
 	const bool mixed = cfg.precision == CARPIO_GPU_MIXED;
 	const int nv64 = 13, nv32 = 4;
@@ -1147,7 +1253,7 @@ static int structured_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
 		carpio_gpu_solver_stats* stats) {
 	using namespace cg_host;
 	if (!g || !bc || !source || !phi || !cfg || cfg->max_iter < 0
-			|| cfg->kind < 0 || cfg->kind > 3 || hist_cap < 0
+			|| cfg->kind < 0 || cfg->kind > CARPIO_GPU_IC_CG || hist_cap < 0
 			|| (hist_cap > 0 && !resid_hist) || !(beta == beta) || !(alpha == alpha))
 		return CARPIO_GPU_EINVAL;
 	if (cfg->precision == CARPIO_GPU_MIXED && cfg->kind != CARPIO_GPU_CG)
@@ -1182,8 +1288,10 @@ static int structured_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
 	CG_CK(cudaEventRecord(e1, s));
 	cg_dev::SolveOut o;
 	CG_CK(cudaMemcpyAsync(&o, w.out.p, sizeof o, cudaMemcpyDeviceToHost, s));
-	Ctl ctl;
-	CG_CK(cudaMemcpyAsync(&ctl, w.lw.ctl.p, sizeof ctl, cudaMemcpyDeviceToHost, s));
+	Ctl ctl{};
+	// the IC kinds run on the algebra-level workspace: no grid control block
+	if (cfg->kind != CARPIO_GPU_IC_CGS && cfg->kind != CARPIO_GPU_IC_CG)
+		CG_CK(cudaMemcpyAsync(&ctl, w.lw.ctl.p, sizeof ctl, cudaMemcpyDeviceToHost, s));
 	CG_CK(cudaStreamSynchronize(s));
 	float ms = 0;
 	cudaEventElapsedTime(&ms, e0, e1);

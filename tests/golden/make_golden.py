@@ -142,6 +142,8 @@ def main():
         ("poisson_mixed_16_jacobi", ["mixed", 16, "jacobi", 20000, 1e-8, 0]),
         ("poisson_mixed_24_cg_stretch", ["mixed", 24, "cg", 5000, 1e-10, 0, "stretch"]),
         ("poisson_vbeta_24_bicgstab", ["vbeta", 24, "bicgstab", 20000, 1e-10, 0]),
+        ("poisson_c1_48_ic_cg", ["c1", 48, "ic_cg", 1000, 1e-10, 0]),
+        ("poisson_mixed_24_ic_cgs", ["mixed", 24, "ic_cgs", 1000, 1e-10, 0]),
         ("poisson_vbeta_20_jacobi", ["vbeta", 20, "jacobi", 20000, 1e-10, 0, "stretch"]),
         ("poisson_neumann_32_cg_stretch", ["neumann", 32, "cg", 5000, 1e-10, 7, "stretch"]),
     ]

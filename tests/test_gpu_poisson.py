@@ -15,7 +15,7 @@ BCS = {
     "vbeta": ([1, 1, 2, 2], [1.0, -0.5, 0.75, -1.25]),
 }
 NAMES = {"cg": "CG", "jacobi": "Jacobi", "dia_bicgstab": "Dia_BiCGSTAB",
-         "bicgstab": "BiCGSTAB"}
+         "bicgstab": "BiCGSTAB", "ic_cgs": "IC_CGS", "ic_cg": "IC_CG"}
 
 
 def make_poisson(n, case, kind, max_iter, tol, source, phi=None, nx=None,
@@ -42,7 +42,7 @@ def make_poisson(n, case, kind, max_iter, tol, source, phi=None, nx=None,
 def iter_band(kind, ref_it):
     if kind == "jacobi":
         return max(2, ref_it // 200)
-    if kind == "cg":
+    if kind in ("cg", "ic_cg"):
         return max(3, ref_it // 20)
     return max(3, ref_it // 5)
 
