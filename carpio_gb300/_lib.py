@@ -115,6 +115,14 @@ SIGNATURES = {
         _VP, _D, _VP, _VP, _VP, _VP, _VP, _VP]),
     "carpio_gpu_ns_run": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, _VP]),
     "carpio_gpu_ns_set_stepper": (ctypes.c_int, [_VP, ctypes.c_int]),
+    "carpio_gpu_advection_create": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
+    "carpio_gpu_advection_destroy": (ctypes.c_int, [_VP]),
+    "carpio_gpu_advection_set_scheme": (ctypes.c_int, [_VP, ctypes.c_int]),
+    "carpio_gpu_advection_set_bc": (ctypes.c_int, [
+        _VP, ctypes.c_int, ctypes.POINTER(BC), _VP]),
+    "carpio_gpu_advection_initial": (ctypes.c_int, [_VP, _VP, _VP, _VP]),
+    "carpio_gpu_advection_step": (ctypes.c_int, [_VP, ctypes.c_double, ctypes.c_int]),
+    "carpio_gpu_advection_get": (ctypes.c_int, [_VP] * 6),
     "carpio_gpu_poisson_solve_beta": (ctypes.c_int, [
         _VP, ctypes.POINTER(BC), _VP, _VP, _VP,
         ctypes.POINTER(SolverCfg), _VP, ctypes.c_int,

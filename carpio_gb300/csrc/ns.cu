@@ -34,6 +34,9 @@ struct Geo {
 struct BcDev {
 	int type[4];
 	double value[4];
+	// optional boundary value per ghost cell (a field in the grid's layout),
+	// for boundary conditions given as functions; null: value[segment]
+	const double* gv;
 };
 
 __host__ __device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
@@ -49,8 +52,7 @@ __device__ __forceinline__ double ghost_value(const Geo& g, const BcDev& bc,
 	oj = j;
 	if (i < 0 || i >= g.nx) { a = 0; seg = i < 0 ? 0 : 1; oi = i < 0 ? 0 : g.nx - 1; }
 	else { a = 1; seg = j < 0 ? 2 : 3; oj = j < 0 ? 0 : g.ny - 1; }
-	(void)src;
-	double val = bc.value[seg];
+	double val = bc.gv ? bc.gv[g.at(i, j)] : bc.value[seg];
 	double cgh = a == 0 ? g.CX(i) : g.CY(j);
 	double co = a == 0 ? g.CX(oi) : g.CY(oj);
 	if (bc.type[seg] == 1) {
@@ -81,12 +83,10 @@ struct BcFields {
 	BcDev bc[2];
 };
 
-__global__ void __launch_bounds__(1024) k_apply_bc(Geo g, BcFields bf) {
-	double* f = bf.f[blockIdx.x];
-	const BcDev bc = bf.bc[blockIdx.x];
+// the fill of one field by one block; s_old holds 2 gl^2 doubles
+__device__ void bc_fill(const Geo& g, double* f, const BcDev& bc, double* s_old) {
 	const int gl = g.gl, nx = g.nx, ny = g.ny;
 	const int NI = g.NI, NJ = g.NJ;
-	extern __shared__ double s_old[];   // [2 * gl (rows) * gl (cols)]
 	const int ncorner = 2 * gl * gl;     // low-x corners: I < gl, J < gl or J >= NJ-gl
 	for (int t = threadIdx.x; t < ncorner; t += blockDim.x) {
 		int r = t / gl, c = t - r * gl;   // r: ghost row 0..2gl-1, c: ghost column
@@ -97,7 +97,6 @@ __global__ void __launch_bounds__(1024) k_apply_bc(Geo g, BcFields bf) {
 		s_old[t] = f[g.at(oi, oj)];
 	}
 	__syncthreads();
-	const long total = (long)NI * NJ;
 	// walk the ghost frame: rows J < gl and J >= NJ-gl fully, columns I < gl
 	// and I >= NI-gl for the other rows
 	const int frame_rows = 2 * gl;
@@ -136,7 +135,11 @@ __global__ void __launch_bounds__(1024) k_apply_bc(Geo g, BcFields bf) {
 		}
 		f[(long)I * g.P + J] = ghost_value(g, bc, i, j, src, oi, oj);
 	}
-	(void)total;
+}
+
+__global__ void __launch_bounds__(1024) k_apply_bc(Geo g, BcFields bf) {
+	extern __shared__ double s_old[];   // [2 * gl (rows) * gl (cols)]
+	bc_fill(g, bf.f[blockIdx.x], bf.bc[blockIdx.x], s_old);
 }
 
 // ------------------------------------------------------ advection schemes --
@@ -259,6 +262,40 @@ __device__ __forceinline__ double diffusion_var(const Geo& g, const double* mu,
 	res += t[0];
 	res += t[1];
 	return res;
+}
+
+// ------------------------------------------------ stand-alone advection --
+// Advection_::run_one_step (s_advection.hpp:185-212) `steps` times: the
+// ghosts of phi refilled, then every normal cell updated in place in Ijk
+// order (x fastest), phi - dt * VdotNabla, so cell (i, j) reads the new
+// values of (i-1, j), (i-2, j), (i, j-1), (i, j-2) and the old values of
+// the cells after it. Every scheme's stencil is the axis cross of radius 2:
+// no cell reads a cell of its own anti-diagonal i + j = L, each reads only
+// lower diagonals (already swept) and higher ones (not yet), so sweeping
+// the diagonals in order, the cells of one in parallel, gives the values
+// of the sequential loop. A diagonal holds at most min(nx, ny) cells: one
+// block runs every step, with a block barrier between diagonals.
+template<int SCH>
+__global__ void __launch_bounds__(1024) k_advect(Geo g, double* phi, BcDev bc,
+		const double* uf, const double* vf, double dt, int steps) {
+	extern __shared__ double s_old[];
+	const int nx = g.nx, ny = g.ny;
+	for (int st = 0; st < steps; ++st) {
+		bc_fill(g, phi, bc, s_old);
+		__syncthreads();
+		for (int L = 0; L <= nx + ny - 2; ++L) {
+			const int i0 = L - (ny - 1) > 0 ? L - (ny - 1) : 0;
+			const int i1 = L < nx - 1 ? L : nx - 1;
+			for (int i = i0 + (int)threadIdx.x; i <= i1; i += blockDim.x) {
+				const int j = L - i;
+				const double adv = adv_cell<SCH>(g, uf, vf, phi, i, j);
+				const int a = g.at(i, j);
+				const double phin = phi[a];
+				phi[a] = phin - dt * adv;
+			}
+			__syncthreads();
+		}
+	}
 }
 
 // ------------------------------------------------------------- NS kernels --
@@ -579,12 +616,13 @@ Geo make_geo(const carpio_gpu_grid* g) {
 	return e;
 }
 
-BcDev to_dev(const carpio_gpu_bc& b) {
+BcDev to_dev(const carpio_gpu_bc& b, const double* gv = nullptr) {
 	BcDev d;
 	for (int k = 0; k < 4; ++k) {
 		d.type[k] = b.type[k];
 		d.value[k] = b.value[k];
 	}
+	d.gv = gv;
 	return d;
 }
 
@@ -595,12 +633,13 @@ int grid_blocks(long n) {
 }
 
 cudaError_t launch_bc(const Geo& geo, double* f0, const carpio_gpu_bc& b0,
-		double* f1, const carpio_gpu_bc* b1, cudaStream_t s) {
+		double* f1, const carpio_gpu_bc* b1, cudaStream_t s,
+		const double* gv0 = nullptr, const double* gv1 = nullptr) {
 	BcFields bf;
 	bf.f[0] = f0;
-	bf.bc[0] = to_dev(b0);
+	bf.bc[0] = to_dev(b0, gv0);
 	bf.f[1] = f1;
-	bf.bc[1] = b1 ? to_dev(*b1) : bf.bc[0];
+	bf.bc[1] = b1 ? to_dev(*b1, gv1) : bf.bc[0];
 	size_t smem = sizeof(double) * 2 * geo.gl * geo.gl;
 	k_apply_bc<<<b1 ? 2 : 1, 1024, smem, s>>>(geo, bf);
 	return cudaGetLastError();
@@ -649,6 +688,20 @@ cudaError_t launch_kim_source(int sch, const Geo& geo, int blocks, cudaStream_t 
 	CASE(CARPIO_GPU_UPWIND2) CASE(CARPIO_GPU_VANLEER) CASE(CARPIO_GPU_SUPERBEE)
 	CASE(CARPIO_GPU_WAHYD) CASE(CARPIO_GPU_QUICK) CASE(CARPIO_GPU_CUI)
 	CASE(CARPIO_GPU_MINMOD)
+#undef CASE
+	}
+	return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_advect(int sch, const Geo& geo, cudaStream_t s, double* phi,
+		const BcDev& bc, const double* uf, const double* vf, double dt, int steps) {
+	const size_t smem = sizeof(double) * 2 * geo.gl * geo.gl;
+	switch (sch) {
+#define CASE(S) case S: k_advect<S><<<1, 1024, smem, s>>>(geo, phi, bc, uf, vf, dt, steps); \
+		return cudaGetLastError();
+	CASE(CARPIO_GPU_UPWIND1) CASE(CARPIO_GPU_CENTER) CASE(CARPIO_GPU_CENTER4)
+	CASE(CARPIO_GPU_UPWIND2) CASE(CARPIO_GPU_VANLEER) CASE(CARPIO_GPU_SUPERBEE)
+	CASE(CARPIO_GPU_WAHYD) CASE(CARPIO_GPU_QUICK) CASE(CARPIO_GPU_CUI)
 #undef CASE
 	}
 	return cudaErrorInvalidValue;
@@ -1048,6 +1101,148 @@ int carpio_gpu_operator(carpio_gpu_grid* g, int which, int scheme,
 			&& (rc = copy_field(g, out2, d[4], false, s)))
 		return rc;
 	CG_CK(cudaStreamSynchronize(s));
+	return 0;
+}
+
+}  // extern "C"
+
+// ----------------------------------------------- stand-alone Advection_ --
+struct carpio_gpu_advection {
+	carpio_gpu_grid* g;
+	cg_host::DevBuf fields;   // u v uf vf phi, then the ghost values of u v phi
+	double* f[8];
+	carpio_gpu_bc bc[3];      // u v phi
+	bool has_gv[3] = {};
+	int scheme = CARPIO_GPU_UPWIND1;   // Advection_::_default_setup
+	bool ready = false;                // initial() done
+	cudaStream_t s;
+};
+
+extern "C" {
+
+int carpio_gpu_advection_create(carpio_gpu_grid* g, carpio_gpu_advection** out) {
+	using namespace cg_host;
+	if (!g || !out) return CARPIO_GPU_EINVAL;
+	*out = nullptr;
+	carpio_gpu_advection* a = new carpio_gpu_advection();
+	a->g = g;
+	g->refs.fetch_add(1);
+	a->s = g->stream;
+	for (int k = 0; k < 3; ++k)
+		for (int sg = 0; sg < 4; ++sg) {   // BoundaryIndex's default: Neumann 0
+			a->bc[k].type[sg] = 2;
+			a->bc[k].value[sg] = 0.0;
+		}
+	const size_t NF = (size_t)g->NI * g->P;
+	if (a->fields.ensure(sizeof(double) * NF * 8)) {
+		delete a;
+		grid_release(g);
+		return CARPIO_GPU_ENOMEM;
+	}
+	for (int k = 0; k < 8; ++k) a->f[k] = a->fields.as<double>() + k * NF;
+	if (cudaMemsetAsync(a->fields.p, 0, a->fields.bytes, a->s) != cudaSuccess
+			|| cudaStreamSynchronize(a->s) != cudaSuccess) {
+		note_cuda_error(cudaGetLastError());
+		delete a;
+		grid_release(g);
+		return CARPIO_GPU_ECUDA;
+	}
+	*out = a;
+	return 0;
+}
+
+int carpio_gpu_advection_destroy(carpio_gpu_advection* a) {
+	if (!a) return CARPIO_GPU_EINVAL;
+	cudaStreamSynchronize(a->s);
+	carpio_gpu_grid* g = a->g;
+	delete a;
+	cg_host::grid_release(g);
+	return 0;
+}
+
+int carpio_gpu_advection_set_scheme(carpio_gpu_advection* a, int scheme) {
+	// set_advection_scheme (s_advection.hpp:140-183): the nine names it
+	// knows; the radius-2 stencils need two ghost layers
+	if (!a || scheme < CARPIO_GPU_UPWIND1 || scheme > CARPIO_GPU_CUI) return CARPIO_GPU_EINVAL;
+	if (a->g->gl < (scheme >= CARPIO_GPU_CENTER4 ? 2 : 1)) return CARPIO_GPU_EINVAL;
+	a->scheme = scheme;
+	return 0;
+}
+
+int carpio_gpu_advection_set_bc(carpio_gpu_advection* a, int field,
+		const carpio_gpu_bc* bc, const double* ghost_values) {
+	if (!a || field < 0 || field > 2 || !bc || !valid_bc(*bc)) return CARPIO_GPU_EINVAL;
+	std::lock_guard<std::mutex> lock(a->g->mu);
+	a->bc[field] = *bc;
+	a->has_gv[field] = ghost_values != nullptr;
+	if (ghost_values) {
+		int rc = copy_field(a->g, a->f[5 + field], ghost_values, true, a->s);
+		if (rc) return rc;
+		CG_CK(cudaStreamSynchronize(a->s));
+	}
+	return 0;
+}
+
+int carpio_gpu_advection_initial(carpio_gpu_advection* a, const double* u,
+		const double* v, const double* phi) {
+	using namespace cg_host;
+	if (!a) return CARPIO_GPU_EINVAL;
+	carpio_gpu_grid* g = a->g;
+	std::lock_guard<std::mutex> lock(g->mu);
+	const size_t NF = (size_t)g->NI * g->P;
+	const double* in[3] = { u, v, phi };
+	double* dst[3] = { a->f[0], a->f[1], a->f[4] };
+	int rc;
+	for (int k = 0; k < 3; ++k) {
+		if (in[k]) {
+			if ((rc = copy_field(g, dst[k], in[k], true, a->s))) return rc;
+		} else {
+			CG_CK(cudaMemsetAsync(dst[k], 0, sizeof(double) * NF, a->s));
+		}
+	}
+	// initial() (s_advection.hpp:101-135): ghosts of the cell velocities,
+	// then the face velocities (new, zeroed face fields) by InterpolateC2F
+	const Geo geo = make_geo(g);
+	CG_CK(launch_bc(geo, a->f[0], a->bc[0], a->f[1], &a->bc[1], a->s,
+			a->has_gv[0] ? a->f[5] : nullptr, a->has_gv[1] ? a->f[6] : nullptr));
+	CG_CK(cudaMemsetAsync(a->f[2], 0, sizeof(double) * NF * 2, a->s));
+	k_c2f<<<grid_blocks((long)g->nx * g->ny), kThreads, 0, a->s>>>(geo, a->f[0], a->f[1],
+			a->f[2], a->f[3]);
+	CG_CK(cudaGetLastError());
+	CG_CK(cudaStreamSynchronize(a->s));
+	a->ready = true;
+	return 0;
+}
+
+int carpio_gpu_advection_step(carpio_gpu_advection* a, double dt, int steps) {
+	using namespace cg_host;
+	if (!a || steps < 0 || !(dt == dt) || !a->ready) return CARPIO_GPU_EINVAL;
+	if (steps == 0) return 0;
+	carpio_gpu_grid* g = a->g;
+	std::lock_guard<std::mutex> lock(g->mu);
+	const Geo geo = make_geo(g);
+	// run_one_step refills the velocities' ghosts too: nothing reads them,
+	// but a second fill changes the corners (they read the y-ghosts the
+	// first fill wrote), and every later fill repeats the second
+	CG_CK(launch_bc(geo, a->f[0], a->bc[0], a->f[1], &a->bc[1], a->s,
+			a->has_gv[0] ? a->f[5] : nullptr, a->has_gv[1] ? a->f[6] : nullptr));
+	CG_CK(launch_advect(a->scheme, geo, a->s, a->f[4],
+			to_dev(a->bc[2], a->has_gv[2] ? a->f[7] : nullptr), a->f[2], a->f[3], dt, steps));
+	CG_CK(cudaStreamSynchronize(a->s));
+	return 0;
+}
+
+int carpio_gpu_advection_get(carpio_gpu_advection* a, double* u, double* v,
+		double* uf, double* vf, double* phi) {
+	if (!a) return CARPIO_GPU_EINVAL;
+	std::lock_guard<std::mutex> lock(a->g->mu);
+	double* out[5] = { u, v, uf, vf, phi };
+	for (int k = 0; k < 5; ++k) {
+		if (!out[k]) continue;
+		int rc = copy_field(a->g, out[k], a->f[k], false, a->s);
+		if (rc) return rc;
+	}
+	CG_CK(cudaStreamSynchronize(a->s));
 	return 0;
 }
 

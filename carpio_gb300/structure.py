@@ -80,17 +80,26 @@ def Output_Scalar(filename, grid, field):
 
 
 class BoundaryCondition:
-    """BoundaryCondition (s_boundary.hpp:10-130); default Neumann 0."""
+    """BoundaryCondition (s_boundary.hpp:10-130); default Neumann 0. The
+    value is a number or a function f(t, x, y, z) (set_default_1_bc(Fun),
+    s_boundary.hpp:109-114); functions are taken by Advection only."""
     BC1, BC2 = 1, 2
 
     def __init__(self):
         self.type, self.value = 2, 0.0
 
+    @staticmethod
+    def _val(val):
+        return val if callable(val) else float(val)
+
     def set_default_1_bc(self, val):
-        self.type, self.value = 1, float(val)
+        self.type, self.value = 1, self._val(val)
 
     def set_default_2_bc(self, val):
-        self.type, self.value = 2, float(val)
+        self.type, self.value = 2, self._val(val)
+
+    def get_val(self, t, x, y, z):
+        return float(self.value(t, x, y, z)) if callable(self.value) else self.value
 
 
 class BoundaryIndex:
@@ -105,13 +114,50 @@ class BoundaryIndex:
             raise ValueError("regular grids have shape 0, segments 0..3")
         self._m[(seg, name)] = bc
 
-    def to_c(self, name):
+    def find(self, seg, name):
+        return self._m.get((seg, name), BoundaryCondition())
+
+    def has_function(self, name):
+        return any(callable(self.find(s, name).value) for s in range(4))
+
+    def to_c(self, name, functions=False):
         c = _lib.BC()
         for s in range(4):
-            bc = self._m.get((s, name), BoundaryCondition())
+            bc = self.find(s, name)
+            if callable(bc.value) and not functions:
+                raise ValueError(f"{name}: function boundary values are taken "
+                                 "by Advection only")
             c.type[s] = bc.type
-            c.value[s] = bc.value
+            c.value[s] = 0.0 if callable(bc.value) else bc.value
         return c
+
+    def ghost_values(self, grid, name, t):
+        """the value Equation_::apply_bc (s_equation.hpp:340-378) takes for
+        every ghost cell: BC::get_val at time t at the face of the ghost's
+        source cell on the ghost's side, on both axes (Grid_::f_,
+        s_grid.hpp:200-211; z = -0.5 / +0.5 in 2-D). A field of the grid's
+        layout, zero in the normal cells."""
+        nx, ny, gl = grid.nx, grid.ny, grid.gl
+        gv = grid.zeros()
+        NI, NJ = gv.shape
+        for I in range(NI):
+            for J in range(NJ):
+                i, j = I - gl, J - gl
+                if 0 <= i < nx and 0 <= j < ny:
+                    continue
+                if i < 0 or i >= nx:
+                    seg, hi = (0, False) if i < 0 else (1, True)
+                    oi, oj = (0 if i < 0 else nx - 1), j
+                else:
+                    seg, hi = (2, False) if j < 0 else (3, True)
+                    oi, oj = i, (0 if j < 0 else ny - 1)
+                cx, hx = grid.cx[oi + gl], grid.sx[oi + gl] * 0.5
+                cy, hy = grid.cy[oj + gl], grid.sy[oj + gl] * 0.5
+                x = cx + hx if hi else cx - hx
+                y = cy + hy if hi else cy - hy
+                z = 0.5 if hi else 0.0 - 0.5
+                gv[I, J] = self.find(seg, name).get_val(t, x, y, z)
+        return gv
 
 
 def solver_cfg(name="CG", max_iter=1000, tol=1e-3, mean_removal=False,
@@ -389,6 +435,128 @@ class NS_explicit:
         h = getattr(self, "handle", None)
         if h is not None and _lib._lib is not None and not sys.is_finalizing():
             _lib._lib.carpio_gpu_ns_destroy(h)
+            self.handle = None
+
+
+class Advection:
+    """Stand-alone Advection_<2> (s_advection.hpp:22-216) on the GPU:
+    initial_CS for u, v and phi (numbers or functions f(t, x, y, z)),
+    add_bc, set_advection_scheme, set_time, then run(); get_CS reads the
+    fields. The velocity field stays fixed; phi is updated in place in the
+    reference's cell order, so results are bit-identical to it."""
+    SCHEMES = ("upwind1", "center", "center4", "upwind2", "VanLeer",
+               "superbee", "WAHYD", "QUICK", "CUI")
+
+    def __init__(self, grid):
+        L = _lib.load()
+        self.grid = grid
+        self._bi = BoundaryIndex()
+        self._fun = {"u": 0.0, "v": 0.0, "phi": 0.0}
+        self.scheme = "upwind1"
+        self.max_step, self.dt = 0, None
+        self.t, self.step = 0.0, 0
+        h = ctypes.c_void_p()
+        rc = L.carpio_gpu_advection_create(grid.handle, ctypes.byref(h))
+        if rc:
+            raise _lib.CarpioGpuError(rc, "advection_create")
+        self.handle = h
+        self._ready = False
+
+    def set_time(self, max_step, dt):
+        self.max_step, self.dt = int(max_step), float(dt)
+
+    def initial_CS(self, name, val):
+        if name not in self._fun:
+            raise ValueError(f"unknown field {name}")
+        self._fun[name] = val
+
+    def add_bc(self, shape, seg, name, bc):
+        self._bi.insert(shape, seg, name, bc)
+
+    def set_advection_scheme(self, name):
+        if name not in self.SCHEMES:
+            raise ValueError(f"unknown scheme {name}")
+        rc = _lib.load().carpio_gpu_advection_set_scheme(
+            self.handle, _lib.SCHEMES[name])
+        if rc:
+            raise _lib.CarpioGpuError(rc, "advection_set_scheme")
+        self.scheme = name
+
+    def _field(self, name):
+        """set_CS (s_equation.hpp:266-287): the function at every cell
+        centre, ghosts included, at the current time"""
+        g, f = self.grid, self._fun[name]
+        if not callable(f):
+            return np.full(g.N(), float(f))
+        out = g.zeros()
+        for I in range(out.shape[0]):
+            for J in range(out.shape[1]):
+                out[I, J] = f(self.t, g.cx[I], g.cy[J], 0.0)
+        return out
+
+    def _set_bc(self, name, t):
+        k = ("u", "v", "phi").index(name)
+        gv = self._bi.ghost_values(self.grid, name, t) \
+            if self._bi.has_function(name) else None
+        c = self._bi.to_c(name, functions=True)
+        rc = _lib.load().carpio_gpu_advection_set_bc(
+            self.handle, k, ctypes.byref(c), _lib.ptr(gv) if gv is not None else None)
+        if rc:
+            raise _lib.CarpioGpuError(rc, "advection_set_bc")
+
+    def initial(self):
+        for nm in ("u", "v", "phi"):
+            self._set_bc(nm, self.t)
+        fs = [self._field(nm) for nm in ("u", "v", "phi")]
+        rc = _lib.load().carpio_gpu_advection_initial(
+            self.handle, *[_lib.ptr(f) for f in fs])
+        if rc:
+            raise _lib.CarpioGpuError(rc, "advection_initial")
+        self._ready = True
+
+    def run(self, steps=None):
+        """Equation_::run (s_equation.hpp:132-178): initial() on the first
+        call, then max_step + 1 steps (Time_::is_end is current > max,
+        s_time.hpp:74-80) unless `steps` is given. Function BCs of phi are
+        evaluated at each step's time, as apply_bc does."""
+        if self.dt is None:
+            raise ValueError("set_time first")
+        if not self._ready:
+            self.initial()
+        n = self.max_step + 1 if steps is None else int(steps)
+        L = _lib.load()
+        if self._bi.has_function("phi"):
+            for _ in range(n):
+                self._set_bc("phi", self.t)
+                rc = L.carpio_gpu_advection_step(self.handle, self.dt, 1)
+                if rc:
+                    raise _lib.CarpioGpuError(rc, "advection_step")
+                self.t += self.dt
+                self.step += 1
+        else:
+            rc = L.carpio_gpu_advection_step(self.handle, self.dt, n)
+            if rc:
+                raise _lib.CarpioGpuError(rc, "advection_step")
+            for _ in range(n):
+                self.t += self.dt
+            self.step += n
+        return 0
+
+    def get_CS(self, name):
+        names = ("u", "v", "uf", "vf", "phi")
+        if name not in names:
+            raise ValueError(f"unknown field {name}")
+        out = self.grid.zeros()
+        args = [_lib.ptr(out) if nm == name else None for nm in names]
+        rc = _lib.load().carpio_gpu_advection_get(self.handle, *args)
+        if rc:
+            raise _lib.CarpioGpuError(rc, "advection_get")
+        return out
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and _lib._lib is not None and not sys.is_finalizing():
+            _lib._lib.carpio_gpu_advection_destroy(h)
             self.handle = None
 
 

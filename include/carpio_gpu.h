@@ -53,8 +53,8 @@ extern "C" {
 #define CARPIO_GPU_JACOBI 1        /* carpio::Jacobi        solver_matrix.hpp:192-260 */
 #define CARPIO_GPU_DIA_BICGSTAB 2  /* carpio::Dia_BiCGSTAB  solver_matrix.hpp:599-672 */
 #define CARPIO_GPU_BICGSTAB 3      /* carpio::BiCGSTAB      solver_matrix.hpp:674-745 */
-#define CARPIO_GPU_IC_CGS 4        /* carpio::IC_CGS        solver_matrix.hpp:376-438 (CSR only) */
-#define CARPIO_GPU_IC_CG 5         /* carpio::IC_CG         solver_matrix.hpp:318-374 (CSR only) */
+#define CARPIO_GPU_IC_CGS 4        /* carpio::IC_CGS        solver_matrix.hpp:376-438 (FP64) */
+#define CARPIO_GPU_IC_CG 5         /* carpio::IC_CG         solver_matrix.hpp:318-374 (FP64) */
 
 /* flags (bitwise OR). 0 = the reference's exact semantics. */
 #define CARPIO_GPU_FLAG_FULL_NRM2 1u   /* use the full 2-norm instead of nrm2's
@@ -152,7 +152,9 @@ typedef struct {
 #define CARPIO_GPU_MIXED 1   /* FP32 inner CG inside FP64 iterative refinement */
 
 typedef struct {
-	int kind;          /* CARPIO_GPU_CG / JACOBI / DIA_BICGSTAB / BICGSTAB */
+	int kind;          /* CARPIO_GPU_CG / JACOBI / DIA_BICGSTAB / BICGSTAB, or
+	                      IC_CGS / IC_CG (FP64, no beta field: the stencil rows
+	                      go to the CSR solver of section 1; synchronous) */
 	int precision;     /* CARPIO_GPU_FP64 or CARPIO_GPU_MIXED (CG only) */
 	int max_iter;      /* Solver_::set_max_iter */
 	double tol;        /* Solver_::set_tolerance (relative residual) */
@@ -292,6 +294,42 @@ int carpio_gpu_operator(carpio_gpu_grid* g, int which, int scheme,
 		double coef, const carpio_gpu_bc* bc, const double* a,
 		const double* b, const double* c, double* out1, double* out2,
 		double* scalar);
+
+/* Stand-alone Advection_<2> (s_advection.hpp:22-216): a scalar phi carried
+ * by a fixed velocity field. Fields are full arrays of the grid's layout
+ * (ghosts included), host or device.
+ *   create       the handle; scheme upwind1, every boundary Neumann 0 (the
+ *                reference's defaults, s_advection.hpp:86-99)
+ *   set_scheme   set_advection_scheme (:140-183): CARPIO_GPU_UPWIND1 .. CUI
+ *                (minmod is not one of its names: CARPIO_GPU_EINVAL); the
+ *                radius-2 schemes need gl >= 2
+ *   set_bc       field 0 u, 1 v, 2 phi. ghost_values: NULL (bc->value per
+ *                segment) or a field holding, for every ghost cell, the value
+ *                a function BC gives there (BC::get_val at the face point
+ *                Equation_::apply_bc evaluates, s_equation.hpp:352-357)
+ *   initial      initial() (:101-135): the cell fields u, v, phi as set_CS
+ *                leaves them (NULL = 0), then the velocities' ghosts and the
+ *                face velocities (InterpolateC2F into zeroed face fields)
+ *   step         `steps` calls of run_one_step (:185-212) with time step dt:
+ *                phi's ghosts refilled, then every normal cell in x-fastest
+ *                order updated in place, phi - dt * VdotNabla, so each cell
+ *                reads the new values of the cells before it. It also
+ *                refills the velocities' ghosts, which changes their corner
+ *                ghosts once (read by no later computation).
+ *                Equation_::run runs max_step + 1 steps (Time_::is_end,
+ *                s_time.hpp:74-80).
+ *   get          any of u, v, uf, vf, phi (NULL skips) */
+typedef struct carpio_gpu_advection carpio_gpu_advection;
+int carpio_gpu_advection_create(carpio_gpu_grid* g, carpio_gpu_advection** out);
+int carpio_gpu_advection_destroy(carpio_gpu_advection* a);
+int carpio_gpu_advection_set_scheme(carpio_gpu_advection* a, int scheme);
+int carpio_gpu_advection_set_bc(carpio_gpu_advection* a, int field,
+		const carpio_gpu_bc* bc, const double* ghost_values);
+int carpio_gpu_advection_initial(carpio_gpu_advection* a, const double* u,
+		const double* v, const double* phi);
+int carpio_gpu_advection_step(carpio_gpu_advection* a, double dt, int steps);
+int carpio_gpu_advection_get(carpio_gpu_advection* a, double* u, double* v,
+		double* uf, double* vf, double* phi);
 
 /* ----- 3. batched Poisson solves -------------------------------------------
  * No counterpart in the reference, which solves one Poisson_ at a time. Many

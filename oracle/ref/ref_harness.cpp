@@ -30,12 +30,22 @@
 //           `stretch` (here and for poisson / cavity) builds the grid from
 //           cell sizes (make_grid). Also writes the
 //           field in_a with Output_Scalar (s_io_file.hpp:43-71) to dump.txt.
+//   advect  <n> <steps> <scheme> <dt> <case> [stretch]
+//           stand-alone Advection_ (s_advection.hpp) run by Equation_::run
+//           with set_time(steps - 1, dt), so `steps` steps. case band: the
+//           shipped 2-D TVD example's set-up (u = v = 1, phi = 0, a function
+//           BC phi = 1 on 0 <= y <= 0.3 of the x- side, 0 elsewhere); case
+//           rotate: solid rotation about (0.5, 0.5) of a cone, default
+//           (Neumann 0) BCs. Writes the initial fields the functions give
+//           (in_u, in_v, in_phi, every cell incl. ghosts) and phi, u, v at
+//           the end.
 
 #include "structure/s_grid.hpp"
 #include "structure/s_poisson.hpp"
 #include "structure/s_ns_explicit.hpp"
 #include "structure/s_ns_kim.hpp"
 #include "structure/s_operation.hpp"
+#include "structure/s_advection.hpp"
 #include "io/mmio.h"
 
 #include <cstdio>
@@ -661,6 +671,68 @@ static int cmd_ops(int argc, char** argv) {
 	return 0;
 }
 
+// ---------------------------------------------------------- advect cmd ---
+static int cmd_advect(int argc, char** argv) {
+	if (argc < 8) return 2;
+	int n = std::atoi(argv[2]);
+	int steps = std::atoi(argv[3]);
+	std::string scheme = argv[4];
+	double dt = std::atof(argv[5]);
+	std::string cs = argv[6];
+	out_open(argv[argc - 1]);
+	const bool stretch = stretch_arg(argc, argv, 7);
+	spGrid g = make_grid(n, n, 2, stretch);
+	put_grid(*g);
+	typedef Advection_<2> Eq;
+	Eq eq(g);
+	eq.set_time(steps - 1, dt);
+	Eq::Function fu, fv, fphi;
+	if (cs == "band") {
+		fu = [](Vt, Vt, Vt, Vt) { return 1.0; };
+		fv = [](Vt, Vt, Vt, Vt) { return 1.0; };
+		fphi = [](Vt, Vt, Vt, Vt) { return 0.0; };
+		Eq::Function fbc = [](Vt, Vt, Vt y, Vt) {
+			return (y >= 0.0 && y <= 0.3) ? 1.0 : 0.0;
+		};
+		Eq::spBC bc0(new Eq::BC()), bc1(new Eq::BC());
+		bc0->set_default_1_bc(0);
+		bc1->set_default_1_bc(fbc);
+		eq.add_bc(0, 0, "phi", bc1);
+		for (int k = 1; k < 4; ++k) eq.add_bc(0, k, "phi", bc0);
+	} else if (cs == "rotate") {
+		fu = [](Vt, Vt, Vt y, Vt) { return -(y - 0.5); };
+		fv = [](Vt, Vt x, Vt, Vt) { return x - 0.5; };
+		fphi = [](Vt, Vt x, Vt y, Vt) {
+			Vt dx = x - 0.5, dy = y - 0.75;
+			Vt r2 = dx * dx + dy * dy;
+			return r2 < 0.04 ? 1.0 - r2 / 0.04 : 0.0;
+		};
+	} else {
+		return 2;
+	}
+	eq.initial_CS("u", fu);
+	eq.initial_CS("v", fv);
+	eq.initial_CS("phi", fphi);
+	// the initial fields as set_CS writes them (s_equation.hpp:266-279)
+	const char* nm[3] = { "in_u", "in_v", "in_phi" };
+	Eq::Function* fn[3] = { &fu, &fv, &fphi };
+	for (int k = 0; k < 3; ++k) {
+		Scalar f(g);
+		for (int I = 0; I < g->N(0); ++I)
+			for (int J = 0; J < g->N(1); ++J)
+				f.VAL(I, J) = (*fn[k])(0.0, g->C_(0, I), g->C_(1, J), 0.0);
+		put_field(nm[k], f);
+	}
+	eq.set_advection_scheme(scheme);
+	eq.run();
+	put_field("phi", *eq.get_CS("phi"));
+	put_field("u", *eq.get_CS("u"));
+	put_field("v", *eq.get_CS("v"));
+	put_field("uf", *eq.get_CS("uf"));
+	put_field("vf", *eq.get_CS("vf"));
+	return 0;
+}
+
 int main(int argc, char** argv) {
 	if (argc < 2) {
 		std::fprintf(stderr, "usage: ref_harness csr|poisson|cavity|ops ...\n");
@@ -673,6 +745,7 @@ int main(int argc, char** argv) {
 	else if (c == "cavity") rc = cmd_cavity(argc, argv);
 	else if (c == "ops") rc = cmd_ops(argc, argv);
 	else if (c == "kim") rc = cmd_kim(argc, argv);
+	else if (c == "advect") rc = cmd_advect(argc, argv);
 	if (rc == 2) std::fprintf(stderr, "bad arguments for %s\n", c.c_str());
 	g_meta.close();
 	return rc;

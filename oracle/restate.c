@@ -673,9 +673,17 @@ int rs_assemble_poisson(int nx, int ny, int gl, const double* cx,
 /* ------------------------------------------------------------ ghosts --- */
 void rs_apply_bc(int nx, int ny, int gl, const double* cx, const double* sx,
 		const double* cy, const double* sy, const rs_bc* bc, double* f) {
+	rs_apply_bc_gv(nx, ny, gl, cx, sx, cy, sy, bc, NULL, f);
+}
+
+void rs_apply_bc_gv(int nx, int ny, int gl, const double* cx, const double* sx,
+		const double* cy, const double* sy, const rs_bc* bc, const double* gv,
+		double* f) {
 	/* Equation_::apply_bc (s_equation.hpp:340-378): every ghost cell in the
 	 * IJK order of begin_IJK (x fastest), in place, so a corner reads the
-	 * neighbouring ghost row as it stands when the corner is visited. */
+	 * neighbouring ghost row as it stands when the corner is visited. gv
+	 * (optional, a cell field) holds the boundary value of each ghost cell
+	 * (BC::get_val at the ghost's face point) in place of bc->value. */
 	const int NI = nx + 2 * gl, NJ = ny + 2 * gl;
 	for (int J = 0; J < NJ; ++J) {
 		for (int I = 0; I < NI; ++I) {
@@ -685,7 +693,7 @@ void rs_apply_bc(int nx, int ny, int gl, const double* cx, const double* sx,
 			int seg, a, oi = i, oj = j, ori;
 			if (gx) { a = 0; seg = i < 0 ? 0 : 1; ori = i < 0 ? 0 : 1; oi = i < 0 ? 0 : nx - 1; }
 			else { a = 1; seg = j < 0 ? 2 : 3; ori = j < 0 ? 0 : 1; oj = j < 0 ? 0 : ny - 1; }
-			double val = bc->value[seg];
+			double val = gv ? AT(gv, i, j) : bc->value[seg];
 			double cg = a == 0 ? CX(i) : CY(j);
 			double co = a == 0 ? CX(oi) : CY(oj);
 			double dl = fabs(cg - co);
@@ -937,6 +945,28 @@ void rs_advection(int scheme, int nx, int ny, int gl, const double* cx,
 		for (int i = 0; i < nx; ++i)
 			AT(out, i, j) = adv_cell(scheme, nx, ny, gl, cx, sx, cy, sy, uf, vf,
 					f, i, j);
+}
+
+void rs_advect_run(int scheme, int nx, int ny, int gl, const double* cx,
+		const double* sx, const double* cy, const double* sy, const rs_bc* bc,
+		const double* gv, const double* uf, const double* vf, double dt,
+		int steps, double* phi) {
+	/* Advection_::run_one_step (s_advection.hpp:185-212), `steps` times: the
+	 * ghosts of phi refilled, then every normal cell in Ijk order (x
+	 * fastest) updated in place, phi - dt * VdotNabla, so a cell reads the
+	 * new values of the cells visited before it. (The step also refills the
+	 * ghosts of the cell velocities, which no later computation reads.) */
+	const int NJ = ny + 2 * gl;
+	for (int st = 0; st < steps; ++st) {
+		rs_apply_bc_gv(nx, ny, gl, cx, sx, cy, sy, bc, gv, phi);
+		for (int j = 0; j < ny; ++j)
+			for (int i = 0; i < nx; ++i) {
+				double adv = adv_cell(scheme, nx, ny, gl, cx, sx, cy, sy, uf, vf,
+						phi, i, j);
+				double phin = AT(phi, i, j);
+				AT(phi, i, j) = phin - dt * adv;
+			}
+	}
 }
 
 double rs_max_magnitude(int nx, int ny, int gl, const double* u,

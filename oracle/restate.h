@@ -69,6 +69,12 @@ int rs_assemble_poisson(int nx, int ny, int gl, const double* cx,
 void rs_apply_bc(int nx, int ny, int gl, const double* cx, const double* sx,
 		const double* cy, const double* sy, const rs_bc* bc, double* f);
 
+/* the same with a boundary value per ghost cell (gv, a cell field; NULL =
+ * bc->value), for boundary conditions given as functions */
+void rs_apply_bc_gv(int nx, int ny, int gl, const double* cx, const double* sx,
+		const double* cy, const double* sy, const rs_bc* bc, const double* gv,
+		double* f);
+
 /* Operation_ (s_operation.hpp): Grad :46-72, Div(VecF) :100-120,
  * InterpolateF2C :141-164, InterpolateC2F :166-187, NablaMuNabla :664-688. */
 void rs_grad(int nx, int ny, int gl, const double* cx, const double* cy,
@@ -96,6 +102,14 @@ enum {
 void rs_advection(int scheme, int nx, int ny, int gl, const double* cx,
 		const double* sx, const double* cy, const double* sy, const double* uf,
 		const double* vf, const double* f, double* out);
+
+/* Advection_::run_one_step (s_advection.hpp:185-212) `steps` times on phi
+ * (in place, x-fastest order) with fixed face velocities uf, vf; scheme as
+ * rs_advection (RS_MINMOD is not one of Advection_'s). */
+void rs_advect_run(int scheme, int nx, int ny, int gl, const double* cx,
+		const double* sx, const double* cy, const double* sy, const rs_bc* bc,
+		const double* gv, const double* uf, const double* vf, double dt,
+		int steps, double* phi);
 
 /* VectorCenter_::max_magnitude (s_vector.hpp:89-103) */
 double rs_max_magnitude(int nx, int ny, int gl, const double* u,

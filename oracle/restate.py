@@ -71,6 +71,10 @@ def lib():
         L.rs_assemble_poisson.restype = ctypes.c_int
         L.rs_apply_bc.argtypes = [ctypes.c_int] * 3 + [_d] * 4 + [
             ctypes.POINTER(BC), _d]
+        L.rs_apply_bc_gv.argtypes = [ctypes.c_int] * 3 + [_d] * 4 + [
+            ctypes.POINTER(BC), _d, _d]
+        L.rs_advect_run.argtypes = [ctypes.c_int] * 4 + [_d] * 4 + [
+            ctypes.POINTER(BC), _d, _d, _d, ctypes.c_double, ctypes.c_int, _d]
         L.rs_grad.argtypes = [ctypes.c_int] * 3 + [_d] * 5
         L.rs_div.argtypes = [ctypes.c_int] * 3 + [_d] * 5
         L.rs_f2c.argtypes = [ctypes.c_int] * 3 + [_d] * 4
@@ -203,10 +207,24 @@ def vec_to_field(grid, vec, f=None):
     return f
 
 
-def apply_bc(grid, bc, f):
+def apply_bc(grid, bc, f, gv=None):
     f = _f64(f).copy()
-    lib().rs_apply_bc(*grid.args(), *grid.geo(), ctypes.byref(bc), _p(f))
+    if gv is None:
+        lib().rs_apply_bc(*grid.args(), *grid.geo(), ctypes.byref(bc), _p(f))
+    else:
+        lib().rs_apply_bc_gv(*grid.args(), *grid.geo(), ctypes.byref(bc),
+                             _p(_f64(gv)), _p(f))
     return f
+
+
+def advect_run(grid, scheme, bc, uf, vf, dt, steps, phi, gv=None):
+    """Advection_::run_one_step (s_advection.hpp:185-212) `steps` times on
+    a copy of phi; gv: optional per-ghost boundary values (a cell field)"""
+    phi = _f64(phi).copy()
+    lib().rs_advect_run(SCHEMES.get(scheme, scheme), *grid.args(), *grid.geo(),
+                        ctypes.byref(bc), None if gv is None else _p(_f64(gv)),
+                        _p(_f64(uf)), _p(_f64(vf)), float(dt), int(steps), _p(phi))
+    return phi
 
 
 def grad(grid, phi):

@@ -86,3 +86,34 @@ def _built_library():
     so the ABI tests always load the library the sources describe."""
     from carpio_gb300 import compile as c
     c.build()
+
+
+def advect_case(d):
+    """the stand-alone Advection_ set-ups of the advect_* fixtures, as the
+    harness writes them: initial functions of u, v, phi and the boundary
+    conditions of phi (a BoundaryIndex of the library's Python mirror)"""
+    from carpio_gb300 import structure as S
+    case = str(d["case"])
+    bi = S.BoundaryIndex()
+    if case == "band":
+        fu = lambda t, x, y, z: 1.0
+        fv = lambda t, x, y, z: 1.0
+        fphi = lambda t, x, y, z: 0.0
+        b0 = S.BoundaryCondition()
+        b0.set_default_1_bc(0)
+        b1 = S.BoundaryCondition()
+        b1.set_default_1_bc(lambda t, x, y, z: 1.0 if (y >= 0.0 and y <= 0.3) else 0.0)
+        bi.insert(0, 0, "phi", b1)
+        for k in (1, 2, 3):
+            bi.insert(0, k, "phi", b0)
+    elif case == "rotate":
+        fu = lambda t, x, y, z: -(y - 0.5)
+        fv = lambda t, x, y, z: x - 0.5
+
+        def fphi(t, x, y, z):
+            dx, dy = x - 0.5, y - 0.75
+            r2 = dx * dx + dy * dy
+            return 1.0 - r2 / 0.04 if r2 < 0.04 else 0.0
+    else:
+        raise ValueError(case)
+    return dict(u=fu, v=fv, phi=fphi, bi=bi)

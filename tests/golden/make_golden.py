@@ -3,6 +3,7 @@ reference's own code (oracle/_ref/ref_harness, compiled from the reference's
 headers by `make -C oracle ref`).
 
     python tests/golden/make_golden.py [--ref /path/to/reference] [--long]
+        [--only NAME_PREFIX]
 
 Each fixture is a compressed .npz of the harness's inputs and outputs.
 Residual histories longer than 64 entries keep their first and last 32
@@ -101,7 +102,12 @@ def main():
     ap.add_argument("--long-dir", default=None)
     ap.add_argument("--only-long", action="store_true",
                     help="write only the 2000-step cavity fixtures")
+    ap.add_argument("--only", default="",
+                    help="write only the fixtures whose name starts with this")
     a = ap.parse_args()
+
+    def want(name):
+        return name.startswith(a.only)
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref",
                     f"REF={a.ref}"], check=True)
     if a.only_long:
@@ -124,6 +130,8 @@ def main():
         ("csr_pde225_ic_cgs", ["pde225.mtx", "ones", "zeros", "ic_cgs", 1000, 1e-10]),
     ]
     for name, c in csr_cases:
+        if not want(name):
+            continue
         args = ["csr", os.path.join(mtx, c[0])]
         args.append(c[1] if c[1] == "ones" else os.path.join(mtx, c[1]))
         args += c[2:]
@@ -149,6 +157,8 @@ def main():
     ]
     csr_kept = {"poisson_c1_64_cg", "poisson_neumann_32_cg", "poisson_mixed_24_cg"}
     for name, c in poisson_cases:
+        if not want(name):
+            continue
         d = trim_hist(run(["poisson"] + c, a.ref))
         if name not in csr_kept:
             for k in ("rowptr", "colind", "val"):
@@ -166,6 +176,8 @@ def main():
                                           "stretch"]),
     ]
     for name, c in cav:
+        if not want(name):
+            continue
         d = run(["cavity"] + c, a.ref)
         if not name.startswith("cavity_32"):
             d = {k: v for k, v in d.items() if not k.startswith("s1_")}
@@ -176,10 +188,35 @@ def main():
         ("kim_16_superbee_6", [16, 6, "superbee", 1e-10, 100000, 0.01, 400]),
     ]
     for name, c in kim:
+        if not want(name):
+            continue
         save(name, run(["kim"] + c, a.ref))
+    # stand-alone Advection_: n steps scheme dt case [stretch]; the first is
+    # the shipped 2-D TVD example (50^2, dt 0.002, set_time(1000) = 1001 steps)
+    adv = [] if a.only_long else [
+        ("advect_50_vanleer_band", [50, 1001, "VanLeer", 0.002, "band"]),
+        ("advect_40_quick_rotate", [40, 60, "QUICK", 0.004, "rotate"]),
+        ("advect_40_superbee_rotate", [40, 60, "superbee", 0.004, "rotate"]),
+        ("advect_30_upwind1_band", [30, 50, "upwind1", 0.003, "band"]),
+        ("advect_30_center4_band", [30, 50, "center4", 0.001, "band"]),
+        ("advect_24_center_rotate", [24, 40, "center", 0.002, "rotate"]),
+        ("advect_24_upwind2_band", [24, 40, "upwind2", 0.002, "band"]),
+        ("advect_32_cui_rotate_stretch", [32, 40, "CUI", 0.003, "rotate", "stretch"]),
+        ("advect_32_wahyd_band_stretch", [32, 40, "WAHYD", 0.002, "band", "stretch"]),
+    ]
+    for name, c in adv:
+        if not want(name):
+            continue
+        d = run(["advect"] + c, a.ref)
+        d.update(n=np.int64(c[0]), steps=np.int64(c[1]), scheme=np.array(c[2]),
+                 dt=np.float64(c[3]), case=np.array(c[4]),
+                 stretch=np.float64(1.0 if len(c) > 5 else 0.0))
+        save(name, d)
     ops = [] if a.only_long else [("ops_13_gl2", [13, 5, 2]), ("ops_9_gl1", [9, 3, 1]),
                                   ("ops_12_gl2_stretch", [12, 7, 2, "stretch"])]
     for name, c in ops:
+        if not want(name):
+            continue
         save(name, run(["ops"] + c, a.ref))
     if a.long:
         for n, dt0 in [(128, 0.5 / 128), (256, 0.5 / 256)]:
