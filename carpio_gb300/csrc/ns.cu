@@ -755,7 +755,13 @@ int carpio_gpu_ns_create(carpio_gpu_grid* g, const carpio_gpu_ns_cfg* cfg,
 	using namespace cg_host;
 	if (!g || !cfg || !out || !(dt0 > 0) || g->gl < 2 || cfg->scheme < 0
 			|| cfg->scheme > 9 || !valid_bc(cfg->bc_u) || !valid_bc(cfg->bc_v)
-			|| !(cfg->rho != 0) || cfg->projection.kind != CARPIO_GPU_CG)
+			|| !(cfg->rho != 0))
+		return CARPIO_GPU_EINVAL;
+	// the projection: CG (the drop-in, any precision) or the shipped IC_CGS /
+	// IC_CG (FP64; solved synchronously through the CSR layer)
+	const int pk = cfg->projection.kind;
+	if (pk != CARPIO_GPU_CG && !((pk == CARPIO_GPU_IC_CGS || pk == CARPIO_GPU_IC_CG)
+			&& cfg->projection.precision == CARPIO_GPU_FP64))
 		return CARPIO_GPU_EINVAL;
 	*out = nullptr;
 	carpio_gpu_ns* ns = new carpio_gpu_ns();

@@ -348,8 +348,14 @@ class NS_explicit:
             raise _lib.CarpioGpuError(rc, "ns_set_learned")
 
     def set_projection_solver(self, name="CG", max_iter=1000, tol=1e-3,
-                              precision="fp64", **kw):
-        self.proj = solver_cfg(name, max_iter, tol, mean_removal=True,
+                              precision="fp64", mean_removal=None, **kw):
+        """NS_::set_projection_solver (s_ns.hpp:120-130). "CG" is the
+        drop-in (with mean removal by default); "IC_CGS" / "IC_CG" are the
+        reference's shipped solvers (Solver_IC_CGS_, s_solver.hpp:329-352,
+        removes no mean), FP64 only."""
+        if mean_removal is None:
+            mean_removal = name == "CG"
+        self.proj = solver_cfg(name, max_iter, tol, mean_removal=mean_removal,
                                precision=precision, **kw)
 
     def initial(self):

@@ -237,9 +237,12 @@ typedef struct {
 	int scheme;          /* CARPIO_GPU_UPWIND1 .. MINMOD */
 	carpio_gpu_bc bc_u;  /* add_bc(0, seg, "u", ...) */
 	carpio_gpu_bc bc_v;  /* add_bc(0, seg, "v", ...) */
-	carpio_gpu_solver_cfg projection; /* set_projection_solver; mean removal
-	                                     is what makes the all-Neumann
-	                                     projection solvable */
+	carpio_gpu_solver_cfg projection; /* set_projection_solver: CG (the
+	                                     drop-in; mean removal is what makes
+	                                     the all-Neumann projection solvable)
+	                                     or the shipped IC_CGS / IC_CG (FP64,
+	                                     usually without mean removal, as
+	                                     Solver_IC_CGS_ does) */
 } carpio_gpu_ns_cfg;
 
 typedef struct carpio_gpu_ns carpio_gpu_ns;

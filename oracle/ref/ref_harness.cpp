@@ -19,8 +19,10 @@
 //           reference's _build_exp/_build_matrix and calls the carpio:: free
 //           function (mean removal of b and x for the all-Neumann case).
 //   cavity  <n> <steps> <scheme> <tol> <max_iter> <dt0> <Re> <dump_every> [stretch]
+//           [proj=<kind>[_nomean]]
 //           NS_explicit_ (s_ns_explicit.hpp) lid-driven cavity on [0,1]^2,
-//           gl = 2, projection by the CG + mean-removal drop-in.
+//           gl = 2, projection by the CG + mean-removal drop-in (proj=: another
+//           carpio:: solver, with or without the mean removal).
 //   kim     <n> <steps> <scheme> <tol> <max_iter> <dt0> <Re>
 //           NS_kim_ (s_ns_kim.hpp) lid-driven cavity, gl = 2, projection by
 //           the CG + mean-removal drop-in.
@@ -400,10 +402,11 @@ static Vt VdotNabla_TVD_minmod(const VectorFace_<2>& vf, const Scalar& c,
 
 class NSAlg_: public NS_explicit_<2> {
 public:
-	NSAlg_(spGrid g, int max_iter, double tol, std::vector<SolveRecord>* rec)
+	NSAlg_(spGrid g, int max_iter, double tol, std::vector<SolveRecord>* rec,
+			const std::string& kind = "cg", bool mean = true)
 		: NS_explicit_<2>(g) {
 		this->_projection = spPoisson(
-				new PoissonAlg_(g, "cg", true, max_iter, tol, rec, false));
+				new PoissonAlg_(g, kind, mean, max_iter, tol, rec, false));
 	}
 	void set_scheme(const std::string& s) {
 		if (s == "minmod") this->fun_v_dot_nabla = &VdotNabla_TVD_minmod;
@@ -431,11 +434,26 @@ static int cmd_cavity(int argc, char** argv) {
 	int dump_every = std::atoi(argv[9]);
 	out_open(argv[argc - 1]);
 	const bool stretch = stretch_arg(argc, argv, 10);
+	// proj=<kind> | proj=<kind>_nomean: another carpio:: solver for the
+	// projection, with or without the mean removal (the shipped
+	// Solver_IC_CGS_, s_solver.hpp:329-352, removes nothing)
+	std::string pkind = "cg";
+	bool pmean = true;
+	for (int k = 10; k < argc - 1; ++k) {
+		std::string a = argv[k];
+		if (a.compare(0, 5, "proj=") != 0) continue;
+		pkind = a.substr(5);
+		const std::string nm = "_nomean";
+		if (pkind.size() > nm.size() && pkind.compare(pkind.size() - nm.size(), nm.size(), nm) == 0) {
+			pkind = pkind.substr(0, pkind.size() - nm.size());
+			pmean = false;
+		}
+	}
 	spGrid g = make_grid(n, n, 2, stretch);
 	put_scalar("stretch", stretch ? 1.0 : 0.0);
 	put_grid(*g);
 	std::vector<SolveRecord> rec;
-	NSAlg_ ns(g, max_iter, tol, &rec);
+	NSAlg_ ns(g, max_iter, tol, &rec, pkind, pmean);
 	ns.set_scheme(scheme);
 	ns.set_time(steps > 0 ? steps - 1 : 0, dt0);
 	NS_<2>::spBC bc0(new NS_<2>::BC()), bc1(new NS_<2>::BC());
@@ -447,10 +465,11 @@ static int cmd_cavity(int argc, char** argv) {
 	ns.set_uniform_rho(Re);
 	ns.set_diffusion_number(0.25, 1.0 / Re);
 	ns.initial();
-	std::vector<double> dts, its, ms, res;
+	std::vector<double> dts, its, ms, res, rets;
 	for (int s = 0; s < steps; ++s) {
 		ns.step_once();
 		dts.push_back(ns.dt());
+		rets.push_back(rec.back().ret);
 		its.push_back(rec.back().iters);
 		ms.push_back(rec.back().ms);
 		res.push_back(rec.back().tol_out);
@@ -478,6 +497,7 @@ static int cmd_cavity(int argc, char** argv) {
 	for (const char* nm : names) put_field(nm, *ns.cs(nm));
 	put_vec("dt", dts);
 	put_vec("cg_iters", its);
+	put_vec("cg_ret", rets);
 	put_vec("cg_ms", ms);
 	put_vec("cg_resid", res);
 	put_scalar("Re", Re);

@@ -1052,24 +1052,29 @@ int rs_ns_run(int nx, int ny, int gl, const double* cx, const double* sx,
 		rs_c2f(nx, ny, gl, sx, sy, us, vs, usf, vsf);
 		rs_div(nx, ny, gl, sx, sy, usf, vsf, div);
 		/* projection: Poisson_::run with set_depend(phi, -, div), the
-		 * CG + mean-removal drop-in solver */
+		 * CG + mean-removal drop-in solver (proj_kind / proj_nomean: another
+		 * carpio:: solver, and the shipped solvers' no removal) */
 		rs_assemble_poisson(nx, ny, gl, cx, sx, cy, sy, &bc_phi, 1.0, div, 0.0,
 				rp, ci, va, b, NULL);
 		for (int j = 0; j < ny; ++j)
 			for (int i = 0; i < nx; ++i) x[i + j * nx] = AT(phi, i, j);
 		double m = 0;
-		for (int k = 0; k < n; ++k) m += b[k];
-		m = m / (double)n;
-		for (int k = 0; k < n; ++k) b[k] = b[k] - m;
+		if (!cfg->proj_nomean) {
+			for (int k = 0; k < n; ++k) m += b[k];
+			m = m / (double)n;
+			for (int k = 0; k < n; ++k) b[k] = b[k] - m;
+		}
 		int mi = cfg->cg_max_iter;
 		double tol = cfg->cg_tol;
-		int r = rs_krylov_csr(RS_CG, n, rp, ci, va, b, x, &mi, &tol, NULL, 0,
+		int r = rs_krylov_csr(cfg->proj_kind, n, rp, ci, va, b, x, &mi, &tol, NULL, 0,
 				NULL, cfg->threads);
 		if (r && !ret) ret = r;
-		m = 0;
-		for (int k = 0; k < n; ++k) m += x[k];
-		m = m / (double)n;
-		for (int k = 0; k < n; ++k) x[k] = x[k] - m;
+		if (!cfg->proj_nomean) {
+			m = 0;
+			for (int k = 0; k < n; ++k) m += x[k];
+			m = m / (double)n;
+			for (int k = 0; k < n; ++k) x[k] = x[k] - m;
+		}
 		for (int j = 0; j < ny; ++j)
 			for (int i = 0; i < nx; ++i) AT(phi, i, j) = x[i + j * nx];
 		rs_apply_bc(nx, ny, gl, cx, sx, cy, sy, &bc_phi, phi);

@@ -129,6 +129,8 @@ typedef struct {
 	int cg_max_iter;
 	double cg_tol;
 	int threads;               /* OpenMP threads for the CG (1 = bit-exact) */
+	int proj_kind;             /* RS_* Krylov kind of the projection (0 = CG) */
+	int proj_nomean;           /* 1: no mean removal (the shipped solvers) */
 } rs_ns_cfg;
 
 int rs_ns_run(int nx, int ny, int gl, const double* cx, const double* sx,

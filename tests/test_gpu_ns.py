@@ -47,8 +47,19 @@ def test_operators_bitwise(gpu_lib, name):
     assert bits_equal(o, d["bc_filled"])
 
 
+def fixture_proj(d):
+    """the projection solver of a cavity fixture: (name, mean removal)"""
+    for x in d.get("case_args", []):
+        x = str(x)
+        if x.startswith("proj="):
+            k = x[5:]
+            mean = not k.endswith("_nomean")
+            return k.replace("_nomean", "").upper(), mean
+    return "CG", True
+
+
 def make_cavity(n, scheme, dt0, Re=1000.0, tol=1e-10, max_iter=100000,
-                precision="fp64", fixture=None, **kw):
+                precision="fp64", fixture=None, proj="CG", mean_removal=None, **kw):
     from carpio_gb300 import structure as S
     g = gpu_grid(fixture or {}, n, n, 2)
     ns = S.NS_explicit(g)
@@ -64,28 +75,58 @@ def make_cavity(n, scheme, dt0, Re=1000.0, tol=1e-10, max_iter=100000,
         ns.add_bc(0, s, "v", bc0)
     ns.set_uniform_rho(Re)
     ns.set_diffusion_number(0.25, 1.0 / Re)
-    ns.set_projection_solver("CG", max_iter, tol, precision=precision, **kw)
+    ns.set_projection_solver(proj, max_iter, tol, precision=precision,
+                             mean_removal=mean_removal, **kw)
     return g, ns
 
 
 @pytest.mark.parametrize("name", [n for n in golden_names("cavity_")
-                                  if not n.endswith("_2000")])
+                                  if not n.endswith("_2000") and "_fail" not in n
+                                  and "_diverge" not in n])
 def test_cavity_matches_reference(gpu_lib, name):
     d = golden(name)
     a = d["case_args"]
     n, steps, scheme = int(a[1]), int(a[2]), str(a[3])
     tol, max_iter, dt0, Re = float(a[4]), int(a[5]), float(a[6]), float(a[7])
-    g, ns = make_cavity(n, scheme, dt0, Re, tol, max_iter, fixture=d)
+    proj, mean = fixture_proj(d)
+    g, ns = make_cavity(n, scheme, dt0, Re, tol, max_iter, fixture=d, proj=proj,
+                        mean_removal=mean)
     assert bits_equal(g.cx, d["grid_cx"]) and bits_equal(g.sy, d["grid_sy"])
     assert ns.run(steps) == 0
     st = ns.state()
     # dt: the diffusion limit is bitwise; the CFL limit follows max|u|
     assert np.allclose(ns.step_dt, d["dt"], rtol=1e-12, atol=0)
     its = np.asarray(ns.step_iters)
-    assert np.all(np.abs(its - d["cg_iters"]) <= np.maximum(2, d["cg_iters"] // 100))
+    # CGS's residual path is erratic: with the GPU's summation order its
+    # iteration counts move by a few (82/65/68 against 82/69/65 on the
+    # 64^2 case), and the fields agree to the solves' tolerance
+    band, frac, rtol = (2, 100, PLAIN_RTOL) if proj == "CG" else (6, 10, 1e-8)
+    assert np.all(np.abs(its - d["cg_iters"]) <= np.maximum(band, d["cg_iters"] // frac))
     for k in ("u", "v", "p", "phi", "uf", "vf"):
         err = rel_l2(g.interior(st[k]), g.interior(d[k]))
-        assert err <= PLAIN_RTOL, (k, err)
+        assert err <= rtol, (k, err)
+
+
+def test_cavity_ic_cgs_fails_at_256_like_reference(gpu_lib):
+    """The shipped IC_CGS projection (no mean removal) on the 256^2
+    cavity's first step: with the example's 100 iterations the reference
+    stops far from tol (code 1), with 1000 it diverges; the GPU solve
+    does the same. (Different summation order: the residual is compared
+    in size, not in bits.)"""
+    for name, lo, hi in (("cavity_256_vanleer_1_ic_cgs_fail", 0.1, 10.0),
+                         ("cavity_256_vanleer_1_ic_cgs_diverge", None, None)):
+        d = golden(name)
+        a = d["case_args"]
+        n, tol, max_iter, dt0 = int(a[1]), float(a[4]), int(a[5]), float(a[6])
+        g, ns = make_cavity(n, "VanLeer", dt0, 1000.0, tol, max_iter, proj="IC_CGS",
+                            mean_removal=False)
+        assert ns.run(1) == 1 == int(d["cg_ret"][0])
+        assert ns.step_iters[0] == max_iter == int(d["cg_iters"][0])
+        r, rr = ns.step_resid[0], float(d["cg_resid"][0])
+        if lo is not None:
+            assert lo * rr <= r <= hi * rr and r > 100 * tol, (r, rr)
+        else:
+            assert rr > 1e20 and not (r < 1e10), (r, rr)
 
 
 def test_cavity_first_step_fields(gpu_lib):

@@ -104,15 +104,30 @@ def cavity_case(d):
     return n, steps, scheme, tol, max_iter, dt0, Re
 
 
+def cavity_proj(d):
+    """the projection solver of a cavity fixture: (kind, mean removal)"""
+    for x in d["case_args"]:
+        x = str(x)
+        if x.startswith("proj="):
+            k = x[5:]
+            if k.endswith("_nomean"):
+                return k[:-7], False
+            return k, True
+    return "cg", True
+
+
 @pytest.mark.parametrize("name", [n for n in golden_names("cavity_")
-                                  if not n.endswith("_2000")])
+                                  if not n.endswith("_2000") and "_fail" not in n
+                                  and "_diverge" not in n])
 def test_cavity_steps_bitwise(name):
     d = golden(name)
     n, steps, scheme, tol, max_iter, dt0, Re = cavity_case(d)
     g = oracle_grid(d, n, n, 2)
     st = R.new_state(g, dt0)
+    proj, mean = cavity_proj(d)
     code, sdt, sit, sres = R.ns_run(g, st, steps, Re=Re, scheme=scheme,
-                                    cg_tol=tol, cg_max_iter=max_iter)
+                                    cg_tol=tol, cg_max_iter=max_iter, proj=proj,
+                                    proj_mean=mean)
     assert code == 0
     assert bits_equal(sdt, d["dt"])
     assert np.array_equal(sit, d["cg_iters"].astype(int))
@@ -215,3 +230,23 @@ def test_advection_bitwise(name):
     phi = R.advect_run(g, str(d["scheme"]).lower(), oracle_bc(bi.to_c("phi", functions=True)),
                        uf, vf, float(d["dt"]), int(d["steps"]), d["in_phi"], gv)
     assert bits_equal(phi, d["phi"])
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names("cavity_256")
+                                  if "_fail" in n or "_diverge" in n])
+def test_cavity_ic_cgs_failure_bitwise(name):
+    """The shipped IC_CGS projection on the 256^2 cavity's first step: the
+    reference stops at max_iter far from tol (100 iterations) or diverges
+    (1000); the oracle reproduces the code, iterations and residual bits"""
+    d = golden(name)
+    n, steps, scheme, tol, max_iter, dt0, Re = cavity_case(d)
+    g = oracle_grid(d, n, n, 2)
+    st = R.new_state(g, dt0)
+    proj, mean = cavity_proj(d)
+    code, sdt, sit, sres = R.ns_run(g, st, steps, Re=Re, scheme=scheme,
+                                    cg_tol=tol, cg_max_iter=max_iter, proj=proj,
+                                    proj_mean=mean)
+    assert code == int(d["cg_ret"][0]) == 1
+    assert bits_equal(sdt, d["dt"])
+    assert np.array_equal(sit, d["cg_iters"].astype(int))
+    assert bits_equal(sres, d["cg_resid"])
