@@ -115,6 +115,7 @@ SIGNATURES = {
         _VP, _D, _VP, _VP, _VP, _VP, _VP, _VP]),
     "carpio_gpu_ns_run": (ctypes.c_int, [_VP, ctypes.c_int, _VP, _VP, _VP]),
     "carpio_gpu_ns_set_stepper": (ctypes.c_int, [_VP, ctypes.c_int]),
+    "carpio_gpu_ns_set_mu_field": (ctypes.c_int, [_VP, _VP]),
     "carpio_gpu_advection_create": (ctypes.c_int, [_VP, ctypes.POINTER(_VP)]),
     "carpio_gpu_advection_destroy": (ctypes.c_int, [_VP]),
     "carpio_gpu_advection_set_scheme": (ctypes.c_int, [_VP, ctypes.c_int]),

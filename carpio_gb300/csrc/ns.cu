@@ -379,22 +379,24 @@ __global__ void __launch_bounds__(kThreads) k_maxmag(Geo g, const double* u,
 template<int SCH>
 __global__ void __launch_bounds__(kThreads) k_predictor(Geo g, const double* u,
 		const double* v, const double* uf, const double* vf, double* us,
-		double* vs, const StepScalars* ss, double rho, double mu) {
+		double* vs, const StepScalars* ss, double rho, double mu, const double* muf) {
 	const double dt = ss->dt;
 	const long n = (long)g.nx * g.ny;
 	for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n;
 			k += (long)gridDim.x * blockDim.x) {
 		int i = (int)(k / g.ny), j = (int)(k - (long)i * g.ny);
 		int a = g.at(i, j);
+		// __diffusion_term (s_ns_explicit.hpp:235-241): the mu field when the
+		// uniform mu was unset
 		{
 			double adv = adv_cell<SCH>(g, uf, vf, u, i, j);
-			double dif = diffusion(g, mu, u, i, j);
+			double dif = muf ? diffusion_var(g, muf, u, i, j) : diffusion(g, mu, u, i, j);
 			double src = 0;
 			us[a] = (-adv + (dif + src) / rho) * dt + u[a];
 		}
 		{
 			double adv = adv_cell<SCH>(g, uf, vf, v, i, j);
-			double dif = diffusion(g, mu, v, i, j);
+			double dif = muf ? diffusion_var(g, muf, v, i, j) : diffusion(g, mu, v, i, j);
 			double src = 0;
 			vs[a] = (-adv + (dif + src) / rho) * dt + v[a];
 		}
@@ -648,16 +650,19 @@ cudaError_t launch_bc(const Geo& geo, double* f0, const carpio_gpu_bc& b0,
 template<int SCH>
 cudaError_t launch_pred(const Geo& geo, int blocks, cudaStream_t s,
 		const double* u, const double* v, const double* uf, const double* vf,
-		double* us, double* vs, const StepScalars* ss, double rho, double mu) {
-	k_predictor<SCH><<<blocks, kThreads, 0, s>>>(geo, u, v, uf, vf, us, vs, ss, rho, mu);
+		double* us, double* vs, const StepScalars* ss, double rho, double mu,
+		const double* muf) {
+	k_predictor<SCH><<<blocks, kThreads, 0, s>>>(geo, u, v, uf, vf, us, vs, ss, rho, mu, muf);
 	return cudaGetLastError();
 }
 
 cudaError_t launch_predictor(int sch, const Geo& geo, int blocks, cudaStream_t s,
 		const double* u, const double* v, const double* uf, const double* vf,
-		double* us, double* vs, const StepScalars* ss, double rho, double mu) {
+		double* us, double* vs, const StepScalars* ss, double rho, double mu,
+		const double* muf) {
 	switch (sch) {
-#define CASE(S) case S: return launch_pred<S>(geo, blocks, s, u, v, uf, vf, us, vs, ss, rho, mu);
+#define CASE(S) case S: return launch_pred<S>(geo, blocks, s, u, v, uf, vf, us, vs, ss, rho, \
+		mu, muf);
 	CASE(CARPIO_GPU_UPWIND1) CASE(CARPIO_GPU_CENTER) CASE(CARPIO_GPU_CENTER4)
 	CASE(CARPIO_GPU_UPWIND2) CASE(CARPIO_GPU_VANLEER) CASE(CARPIO_GPU_SUPERBEE)
 	CASE(CARPIO_GPU_WAHYD) CASE(CARPIO_GPU_QUICK) CASE(CARPIO_GPU_CUI)
@@ -743,6 +748,9 @@ struct carpio_gpu_ns {
 	cg_host::StencilCoeffs kim_coeffs;   // the predictor's Helmholtz rows
 	cg_host::DevBuf kim_out;      // SolveOut of the predictor solves
 	long steps_done = 0;          // Time_::current_step
+	// a mu field in place of the uniform mu (carpio_gpu_ns_set_mu_field)
+	cg_host::DevBuf muf;
+	bool has_mu = false;
 	~carpio_gpu_ns() {
 		for (cudaEvent_t e : ev) cudaEventDestroy(e);
 	}
@@ -945,7 +953,8 @@ int carpio_gpu_ns_run(carpio_gpu_ns* ns, int steps, double* step_dt,
 				ns->rec_dt.as<double>(), st);
 		CG_CK(cudaGetLastError());
 		CG_CK(launch_bc(geo, u, c.bc_u, v, &c.bc_v, s));
-		CG_CK(launch_predictor(c.scheme, geo, nb, s, u, v, uf, vf, us, vs, ss, c.rho, c.mu));
+		CG_CK(launch_predictor(c.scheme, geo, nb, s, u, v, uf, vf, us, vs, ss, c.rho, c.mu,
+				ns->has_mu ? ns->muf.as<double>() : nullptr));
 		CG_CK(launch_bc(geo, us, c.bc_u, vs, &c.bc_v, s));
 		k_c2f<<<nb, kThreads, 0, s>>>(geo, us, vs, usf, vsf);
 		CG_CK(cudaGetLastError());
@@ -1001,7 +1010,7 @@ int carpio_gpu_ns_set_stepper(carpio_gpu_ns* ns, int stepper) {
 	if (!ns || (stepper != CARPIO_GPU_STEPPER_EXPLICIT && stepper != CARPIO_GPU_STEPPER_KIM))
 		return CARPIO_GPU_EINVAL;
 	if (stepper == CARPIO_GPU_STEPPER_KIM) {
-		if (ns->learned) return CARPIO_GPU_EINVAL;
+		if (ns->learned || ns->has_mu) return CARPIO_GPU_EINVAL;
 		carpio_gpu_grid* g = ns->g;
 		const size_t fn = (size_t)g->NI * g->P;
 		if (!ns->kim_fields.p) {
@@ -1013,6 +1022,21 @@ int carpio_gpu_ns_set_stepper(carpio_gpu_ns* ns, int stepper) {
 		for (int k = 0; k < 6; ++k) ns->k[k] = ns->kim_fields.as<double>() + k * fn;
 	}
 	ns->stepper = stepper;
+	return 0;
+}
+
+int carpio_gpu_ns_set_mu_field(carpio_gpu_ns* ns, const double* mu) {
+	if (!ns || ns->stepper != CARPIO_GPU_STEPPER_EXPLICIT) return CARPIO_GPU_EINVAL;
+	if (!mu) {
+		ns->has_mu = false;
+		return 0;
+	}
+	carpio_gpu_grid* g = ns->g;
+	int rc;
+	if ((rc = ns->muf.ensure(sizeof(double) * (size_t)g->NI * g->P))) return rc;
+	if ((rc = copy_field(g, ns->muf.as<double>(), mu, true, ns->s))) return rc;
+	CG_CK(cudaStreamSynchronize(ns->s));
+	ns->has_mu = true;
 	return 0;
 }
 

@@ -322,6 +322,25 @@ class NS_explicit:
 
     def set_uniform_mu(self, mu=1.0):
         self.mu = float(mu)
+        self._mu_fun = None
+
+    def unset_uniform_mu(self):
+        """with initial_CS("mu", f): a mu field (s_ns.hpp:111-118, 277-280)"""
+        self._mu_fun = getattr(self, "_mu_fun", None) or (lambda t, x, y, z: 1.0)
+
+    def initial_CS(self, name, fun):
+        if name != "mu":
+            raise ValueError("NS_explicit.initial_CS takes the mu field only")
+        self._mu_fun = fun if callable(fun) else (lambda t, x, y, z, v=float(fun): v)
+
+    def _mu_field(self):
+        """set_CS("mu", f): f at every cell centre, ghosts included, t = 0"""
+        g, f = self.grid, self._mu_fun
+        out = g.zeros()
+        for I in range(out.shape[0]):
+            for J in range(out.shape[1]):
+                out[I, J] = f(0.0, g.cx[I], g.cy[J], 0.0)
+        return out
 
     def set_CFL_number(self, v=0.5):
         self.cfl = float(v)
@@ -373,6 +392,10 @@ class NS_explicit:
         if rc:
             raise _lib.CarpioGpuError(rc, "ns_create")
         self.handle = h
+        if getattr(self, "_mu_fun", None) is not None:
+            rc = L.carpio_gpu_ns_set_mu_field(h, _lib.ptr(self._mu_field()))
+            if rc:
+                raise _lib.CarpioGpuError(rc, "ns_set_mu_field")
 
     def run(self, steps=None):
         """Equation_::run: max_step + 1 steps (s_time.hpp:335-341) unless

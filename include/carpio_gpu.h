@@ -272,6 +272,14 @@ int carpio_gpu_ns_run(carpio_gpu_ns* ns, int steps, double* step_dt,
 #define CARPIO_GPU_STEPPER_EXPLICIT 0
 #define CARPIO_GPU_STEPPER_KIM 1
 int carpio_gpu_ns_set_stepper(carpio_gpu_ns* ns, int stepper);
+/* A mu field (a cell field of the grid's layout, host or device) in place of
+ * the uniform mu: NablaMuNabla(mu field) in the predictor
+ * (__diffusion_term, s_ns_explicit.hpp:235-241), as unset_uniform_mu +
+ * initial_CS("mu", f) give it in the reference (s_ns.hpp:111-118,
+ * 277-280; its set_mu cannot be instantiated). NULL: back to the uniform
+ * mu. Explicit stepper only. A rho field has no counterpart: the
+ * reference's run_one_step asserts a uniform rho (s_ns_explicit.hpp:134). */
+int carpio_gpu_ns_set_mu_field(carpio_gpu_ns* ns, const double* mu);
 
 /* Timing of the last carpio_gpu_ns_run, per step (host arrays of length
  * `cap`, any may be NULL): device time of the projection solve launch and of

@@ -19,10 +19,11 @@
 //           reference's _build_exp/_build_matrix and calls the carpio:: free
 //           function (mean removal of b and x for the all-Neumann case).
 //   cavity  <n> <steps> <scheme> <tol> <max_iter> <dt0> <Re> <dump_every> [stretch]
-//           [proj=<kind>[_nomean]]
+//           [proj=<kind>[_nomean]] [mu=field]
 //           NS_explicit_ (s_ns_explicit.hpp) lid-driven cavity on [0,1]^2,
 //           gl = 2, projection by the CG + mean-removal drop-in (proj=: another
-//           carpio:: solver, with or without the mean removal).
+//           carpio:: solver, with or without the mean removal; mu=field:
+//           mu(x, y) = 1 + x y / 2 in place of the uniform mu).
 //   kim     <n> <steps> <scheme> <tol> <max_iter> <dt0> <Re>
 //           NS_kim_ (s_ns_kim.hpp) lid-driven cavity, gl = 2, projection by
 //           the CG + mean-removal drop-in.
@@ -439,8 +440,10 @@ static int cmd_cavity(int argc, char** argv) {
 	// Solver_IC_CGS_, s_solver.hpp:329-352, removes nothing)
 	std::string pkind = "cg";
 	bool pmean = true;
+	bool mufield = false;
 	for (int k = 10; k < argc - 1; ++k) {
 		std::string a = argv[k];
+		if (a == "mu=field") mufield = true;
 		if (a.compare(0, 5, "proj=") != 0) continue;
 		pkind = a.substr(5);
 		const std::string nm = "_nomean";
@@ -464,7 +467,15 @@ static int cmd_cavity(int argc, char** argv) {
 	for (int s = 0; s < 4; ++s) ns.add_bc(0, s, "v", bc0);
 	ns.set_uniform_rho(Re);
 	ns.set_diffusion_number(0.25, 1.0 / Re);
+	if (mufield) {
+		// a mu field (s_ns.hpp:111-118, 277-280): NS_::set_mu calls
+		// unset_uniform_beta, which NS_ lacks, so it cannot be instantiated;
+		// unset_uniform_mu + initial_CS("mu", f) is the working route
+		ns.unset_uniform_mu();
+		ns.initial_CS("mu", [](Vt, Vt x, Vt y, Vt) { return 1.0 + 0.5 * x * y; });
+	}
 	ns.initial();
+	if (mufield) put_field("mu", *ns.cs("mu"));
 	std::vector<double> dts, its, ms, res, rets;
 	for (int s = 0; s < steps; ++s) {
 		ns.step_once();

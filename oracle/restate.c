@@ -818,36 +818,42 @@ void rs_diffusion(int nx, int ny, int gl, const double* cx, const double* sx,
 			AT(out, i, j) = nmn(nx, ny, gl, cx, sx, cy, sy, mu, f, i, j);
 }
 
-/* NablaMuNabla(const Scalar& mu, ...) (s_operation.hpp:630-662): face mu
- * from the cell and its neighbour weighted by the half sizes */
+/* NablaMuNabla(const Scalar& mu, ...) (s_operation.hpp:630-662) at one
+ * cell: face mu from the cell and its neighbour weighted by the half sizes */
+static double nmn_var(int nx, int ny, int gl, const double* cx, const double* sx,
+		const double* cy, const double* sy, const double* mu, const double* f,
+		int i, int j) {
+	const int NJ = ny + 2 * gl;
+	double t[2];
+	for (int d = 0; d < 2; ++d) {
+		int ip = d == 0 ? i + 1 : i, jp = d == 0 ? j : j + 1;
+		int im = d == 0 ? i - 1 : i, jm = d == 0 ? j : j - 1;
+		double hs = (d == 0 ? SX(i) : SY(j)) * 0.5;
+		double hsp = (d == 0 ? SX(ip) : SY(jp)) * 0.5;
+		double hsm = (d == 0 ? SX(im) : SY(jm)) * 0.5;
+		double c = d == 0 ? CX(i) : CY(j);
+		double cp = d == 0 ? CX(ip) : CY(jp);
+		double cm = d == 0 ? CX(im) : CY(jm);
+		double mufp = (hs * AT(mu, ip, jp) + hsp * AT(mu, i, j)) / (hsp + hs);
+		double mufm = (hs * AT(mu, im, jm) + hsm * AT(mu, i, j)) / (hsm + hs);
+		double dp = mufp * (AT(f, ip, jp) - AT(f, i, j)) / (cp - c);
+		double dm = mufm * (AT(f, i, j) - AT(f, im, jm)) / (c - cm);
+		t[d] = (dp - dm) / (d == 0 ? SX(i) : SY(j));
+	}
+	double res = 0.0;
+	res += t[0];
+	res += t[1];
+	return res;
+}
+
 void rs_diffusion_var(int nx, int ny, int gl, const double* cx, const double* sx,
 		const double* cy, const double* sy, const double* mu, const double* f,
 		double* out) {
 	const int NJ = ny + 2 * gl;
 	memset(out, 0, sizeof(double) * (size_t)(nx + 2 * gl) * NJ);
 	for (int j = 0; j < ny; ++j)
-		for (int i = 0; i < nx; ++i) {
-			double t[2];
-			for (int d = 0; d < 2; ++d) {
-				int ip = d == 0 ? i + 1 : i, jp = d == 0 ? j : j + 1;
-				int im = d == 0 ? i - 1 : i, jm = d == 0 ? j : j - 1;
-				double hs = (d == 0 ? SX(i) : SY(j)) * 0.5;
-				double hsp = (d == 0 ? SX(ip) : SY(jp)) * 0.5;
-				double hsm = (d == 0 ? SX(im) : SY(jm)) * 0.5;
-				double c = d == 0 ? CX(i) : CY(j);
-				double cp = d == 0 ? CX(ip) : CY(jp);
-				double cm = d == 0 ? CX(im) : CY(jm);
-				double mufp = (hs * AT(mu, ip, jp) + hsp * AT(mu, i, j)) / (hsp + hs);
-				double mufm = (hs * AT(mu, im, jm) + hsm * AT(mu, i, j)) / (hsm + hs);
-				double dp = mufp * (AT(f, ip, jp) - AT(f, i, j)) / (cp - c);
-				double dm = mufm * (AT(f, i, j) - AT(f, im, jm)) / (c - cm);
-				t[d] = (dp - dm) / (d == 0 ? SX(i) : SY(j));
-			}
-			double res = 0.0;
-			res += t[0];
-			res += t[1];
-			AT(out, i, j) = res;
-		}
+		for (int i = 0; i < nx; ++i)
+			AT(out, i, j) = nmn_var(nx, ny, gl, cx, sx, cy, sy, mu, f, i, j);
 }
 
 /* std::min / std::max semantics ((b < a) ? b : a, (a < b) ? b : a) */
@@ -1040,7 +1046,11 @@ int rs_ns_run(int nx, int ny, int gl, const double* cx, const double* sx,
 				for (int i = 0; i < nx; ++i) {
 					double adv = adv_cell(cfg->scheme, nx, ny, gl, cx, sx, cy,
 							sy, uf, vf, s, i, j);
-					double dif = nmn(nx, ny, gl, cx, sx, cy, sy, cfg->mu, s, i, j);
+					/* __diffusion_term (s_ns_explicit.hpp:235-241): the mu
+					 * field when set_mu replaced the uniform mu */
+					double dif = cfg->mu_field
+							? nmn_var(nx, ny, gl, cx, sx, cy, sy, cfg->mu_field, s, i, j)
+							: nmn(nx, ny, gl, cx, sx, cy, sy, cfg->mu, s, i, j);
 					double src = 0;
 					AT(ss, i, j) = (-adv + (dif + src) / cfg->rho) * DT + AT(s, i, j);
 				}

@@ -131,6 +131,7 @@ typedef struct {
 	int threads;               /* OpenMP threads for the CG (1 = bit-exact) */
 	int proj_kind;             /* RS_* Krylov kind of the projection (0 = CG) */
 	int proj_nomean;           /* 1: no mean removal (the shipped solvers) */
+	const double* mu_field;    /* set_mu field (NULL: the uniform mu) */
 } rs_ns_cfg;
 
 int rs_ns_run(int nx, int ny, int gl, const double* cx, const double* sx,

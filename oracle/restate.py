@@ -37,7 +37,7 @@ class NSCfg(ctypes.Structure):
                 ("diff_coef", ctypes.c_double), ("scheme", ctypes.c_int),
                 ("cg_max_iter", ctypes.c_int), ("cg_tol", ctypes.c_double),
                 ("threads", ctypes.c_int), ("proj_kind", ctypes.c_int),
-                ("proj_nomean", ctypes.c_int)]
+                ("proj_nomean", ctypes.c_int), ("mu_field", ctypes.c_void_p)]
 
 
 def build():
@@ -290,7 +290,7 @@ def cavity_bcs():
 def ns_run(grid, state, steps, *, Re=1000.0, mu=1.0, cfl=0.5,
            diff_number=0.25, diff_coef=None, scheme="vanleer",
            cg_max_iter=100000, cg_tol=1e-10, threads=1, bc_u=None, bc_v=None,
-           proj="cg", proj_mean=True):
+           proj="cg", proj_mean=True, mu_field=None):
     """Runs `steps` explicit projection steps in place on
     state = dict(dt=float, u, v, uf, vf, phi, p). Returns (code, step_dt,
     step_iters, step_resid)."""
@@ -301,6 +301,9 @@ def ns_run(grid, state, steps, *, Re=1000.0, mu=1.0, cfl=0.5,
                 scheme=SCHEMES.get(scheme, scheme), cg_max_iter=cg_max_iter,
                 cg_tol=cg_tol, threads=threads, proj_kind=KINDS[proj],
                 proj_nomean=0 if proj_mean else 1)
+    if mu_field is not None:
+        mu_field = _f64(mu_field)
+        cfg.mu_field = mu_field.ctypes.data
     for k in ("u", "v", "uf", "vf", "phi", "p"):
         state[k] = _f64(state[k])
     dt = ctypes.c_double(state["dt"])

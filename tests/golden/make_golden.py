@@ -177,6 +177,8 @@ def main():
         # the shipped projection solver (Solver_IC_CGS_: no mean removal):
         # converges at 64^2; at 256^2 it stops at the example's max_iter 100
         # far from tol, and with 1000 iterations it diverges
+        ("cavity_24_vanleer_10_mu", [24, 10, "VanLeer", 1e-10, 100000, 0.01, 1000, 0,
+                                     "mu=field"]),
         ("cavity_64_vanleer_3_ic_cgs", [64, 3, "VanLeer", 1e-10, 1000, 0.0078125, 1000, 0,
                                         "proj=ic_cgs_nomean"]),
         ("cavity_256_vanleer_1_ic_cgs_fail", [256, 1, "VanLeer", 1e-6, 100, 0.001953125,

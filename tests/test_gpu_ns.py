@@ -91,6 +91,12 @@ def test_cavity_matches_reference(gpu_lib, name):
     proj, mean = fixture_proj(d)
     g, ns = make_cavity(n, scheme, dt0, Re, tol, max_iter, fixture=d, proj=proj,
                         mean_removal=mean)
+    if "mu=field" in [str(x) for x in a]:
+        # the harness's mu field, through unset_uniform_mu + initial_CS
+        ns.unset_uniform_mu()
+        ns.initial_CS("mu", lambda t, x, y, z: 1.0 + 0.5 * x * y)
+        ns.initial()
+        assert bits_equal(ns._mu_field(), d["mu"])
     assert bits_equal(g.cx, d["grid_cx"]) and bits_equal(g.sy, d["grid_sy"])
     assert ns.run(steps) == 0
     st = ns.state()

@@ -116,6 +116,16 @@ def cavity_proj(d):
     return "cg", True
 
 
+def cavity_mu(d, g):
+    """the mu field of a fixture run with mu=field (1 + x y / 2 at every
+    cell centre, as set_CS writes it), checked against the reference's"""
+    if "mu=field" not in [str(x) for x in d["case_args"]]:
+        return None
+    mu = np.array([[1.0 + 0.5 * x * y for y in g.cy] for x in g.cx])
+    assert bits_equal(mu, d["mu"])
+    return mu
+
+
 @pytest.mark.parametrize("name", [n for n in golden_names("cavity_")
                                   if not n.endswith("_2000") and "_fail" not in n
                                   and "_diverge" not in n])
@@ -127,7 +137,7 @@ def test_cavity_steps_bitwise(name):
     proj, mean = cavity_proj(d)
     code, sdt, sit, sres = R.ns_run(g, st, steps, Re=Re, scheme=scheme,
                                     cg_tol=tol, cg_max_iter=max_iter, proj=proj,
-                                    proj_mean=mean)
+                                    proj_mean=mean, mu_field=cavity_mu(d, g))
     assert code == 0
     assert bits_equal(sdt, d["dt"])
     assert np.array_equal(sit, d["cg_iters"].astype(int))
