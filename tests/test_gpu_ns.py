@@ -196,6 +196,11 @@ def test_output_scalar_matches_reference(gpu_lib, name, tmp_path):
     dev = torch.from_numpy(np.ascontiguousarray(d["in_a"])).cuda()
     rc = gpu_lib.carpio_gpu_output_scalar(g.handle, str(f).encode(), dev.data_ptr())
     assert rc == 0 and f.read_bytes() == ref
+    # read back with the reader of the reference's dumps
+    from carpio_gb300 import dump
+    t = dump.TextFile(str(f))
+    assert np.allclose(t.field(), g.interior(d["in_a"]), rtol=1e-6, atol=1e-6)
+    assert np.allclose(t.get_coo_x(), g.cx[gl:gl + nx], rtol=1e-6)
 
 
 def make_kim(n, scheme, dt0, Re, tol, max_iter):
