@@ -148,6 +148,14 @@ int learned_solve(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& pws, LearnedW
 		const carpio_gpu_learned_cfg& lc, cg_dev::SolveOut& out, cudaStream_t s,
 		std::vector<double>* hist = nullptr);
 
+// the U-Net forward for the library's own loops (nn.cu): stream-ordered,
+// no host synchronisation; device-side failures land in *unet_err_flag(u),
+// unet_take_err reads and clears it (synchronising the net's stream)
+int unet_forward_async(carpio_gpu_unet* u, int n, int h, int w, const float* x,
+		float* z, cudaStream_t st);
+int* unet_err_flag(carpio_gpu_unet* u);
+int unet_take_err(carpio_gpu_unet* u);
+
 }  // namespace cg_host
 
 // Grid handle (defined here so poisson.cu and ns.cu share it).

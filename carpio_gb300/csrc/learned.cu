@@ -23,8 +23,6 @@
 #include <cmath>
 #include <vector>
 
-extern "C" int carpio_gpu_unet_forward(carpio_gpu_unet* u, int n, int h, int w,
-		const float* x, float* z, void* stream);
 
 namespace {
 
@@ -367,7 +365,7 @@ int learned_solve(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& pws, LearnedW
 			if (!(scl > 0)) break;
 			k_pack<<<nb, kLT, 0, s>>>(sp, r, 1.0 / scl, x32);
 			CG_CK(cudaGetLastError());
-			if ((rc = carpio_gpu_unet_forward(net, 1, nx, ny, x32, z32, s))) return rc;
+			if ((rc = unet_forward_async(net, 1, nx, ny, x32, z32, s))) return rc;
 			k_unpack<<<nb, kLT, 0, s>>>(sp, z32, scl, z, part);
 		} else {
 			CG_CK(cudaMemsetAsync(z, 0, sizeof(double) * NF, s));
@@ -406,10 +404,16 @@ int learned_solve(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& pws, LearnedW
 		k_step<<<nb, kLT, 0, s>>>(sp, sc, pnew, qnew, x, r, full, part);
 		k_reduce<3><<<1, 32, 0, s>>>(part, nb, sc);
 		CG_CK(cudaGetLastError());
-		// one host read per iteration: the new residual and the failure flag
+		// one host read per iteration: the new residual, the failure flag
+		// and the network's device-side error flag
 		double hs[10];
+		int nerr = 0;
 		CG_CK(cudaMemcpyAsync(hs, sc, sizeof(double) * 10, cudaMemcpyDeviceToHost, s));
+		if (use_net)
+			CG_CK(cudaMemcpyAsync(&nerr, unet_err_flag(net), sizeof(int),
+					cudaMemcpyDeviceToHost, s));
 		CG_CK(cudaStreamSynchronize(s));
+		if (nerr) return unet_take_err(net);
 		if (hs[S_FAIL] != 0.0) { stalled = true; break; }
 		rr = hs[S_RED + 1];
 		head = (head + 1) % (m + 1);

@@ -927,6 +927,30 @@ static int unet_err(carpio_gpu_unet* u) {
 	return e;
 }
 
+}  // extern "C"
+
+namespace cg_host {
+// The forward for the library's own solvers: stream-ordered on `st`, no
+// host synchronisation and no pointer checks (the caller passes device
+// buffers it owns); a device-side failure is left in the flag unet_err_flag
+// points to, for the caller to read with its next synchronisation.
+int unet_forward_async(carpio_gpu_unet* u, int n, int h, int w, const float* x,
+		float* z, cudaStream_t st) {
+	if (!u || !x || !z || !shape_ok(n, h, w)) return CARPIO_GPU_EINVAL;
+	std::lock_guard<std::mutex> lk(u->mu);
+	int rc = 0;
+	Shape* S = get_shape(u, n, h, w, &rc);
+	if (!S) return rc;
+	return forward(u, *S, x, z, st);
+}
+
+int* unet_err_flag(carpio_gpu_unet* u) { return u->err.as<int>(); }
+
+int unet_take_err(carpio_gpu_unet* u) { return unet_err(u); }
+}  // namespace cg_host
+
+extern "C" {
+
 int carpio_gpu_unet_forward(carpio_gpu_unet* u, int n, int h, int w, const float* x,
 		float* z, void* stream) {
 	if (!u || !x || !z || !shape_ok(n, h, w)) return CARPIO_GPU_EINVAL;

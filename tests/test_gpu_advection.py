@@ -73,3 +73,57 @@ def test_advection_arguments():
         assert not out.any()   # zero velocity, zero phi, Neumann 0
     finally:
         L.carpio_gpu_advection_destroy(h)
+
+
+def oracle_bc(c):
+    from oracle import restate as R
+    o = R.BC()
+    for k in range(4):
+        o.type[k], o.value[k] = c.type[k], c.value[k]
+    return o
+
+
+@pytest.mark.parametrize("nx,ny,scheme", [(7, 19, "VanLeer"), (1, 9, "QUICK"),
+                                          (13, 2, "upwind1"), (16, 16, "center4")])
+def test_advection_ragged_grids_match_oracle(nx, ny, scheme):
+    """ragged and one-cell-wide grids, random velocity and phi fields, a
+    Dirichlet function BC and Neumann values: the GPU sweep against the
+    oracle's sequential loop, bit for bit"""
+    from carpio_gb300 import structure as S
+    from oracle import restate as R
+    rng = np.random.default_rng(nx * 100 + ny)
+    g = S.Grid((0.0, 0.0), (1.0, 0.7), (nx, ny), 2)
+    og = R.Grid(nx, ny, 2, 0.0, 1.0, 0.0, 0.7)
+    assert bits_equal(og.cx, g.cx) and bits_equal(og.sy, g.sy)
+    eq = S.Advection(g)
+    eq.set_time(11, 0.01)
+    u0, v0, p0 = (rng.uniform(-1, 1, g.N()) for _ in range(3))
+    eq.initial_CS("u", 0.0)
+    bi = S.BoundaryIndex()
+    b_fun = S.BoundaryCondition()
+    b_fun.set_default_1_bc(lambda t, x, y, z: 0.5 + y)
+    b_n = S.BoundaryCondition()
+    b_n.set_default_2_bc(0.25)
+    for seg, b in ((0, b_fun), (1, b_n), (2, b_n), (3, b_fun)):
+        eq.add_bc(0, seg, "phi", b)
+        bi.insert(0, seg, "phi", b)
+    eq.set_advection_scheme(scheme)
+    # the library's initial() with explicit fields in place of functions
+    for nm in ("u", "v", "phi"):
+        eq._set_bc(nm, 0.0)
+    from carpio_gb300 import _lib
+    rc = _lib.load().carpio_gpu_advection_initial(eq.handle, _lib.ptr(u0), _lib.ptr(v0),
+                                                  _lib.ptr(p0))
+    assert rc == 0
+    eq._ready = True
+    eq.run()
+    # the oracle: default (Neumann 0) velocity BCs, C2F, 12 in-place steps
+    nb = oracle_bc(S.BoundaryIndex().to_c("u"))
+    u = R.apply_bc(og, nb, u0)
+    v = R.apply_bc(og, nb, v0)
+    uf, vf = R.c2f(og, u, v)
+    gv = bi.ghost_values(g, "phi", 0.0)
+    phi = R.advect_run(og, scheme.lower(), oracle_bc(bi.to_c("phi", functions=True)),
+                       uf, vf, 0.01, 12, p0, gv)
+    assert bits_equal(eq.get_CS("uf"), uf) and bits_equal(eq.get_CS("vf"), vf)
+    assert bits_equal(eq.get_CS("phi"), phi)
