@@ -402,6 +402,7 @@ def main():
         out["learned_cavity"] = learned_cavity_leg(n, a.inner_tol)
         out["unet_forward"] = unet_leg(n)
         out["batched_512"] = batched_leg()
+        out["next_rows"] = next_rows_leg()
         # CPU baseline: the reference's CPU step (restatement) on a bounded
         # sample of the same workload, scaled to the timed steps' iterations
         if ws == 1:
@@ -418,12 +419,145 @@ def main():
                           f"{1e3 * per_it:.2f} ms per CG iteration), scaled to "
                           f"the reference's {its:.0f} FP64 CG iterations per "
                           f"step at the timed steps; oracle restatement, "
-                          f"{threads} threads"}
+                          f"{threads} threads",
+                "next_rows": cpu_next_rows(threads)}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def cone_fields(g):
+    """solid rotation of a cone on a grid's cells (ghosts included):
+    u = -(y - 1/2), v = x - 1/2, phi = 1 - r^2 / 0.04 within r < 0.2 of
+    (0.5, 0.75)"""
+    X, Y = np.meshgrid(g.cx, g.cy, indexing="ij")
+    dx, dy = X - 0.5, Y - 0.75
+    r2 = dx * dx + dy * dy
+    return -(Y - 0.5), X - 0.5, np.where(r2 < 0.04, 1.0 - r2 / 0.04, 0.0)
+
+
+def advection_case(n):
+    """stand-alone Advection_ on n^2: the rotating cone, van Leer, the
+    default (Neumann 0) boundaries, dt = 0.25 / n"""
+    from carpio_gb300 import _lib, structure as S
+    g = S.Grid((0.0, 0.0), (1.0, 1.0), (n, n), 2)
+    eq = S.Advection(g)
+    eq.set_time(0, 0.25 / n)
+    eq.set_advection_scheme("VanLeer")
+    for nm in ("u", "v", "phi"):
+        eq._set_bc(nm, 0.0)
+    u, v, phi = cone_fields(g)
+    rc = _lib.load().carpio_gpu_advection_initial(eq.handle, _lib.ptr(u), _lib.ptr(v),
+                                                  _lib.ptr(phi))
+    assert rc == 0, _lib.strerror(rc)
+    eq._ready = True
+    return g, eq
+
+
+def ic_case(n, kind):
+    """the shipped IC solvers at the structure level: n^2 Dirichlet-0
+    Poisson with a unit source, to 1e-8 (FP64)"""
+    from carpio_gb300 import structure as S
+    g = S.Grid((0.0, 0.0), (1.0, 1.0), (n, n), 1)
+    p = S.Poisson(g)
+    bc = S.BoundaryCondition()
+    bc.set_default_1_bc(0.0)
+    for seg in range(4):
+        p.add_bc(0, seg, "phi", bc)
+    p.set_source(np.ones(g.N()))
+    p.set_solver(kind, max_iter=10000, tol=TOL)
+    return g, p
+
+
+def next_rows_leg(steps=5):
+    """The rows beyond the projection path, on the GPU: stand-alone
+    Advection_ (1024^2 rotating cone), the NS_kim_ stepper (256^2 cavity),
+    the structure-level IC_CGS / IC_CG (128^2 Poisson); wall time of the
+    synchronous calls, after one warm-up"""
+    import torch
+    out = {}
+    n = 1024
+    g, eq = advection_case(n)
+    eq.run(1)
+    t0 = time.perf_counter()
+    eq.run(steps)
+    ms = 1e3 * (time.perf_counter() - t0) / steps
+    out["advection_1024"] = {"ms_per_step": ms, "mcell_steps_per_s": n * n / ms / 1e3,
+                             "steps": steps, "scheme": "VanLeer",
+                             "kernel": "k_advect_grid (anti-diagonal sweep over all SMs)"}
+    del eq
+    from carpio_gb300 import structure as S
+    m = 256
+    gk = S.Grid((0.0, 0.0), (1.0, 1.0), (m, m), 2)
+    ns = S.NS_kim(gk)
+    ns.set_advection_scheme("VanLeer")
+    ns.set_time(0, 0.5 / m)
+    bc0, bc1 = S.BoundaryCondition(), S.BoundaryCondition()
+    bc0.set_default_1_bc(0.0)
+    bc1.set_default_1_bc(1.0)
+    for sg in range(3):
+        ns.add_bc(0, sg, "u", bc0)
+    ns.add_bc(0, 3, "u", bc1)
+    for sg in range(4):
+        ns.add_bc(0, sg, "v", bc0)
+    ns.set_uniform_rho(RE)
+    ns.set_projection_solver("CG", 200000, TOL)
+    ns.initial()
+    ns.run(1)
+    torch.cuda.synchronize()
+    ns.run(steps)
+    pk = ns.profile()
+    out["ns_kim_256"] = {"steps_per_s": steps / (float(np.sum(pk["step_ms"])) / 1e3),
+                         "projection_iters": float(np.mean(pk["inner"])), "steps": steps}
+    del ns
+    for kind in ("IC_CGS", "IC_CG"):
+        gi, p = ic_case(128, kind)
+        p.run()
+        gi, p = ic_case(128, kind)   # a fresh solve from phi = 0
+        t0 = time.perf_counter()
+        p.run()
+        out[f"{kind.lower()}_128"] = {"ms": 1e3 * (time.perf_counter() - t0),
+                                      "iters": int(p.stats.iters),
+                                      "resid": float(p.stats.tol_out),
+                                      "code": int(p.stats.code)}
+    return out
+
+
+def cpu_next_rows(threads):
+    """The same rows on the host, by the oracle restatement (one thread:
+    the reference's loops are sequential): Advection_ one step at 1024^2,
+    IC_CGS / IC_CG on the assembled 128^2 system. NS_kim_ has no
+    restatement (its parity rests on the reference's own runs)."""
+    from oracle import restate as R
+    out = {}
+    n = 1024
+    og = R.Grid(n, n, 2)
+    u, v, phi = cone_fields(og)
+    nb = R.BC()
+    for k in range(4):
+        nb.type[k], nb.value[k] = 2, 0.0
+    u = R.apply_bc(og, nb, u)
+    v = R.apply_bc(og, nb, v)
+    uf, vf = R.c2f(og, u, v)
+    t0 = time.perf_counter()
+    R.advect_run(og, "vanleer", nb, uf, vf, 0.25 / n, 1, phi)
+    ms = 1e3 * (time.perf_counter() - t0)
+    out["advection_1024"] = {"ms_per_step": ms, "cores": 1, "sample": "one step"}
+    m = 128
+    gi = R.Grid(m, m, 1)
+    db = R.BC()
+    for k in range(4):
+        db.type[k], db.value[k] = 1, 0.0
+    rp, ci, va, b = R.assemble_poisson(gi, db, 1.0, None, 1.0)
+    for kind in ("ic_cgs", "ic_cg"):
+        t0 = time.perf_counter()
+        code, x, its, tol_out, _ = R.krylov_csr(kind, rp, ci, va, b, np.zeros(b.size),
+                                                10000, TOL)
+        out[f"{kind}_128"] = {"ms": 1e3 * (time.perf_counter() - t0), "iters": int(its),
+                              "cores": 1, "sample": "one solve, assembled system"}
+    return out
 
 
 def poisson_leg(n, inner_tol):

@@ -60,8 +60,15 @@ __device__ __forceinline__ void set_err(const GridCtl& c, int code) {
 // block waits until the top bit differs from the value its own atomicAdd
 // returned. No reset is needed between barriers and the critical path is one
 // atomic plus one poll.
+// ONE: the caller may launch a single block, and then the block barrier
+// is the grid barrier (the solve deadline is checked by the all-reduces).
+template<bool ONE = false>
 __device__ __forceinline__ bool grid_sync(const GridCtl& c) {
 	__shared__ int s_ok;
+	if (ONE && gridDim.x == 1) {
+		__syncthreads();
+		return true;
+	}
 	__syncthreads();
 	if (threadIdx.x == 0) {
 		const unsigned inc = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1) : 1u;
@@ -205,11 +212,24 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
 // first __syncthreads also orders every thread's earlier global writes before
 // thread 0's release, so data published before the call is visible to every
 // block after it. Returns false on error.
-template<class R, int NV>
+template<class R, int NV, bool ONE = false>
 __device__ __forceinline__ bool grid_allreduce(R (&v)[NV], const GridCtl& c,
 		int& bank) {
 	__shared__ R s_res[2][NV];
 	__shared__ int s_ok[2];
+	if (ONE && gridDim.x == 1) {
+		// one block: its sum is the grid's; only the solve deadline binds.
+		// block_sum_light's barrier publishes the flag.
+		if (threadIdx.x == 0) {
+			const bool late = globaltimer() > c.deadline;
+			if (late) set_err(c, CARPIO_GPU_ETIMEOUT);
+			s_ok[bank] = late ? 0 : 1;
+		}
+		block_sum_light<R, NV>(v, 0);
+		const bool ok1 = s_ok[bank] != 0;
+		bank ^= 1;
+		return ok1;
+	}
 	block_sum_light<R, NV>(v, 0);
 	double* part = c.partials + (size_t)bank * kMaxReduce * gridDim.x;
 	const int lane = threadIdx.x & 31;

@@ -222,6 +222,14 @@ extern "C" int carpio_gpu_krylov_csr(int kind, int n, int nnz,
 		icop.bptr = w.icb[0].as<uint32_t>();
 		icop.brows = w.icb[1].as<uint32_t>();
 		icop.nbl = (int)bptr.size() - 1;
+		// every level ends in a barrier: one block (block barriers, ~0.15 us)
+		// when that beats the grid (grid barriers, ~1.5 us, but all SMs on
+		// the ~10 vector passes of an iteration); a rough cost model, it
+		// only picks between two correct launch shapes
+		const double nlev = (double)icop.nfl + icop.nbl;
+		const double t1 = nlev * 0.15 + 10.0 * n / kThreads * 0.05;
+		const double tb = nlev * 1.5 + 10.0 * ((double)n / ((double)blocks * kThreads) * 0.05 + 1.5);
+		if (t1 < tb) blocks = 1;
 	}
 	SolveCtl sc;
 	sc.kind = kind;

@@ -34,7 +34,7 @@ struct IcOp {
 __device__ bool ic_apply(const IcOp& ic, const double* in, double* out,
 		const GridCtl& gc) {
 	GLOOP(ic.n) out[t] = in[t];
-	if (!grid_sync(gc)) return false;
+	if (!grid_sync<true>(gc)) return false;
 	for (int l = 0; l < ic.nfl; ++l) {
 		const uint32_t b0 = ic.fptr[l];
 		GLOOP((int)(ic.fptr[l + 1] - b0)) {
@@ -44,7 +44,7 @@ __device__ bool ic_apply(const IcOp& ic, const double* in, double* out,
 				y = __dsub_rn(y, __dmul_rn(ldcg(out + ic.li[e]), ic.lv[e]));
 			out[k] = __ddiv_rn(y, ic.d[k]);
 		}
-		if (!grid_sync(gc)) return false;
+		if (!grid_sync<true>(gc)) return false;
 	}
 	for (int l = 0; l < ic.nbl; ++l) {
 		const uint32_t b0 = ic.bptr[l];
@@ -55,7 +55,7 @@ __device__ bool ic_apply(const IcOp& ic, const double* in, double* out,
 				z = __dadd_rn(z, __dmul_rn(ldcg(out + ic.ui[e]), ic.uv[e]));
 			out[i] = __ddiv_rn(__dsub_rn(ldcg(out + i), z), ic.d[i]);
 		}
-		if (!grid_sync(gc)) return false;
+		if (!grid_sync<true>(gc)) return false;
 	}
 	return true;
 }
@@ -71,7 +71,7 @@ __device__ __forceinline__ bool dots(const double* const (&a)[NV], const double*
 #pragma unroll
 		for (int m = 0; m < NV; ++m) acc[m] = fma(ldcg(a[m] + t), ldcg(b[m] + t), acc[m]);
 	}
-	if (!grid_allreduce<double, NV>(acc, gc, bank)) return false;
+	if (!grid_allreduce<double, NV, true>(acc, gc, bank)) return false;
 #pragma unroll
 	for (int m = 0; m < NV; ++m) res[m] = acc[m];
 	return true;
@@ -85,7 +85,7 @@ __device__ __forceinline__ bool nrm2_rel(const double* r, int n, bool full, doub
 	GLOOP(n) {
 		if (t != n - 1 || full) { const double x = ldcg(r + t); acc[0] = fma(x, x, acc[0]); }
 	}
-	if (!grid_allreduce<double, 1>(acc, gc, bank)) return false;
+	if (!grid_allreduce<double, 1, true>(acc, gc, bank)) return false;
 	resid = sqrt(acc[0]) / normb;
 	return true;
 }
@@ -101,7 +101,7 @@ __device__ bool ic_start(const Op& op, const Vecs<double>& v, int n, bool full,
 		v.r[t] = rr;
 		if (t != n - 1 || full) { acc[0] = fma(bb, bb, acc[0]); acc[1] = fma(rr, rr, acc[1]); }
 	}
-	if (!grid_allreduce<double, 2>(acc, gc, bank)) return false;
+	if (!grid_allreduce<double, 2, true>(acc, gc, bank)) return false;
 	normb = sqrt(acc[0]);
 	if (normb == 0.0) normb = 1;
 	resid = sqrt(acc[1]) / normb;
@@ -119,7 +119,7 @@ __device__ void ic_cg_run(int n, const Op& op, const IcOp& ic, const Vecs<double
 	if (resid <= sc.tol) { finish(sc, 0, 0, resid, hl); return; }
 	double rho_1 = 0.0;
 	for (int it = 1; it <= sc.max_iter; ++it) {
-		if (!grid_sync(gc)) return;
+		if (!grid_sync<true>(gc)) return;
 		if (!ic_apply(ic, v.r, v.z, gc)) return;           // z = M^-1 r
 		double rz[1];
 		{
@@ -130,9 +130,9 @@ __device__ void ic_cg_run(int n, const Op& op, const IcOp& ic, const Vecs<double
 		const double rho = rz[0];
 		const double beta = it == 1 ? 0.0 : rho / rho_1;
 		GLOOP(n) v.p[t] = it == 1 ? v.z[t] : fma(beta, v.p[t], v.z[t]);
-		if (!grid_sync(gc)) return;
+		if (!grid_sync<true>(gc)) return;
 		GLOOP(n) v.q[t] = op.apply(v.p, t, t);
-		if (!grid_sync(gc)) return;
+		if (!grid_sync<true>(gc)) return;
 		double pq[1];
 		{
 			const double* a[1] = { v.p };
@@ -144,7 +144,7 @@ __device__ void ic_cg_run(int n, const Op& op, const IcOp& ic, const Vecs<double
 			v.x[t] = fma(alpha, v.p[t], v.x[t]);
 			v.r[t] = fma(-alpha, v.q[t], v.r[t]);
 		}
-		if (!grid_sync(gc)) return;
+		if (!grid_sync<true>(gc)) return;
 		if (!nrm2_rel(v.r, n, full, normb, gc, bank, resid)) return;
 		hist_push(sc, hl, resid);
 		if (resid <= sc.tol) { finish(sc, 0, it, resid, hl); return; }
@@ -166,7 +166,7 @@ __device__ void ic_cgs_run(int n, const Op& op, const IcOp& ic, const Vecs<doubl
 	if (resid <= sc.tol) { finish(sc, 0, 0, resid, hl); return; }
 	double rho_2 = 0.0;
 	for (int it = 1; it <= sc.max_iter; ++it) {
-		if (!grid_sync(gc)) return;
+		if (!grid_sync<true>(gc)) return;
 		double r1[1];
 		{
 			const double* a[1] = { v.rt };
@@ -190,10 +190,10 @@ __device__ void ic_cgs_run(int n, const Op& op, const IcOp& ic, const Vecs<doubl
 				v.p[t] = fma(beta, fma(beta, v.p[t], v.q[t]), u);
 			}
 		}
-		if (!grid_sync(gc)) return;
+		if (!grid_sync<true>(gc)) return;
 		if (!ic_apply(ic, v.p, v.ph, gc)) return;          // phat = M^-1 p
 		GLOOP(n) v.v[t] = op.apply(v.ph, t, t);            // vhat = A phat
-		if (!grid_sync(gc)) return;
+		if (!grid_sync<true>(gc)) return;
 		double rv[1];
 		{
 			const double* a[1] = { v.rt };
@@ -206,15 +206,15 @@ __device__ void ic_cgs_run(int n, const Op& op, const IcOp& ic, const Vecs<doubl
 			v.q[t] = q;
 			v.d[t] = v.s[t] + q;                           // u + q
 		}
-		if (!grid_sync(gc)) return;
+		if (!grid_sync<true>(gc)) return;
 		if (!ic_apply(ic, v.d, v.sh, gc)) return;          // uhat = M^-1 (u + q)
 		GLOOP(n) {
 			v.x[t] = fma(alpha, v.sh[t], v.x[t]);
 			v.t[t] = op.apply(v.sh, t, t);                 // qhat = A uhat
 		}
-		if (!grid_sync(gc)) return;
+		if (!grid_sync<true>(gc)) return;
 		GLOOP(n) v.r[t] = fma(-alpha, v.t[t], v.r[t]);
-		if (!grid_sync(gc)) return;
+		if (!grid_sync<true>(gc)) return;
 		rho_2 = rho_1;
 		if (!nrm2_rel(v.r, n, full, normb, gc, bank, resid)) return;
 		hist_push(sc, hl, resid);

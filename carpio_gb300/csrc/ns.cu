@@ -298,6 +298,36 @@ __global__ void __launch_bounds__(1024) k_advect(Geo g, double* phi, BcDev bc,
 	}
 }
 
+// The same sweep over the whole GPU, for grids whose diagonals are long: a
+// cooperative launch, the cells of a diagonal dealt round-robin over the
+// blocks (cell k to block k mod gridDim, so every SM takes a share of the
+// FP64 work), a grid barrier between diagonals; block 0 refills the ghosts.
+template<int SCH>
+__global__ void __launch_bounds__(kThreads) k_advect_grid(Geo g, double* phi, BcDev bc,
+		const double* uf, const double* vf, double dt, int steps, GridCtl gc) {
+	extern __shared__ double s_old[];
+	gc.start();
+	const int nx = g.nx, ny = g.ny;
+	const int tid = (int)(threadIdx.x * gridDim.x + blockIdx.x);
+	const int nthr = (int)(gridDim.x * blockDim.x);
+	for (int st = 0; st < steps; ++st) {
+		if (blockIdx.x == 0) bc_fill(g, phi, bc, s_old);
+		if (!grid_sync(gc)) return;
+		for (int L = 0; L <= nx + ny - 2; ++L) {
+			const int i0 = L - (ny - 1) > 0 ? L - (ny - 1) : 0;
+			const int i1 = L < nx - 1 ? L : nx - 1;
+			for (int i = i0 + tid; i <= i1; i += nthr) {
+				const int j = L - i;
+				const double adv = adv_cell<SCH>(g, uf, vf, phi, i, j);
+				const int a = g.at(i, j);
+				const double phin = phi[a];
+				phi[a] = phin - dt * adv;
+			}
+			if (!grid_sync(gc)) return;
+		}
+	}
+}
+
 // ------------------------------------------------------------- NS kernels --
 struct StepScalars {
 	double dt;                // current time step (Time_::_dt)
@@ -696,6 +726,24 @@ cudaError_t launch_kim_source(int sch, const Geo& geo, int blocks, cudaStream_t 
 #undef CASE
 	}
 	return cudaErrorInvalidValue;
+}
+
+template<int S>
+const void* advect_grid_kernel() { return (const void*)k_advect_grid<S>; }
+
+const void* pick_advect_grid(int sch) {
+	switch (sch) {
+	case CARPIO_GPU_UPWIND1: return advect_grid_kernel<CARPIO_GPU_UPWIND1>();
+	case CARPIO_GPU_CENTER: return advect_grid_kernel<CARPIO_GPU_CENTER>();
+	case CARPIO_GPU_CENTER4: return advect_grid_kernel<CARPIO_GPU_CENTER4>();
+	case CARPIO_GPU_UPWIND2: return advect_grid_kernel<CARPIO_GPU_UPWIND2>();
+	case CARPIO_GPU_VANLEER: return advect_grid_kernel<CARPIO_GPU_VANLEER>();
+	case CARPIO_GPU_SUPERBEE: return advect_grid_kernel<CARPIO_GPU_SUPERBEE>();
+	case CARPIO_GPU_WAHYD: return advect_grid_kernel<CARPIO_GPU_WAHYD>();
+	case CARPIO_GPU_QUICK: return advect_grid_kernel<CARPIO_GPU_QUICK>();
+	case CARPIO_GPU_CUI: return advect_grid_kernel<CARPIO_GPU_CUI>();
+	}
+	return nullptr;
 }
 
 cudaError_t launch_advect(int sch, const Geo& geo, cudaStream_t s, double* phi,
@@ -1139,6 +1187,7 @@ int carpio_gpu_operator(carpio_gpu_grid* g, int which, int scheme,
 // ----------------------------------------------- stand-alone Advection_ --
 struct carpio_gpu_advection {
 	carpio_gpu_grid* g;
+	cg_host::LaunchWs lw;     // control words of the grid-wide sweep
 	cg_host::DevBuf fields;   // u v uf vf phi, then the ghost values of u v phi
 	double* f[8];
 	carpio_gpu_bc bc[3];      // u v phi
@@ -1256,10 +1305,38 @@ int carpio_gpu_advection_step(carpio_gpu_advection* a, double dt, int steps) {
 	// first fill wrote), and every later fill repeats the second
 	CG_CK(launch_bc(geo, a->f[0], a->bc[0], a->f[1], &a->bc[1], a->s,
 			a->has_gv[0] ? a->f[5] : nullptr, a->has_gv[1] ? a->f[6] : nullptr));
-	CG_CK(launch_advect(a->scheme, geo, a->s, a->f[4],
-			to_dev(a->bc[2], a->has_gv[2] ? a->f[7] : nullptr), a->f[2], a->f[3], dt, steps));
+	const BcDev bcp = to_dev(a->bc[2], a->has_gv[2] ? a->f[7] : nullptr);
+	// one block while the diagonals are short: it clears ~0.06 us of FP64
+	// work per cell (van Leer: ~20 divisions a cell), while a diagonal swept
+	// over all SMs costs ~20 us (grid barrier and load latency), so the
+	// whole GPU pays off from ~300 cells a diagonal
+	const double avg_diag = (double)g->nx * g->ny / (double)(g->nx + g->ny - 1);
+	if (avg_diag < 256.0) {
+		CG_CK(launch_advect(a->scheme, geo, a->s, a->f[4], bcp, a->f[2], a->f[3], dt, steps));
+		CG_CK(cudaStreamSynchronize(a->s));
+		return 0;
+	}
+	const void* k = pick_advect_grid(a->scheme);
+	if (!k) return CARPIO_GPU_EINVAL;
+	const int max_diag = std::min(g->nx, g->ny);
+	// one block per SM at most: more blocks only add barrier arrivals
+	int blocks = coop_blocks(k, (long)max_diag * kThreads, 1);
+	blocks = std::min(blocks, std::min(sm_count(), std::max(1, max_diag)));
+	int rc;
+	if ((rc = a->lw.ensure(blocks))) return rc;
+	CG_CK(cudaMemsetAsync(a->lw.ctl.p, 0, sizeof(Ctl), a->s));
+	GridCtl gc = make_gridctl(a->lw);
+	double* phi = a->f[4];
+	const double* uf = a->f[2];
+	const double* vf = a->f[3];
+	Geo gg = geo;
+	BcDev bb = bcp;
+	void* args[] = { &gg, &phi, &bb, &uf, &vf, &dt, &steps, &gc };
+	const size_t smem = sizeof(double) * 2 * geo.gl * geo.gl;
+	CG_CK(cudaLaunchCooperativeKernel(k, blocks, kThreads, args, smem, a->s));
+	CG_CK(cudaMemcpyAsync(a->lw.host_ctl, a->lw.ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, a->s));
 	CG_CK(cudaStreamSynchronize(a->s));
-	return 0;
+	return a->lw.host_ctl->err;
 }
 
 int carpio_gpu_advection_get(carpio_gpu_advection* a, double* u, double* v,

@@ -140,23 +140,25 @@ class BoundaryIndex:
         nx, ny, gl = grid.nx, grid.ny, grid.gl
         gv = grid.zeros()
         NI, NJ = gv.shape
-        for I in range(NI):
-            for J in range(NJ):
-                i, j = I - gl, J - gl
-                if 0 <= i < nx and 0 <= j < ny:
-                    continue
-                if i < 0 or i >= nx:
-                    seg, hi = (0, False) if i < 0 else (1, True)
-                    oi, oj = (0 if i < 0 else nx - 1), j
-                else:
-                    seg, hi = (2, False) if j < 0 else (3, True)
-                    oi, oj = i, (0 if j < 0 else ny - 1)
-                cx, hx = grid.cx[oi + gl], grid.sx[oi + gl] * 0.5
-                cy, hy = grid.cy[oj + gl], grid.sy[oj + gl] * 0.5
-                x = cx + hx if hi else cx - hx
-                y = cy + hy if hi else cy - hy
-                z = 0.5 if hi else 0.0 - 0.5
-                gv[I, J] = self.find(seg, name).get_val(t, x, y, z)
+        # the ghost frame only: full rows I < gl, I >= NI - gl, and the
+        # columns J < gl, J >= NJ - gl of the other rows
+        frame = [(I, J) for I in list(range(gl)) + list(range(NI - gl, NI)) for J in range(NJ)]
+        frame += [(I, J) for I in range(gl, NI - gl)
+                  for J in list(range(gl)) + list(range(NJ - gl, NJ))]
+        for I, J in frame:
+            i, j = I - gl, J - gl
+            if i < 0 or i >= nx:
+                seg, hi = (0, False) if i < 0 else (1, True)
+                oi, oj = (0 if i < 0 else nx - 1), j
+            else:
+                seg, hi = (2, False) if j < 0 else (3, True)
+                oi, oj = i, (0 if j < 0 else ny - 1)
+            cx, hx = grid.cx[oi + gl], grid.sx[oi + gl] * 0.5
+            cy, hy = grid.cy[oj + gl], grid.sy[oj + gl] * 0.5
+            x = cx + hx if hi else cx - hx
+            y = cy + hy if hi else cy - hy
+            z = 0.5 if hi else 0.0 - 0.5
+            gv[I, J] = self.find(seg, name).get_val(t, x, y, z)
         return gv
 
 
@@ -187,7 +189,8 @@ def learned_cfg(use_net=True, smooth=4, omega=0.8, memory=2, stall=20, fallback=
 class Poisson:
     """Poisson_<2> (s_poisson.hpp:265-594) with the GPU solver behind
     Solver_<2>::solve. set_solver accepts "CG", "Jacobi", "Dia_BiCGSTAB",
-    "BiCGSTAB" (the carpio:: solvers)."""
+    "BiCGSTAB" and "IC_CGS", "IC_CG" (the carpio:: solvers; the IC ones in
+    FP64, through the CSR layer)."""
 
     def __init__(self, grid):
         self.grid = grid
