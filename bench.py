@@ -486,7 +486,7 @@ def next_rows_leg(steps=5):
     ms = 1e3 * (time.perf_counter() - t0) / steps
     out["advection_1024"] = {"ms_per_step": ms, "mcell_steps_per_s": n * n / ms / 1e3,
                              "steps": steps, "scheme": "VanLeer",
-                             "kernel": "k_advect_grid (anti-diagonal sweep over all SMs)"}
+                             "kernel": "k_advect_band (pipelined bands of rows, one per SM)"}
     del eq
     from carpio_gb300 import structure as S
     m = 256

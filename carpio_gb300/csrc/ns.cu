@@ -298,33 +298,79 @@ __global__ void __launch_bounds__(1024) k_advect(Geo g, double* phi, BcDev bc,
 	}
 }
 
-// The same sweep over the whole GPU, for grids whose diagonals are long: a
-// cooperative launch, the cells of a diagonal dealt round-robin over the
-// blocks (cell k to block k mod gridDim, so every SM takes a share of the
-// FP64 work), a grid barrier between diagonals; block 0 refills the ghosts.
+// The sweep as pipelined bands: block b owns rows [b R, b R + R) and sweeps
+// its own anti-diagonals (local level l: cells (b R + k, l - k)). Its first
+// rows read the new values of the two rows above, which the band above
+// writes at its levels R - 1 + l and R - 2 + l, so block b starts level l
+// once the band above has published R + l finished levels; the same chain
+// keeps the band below from overwriting (i + 1, j), (i + 2, j) before they
+// are read. No grid barrier per diagonal: one progress word per band
+// (release store / acquire poll, bounded by the watchdog), and two grid
+// barriers per step around block 0's ghost refill.
+__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
+	asm volatile("st.release.gpu.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
+}
+
 template<int SCH>
-__global__ void __launch_bounds__(kThreads) k_advect_grid(Geo g, double* phi, BcDev bc,
-		const double* uf, const double* vf, double dt, int steps, GridCtl gc) {
+__global__ void __launch_bounds__(kThreads) k_advect_band(Geo g, double* phi, BcDev bc,
+		const double* uf, const double* vf, double dt, int steps, int R,
+		unsigned* prog, GridCtl gc) {
 	extern __shared__ double s_old[];
+	__shared__ int s_ok;
 	gc.start();
-	const int nx = g.nx, ny = g.ny;
-	const int tid = (int)(threadIdx.x * gridDim.x + blockIdx.x);
-	const int nthr = (int)(gridDim.x * blockDim.x);
+	const int nx = g.nx, ny = g.ny, b = blockIdx.x;
+	const int r0 = b * R;
+	const int rb = min(R, nx - r0);                  // rows of this band
+	const int rp = b > 0 ? R : 0;                     // rows of the band above
+	const unsigned T = (unsigned)(R + ny);            // > any band's levels per step
 	for (int st = 0; st < steps; ++st) {
-		if (blockIdx.x == 0) bc_fill(g, phi, bc, s_old);
+		if (b == 0) bc_fill(g, phi, bc, s_old);
 		if (!grid_sync(gc)) return;
-		for (int L = 0; L <= nx + ny - 2; ++L) {
-			const int i0 = L - (ny - 1) > 0 ? L - (ny - 1) : 0;
-			const int i1 = L < nx - 1 ? L : nx - 1;
-			for (int i = i0 + tid; i <= i1; i += nthr) {
-				const int j = L - i;
-				const double adv = adv_cell<SCH>(g, uf, vf, phi, i, j);
-				const int a = g.at(i, j);
-				const double phin = phi[a];
-				phi[a] = phin - dt * adv;
+		const unsigned base = (unsigned)st * T;
+		const int nl = rb + ny - 1;
+		const int nlp = rp + ny - 1;
+		for (int l = 0; l < nl; ++l) {
+			if (b > 0) {
+				const unsigned need = base + (unsigned)min(rp + l, nlp);
+				if (threadIdx.x == 0) {
+					int ok = 1;
+					unsigned polls = 0;
+					unsigned long long t0 = 0;
+					while (ld_acquire_gpu(&prog[b - 1]) < need) {
+						if ((++polls & 63u) == 0) {
+							if (*(volatile int*)gc.err) { ok = 0; break; }
+							const unsigned long long t = globaltimer();
+							if (t0 == 0) t0 = t;
+							if (t - t0 > gc.wait_ns || t > gc.deadline) {
+								set_err(gc, CARPIO_GPU_ETIMEOUT);
+								ok = 0;
+								break;
+							}
+						}
+					}
+					s_ok = ok;
+				}
+				// the acquire poll plus the block barrier order this band's
+				// loads after the band above's writes (no full fence needed)
+				__syncthreads();
+				if (!s_ok) return;
 			}
-			if (!grid_sync(gc)) return;
+			for (int k = threadIdx.x; k < rb; k += blockDim.x) {
+				const int j = l - k;
+				if (j >= 0 && j < ny) {
+					const int i = r0 + k;
+					const double adv = adv_cell<SCH>(g, uf, vf, phi, i, j);
+					const int a = g.at(i, j);
+					const double phin = phi[a];
+					phi[a] = phin - dt * adv;
+				}
+			}
+			// the block barrier orders every thread's writes before thread 0's
+			// release store (release is cumulative over what it has observed)
+			__syncthreads();
+			if (threadIdx.x == 0) st_release_gpu(&prog[b], base + (unsigned)l + 1u);
 		}
+		if (!grid_sync(gc)) return;
 	}
 }
 
@@ -729,19 +775,19 @@ cudaError_t launch_kim_source(int sch, const Geo& geo, int blocks, cudaStream_t 
 }
 
 template<int S>
-const void* advect_grid_kernel() { return (const void*)k_advect_grid<S>; }
+const void* advect_band_kernel() { return (const void*)k_advect_band<S>; }
 
-const void* pick_advect_grid(int sch) {
+const void* pick_advect_band(int sch) {
 	switch (sch) {
-	case CARPIO_GPU_UPWIND1: return advect_grid_kernel<CARPIO_GPU_UPWIND1>();
-	case CARPIO_GPU_CENTER: return advect_grid_kernel<CARPIO_GPU_CENTER>();
-	case CARPIO_GPU_CENTER4: return advect_grid_kernel<CARPIO_GPU_CENTER4>();
-	case CARPIO_GPU_UPWIND2: return advect_grid_kernel<CARPIO_GPU_UPWIND2>();
-	case CARPIO_GPU_VANLEER: return advect_grid_kernel<CARPIO_GPU_VANLEER>();
-	case CARPIO_GPU_SUPERBEE: return advect_grid_kernel<CARPIO_GPU_SUPERBEE>();
-	case CARPIO_GPU_WAHYD: return advect_grid_kernel<CARPIO_GPU_WAHYD>();
-	case CARPIO_GPU_QUICK: return advect_grid_kernel<CARPIO_GPU_QUICK>();
-	case CARPIO_GPU_CUI: return advect_grid_kernel<CARPIO_GPU_CUI>();
+	case CARPIO_GPU_UPWIND1: return advect_band_kernel<CARPIO_GPU_UPWIND1>();
+	case CARPIO_GPU_CENTER: return advect_band_kernel<CARPIO_GPU_CENTER>();
+	case CARPIO_GPU_CENTER4: return advect_band_kernel<CARPIO_GPU_CENTER4>();
+	case CARPIO_GPU_UPWIND2: return advect_band_kernel<CARPIO_GPU_UPWIND2>();
+	case CARPIO_GPU_VANLEER: return advect_band_kernel<CARPIO_GPU_VANLEER>();
+	case CARPIO_GPU_SUPERBEE: return advect_band_kernel<CARPIO_GPU_SUPERBEE>();
+	case CARPIO_GPU_WAHYD: return advect_band_kernel<CARPIO_GPU_WAHYD>();
+	case CARPIO_GPU_QUICK: return advect_band_kernel<CARPIO_GPU_QUICK>();
+	case CARPIO_GPU_CUI: return advect_band_kernel<CARPIO_GPU_CUI>();
 	}
 	return nullptr;
 }
@@ -1187,7 +1233,8 @@ int carpio_gpu_operator(carpio_gpu_grid* g, int which, int scheme,
 // ----------------------------------------------- stand-alone Advection_ --
 struct carpio_gpu_advection {
 	carpio_gpu_grid* g;
-	cg_host::LaunchWs lw;     // control words of the grid-wide sweep
+	cg_host::LaunchWs lw;     // control words of the band sweep
+	cg_host::DevBuf prog;     // its progress word per band
 	cg_host::DevBuf fields;   // u v uf vf phi, then the ghost values of u v phi
 	double* f[8];
 	carpio_gpu_bc bc[3];      // u v phi
@@ -1307,31 +1354,36 @@ int carpio_gpu_advection_step(carpio_gpu_advection* a, double dt, int steps) {
 			a->has_gv[0] ? a->f[5] : nullptr, a->has_gv[1] ? a->f[6] : nullptr));
 	const BcDev bcp = to_dev(a->bc[2], a->has_gv[2] ? a->f[7] : nullptr);
 	// one block while the diagonals are short: it clears ~0.06 us of FP64
-	// work per cell (van Leer: ~20 divisions a cell), while a diagonal swept
-	// over all SMs costs ~20 us (grid barrier and load latency), so the
-	// whole GPU pays off from ~300 cells a diagonal
+	// work per cell (van Leer: ~20 divisions a cell); longer ones go to the
+	// pipelined bands, one per SM, whose diagonals cost ~20 us (one cell's
+	// dependent FP64 chain plus the hand-off) whatever their length
 	const double avg_diag = (double)g->nx * g->ny / (double)(g->nx + g->ny - 1);
-	if (avg_diag < 256.0) {
+	if (avg_diag < 64.0 || g->nx < 8) {
 		CG_CK(launch_advect(a->scheme, geo, a->s, a->f[4], bcp, a->f[2], a->f[3], dt, steps));
 		CG_CK(cudaStreamSynchronize(a->s));
 		return 0;
 	}
-	const void* k = pick_advect_grid(a->scheme);
+	const void* k = pick_advect_band(a->scheme);
 	if (!k) return CARPIO_GPU_EINVAL;
-	const int max_diag = std::min(g->nx, g->ny);
-	// one block per SM at most: more blocks only add barrier arrivals
-	int blocks = coop_blocks(k, (long)max_diag * kThreads, 1);
-	blocks = std::min(blocks, std::min(sm_count(), std::max(1, max_diag)));
+	// bands of R rows, one block each, at most one per SM (all co-resident)
+	const int maxb = std::min(coop_blocks(k, (long)g->nx * kThreads, 1), sm_count());
+	int R = (g->nx + maxb - 1) / maxb;
+	const int blocks = (g->nx + R - 1) / R;
+	// progress words count levels over all steps: keep them below 2^32
+	if ((double)(R + g->ny) * steps >= 4.0e9) return CARPIO_GPU_EINVAL;
 	int rc;
 	if ((rc = a->lw.ensure(blocks))) return rc;
+	if ((rc = a->prog.ensure(sizeof(unsigned) * (size_t)blocks))) return rc;
 	CG_CK(cudaMemsetAsync(a->lw.ctl.p, 0, sizeof(Ctl), a->s));
+	CG_CK(cudaMemsetAsync(a->prog.p, 0, sizeof(unsigned) * (size_t)blocks, a->s));
 	GridCtl gc = make_gridctl(a->lw);
 	double* phi = a->f[4];
 	const double* uf = a->f[2];
 	const double* vf = a->f[3];
+	unsigned* prog = a->prog.as<unsigned>();
 	Geo gg = geo;
 	BcDev bb = bcp;
-	void* args[] = { &gg, &phi, &bb, &uf, &vf, &dt, &steps, &gc };
+	void* args[] = { &gg, &phi, &bb, &uf, &vf, &dt, &steps, &R, &prog, &gc };
 	const size_t smem = sizeof(double) * 2 * geo.gl * geo.gl;
 	CG_CK(cudaLaunchCooperativeKernel(k, blocks, kThreads, args, smem, a->s));
 	CG_CK(cudaMemcpyAsync(a->lw.host_ctl, a->lw.ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, a->s));
