@@ -441,18 +441,12 @@ def cone_fields(g):
 def advection_case(n):
     """stand-alone Advection_ on n^2: the rotating cone, van Leer, the
     default (Neumann 0) boundaries, dt = 0.25 / n"""
-    from carpio_gb300 import _lib, structure as S
+    from carpio_gb300 import structure as S
     g = S.Grid((0.0, 0.0), (1.0, 1.0), (n, n), 2)
     eq = S.Advection(g)
     eq.set_time(0, 0.25 / n)
     eq.set_advection_scheme("VanLeer")
-    for nm in ("u", "v", "phi"):
-        eq._set_bc(nm, 0.0)
-    u, v, phi = cone_fields(g)
-    rc = _lib.load().carpio_gpu_advection_initial(eq.handle, _lib.ptr(u), _lib.ptr(v),
-                                                  _lib.ptr(phi))
-    assert rc == 0, _lib.strerror(rc)
-    eq._ready = True
+    eq.initial_fields(*cone_fields(g))
     return g, eq
 
 

@@ -546,6 +546,17 @@ class Advection:
             raise _lib.CarpioGpuError(rc, "advection_initial")
         self._ready = True
 
+    def initial_fields(self, u, v, phi):
+        """initial() from arrays (the grid's layout, ghosts included, host
+        or device) in place of the initial_CS functions"""
+        for nm in ("u", "v", "phi"):
+            self._set_bc(nm, self.t)
+        rc = _lib.load().carpio_gpu_advection_initial(
+            self.handle, _lib.ptr(u), _lib.ptr(v), _lib.ptr(phi))
+        if rc:
+            raise _lib.CarpioGpuError(rc, "advection_initial")
+        self._ready = True
+
     def run(self, steps=None):
         """Equation_::run (s_equation.hpp:132-178): initial() on the first
         call, then max_step + 1 steps (Time_::is_end is current > max,

@@ -109,13 +109,7 @@ def test_advection_ragged_grids_match_oracle(nx, ny, scheme):
         bi.insert(0, seg, "phi", b)
     eq.set_advection_scheme(scheme)
     # the library's initial() with explicit fields in place of functions
-    for nm in ("u", "v", "phi"):
-        eq._set_bc(nm, 0.0)
-    from carpio_gb300 import _lib
-    rc = _lib.load().carpio_gpu_advection_initial(eq.handle, _lib.ptr(u0), _lib.ptr(v0),
-                                                  _lib.ptr(p0))
-    assert rc == 0
-    eq._ready = True
+    eq.initial_fields(u0, v0, p0)
     eq.run()
     # the oracle: default (Neumann 0) velocity BCs, C2F, 12 in-place steps
     nb = oracle_bc(S.BoundaryIndex().to_c("u"))
@@ -134,7 +128,6 @@ def test_advection_grid_wide_sweep_matches_oracle(n, scheme):
     """grids whose diagonals are long run the sweep over all SMs (grid
     barriers between diagonals): still the oracle's sequential values, bit
     for bit"""
-    from carpio_gb300 import _lib
     from carpio_gb300 import structure as S
     from oracle import restate as R
     g = S.Grid((0.0, 0.0), (1.0, 1.0), (n, n), 2)
@@ -142,15 +135,11 @@ def test_advection_grid_wide_sweep_matches_oracle(n, scheme):
     eq = S.Advection(g)
     eq.set_time(1, 0.25 / n)
     eq.set_advection_scheme(scheme)
-    for nm in ("u", "v", "phi"):
-        eq._set_bc(nm, 0.0)
     X, Y = np.meshgrid(g.cx, g.cy, indexing="ij")
     u0, v0 = -(Y - 0.5), X - 0.5
     r2 = (X - 0.5) ** 2 + (Y - 0.75) ** 2
     p0 = np.where(r2 < 0.04, 1.0 - r2 / 0.04, 0.0)
-    assert _lib.load().carpio_gpu_advection_initial(
-        eq.handle, _lib.ptr(u0), _lib.ptr(v0), _lib.ptr(p0)) == 0
-    eq._ready = True
+    eq.initial_fields(u0, v0, p0)
     eq.run()
     nb = oracle_bc(S.BoundaryIndex().to_c("u"))
     uf, vf = R.c2f(og, R.apply_bc(og, nb, u0), R.apply_bc(og, nb, v0))
