@@ -58,7 +58,7 @@ def parse():
                     help="band-local Chebyshev degree of the FP32 CG (0 default, -1 none)")
     ap.add_argument("--poly-ratio", type=float, default=0.0)
     ap.add_argument("--no-extras", action="store_true",
-                    help="skip the FP64 comparison, Poisson, learned, batched and CPU legs")
+                    help="skip the FP64 comparison, Poisson, learned, batched, next-row and CPU legs")
     ap.add_argument("--oracle-steps", type=int, default=3,
                     help="accuracy run: steps also run by the CPU oracle")
     ap.add_argument("--accuracy-steps", type=int, default=0,
