@@ -95,7 +95,8 @@ int carpio_gpu_krylov_csr(int kind, int n, int nnz, const uint32_t* rowptr,
 /* The same solve for callers that cannot allocate device memory during a
  * solve (a framework that owns all device memory through its own pool, or a
  * time-stepping service that forbids cudaMalloc/cudaFree after start-up).
- * No counterpart in the reference. All arrays must be device memory the
+ * No counterpart in the reference. Kinds CG .. BICGSTAB only (the IC kinds
+ * build their factor on the host and in device buffers: CARPIO_GPU_EINVAL). All arrays must be device memory the
  * caller owns; the solver's scratch is a fixed ~3 MiB array compiled into
  * the library (held by every device that loads it) and n is limited to
  * 32768 rows (larger n: CARPIO_GPU_EINVAL). The first call on a device sets
