@@ -520,10 +520,10 @@ def next_rows_leg(steps=5):
 
 
 def cpu_next_rows(threads):
-    """The same rows on the host, by the oracle restatement (one thread:
-    the reference's loops are sequential): Advection_ one step at 1024^2,
-    IC_CGS / IC_CG on the assembled 128^2 system. NS_kim_ has no
-    restatement (its parity rests on the reference's own runs)."""
+    """The same rows on the host, by the oracle restatement: Advection_ one
+    step at 1024^2 and IC_CGS / IC_CG on the assembled 128^2 system on one
+    thread (the reference's loops are sequential), an NS_kim_ step at 256^2
+    with the projection CG on all threads."""
     from oracle import restate as R
     out = {}
     n = 1024
@@ -539,6 +539,19 @@ def cpu_next_rows(threads):
     R.advect_run(og, "vanleer", nb, uf, vf, 0.25 / n, 1, phi)
     ms = 1e3 * (time.perf_counter() - t0)
     out["advection_1024"] = {"ms_per_step": ms, "cores": 1, "sample": "one step"}
+    # NS_kim_: one step of the 256^2 cavity (dt 0.5 / 256) after one from rest
+    k = 256
+    gk = R.Grid(k, k, 2)
+    stk = {nm: gk.zeros() for nm in ("u", "v", "uf", "vf", "phi", "p", "us", "vs",
+                                     "usf", "vsf")}
+    stk["step"] = 0
+    R.kim_run(gk, stk, 1, 0.5 / k, Re=RE, scheme="vanleer", cg_tol=TOL,
+              cg_max_iter=200000, threads=threads)
+    t0 = time.perf_counter()
+    R.kim_run(gk, stk, 1, 0.5 / k, Re=RE, scheme="vanleer", cg_tol=TOL,
+              cg_max_iter=200000, threads=threads)
+    out["ns_kim_256"] = {"steps_per_s": 1.0 / (time.perf_counter() - t0),
+                         "cores": threads, "sample": "the second step from rest"}
     m = 128
     gi = R.Grid(m, m, 1)
     db = R.BC()

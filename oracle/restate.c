@@ -560,10 +560,13 @@ static void poly_insert(term* row, int* len, double c, int i, int j, int e) {
 	(*len)++;
 }
 
-int rs_assemble_poisson(int nx, int ny, int gl, const double* cx,
+/* the rows of StencilPoisson_ (helm 0) or StencilHelmholtz_ (helm 1,
+ * s_poisson.hpp:185-260: centre coec + s_x s_y alpha, source s_x s_y f) */
+static int assemble_rows(int nx, int ny, int gl, const double* cx,
 		const double* sx, const double* cy, const double* sy, const rs_bc* bc,
 		double beta, const double* src, double src_value, unsigned* rowptr,
-		unsigned* col, double* val, double* b, const double* bfield) {
+		unsigned* col, double* val, double* b, const double* bfield, int helm,
+		double alpha) {
 	const int NJ = ny + 2 * gl;
 	int nz = 0;
 	rowptr[0] = 0;
@@ -605,11 +608,14 @@ int rs_assemble_poisson(int nx, int ny, int gl, const double* cx,
 			coec += -cxp;
 			coec += -cym;
 			coec += -cyp;
-			poly_insert(row, &len, coec, i, j, 1);
-			/* src (s_poisson.hpp:75-83): s_(0)^DIM * source */
+			/* StencilHelmholtz_::coe_row inserts coec + v alpha, v = s_x s_y */
 			double v = 1.0;
 			v *= SX(i);
-			v *= SX(i);
+			v *= helm ? SY(j) : SX(i);
+			if (helm) coec = coec + v * alpha;
+			poly_insert(row, &len, coec, i, j, 1);
+			/* src (s_poisson.hpp:75-83): s_(0)^DIM * source; Helmholtz:
+			 * s_x s_y * source */
 			double f = src ? AT(src, i, j) : src_value;
 			poly_insert(row, &len, v * f, i, j, 0);
 			/* GhostRegular_::substitute (s_ghost.hpp:334-357), in key order */
@@ -668,6 +674,22 @@ int rs_assemble_poisson(int nx, int ny, int gl, const double* cx,
 		}
 	}
 	return nz;
+}
+
+int rs_assemble_poisson(int nx, int ny, int gl, const double* cx,
+		const double* sx, const double* cy, const double* sy, const rs_bc* bc,
+		double beta, const double* src, double src_value, unsigned* rowptr,
+		unsigned* col, double* val, double* b, const double* bfield) {
+	return assemble_rows(nx, ny, gl, cx, sx, cy, sy, bc, beta, src, src_value,
+			rowptr, col, val, b, bfield, 0, 0.0);
+}
+
+int rs_assemble_helmholtz(int nx, int ny, int gl, const double* cx,
+		const double* sx, const double* cy, const double* sy, const rs_bc* bc,
+		double alpha, double beta, const double* src, unsigned* rowptr,
+		unsigned* col, double* val, double* b) {
+	return assemble_rows(nx, ny, gl, cx, sx, cy, sy, bc, beta, src, 0.0,
+			rowptr, col, val, b, NULL, 1, alpha);
 }
 
 /* ------------------------------------------------------------ ghosts --- */
@@ -1111,5 +1133,147 @@ int rs_ns_run(int nx, int ny, int gl, const double* cx, const double* sx,
 	}
 	free(us); free(vs); free(usf); free(vsf); free(div); free(gx); free(gy);
 	free(gcx); free(gcy); free(rp); free(ci); free(va); free(b); free(x);
+	return ret;
+}
+
+/* ------------------------------------------------------------ NS_kim_ --- */
+/* Jacobi on an assembled system from x0 (the reference's Solver_Jacobi_
+ * gives the same iterate as carpio::Jacobi) */
+static int solve_rows(int kind, int nx, int ny, int gl, const unsigned* rp,
+		const unsigned* ci, const double* va, const double* b, double* x,
+		double* f, int mi, double tol, int nomean, int threads, int* its,
+		double* res) {
+	const int NJ = ny + 2 * gl;
+	const int n = nx * ny;
+	double* bb = malloc(sizeof(double) * n);
+	memcpy(bb, b, sizeof(double) * n);
+	for (int j = 0; j < ny; ++j)
+		for (int i = 0; i < nx; ++i) x[i + j * nx] = AT(f, i, j);
+	double m = 0;
+	if (!nomean) {
+		for (int k = 0; k < n; ++k) m += bb[k];
+		m = m / (double)n;
+		for (int k = 0; k < n; ++k) bb[k] = bb[k] - m;
+	}
+	int r = rs_krylov_csr(kind, n, rp, ci, va, bb, x, &mi, &tol, NULL, 0, NULL, threads);
+	if (!nomean) {
+		m = 0;
+		for (int k = 0; k < n; ++k) m += x[k];
+		m = m / (double)n;
+		for (int k = 0; k < n; ++k) x[k] = x[k] - m;
+	}
+	for (int j = 0; j < ny; ++j)
+		for (int i = 0; i < nx; ++i) AT(f, i, j) = x[i + j * nx];
+	if (its) *its = mi;
+	if (res) *res = tol;
+	free(bb);
+	return r;
+}
+
+int rs_kim_run(int nx, int ny, int gl, const double* cx, const double* sx,
+		const double* cy, const double* sy, const rs_bc* bc_u,
+		const rs_bc* bc_v, const rs_ns_cfg* cfg, int steps, int first, double dt,
+		double* u, double* v, double* uf, double* vf, double* phi, double* p,
+		double* us, double* vs, double* usf, double* vsf, int* step_iters,
+		double* step_resid) {
+	/* NS_kim_::run_one_step (s_ns_kim.hpp:130-187, predictor :228-280): no
+	 * restrict_time; um/umf copied from u/uf before the ghosts are refilled;
+	 * per component the AB2 source and a Helmholtz predictor (alpha 1, beta
+	 * dt 0.5 / rho, Neumann 0, default Jacobi 1000 / 1e-4, x0 = the star
+	 * field); projection as NS_explicit_; p = phi / dt - NablaMuNabla(mu,
+	 * phi) 0.5 / rho. */
+	const int NJ = ny + 2 * gl;
+	const size_t N = (size_t)(nx + 2 * gl) * NJ;
+	const int n = nx * ny;
+	double* um = malloc(sizeof(double) * N);
+	double* vm = malloc(sizeof(double) * N);
+	double* umf = malloc(sizeof(double) * N);
+	double* vmf = malloc(sizeof(double) * N);
+	double* scr = calloc(N, sizeof(double));
+	double* div = calloc(N, sizeof(double));
+	double* gx = calloc(N, sizeof(double));
+	double* gy = calloc(N, sizeof(double));
+	double* gcx = calloc(N, sizeof(double));
+	double* gcy = calloc(N, sizeof(double));
+	unsigned* rp = malloc(sizeof(unsigned) * (n + 1));
+	unsigned* ci = malloc(sizeof(unsigned) * 5 * (size_t)n);
+	double* va = malloc(sizeof(double) * 5 * (size_t)n);
+	double* b = malloc(sizeof(double) * n);
+	double* x = malloc(sizeof(double) * n);
+	rs_bc bc_n;
+	for (int k = 0; k < 4; ++k) { bc_n.type[k] = 2; bc_n.value[k] = 0.0; }
+	const double rho = cfg->rho, mu = cfg->mu;
+	int ret = 0;
+	for (int st = 0; st < steps; ++st) {
+		const int step0 = first && st == 0;
+		memcpy(um, u, sizeof(double) * N);
+		memcpy(vm, v, sizeof(double) * N);
+		memcpy(umf, uf, sizeof(double) * N);
+		memcpy(vmf, vf, sizeof(double) * N);
+		rs_apply_bc(nx, ny, gl, cx, sx, cy, sy, bc_u, u);
+		rs_apply_bc(nx, ny, gl, cx, sx, cy, sy, bc_v, v);
+		for (int d = 0; d < 2; ++d) {
+			double* f = d == 0 ? u : v;
+			double* fm = d == 0 ? um : vm;
+			double* fs = d == 0 ? us : vs;
+			for (int j = 0; j < ny; ++j)
+				for (int i = 0; i < nx; ++i) {
+					double advn = adv_cell(cfg->scheme, nx, ny, gl, cx, sx, cy, sy,
+							uf, vf, f, i, j);
+					double advnm1 = adv_cell(cfg->scheme, nx, ny, gl, cx, sx, cy, sy,
+							umf, vmf, fm, i, j);
+					double adv = 1.5 * advn - 0.5 * advnm1;
+					double dif = nmn(nx, ny, gl, cx, sx, cy, sy, mu, f, i, j);
+					double src = 0.0;
+					double veos;
+					if (step0) veos = (advn - (0.5 * dif + src) / rho) * dt - AT(f, i, j);
+					else veos = (adv - (0.5 * dif + src) / rho) * dt - AT(f, i, j);
+					AT(scr, i, j) = veos;
+				}
+			const double smu = dt * 0.5 / rho;
+			assemble_rows(nx, ny, gl, cx, sx, cy, sy, &bc_n, smu, scr, 0.0, rp, ci,
+					va, b, NULL, 1, 1.0);
+			solve_rows(RS_JACOBI, nx, ny, gl, rp, ci, va, b, x, fs, 1000, 1e-4, 1,
+					1, NULL, NULL);
+		}
+		rs_apply_bc(nx, ny, gl, cx, sx, cy, sy, bc_u, us);
+		rs_apply_bc(nx, ny, gl, cx, sx, cy, sy, bc_v, vs);
+		rs_c2f(nx, ny, gl, sx, sy, us, vs, usf, vsf);
+		rs_div(nx, ny, gl, sx, sy, usf, vsf, div);
+		assemble_rows(nx, ny, gl, cx, sx, cy, sy, &bc_n, 1.0, div, 0.0, rp, ci, va,
+				b, NULL, 0, 0.0);
+		int its = 0;
+		double res = 0;
+		int r = solve_rows(cfg->proj_kind, nx, ny, gl, rp, ci, va, b, x, phi,
+				cfg->cg_max_iter, cfg->cg_tol, cfg->proj_nomean, cfg->threads, &its, &res);
+		if (r && !ret) ret = r;
+		rs_apply_bc(nx, ny, gl, cx, sx, cy, sy, &bc_n, phi);
+		rs_grad(nx, ny, gl, cx, cy, phi, gx, gy);
+		memcpy(p, phi, sizeof(double) * N);
+		{
+			double inv = 1.0 / dt;
+			for (int j = 0; j < ny; ++j)
+				for (int i = 0; i < nx; ++i) AT(p, i, j) = AT(p, i, j) * inv;
+			for (int j = 0; j < ny; ++j)
+				for (int i = 0; i < nx; ++i) {
+					double lap = nmn(nx, ny, gl, cx, sx, cy, sy, mu, phi, i, j);
+					lap = lap * (0.5 / rho);
+					AT(p, i, j) = AT(p, i, j) - lap;
+				}
+		}
+		for (size_t k = 0; k < N; ++k) usf[k] = usf[k] - gx[k];
+		for (size_t k = 0; k < N; ++k) vsf[k] = vsf[k] - gy[k];
+		rs_f2c(nx, ny, gl, gx, gy, gcx, gcy);
+		for (size_t k = 0; k < N; ++k) us[k] = us[k] - gcx[k];
+		for (size_t k = 0; k < N; ++k) vs[k] = vs[k] - gcy[k];
+		memcpy(u, us, sizeof(double) * N);
+		memcpy(v, vs, sizeof(double) * N);
+		memcpy(uf, usf, sizeof(double) * N);
+		memcpy(vf, vsf, sizeof(double) * N);
+		if (step_iters) step_iters[st] = its;
+		if (step_resid) step_resid[st] = res;
+	}
+	free(um); free(vm); free(umf); free(vmf); free(scr); free(div); free(gx);
+	free(gy); free(gcx); free(gcy); free(rp); free(ci); free(va); free(b); free(x);
 	return ret;
 }

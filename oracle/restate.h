@@ -140,6 +140,24 @@ int rs_ns_run(int nx, int ny, int gl, const double* cx, const double* sx,
 		double* u, double* v, double* uf, double* vf, double* phi, double* p,
 		double* step_dt, int* step_iters, double* step_resid);
 
+/* StencilHelmholtz_ rows (s_poisson.hpp:185-260) assembled like
+ * rs_assemble_poisson (uniform alpha and beta, source field src). */
+int rs_assemble_helmholtz(int nx, int ny, int gl, const double* cx,
+		const double* sx, const double* cy, const double* sy, const rs_bc* bc,
+		double alpha, double beta, const double* src, unsigned* rowptr,
+		unsigned* col, double* val, double* b);
+
+/* NS_kim_ stepping (s_ns_kim.hpp:130-280), `steps` steps at time step dt;
+ * first: the first of them is the stepper's step 0 (advection without the
+ * Adams-Bashforth term). us, vs, usf, vsf persist between calls as the
+ * reference's star fields do. The projection uses cfg's solver. */
+int rs_kim_run(int nx, int ny, int gl, const double* cx, const double* sx,
+		const double* cy, const double* sy, const rs_bc* bc_u,
+		const rs_bc* bc_v, const rs_ns_cfg* cfg, int steps, int first, double dt,
+		double* u, double* v, double* uf, double* vf, double* phi, double* p,
+		double* us, double* vs, double* usf, double* vsf, int* step_iters,
+		double* step_resid);
+
 #ifdef __cplusplus
 }
 #endif

@@ -76,6 +76,11 @@ def lib():
             ctypes.POINTER(BC), _d, _d]
         L.rs_advect_run.argtypes = [ctypes.c_int] * 4 + [_d] * 4 + [
             ctypes.POINTER(BC), _d, _d, _d, ctypes.c_double, ctypes.c_int, _d]
+        L.rs_kim_run.argtypes = (
+            [ctypes.c_int] * 3 + [_d] * 4
+            + [ctypes.POINTER(BC), ctypes.POINTER(BC), ctypes.POINTER(NSCfg),
+               ctypes.c_int, ctypes.c_int, ctypes.c_double] + [_d] * 10 + [_i, _d])
+        L.rs_kim_run.restype = ctypes.c_int
         L.rs_grad.argtypes = [ctypes.c_int] * 3 + [_d] * 5
         L.rs_div.argtypes = [ctypes.c_int] * 3 + [_d] * 5
         L.rs_f2c.argtypes = [ctypes.c_int] * 3 + [_d] * 4
@@ -323,3 +328,27 @@ def new_state(grid, dt0):
     return dict(dt=float(dt0), u=grid.zeros(), v=grid.zeros(),
                 uf=grid.zeros(), vf=grid.zeros(), phi=grid.zeros(),
                 p=grid.zeros())
+
+
+def kim_run(grid, state, steps, dt, *, Re=1000.0, mu=1.0, scheme="vanleer",
+            cg_max_iter=100000, cg_tol=1e-10, threads=1, bc_u=None, bc_v=None,
+            proj="cg", proj_mean=True):
+    """NS_kim_ steps (s_ns_kim.hpp:130-280) in place on state = dict(step=int,
+    u, v, uf, vf, phi, p, us, vs, usf, vsf); dt fixed (the stepper has no
+    restrict_time). Returns (code, step_iters, step_resid)."""
+    if bc_u is None or bc_v is None:
+        bc_u, bc_v = cavity_bcs()
+    cfg = NSCfg(rho=Re, mu=mu, scheme=SCHEMES.get(scheme, scheme),
+                cg_max_iter=cg_max_iter, cg_tol=cg_tol, threads=threads,
+                proj_kind=KINDS[proj], proj_nomean=0 if proj_mean else 1)
+    keys = ("u", "v", "uf", "vf", "phi", "p", "us", "vs", "usf", "vsf")
+    for k in keys:
+        state[k] = _f64(state[k])
+    sit = np.zeros(max(steps, 1), dtype=np.int32)
+    sres = np.zeros(max(steps, 1))
+    code = lib().rs_kim_run(*grid.args(), *grid.geo(), ctypes.byref(bc_u),
+                            ctypes.byref(bc_v), ctypes.byref(cfg), int(steps),
+                            1 if state["step"] == 0 else 0, float(dt),
+                            *(_p(state[k]) for k in keys), _p(sit, _i), _p(sres))
+    state["step"] += steps
+    return code, sit[:steps], sres[:steps]

@@ -260,3 +260,28 @@ def test_cavity_ic_cgs_failure_bitwise(name):
     assert bits_equal(sdt, d["dt"])
     assert np.array_equal(sit, d["cg_iters"].astype(int))
     assert bits_equal(sres, d["cg_resid"])
+
+
+@pytest.mark.parametrize("name", golden_names("kim_"))
+def test_kim_steps_bitwise(name):
+    """NS_kim_ (s_ns_kim.hpp): the oracle's stepper against the reference's
+    own run, first-step fields and final fields bit for bit, with the
+    projection's iteration counts"""
+    d = golden(name)
+    a = d["case_args"]
+    n, steps, scheme = int(a[1]), int(a[2]), str(a[3]).lower()
+    tol, mi, dt0, Re = float(a[4]), int(a[5]), float(a[6]), float(a[7])
+    g = R.Grid(n, n, 2)
+    st = {k: g.zeros() for k in ("u", "v", "uf", "vf", "phi", "p", "us", "vs", "usf", "vsf")}
+    st["step"] = 0
+    code, its1, _ = R.kim_run(g, st, 1, dt0, Re=Re, scheme=scheme, cg_tol=tol, cg_max_iter=mi)
+    assert code == 0
+    for k in ("phi", "p", "u", "v", "uf", "vf"):
+        assert bits_equal(st[k], d["s1_" + k]), k
+    code, its, res = R.kim_run(g, st, steps - 1, dt0, Re=Re, scheme=scheme, cg_tol=tol,
+                               cg_max_iter=mi)
+    assert code == 0
+    for k in ("u", "v", "p", "phi", "uf", "vf", "us", "vs"):
+        assert bits_equal(st[k], d[k]), k
+    assert np.array_equal(np.concatenate([its1, its]), d["cg_iters"].astype(int))
+    assert bits_equal(res, d["cg_resid"][1:])
