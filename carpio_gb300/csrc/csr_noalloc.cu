@@ -72,6 +72,24 @@ int scratch_address(int dev, unsigned char** out) {
 	return 0;
 }
 
+// The rule on_this_device applies to cudaPointerGetAttributes' answer.
+bool noalloc_pointer_ok(int type, int owner, int dev) {
+	if (type == (int)cudaMemoryTypeManaged) return true;
+	return type == (int)cudaMemoryTypeDevice && owner == dev;
+}
+
+// Device memory of the current device, or managed memory. Memory of another
+// GPU is refused: without peer access the kernel would fault on it, and with
+// peer access every load would cross the link.
+bool on_this_device(const void* p, int dev) {
+	cudaPointerAttributes a;
+	if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+		cudaGetLastError();
+		return false;
+	}
+	return noalloc_pointer_ok((int)a.type, a.device, dev);
+}
+
 }  // namespace
 
 extern "C" int carpio_gpu_krylov_csr_noalloc(int kind, int n, int nnz,
@@ -85,13 +103,14 @@ extern "C" int carpio_gpu_krylov_csr_noalloc(int kind, int n, int nnz,
 		return CARPIO_GPU_EINVAL;
 	if (n > kNoallocMaxRows) return CARPIO_GPU_EINVAL;   // beyond the static scratch
 	if (hist_cap < 0 || (hist_cap > 0 && !resid_hist)) return CARPIO_GPU_EINVAL;
-	// every array must already be device memory: nothing is staged here
-	const void* ptrs[] = { rowptr, col, val, b, x };
-	for (const void* p : ptrs)
-		if (p && !is_device_ptr(p)) return CARPIO_GPU_EINVAL;
-	if (hist_cap > 0 && !is_device_ptr(resid_hist)) return CARPIO_GPU_EINVAL;
 	int dev = 0;
 	CG_CK(cudaGetDevice(&dev));
+	// every array must already be memory this device can address directly:
+	// nothing is staged here
+	const void* ptrs[] = { rowptr, col, val, b, x };
+	for (const void* p : ptrs)
+		if (p && !on_this_device(p, dev)) return CARPIO_GPU_EINVAL;
+	if (hist_cap > 0 && !on_this_device(resid_hist, dev)) return CARPIO_GPU_EINVAL;
 	unsigned char* base = nullptr;
 	int rc = scratch_address(dev, &base);
 	if (rc) return rc;

@@ -14,7 +14,9 @@ from conftest import PLAIN_RTOL, golden, rel_l2
 pytestmark = pytest.mark.gpu
 
 
-def noalloc_solve(L, kind, d, tol, max_iter):
+def noalloc_solve(L, kind, d, tol, max_iter, stream=None):
+    """one call of the no-alloc entry point on device copies of a fixture's
+    system, on `stream` (a torch.cuda.Stream) or the default stream"""
     torch = pytest.importorskip("torch")
     dev = "cuda"
     rp = torch.from_numpy(d["rowptr"].astype(np.int32)).to(dev)
@@ -30,7 +32,8 @@ def noalloc_solve(L, kind, d, tol, max_iter):
         ctypes.c_void_p(ci.data_ptr()), ctypes.c_void_p(va.data_ptr()),
         ctypes.c_void_p(b.data_ptr()), ctypes.c_void_p(x.data_ptr()),
         ctypes.byref(mi), ctypes.byref(t), ctypes.c_void_p(hist.data_ptr()),
-        hist.numel(), ctypes.byref(hl), 0, None)
+        hist.numel(), ctypes.byref(hl), 0,
+        None if stream is None else ctypes.c_void_p(stream.cuda_stream))
     return code, x.cpu().numpy(), mi.value, t.value, hist[:hl.value].cpu().numpy()
 
 
@@ -43,19 +46,49 @@ def alloc_solve(kind, d, tol, max_iter):
     return code, x, it, t, np.asarray(lr)
 
 
+def check_same(name, kind, tol, r1, r2):
+    c1, x1, it1, t1, h1 = r1
+    c2, x2, it2, t2, h2 = r2
+    assert c1 == c2 == 0, (name, kind, c1, c2)
+    bar = 1e-9 if "bus685" in name else PLAIN_RTOL   # as in test_gpu_csr
+    if kind == 1:
+        bar = 1e-8   # Jacobi stops at tol; its iterates differ by rounding only
+    assert rel_l2(x1, x2) <= bar, (name, kind, rel_l2(x1, x2))
+    assert abs(len(h1) - len(h2)) <= max(3, len(h2) // 20)
+    assert t1 < tol or (kind in (0, 1) and t1 <= tol)
+
+
+# (fixture, kind, tol, max_iter): CG 0, JACOBI 1, DIA_BICGSTAB 2, BICGSTAB 3
+CASES = [("csr_pde225_dia_bicgstab", 2, 1e-13, 2000),
+         ("csr_bus685_cg", 0, 1e-13, 20000),
+         ("csr_pde225_jacobi", 1, 1e-10, 20000),
+         ("csr_pde225_bicgstab", 3, 1e-13, 2000)]
+
+
 def test_noalloc_matches_allocating_entry_point_twice(gpu_lib):
+    """every kind, each called twice in a row (the second call reuses the
+    array the first one left behind), against carpio_gpu_krylov_csr"""
     L = gpu_lib
-    cases = [("csr_pde225_dia_bicgstab", 2, 1e-13, 2000),
-             ("csr_bus685_cg", 0, 1e-13, 20000)]
-    for name, kind, tol, max_iter in cases:   # two calls in a row
+    for name, kind, tol, max_iter in CASES:
         d = golden(name)
-        c1, x1, it1, t1, h1 = noalloc_solve(L, kind, d, tol, max_iter)
-        c2, x2, it2, t2, h2 = alloc_solve(kind, d, tol, max_iter)
-        assert c1 == c2 == 0
-        bar = 1e-9 if "bus685" in name else PLAIN_RTOL   # as in test_gpu_csr
-        assert rel_l2(x1, x2) <= bar, (name, rel_l2(x1, x2))
-        assert abs(len(h1) - len(h2)) <= max(3, len(h2) // 20)
-        assert t1 < tol or (kind == 0 and t1 <= tol)
+        ref = alloc_solve(kind, d, tol, max_iter)
+        for _ in range(2):
+            check_same(name, kind, tol, noalloc_solve(L, kind, d, tol, max_iter), ref)
+
+
+def test_noalloc_on_a_stream_after_a_failed_call(gpu_lib):
+    """on a caller's stream: a call that stops at max_iter (code 1) leaves
+    the shared array dirty; the next call starts clean and matches the
+    allocating entry point"""
+    torch = pytest.importorskip("torch")
+    L = gpu_lib
+    s = torch.cuda.Stream()
+    for name, kind, tol, max_iter in CASES[1:3]:
+        d = golden(name)
+        code, _, it, _, _ = noalloc_solve(L, kind, d, tol, 1, stream=s)
+        assert code == 1 and it == 1
+        check_same(name, kind, tol, noalloc_solve(L, kind, d, tol, max_iter, stream=s),
+                   alloc_solve(kind, d, tol, max_iter))
 
 
 def test_noalloc_rejects_oversize_and_host_arrays(gpu_lib):
@@ -76,5 +109,11 @@ def test_noalloc_rejects_oversize_and_host_arrays(gpu_lib):
     hb = np.ones(4)
     assert L.carpio_gpu_krylov_csr_noalloc(
         0, 4, 4, args[0], args[1], args[2], ctypes.c_void_p(hb.ctypes.data),
+        args[4], ctypes.byref(mi), ctypes.byref(t), None, 0, None, 0,
+        None) == _lib.EINVAL
+    # pinned host memory is addressable by the GPU but is not device memory
+    hp = torch.ones(4, dtype=torch.float64).pin_memory()
+    assert L.carpio_gpu_krylov_csr_noalloc(
+        0, 4, 4, args[0], args[1], args[2], ctypes.c_void_p(hp.data_ptr()),
         args[4], ctypes.byref(mi), ctypes.byref(t), None, 0, None, 0,
         None) == _lib.EINVAL
