@@ -11,8 +11,17 @@ warm-up steps, then K timed steps. One "step" = NS_explicit_::run_one_step.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 --impl reference times the reference's CPU implementation of the same step
-(its restatement in oracle/, FP64 CG with mean removal, all host threads) on
-rank 0; the reference has no GPU path.
+(its restatement in oracle/: CSR assembly + carpio::CG to 1e-8 with mean
+removal, FP64, on all host threads) on rank 0: W untimed steps from rest,
+then K timed full steps. The reference has no GPU path.
+
+The line also carries: `roofline` of the projection solve on the Krylov bytes
+of the measurement contract (40 B/cell per FP32 CG iteration, 40 B/cell per
+FP64 refinement step), `accuracy` (the mixed against the FP64 projection
+after the same steps, and both against the CPU oracle on the first step),
+`cpu_baseline` (the oracle timed on steps 2..4 from rest), and the legs of
+the other configurations (FP64 projection, Poisson to 1e-8, learned,
+batched, next rows).
 
 Timing: CUDA events on the library's launching stream around each step
 (carpio_gpu_ns_profile), max over ranks. The per-step working set (10
@@ -75,18 +84,24 @@ def dist_env():
     return ws, rank, local
 
 
-def config(n, precision, inner_tol):
+def config(n):
+    """the workload, identical in both arms (what is solved, not how)"""
     return {"workload": f"lid-driven cavity {n}x{n}, Re 1000, van Leer, "
-                        f"CG to {TOL:g} with mean removal "
-                        f"({'FP32 inner / FP64 refinement' if precision == 'mixed' else 'FP64'})",
+                        f"all-Neumann pressure Poisson to {TOL:g} relative "
+                        f"residual with mean removal",
             "n": n, "Re": RE, "scheme": "VanLeer", "tol": TOL,
-            "precision": precision, "inner_tol": inner_tol,
-            "fp32_preconditioner": (None if precision != "mixed" else "none" if POLY[0] < 0 else
-                                    f"band-local Chebyshev degree {POLY[0] or 5}, "
-                                    f"interval [2/{POLY[1] or 30:g}, 2] of D^-1 A"),
             "cfl": 0.5, "diffusion_number": 0.25, "dt0": 0.5 / n,
+            "start": "from rest; W untimed steps, then K timed steps",
             "l2": "per-step working set ~200 MB > 129 MB L2; no flush",
             "parallelism": "replicas"}
+
+
+def solver_desc(precision, inner_tol):
+    """how our arm solves the projection"""
+    return {"precision": precision, "inner_tol": inner_tol,
+            "fp32_preconditioner": (None if precision != "mixed" else "none" if POLY[0] < 0 else
+                                    f"band-local Chebyshev degree {POLY[0] or 5}, "
+                                    f"interval [2/{POLY[1] or 30:g}, 2] of D^-1 A")}
 
 
 # band-local Chebyshev preconditioner of the FP32 CG: (degree, ratio), 0 = defaults
@@ -185,94 +200,121 @@ def poly_degree():
     return 0 if POLY[0] < 0 else (POLY[0] or 5)
 
 
-def solve_bytes_per_cell(precision, inner, outer, deg=0):
-    """Algorithmic bytes of one projection-solve launch per cell, i.e. what
-    the algorithm moves when its vectors live in memory: prologue (read 2
-    face fields + phi, write b and x: 40 B), per FP32 inner CG iteration
-    40 B (read p, q, r, x, D; write p, q, x, r: 4 B each, the operator's
-    neighbours counted once) plus the preconditioner's (first Chebyshev step:
-    read r, D, write d, z, r_k: 20 B; each further step: read d, r_k, z, D,
-    write d, r_k, z: 28 B; the (r, z) dot: 8 B), per FP64 refinement step
-    40 B (read x, b, D; write r; write x), per FP64 CG iteration 80 B,
-    epilogue (mean removal + scatter: read x twice, write phi: 24 B)."""
+def solve_bytes(precision, inner, outer, deg=0):
+    """Algorithmic bytes per cell of one projection-solve launch, split into
+    the Krylov part (the per-kernel figures of the measurement contract) and
+    the band-local preconditioner's passes, which that table does not list.
+
+    Krylov: FP32 inner CG iteration 40 B (K1: p = z + beta p, q = A p, p.q;
+    K2: x += alpha p, r -= alpha q, r.r; 4 B vectors, neighbours counted
+    once); FP64 refinement step 40 B (r = b - A x, update x, mean removal),
+    one more for the first residual; FP64 CG iteration 80 B.
+    Preconditioner, per FP32 iteration: first Chebyshev step 20 B (read r,
+    D; write d, z, r_k), each further step 28 B (read d, r_k, z, D; write d,
+    r_k, z), the (r, z) dot 8 B."""
     if precision == "mixed":
-        it = 40 + (20 + 28 * (deg - 1) + 8 if deg > 0 else 0)
-        return 40 + it * inner + 40 * (outer + 1) + 24
-    return 40 + 80 * inner + 24 + 24
+        krylov = 40 * inner + 40 * (outer + 1)
+        pre = (20 + 28 * (deg - 1) + 8) * inner if deg > 0 else 0
+        return krylov, pre
+    return 80 * inner, 0
 
 
 def traffic_per_launch(n, precision):
     """DRAM bytes of one projection-solve launch from the committed ncu
-    capture (a smaller case of the same kernel, scaled by cells), or None."""
+    capture of this kernel at this size, or None"""
     if precision != "mixed":
         return None
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
             t = json.load(f)
-        return float(t["dram_bytes_per_cell_per_launch"]) * n * n
+        rec = t["launches"][str(n)]
+        return float(rec["dram_bytes"])
     except (OSError, KeyError, ValueError):
         return None
 
 
-def reference_iters(n):
-    """CG iterations per step of the reference algorithm (FP64 CG to 1e-8,
-    mean removal) on this workload, recorded by a full run of the oracle
-    restatement (oracle/record_cg_iters.py -> oracle/cavity_cg_iters_<n>.json)."""
-    path = os.path.join(ROOT, "oracle", f"cavity_cg_iters_{n}.json")
-    with open(path) as f:
-        return {r["step"]: r["cg_iters"] for r in json.load(f)["rows"]}
-
-
-def cpu_step_model(n, threads, caps=(20, 120)):
-    """Times the reference CPU step (oracle restatement of NS_explicit_ with
-    CSR assembly + carpio::CG, FP64) at size n on a bounded sample: step 1
-    from rest with the CG capped at each of `caps` iterations. Returns
-    (fixed seconds per step, seconds per CG iteration)."""
+def oracle_cavity(n, threads):
+    """the reference's CPU step (oracle restatement of NS_explicit_ with CSR
+    assembly + carpio::CG to 1e-8 and mean removal, FP64) on a cavity of n^2
+    from rest; returns (grid, state, step function) where step() runs one
+    full step and returns (seconds, CG iterations, code)"""
     from oracle import restate as R
     R.lib()
     g = R.Grid(n, n, 2)
-    t = []
-    for m in caps:
-        st = R.new_state(g, 0.5 / n)
+    st = R.new_state(g, 0.5 / n)
+
+    def step():
         t0 = time.perf_counter()
-        R.ns_run(g, st, 1, scheme="vanleer", cg_tol=1e-300, cg_max_iter=m,
-                 threads=threads)
-        t.append(time.perf_counter() - t0)
-    per_it = max((t[1] - t[0]) / (caps[1] - caps[0]), 1e-9)
-    fixed = max(t[0] - caps[0] * per_it, 0.0)
-    return fixed, per_it
+        code, _, its, _ = R.ns_run(g, st, 1, scheme="vanleer", cg_tol=TOL,
+                                   cg_max_iter=200000, threads=threads)
+        return time.perf_counter() - t0, int(its[0]), int(code)
+    return g, st, step
 
 
 def run_reference(a):
+    """the reference arm: the reference algorithm on the host cores, W
+    untimed steps from rest, then K timed full steps"""
     ws, rank, local = dist_env()
     if rank != 0:
         return
     threads = os.cpu_count() or 1
     n = a.n
-    iters = reference_iters(n)
-    steps = list(range(a.warmup + 1, a.warmup + a.steps + 1))
-    fixed, per_it = cpu_step_model(n, threads)
-    # each timed step: the fixed part plus the step's own CG iteration count
-    per_step = [fixed + per_it * iters.get(s, iters[max(iters)]) for s in steps]
-    el = float(np.sum(per_step))
+    _, _, step = oracle_cavity(n, threads)
+    for _ in range(a.warmup):
+        step()
+    t, its = [], []
+    for _ in range(a.steps):
+        dt, it, code = step()
+        assert code == 0, f"reference step failed: code {code}"
+        t.append(dt)
+        its.append(it)
+    el = float(np.sum(t))
     v = a.steps / el
-    sample = (f"{n}^2 cavity step sampled with CG capped at 20 and 120 "
-              f"iterations (fixed {fixed:.3f} s + {1e3 * per_it:.2f} ms/CG "
-              f"iteration on {threads} threads), scaled to the reference's "
-              f"{int(np.mean([iters.get(s, 0) for s in steps]))} CG iterations "
-              f"per step at steps {steps[0]}..{steps[-1]}")
+    sample = (f"steps {a.warmup + 1}..{a.warmup + a.steps} of the {n}^2 cavity from "
+              f"rest, each a full step (FP64 CG to {TOL:g}, mean removal; "
+              f"{int(np.mean(its))} CG iterations a step on average), oracle "
+              f"restatement of the reference on {threads} threads")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s",
         "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": 1e3 * el / a.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (cavity from rest)",
-        "config": config(n, "fp64", None),
+        "config": config(n),
+        "solver": {"precision": "fp64", "kind": "carpio::CG with mean removal"},
         "cpu_baseline": {"value": v, "unit": "steps/s", "cores": threads,
                          "kind": "port", "sample": sample},
+        "cg_iters_per_step": float(np.mean(its)),
         "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0}}), flush=True)
+
+
+def rel_l2(x, y):
+    ref = np.linalg.norm(y)
+    return float(np.linalg.norm(x - y) / ref) if ref > 0 else float(np.linalg.norm(x))
+
+
+def cpu_baseline_leg(n, threads, gpu_step1):
+    """The reference's CPU step on the host cores, on a bounded sample: the
+    oracle runs steps 1..4 of the cavity from rest, full steps; steps 2..4
+    are timed. Step 1 also checks the GPU's first step (FP64 and mixed
+    projections) against the oracle: relative L2 of u, v, p."""
+    g, st, step = oracle_cavity(n, threads)
+    step()
+    check = {}
+    for label, fields in gpu_step1.items():
+        check[label] = {k: rel_l2(fields[k], g.interior(st[k])) for k in ("u", "v", "p")}
+    t, its = [], []
+    for _ in range(3):
+        dt, it, _ = step()
+        t.append(dt)
+        its.append(it)
+    return {"value": len(t) / float(np.sum(t)), "unit": "steps/s", "cores": threads,
+            "kind": "port",
+            "sample": f"steps 2..4 of the {n}^2 cavity from rest, full steps "
+                      f"(FP64 CG to {TOL:g} with mean removal, {int(np.mean(its))} "
+                      f"CG iterations a step), oracle restatement on {threads} threads"}, check
 
 
 def main():
@@ -340,26 +382,39 @@ def main():
         "scaling": "weak", "vs_baseline": None,
         "dtype": "f32+f64" if a.precision == "mixed" else "f64",
         "data": "synthetic (cavity from rest)",
-        "config": config(n, a.precision, a.inner_tol),
+        "config": config(n),
+        "solver": solver_desc(a.precision, a.inner_tol),
         "gpu_launches": LAUNCHES_PER_STEP * a.steps,
         "clocks": clk,
         "wall_ms_per_step": 1e3 * wall / a.steps,
         "projection": {"solve_ms": solve_ms, "inner_iters": inner,
                        "outer_iters": outer,
+                       "us_per_inner_iter": 1e3 * solve_ms / max(inner, 1.0),
                        "share_of_step": solve_ms / (1e3 * dev_s / a.steps)},
     }
-    # roofline of the dominant kernel (the persistent projection solve)
+    # roofline of the dominant kernel (the persistent projection solve) on
+    # the Krylov bytes of the measurement contract; the preconditioner's
+    # passes are reported beside it
     peak, how = peaks()
-    bpc = solve_bytes_per_cell(a.precision, inner, outer,
-                               poly_degree() if a.precision == "mixed" else 0)
-    achieved = bpc * n * n / (solve_ms / 1e3) / 1e9
+    kry, pre = solve_bytes(a.precision, inner, outer,
+                           poly_degree() if a.precision == "mixed" else 0)
+    achieved = kry * n * n / (solve_ms / 1e3) / 1e9
     out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak,
                        "unit": "GB/s", "frac": achieved / peak,
                        "peak_source": how,
                        "traffic": traffic_per_launch(n, a.precision),
-                       "algorithmic_bytes_per_launch": bpc * n * n,
+                       "algorithmic_bytes_per_launch": kry * n * n,
+                       "bytes_model": ("40 B/cell per FP32 CG iteration + 40 B/cell per "
+                                       "FP64 refinement step" if a.precision == "mixed"
+                                       else "80 B/cell per FP64 CG iteration"),
+                       "preconditioner_bytes_per_launch": pre * n * n,
                        "kernel": ("k_poisson_mixed_tile" if a.precision == "mixed"
                                   else "k_poisson") + " (persistent projection solve)"}
+    if a.precision == "mixed":
+        out["roofline"]["note"] = (
+            "the Krylov vectors stay in shared memory and registers: DRAM "
+            "traffic is `traffic`, far below the algorithmic bytes; the kernel "
+            "is bound by grid all-reduce latency, two per FP32 iteration")
     # e2e through the public API with host buffers: the timed steps again,
     # from the same starting state, each step copying the whole state in
     # from pinned host memory and back out
@@ -383,17 +438,28 @@ def main():
                   "d2h_bytes_per_step": nbytes + 8,
                   "steps": a.steps}
     if not a.no_extras and rank == 0:
-        # FP64-CG projection on the same workload, same GPU
+        # the other projection on the same workload, same GPU, same steps
         other = "fp64" if a.precision == "mixed" else "mixed"
         g2, ns2 = make_cavity(n, other, a.inner_tol)
         ns2.run(a.warmup)
         torch.cuda.synchronize()
         ns2.run(a.steps)
         p2 = ns2.profile()
-        out[f"{other}_projection"] = {
-            "steps_per_s": a.steps / (float(np.sum(p2["step_ms"])) / 1e3),
-            "solve_ms": float(np.mean(p2["solve_ms"])),
-            "iters": float(np.mean(p2["inner"]))}
+        leg = {"steps_per_s": a.steps / (float(np.sum(p2["step_ms"])) / 1e3),
+               "solve_ms": float(np.mean(p2["solve_ms"])),
+               "iters": float(np.mean(p2["inner"]))}
+        if other == "fp64":
+            # k_poisson's own roofline: 80 B/cell per FP64 CG iteration
+            gbs = 80.0 * leg["iters"] * n * n / (leg["solve_ms"] / 1e3) / 1e9
+            leg["roofline"] = {"achieved": gbs, "peak": peak, "frac": gbs / peak,
+                               "unit": "GB/s", "peak_source": how,
+                               "us_per_iter": 1e3 * leg["solve_ms"] / max(leg["iters"], 1.0)}
+        out[f"{other}_projection"] = leg
+        # accuracy: the two projections after the same W + K steps
+        s1, s2 = ns.state(), ns2.state()
+        out["accuracy"] = {
+            f"{a.precision}_vs_{other}_after_{a.warmup + a.steps}_steps":
+                {k: rel_l2(g.interior(s1[k]), g2.interior(s2[k])) for k in ("u", "v", "p")}}
         del ns2
         # Poisson ms to 1e-8 on the same divergence field: FP64 CG vs mixed
         # vs the learned preconditioner, and on a held-out 512^2 field
@@ -403,24 +469,22 @@ def main():
         out["unet_forward"] = unet_leg(n)
         out["batched_512"] = batched_leg()
         out["next_rows"] = next_rows_leg()
-        # CPU baseline: the reference's CPU step (restatement) on a bounded
-        # sample of the same workload, scaled to the timed steps' iterations
         if ws == 1:
+            # the first step of both projections from rest, for the check
+            # against the CPU oracle inside the CPU-baseline leg
+            first = {}
+            for prec in ("fp64", "mixed"):
+                gq, nq = make_cavity(n, prec, a.inner_tol)
+                assert nq.run(1) == 0
+                sq = nq.state()
+                first[prec] = {k: gq.interior(sq[k]) for k in ("u", "v", "p")}
+                del nq
             threads = os.cpu_count() or 1
-            fixed, per_it = cpu_step_model(n, threads)
-            iters = reference_iters(n)
-            steps = range(a.warmup + 1, a.warmup + a.steps + 1)
-            its = float(np.mean([iters.get(s, iters[max(iters)]) for s in steps]))
-            out["cpu_baseline"] = {
-                "value": 1.0 / (fixed + per_it * its), "unit": "steps/s",
-                "cores": threads, "kind": "port",
-                "sample": f"{n}^2 cavity step with CG capped at 20/120 "
-                          f"iterations (fixed {fixed:.3f} s, "
-                          f"{1e3 * per_it:.2f} ms per CG iteration), scaled to "
-                          f"the reference's {its:.0f} FP64 CG iterations per "
-                          f"step at the timed steps; oracle restatement, "
-                          f"{threads} threads",
-                "next_rows": cpu_next_rows(threads)}
+            cb, check = cpu_baseline_leg(n, threads, first)
+            cb["next_rows"] = cpu_next_rows(threads)
+            out["cpu_baseline"] = cb
+            for prec, errs in check.items():
+                out["accuracy"][f"{prec}_vs_cpu_oracle_step1"] = errs
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:
@@ -671,7 +735,8 @@ def learned_cavity_leg(n, inner_tol, steps=2, warmup=1):
     pr = ns.profile()
     return {"steps_per_s": steps / (float(np.sum(pr["step_ms"])) / 1e3),
             "solve_ms": float(np.mean(pr["solve_ms"])),
-            "iters": float(np.mean(pr["inner"])), "steps": steps}
+            "iters": float(np.mean(pr["inner"])),
+            "fcg_iters": float(np.mean(pr["outer"])), "steps": steps}
 
 
 def unet_leg(n):

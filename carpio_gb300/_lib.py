@@ -19,6 +19,7 @@ KINDS = {"cg": CG, "jacobi": JACOBI, "dia_bicgstab": DIA_BICGSTAB,
 FP64, MIXED = 0, 1
 FLAG_FULL_NRM2 = 1
 FLAG_NO_TILE = 2
+FLAG_MIXED = 4
 SCHEMES = {"upwind1": 0, "center": 1, "center4": 2, "upwind2": 3,
            "VanLeer": 4, "vanleer": 4, "superbee": 5, "WAHYD": 6, "wahyd": 6,
            "QUICK": 7, "quick": 7, "CUI": 8, "cui": 8, "minmod": 9}
@@ -89,6 +90,8 @@ SIGNATURES = {
     "carpio_gpu_krylov_csr": (ctypes.c_int, [
         ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, _VP, _VP, _VP,
         _I, _D, _VP, ctypes.c_int, _I, ctypes.c_uint32]),
+    "carpio_gpu_residual": (ctypes.c_int, [
+        ctypes.c_int, ctypes.c_int, _VP, _VP, _VP, _VP, _VP, ctypes.c_uint32, _D]),
     "carpio_gpu_krylov_csr_noalloc": (ctypes.c_int, [
         ctypes.c_int, ctypes.c_int, ctypes.c_int, _VP, _VP, _VP, _VP, _VP,
         _I, _D, _VP, ctypes.c_int, _I, ctypes.c_uint32, _VP]),

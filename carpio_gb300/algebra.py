@@ -98,6 +98,21 @@ def BiCGSTAB(A, x, b, max_iter, tol, lresid=None, flags=0):
     return krylov(_lib.BICGSTAB, A, x, b, max_iter, tol, lresid, flags)
 
 
+def Residual(A, x, b, flags=0):
+    """carpio::Residual (solver_matrix.hpp:583-597): nrm2(b - A x) / nrm2(b)
+    with nrm2's drop-last quirk, on the GPU (carpio_gpu_residual)"""
+    L = _lib.load()
+    x = _as_f64(x, "x")
+    b = _as_f64(b, "b")
+    r = ctypes.c_double(0.0)
+    code = L.carpio_gpu_residual(A.iLen(), A.NumNonzeros(), _lib.ptr(A.rowptr),
+                                 _lib.ptr(A.colind), _lib.ptr(A.val), _lib.ptr(x),
+                                 _lib.ptr(b), int(flags), ctypes.byref(r))
+    if code < 0:
+        raise _lib.CarpioGpuError(code, "carpio_gpu_residual")
+    return r.value
+
+
 class Solver_Jacobi_:
     """carpio::Solver_Jacobi_ (solver_matrix.hpp:820-910): class form with
     num_iter() / residual() / get_residual_array()."""

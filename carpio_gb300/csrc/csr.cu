@@ -3,9 +3,11 @@
 // matrix, one persistent cooperative launch per solve.
 #include "internal.hpp"
 #include "ic.cuh"
+#include "mixed.cuh"
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <mutex>
 #include <numeric>
 #include <vector>
@@ -21,6 +23,19 @@ __global__ void __launch_bounds__(kThreads) k_csr_solve(CsrOp op, FlatSpace sp,
 	krylov_run<double>(sp, op, v, sc, gc, bank);
 }
 
+// CARPIO_GPU_FLAG_MIXED: the kind's FP32 iterations inside FP64 refinement
+__global__ void __launch_bounds__(kThreads) k_csr_solve_mixed(CsrOp op, FlatSpace sp,
+		Vecs<double> v, MixedT<CsrOp32> mx, SolveCtl sc, GridCtl gc) {
+	gc.start();
+	int bank = 0;
+	mixed_run(sp, op, v, mx, sc, false, gc, bank);
+}
+
+__global__ void k_to_float(const double* a, float* b, int n) {
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+		b[i] = (float)a[i];
+}
+
 __global__ void __launch_bounds__(kThreads) k_csr_solve_ic(CsrOp op, IcOp ic,
 		Vecs<double> v, SolveCtl sc, GridCtl gc) {
 	gc.start();
@@ -29,12 +44,59 @@ __global__ void __launch_bounds__(kThreads) k_csr_solve_ic(CsrOp op, IcOp ic,
 	else ic_cg_run(ic.n, op, ic, v, sc, gc, bank);
 }
 
+// carpio::Residual (solver_matrix.hpp:583-597), first part: r = b - A x per
+// row in MatrixSCR_::operator*'s order (matrix_SparCompRow.hpp:236-249: from
+// 0, s += x[col] * val, two roundings per term, so r is bit-exact), and per
+// block the sums of squares nrm2 takes of b and of r (BLAS_Level1.hpp:556-577:
+// the last element left out unless `full`; one element: |x[0]|).
+__global__ void __launch_bounds__(kThreads) k_residual_part(CsrOp op, int n,
+		const double* x, const double* b, int full, double* part) {
+	double s[2] = { 0.0, 0.0 };
+	const int counted = (full || n == 1) ? n : n - 1;
+	for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		double ax = 0.0;
+		for (uint32_t e = op.rp[i]; e < op.rp[i + 1]; ++e)
+			ax = __dadd_rn(ax, __dmul_rn(x[op.ci[e]], op.va[e]));
+		const double r = __dsub_rn(b[i], ax);
+		if (i < counted) {
+			s[0] = fma(b[i], b[i], s[0]);
+			s[1] = fma(r, r, s[1]);
+		}
+	}
+	block_sum<double, 2>(s);
+	if (threadIdx.x == 0) {
+		part[2 * blockIdx.x] = s[0];
+		part[2 * blockIdx.x + 1] = s[1];
+	}
+}
+
+// second part, one warp: the partials in a fixed order, then
+// nrm2(r) / nrm2(b) with normb = 1 when it is 0
+__global__ void k_residual_final(int nb, const double* part, double* out) {
+	double sb = 0.0, sr = 0.0;
+	for (int k = threadIdx.x; k < nb; k += 32) {
+		sb += part[2 * k];
+		sr += part[2 * k + 1];
+	}
+	for (int o = 16; o > 0; o >>= 1) {
+		sb += __shfl_down_sync(0xffffffffu, sb, o);
+		sr += __shfl_down_sync(0xffffffffu, sr, o);
+	}
+	if (threadIdx.x == 0) {
+		double normb = sqrt(sb);
+		if (normb == 0.0) normb = 1;
+		out[0] = sqrt(sr) / normb;
+	}
+}
+
 struct CsrWs {
 	std::mutex mu;
 	cudaStream_t s = nullptr;
 	cg_host::LaunchWs lw;
 	cg_host::DevBuf rp, ci, va, vec, hist;
 	cg_host::DevBuf icd, icu[3], icl[3], icf[2], icb[2];   // IC factor, levels
+	cg_host::DevBuf rx, rb, rpart;   // Residual: staged x, b; partials + result
+	cg_host::DevBuf va32, vec32;     // MIXED: FP32 values and vectors
 };
 
 // ICPre (preconditioner.hpp:97-136): the upper triangle with its diagonal,
@@ -121,6 +183,10 @@ extern "C" int carpio_gpu_krylov_csr(int kind, int n, int nnz,
 			|| !x || !max_iter || !tol || kind < 0 || kind > CARPIO_GPU_IC_CG)
 		return CARPIO_GPU_EINVAL;
 	if (hist_cap < 0 || (hist_cap > 0 && !resid_hist)) return CARPIO_GPU_EINVAL;
+	const bool mixed = (flags & CARPIO_GPU_FLAG_MIXED) != 0;
+	if (mixed && kind != CARPIO_GPU_CG && kind != CARPIO_GPU_DIA_BICGSTAB
+			&& kind != CARPIO_GPU_BICGSTAB)
+		return CARPIO_GPU_EINVAL;
 	CsrWs& w = ws();
 	std::lock_guard<std::mutex> lock(w.mu);
 	if (!w.s) CG_CK(cudaStreamCreateWithFlags(&w.s, cudaStreamNonBlocking));
@@ -144,7 +210,9 @@ extern "C" int carpio_gpu_krylov_csr(int kind, int n, int nnz,
 	CG_CK(cudaMemcpyAsync(v.x, x, sizeof(double) * n, cudaMemcpyDefault, s));
 	CG_CK(cudaMemcpyAsync(v.b, b, sizeof(double) * n, cudaMemcpyDefault, s));
 	const bool ic = kind == CARPIO_GPU_IC_CGS || kind == CARPIO_GPU_IC_CG;
-	int blocks = coop_blocks(ic ? (const void*)k_csr_solve_ic : (const void*)k_csr_solve, n, 2);
+	const void* kern = ic ? (const void*)k_csr_solve_ic
+	                      : mixed ? (const void*)k_csr_solve_mixed : (const void*)k_csr_solve;
+	int blocks = coop_blocks(kern, n, 2);
 	if ((rc = w.lw.ensure(blocks))) return rc;
 	if ((rc = w.hist.ensure(sizeof(double) * (size_t)(hist_cap > 0 ? hist_cap : 1)))) return rc;
 	CG_CK(cudaMemsetAsync(w.lw.ctl.p, 0, sizeof(Ctl), s));
@@ -244,6 +312,27 @@ extern "C" int carpio_gpu_krylov_csr(int kind, int n, int nnz,
 		void* args[] = { &op, &icop, &v, &sc, &gc };
 		CG_CK(cudaLaunchCooperativeKernel((const void*)k_csr_solve_ic, blocks,
 				kThreads, args, 0, s));
+	} else if (mixed) {
+		// FP32 copies of the values; 13 FP32 vectors (CG uses four)
+		if ((rc = w.va32.ensure(sizeof(float) * (size_t)(nnz ? nnz : 1)))) return rc;
+		if ((rc = w.vec32.ensure(sizeof(float) * (size_t)n * 13))) return rc;
+		if (nnz) {
+			const int nb = std::max(1, std::min((nnz + kThreads - 1) / kThreads, 4 * sm_count()));
+			k_to_float<<<nb, kThreads, 0, s>>>(w.va.as<double>(), w.va32.as<float>(), nnz);
+			CG_CK(cudaGetLastError());
+		}
+		MixedT<CsrOp32> mx;
+		std::memset(&mx, 0, sizeof mx);
+		mx.op32 = CsrOp32{ w.rp.as<uint32_t>(), w.ci.as<uint32_t>(), w.va32.as<float>() };
+		float* fb = w.vec32.as<float>();
+		float** fs[13] = { &mx.f.x, &mx.f.r, &mx.f.p, &mx.f.q, &mx.f.b, &mx.f.z,
+			&mx.f.rt, &mx.f.ph, &mx.f.s, &mx.f.sh, &mx.f.t, &mx.f.v, &mx.f.d };
+		for (int i = 0; i < 13; ++i) *fs[i] = fb + (size_t)i * n;
+		mx.inner_tol = 1e-4;
+		mx.inner_max = 1 << 30;
+		void* args[] = { &op, &sp, &v, &mx, &sc, &gc };
+		CG_CK(cudaLaunchCooperativeKernel((const void*)k_csr_solve_mixed, blocks,
+				kThreads, args, 0, s));
 	} else {
 		void* args[] = { &op, &sp, &v, &sc, &gc };
 		CG_CK(cudaLaunchCooperativeKernel((const void*)k_csr_solve, blocks,
@@ -266,4 +355,37 @@ extern "C" int carpio_gpu_krylov_csr(int kind, int n, int nnz,
 	*tol = c.out.tol;
 	if (hist_len) *hist_len = c.out.hist_len;
 	return code;
+}
+
+extern "C" int carpio_gpu_residual(int n, int nnz, const uint32_t* rowptr,
+		const uint32_t* col, const double* val, const double* x, const double* b,
+		uint32_t flags, double* resid) {
+	using namespace cg_host;
+	if (n <= 0 || nnz < 0 || !rowptr || (!col && nnz) || (!val && nnz) || !x || !b
+			|| !resid)
+		return CARPIO_GPU_EINVAL;
+	CsrWs& w = ws();
+	std::lock_guard<std::mutex> lock(w.mu);
+	if (!w.s) CG_CK(cudaStreamCreateWithFlags(&w.s, cudaStreamNonBlocking));
+	cudaStream_t s = w.s;
+	int rc;
+	if ((rc = to_device(w.rp, rowptr, sizeof(uint32_t) * (n + 1), s))) return rc;
+	if ((rc = to_device(w.ci, col, sizeof(uint32_t) * (size_t)nnz, s))) return rc;
+	if ((rc = to_device(w.va, val, sizeof(double) * (size_t)nnz, s))) return rc;
+	if ((rc = to_device(w.rx, x, sizeof(double) * n, s))) return rc;
+	if ((rc = to_device(w.rb, b, sizeof(double) * n, s))) return rc;
+	const int nb = std::max(1, std::min((n + kThreads - 1) / kThreads, 4 * sm_count()));
+	if ((rc = w.rpart.ensure(sizeof(double) * (2 * (size_t)nb + 1)))) return rc;
+	double* part = w.rpart.as<double>();
+	CsrOp op{ w.rp.as<uint32_t>(), w.ci.as<uint32_t>(), w.va.as<double>() };
+	k_residual_part<<<nb, kThreads, 0, s>>>(op, n, w.rx.as<double>(), w.rb.as<double>(),
+			(flags & CARPIO_GPU_FLAG_FULL_NRM2) ? 1 : 0, part);
+	CG_CK(cudaGetLastError());
+	k_residual_final<<<1, 32, 0, s>>>(nb, part, part + 2 * nb);
+	CG_CK(cudaGetLastError());
+	double r = 0.0;
+	CG_CK(cudaMemcpyAsync(&r, part + 2 * nb, sizeof r, cudaMemcpyDeviceToHost, s));
+	CG_CK(cudaStreamSynchronize(s));
+	*resid = r;
+	return 0;
 }

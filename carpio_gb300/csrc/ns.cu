@@ -859,10 +859,13 @@ int carpio_gpu_ns_create(carpio_gpu_grid* g, const carpio_gpu_ns_cfg* cfg,
 			|| cfg->scheme > 9 || !valid_bc(cfg->bc_u) || !valid_bc(cfg->bc_v)
 			|| !(cfg->rho != 0))
 		return CARPIO_GPU_EINVAL;
-	// the projection: CG (the drop-in, any precision) or the shipped IC_CGS /
-	// IC_CG (FP64; solved synchronously through the CSR layer)
+	// the projection: CG (the drop-in) or Dia_BiCGSTAB / BiCGSTAB, in either
+	// precision, or the shipped IC_CGS / IC_CG (FP64; solved synchronously
+	// through the CSR layer)
 	const int pk = cfg->projection.kind;
-	if (pk != CARPIO_GPU_CG && !((pk == CARPIO_GPU_IC_CGS || pk == CARPIO_GPU_IC_CG)
+	const bool krylov = pk == CARPIO_GPU_CG || pk == CARPIO_GPU_DIA_BICGSTAB
+			|| pk == CARPIO_GPU_BICGSTAB;
+	if (!krylov && !((pk == CARPIO_GPU_IC_CGS || pk == CARPIO_GPU_IC_CG)
 			&& cfg->projection.precision == CARPIO_GPU_FP64))
 		return CARPIO_GPU_EINVAL;
 	*out = nullptr;
@@ -1163,9 +1166,11 @@ int carpio_gpu_ns_profile(carpio_gpu_ns* ns, int cap, int* n,
 		if (solve_ms) solve_ms[st] = a;
 		if (step_ms) step_ms[st] = b;
 		const cg_dev::SolveOut& o = ns->last_rec[st];
+		// learned: all iterations (flexible CG + fallback) and the flexible
+		// CG's alone; mixed: FP32 iterations and FP64 refinements
 		bool mixed = ns->cfg.projection.precision == CARPIO_GPU_MIXED;
-		if (inner_iters) inner_iters[st] = mixed ? o.inner : o.iters;
-		if (outer_iters) outer_iters[st] = mixed ? o.outer : 0;
+		if (inner_iters) inner_iters[st] = ns->learned ? o.iters : mixed ? o.inner : o.iters;
+		if (outer_iters) outer_iters[st] = (ns->learned || mixed) ? o.outer : 0;
 	}
 	return 0;
 }

@@ -9,6 +9,7 @@
 // sums are ordered differently.
 #include "internal.hpp"
 #include "poisson_rhs.cuh"
+#include "mixed.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -22,127 +23,12 @@ using namespace cg_dev;
 
 // ------------------------------------------------------------ device side --
 template<bool NU>
-struct MixedArgsT {
-	StencilOp<float, NU> op32;
-	Vecs<float> f;         // e (x), r, p, q
-	double inner_tol;
-	int inner_max;
-	int pdeg;              // on-chip path: degree of the band-local Chebyshev
-	                       // preconditioner (0 = none)
-	float pratio;          // its eigenvalue interval [2 / pratio, 2] of D^-1 A
-};
+using MixedArgsT = MixedT<StencilOp<float, NU>>;
 using MixedArgs = MixedArgsT<false>;
 // the uniform and non-uniform specialisations differ in code only, so one
 // host-side argument block serves the kernels of either
 static_assert(sizeof(MixedArgsT<true>) == sizeof(MixedArgs), "layout");
 static_assert(sizeof(StencilOp<double, true>) == sizeof(StencilOp<double>), "layout");
-
-// FP32 CG on A32 e = r32 from e = 0 (one inner solve of the refinement).
-// Returns the number of iterations, or -1 on a barrier error.
-template<bool NU>
-__device__ int inner_cg(const GridSpace& sp, const MixedArgsT<NU>& m, int cap,
-		const GridCtl& gc, int& bank) {
-	const Vecs<float>& f = m.f;
-	const StencilOp<float, NU>& op = m.op32;
-	float rr0[1] = { 0 };
-	KLOOP(sp) {
-		int a = sp.addr(k);
-		float r = f.r[a];
-		f.x[a] = 0.f;
-		f.p[a] = r;
-		rr0[0] = fmaf(r, r, rr0[0]);
-	}
-	if (!grid_allreduce<float, 1>(rr0, gc, bank)) return -1;
-	float rho = rr0[0];
-	const float stop = (float)(m.inner_tol * m.inner_tol) * rho;
-	int it = 0;
-	while (it < cap && rho > stop && rho > 0.f) {
-		float pq[1] = { 0 };
-		KLOOP(sp) {
-			int a = sp.addr(k);
-			float q = op.apply(f.p, k, a);
-			f.q[a] = q;
-			pq[0] = fmaf(f.p[a], q, pq[0]);
-		}
-		if (!grid_allreduce<float, 1>(pq, gc, bank)) return -1;
-		float alpha = rho / pq[0];
-		float rr[1] = { 0 };
-		KLOOP(sp) {
-			int a = sp.addr(k);
-			f.x[a] = fmaf(alpha, f.p[a], f.x[a]);
-			float r = fmaf(-alpha, f.q[a], f.r[a]);
-			f.r[a] = r;
-			rr[0] = fmaf(r, r, rr[0]);
-		}
-		if (!grid_allreduce<float, 1>(rr, gc, bank)) return -1;
-		float beta = rr[0] / rho;
-		rho = rr[0];
-		++it;
-		if (it < cap && rho > stop) {
-			KLOOP(sp) { int a = sp.addr(k); f.p[a] = fmaf(beta, f.p[a], f.r[a]); }
-			if (!grid_sync(gc)) return -1;
-		}
-	}
-	return it;
-}
-
-// FP32 inner CG inside FP64 iterative refinement: r = b - A x, the stopping
-// test and the update of x in FP64; the correction solve in FP32 with FP32
-// accumulation, on the residual scaled to unit norm.
-template<bool NU>
-__device__ void mixed_run(const GridSpace& sp, const StencilOp<double, NU>& op,
-		const Vecs<double>& v, const MixedArgsT<NU>& m, const SolveCtl& sc,
-		bool mean, const GridCtl& gc, int& bank) {
-	const bool full = (sc.flags & CARPIO_GPU_FLAG_FULL_NRM2) || sp.count() == 1;
-	const int la = sp.last_addr();
-	const double n = (double)sp.count();
-	int hl = 0, total = 0, outer = 0;
-	double acc[1] = { 0 };
-	KLOOP(sp) {
-		int a = sp.addr(k);
-		double bb = v.b[a];
-		if (a != la || full) acc[0] = fma(bb, bb, acc[0]);
-	}
-	if (!grid_allreduce<double, 1>(acc, gc, bank)) return;
-	double normb = sqrt(acc[0]);
-	if (normb == 0.0) normb = 1;
-	double resid = 0;
-	for (;;) {
-		double rs[3] = { 0, 0, 0 };
-		KLOOP(sp) {
-			int a = sp.addr(k);
-			double r = v.b[a] - op.apply(v.x, k, a);
-			v.r[a] = r;
-			if (a != la || full) rs[0] = fma(r, r, rs[0]);
-			rs[1] += r;
-			rs[2] = fma(r, r, rs[2]);
-		}
-		if (!grid_allreduce<double, 3>(rs, gc, bank)) return;
-		resid = sqrt(rs[0]) / normb;
-		hist_push(sc, hl, resid);
-		if (resid <= sc.tol) {
-			if (blockIdx.x == 0 && threadIdx.x == 0) { sc.out->outer = outer; sc.out->inner = total; }
-			finish(sc, 0, total, resid, hl);
-			return;
-		}
-		if (total >= sc.max_iter) break;
-		double mr = mean ? rs[1] / n : 0.0;
-		double rn = sqrt(mean ? fmax(rs[2] - rs[1] * mr, 0.0) : rs[2]);
-		if (!(rn > 0.0)) break;
-		double sc_in = 1.0 / rn;
-		KLOOP(sp) { int a = sp.addr(k); m.f.r[a] = (float)((v.r[a] - mr) * sc_in); }
-		if (!grid_sync(gc)) return;
-		int it = inner_cg(sp, m, min(m.inner_max, sc.max_iter - total), gc, bank);
-		if (it < 0) return;
-		total += it;
-		++outer;
-		KLOOP(sp) { int a = sp.addr(k); v.x[a] = fma(rn, (double)m.f.x[a], v.x[a]); }
-		if (!grid_sync(gc)) return;
-		if (it == 0) break;
-	}
-	if (blockIdx.x == 0 && threadIdx.x == 0) { sc.out->outer = outer; sc.out->inner = total; }
-	finish(sc, 1, total, resid, hl);
-}
 
 template<int SRC, int KIND, bool NU>
 __global__ void __launch_bounds__(kThreads) k_poisson(StencilOp<double, NU> op,
@@ -974,7 +860,9 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 	}
 	const size_t NF = (size_t)g->NI * g->P;
 	const bool mixed = cfg.precision == CARPIO_GPU_MIXED;
-	const int nv64 = 13, nv32 = 4;
+	// FP32 vectors: x r p q for the inner CG, 13 (all of Vecs) for the
+	// inner BiCGSTAB
+	const int nv64 = 13, nv32 = cfg.kind == CARPIO_GPU_CG ? 4 : 13;
 	int rc;
 	if (w.v64.bytes < sizeof(double) * NF * nv64) {
 		if ((rc = w.v64.ensure(sizeof(double) * NF * nv64))) return rc;
@@ -1013,10 +901,9 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 	std::memset(&mx.f, 0, sizeof mx.f);
 	if (mixed) {
 		float* fb = w.v32.as<float>();
-		mx.f.x = fb;
-		mx.f.r = fb + NF;
-		mx.f.p = fb + 2 * NF;
-		mx.f.q = fb + 3 * NF;
+		float** fs[13] = { &mx.f.x, &mx.f.r, &mx.f.p, &mx.f.q, &mx.f.b, &mx.f.z,
+			&mx.f.rt, &mx.f.ph, &mx.f.s, &mx.f.sh, &mx.f.t, &mx.f.v, &mx.f.d };
+		for (int i = 0; i < nv32; ++i) *fs[i] = fb + (size_t)i * NF;
 	}
 	mx.inner_tol = cfg.inner_tol > 0 ? cfg.inner_tol : 1e-4;
 	mx.inner_max = cfg.inner_max_iter > 0 ? cfg.inner_max_iter : 1 << 30;
@@ -1042,7 +929,7 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 	// mixed solves whose bands fit the tile kernel run on chip
 	// the on-chip kernel keeps one coefficient per face row / column: uniform
 	// grids only (non-uniform ones run the global-memory FP32 inner CG)
-	if (mixed && c.uniform && !(cfg.flags & CARPIO_GPU_FLAG_NO_TILE)) {
+	if (mixed && c.uniform && cfg.kind == CARPIO_GPU_CG && !(cfg.flags & CARPIO_GPU_FLAG_NO_TILE)) {
 		const int C = std::min(sm_count(), g->nx);
 		const int rows_max = (g->nx + C - 1) / C;
 		const int nc = (g->ny + kTileThreads - 1) / kTileThreads;
@@ -1256,7 +1143,9 @@ static int structured_solve(carpio_gpu_grid* g, const carpio_gpu_bc* bc,
 			|| cfg->kind < 0 || cfg->kind > CARPIO_GPU_IC_CG || hist_cap < 0
 			|| (hist_cap > 0 && !resid_hist) || !(beta == beta) || !(alpha == alpha))
 		return CARPIO_GPU_EINVAL;
-	if (cfg->precision == CARPIO_GPU_MIXED && cfg->kind != CARPIO_GPU_CG)
+	// FP32 inner iterations: CG, Dia_BiCGSTAB and BiCGSTAB
+	if (cfg->precision == CARPIO_GPU_MIXED && cfg->kind != CARPIO_GPU_CG
+			&& cfg->kind != CARPIO_GPU_DIA_BICGSTAB && cfg->kind != CARPIO_GPU_BICGSTAB)
 		return CARPIO_GPU_EINVAL;
 	for (int k = 0; k < 4; ++k)
 		if (bc->type[k] != 1 && bc->type[k] != 2) return CARPIO_GPU_EINVAL;

@@ -61,6 +61,13 @@ extern "C" {
                                           drop-last-element (BLAS_Level1.hpp:569) */
 #define CARPIO_GPU_FLAG_NO_TILE 2u     /* MIXED: run the inner FP32 CG from global
                                           memory instead of the on-chip tile kernel */
+#define CARPIO_GPU_FLAG_MIXED 4u       /* CSR layer: the kind's iterations in FP32
+                                          inside FP64 iterative refinement (CG,
+                                          DIA_BICGSTAB, BICGSTAB; the stopping
+                                          test the reference's, in FP64 on
+                                          b - A x; max_iter out = FP32
+                                          iterations, lresid = one FP64
+                                          residual per refinement) */
 
 /* ----- library ----------------------------------------------------------- */
 const char* carpio_gpu_version(void);
@@ -92,18 +99,34 @@ int carpio_gpu_krylov_csr(int kind, int n, int nnz, const uint32_t* rowptr,
 		int* max_iter, double* tol, double* resid_hist, int hist_cap,
 		int* hist_len, uint32_t flags);
 
+/* Replaces   double Residual(const MatrixSCR_<V>& A, const ArrayListV<V>& x,
+ *                             const ArrayListV<V>& b)
+ * (lib/algebra/solver_matrix.hpp:583-597): *resid = nrm2(b - A x) / nrm2(b),
+ * nrm2(b) taken as 1 when it is 0, nrm2 leaving out the last element as
+ * the reference's does (CARPIO_GPU_FLAG_FULL_NRM2: all of them). b - A x is
+ * formed row by row in the reference's order (bit-exact); the sums of
+ * squares are fixed-order trees. Arrays host or device. */
+int carpio_gpu_residual(int n, int nnz, const uint32_t* rowptr,
+		const uint32_t* col, const double* val, const double* x, const double* b,
+		uint32_t flags, double* resid);
+
 /* The same solve for callers that cannot allocate device memory during a
  * solve (a framework that owns all device memory through its own pool, or a
  * time-stepping service that forbids cudaMalloc/cudaFree after start-up).
  * No counterpart in the reference. Kinds CG .. BICGSTAB only (the IC kinds
- * build their factor on the host and in device buffers: CARPIO_GPU_EINVAL). All arrays must be device memory the
- * caller owns; the solver's scratch is a fixed ~3 MiB array compiled into
- * the library (held by every device that loads it) and n is limited to
- * 32768 rows (larger n: CARPIO_GPU_EINVAL). The first call on a device sets
- * up the array's address and should come before any stream capture. Calls
- * share the array: calls that overlap on the GPU race and must be
- * serialised by the caller. `stream` is a cudaStream_t (NULL = default);
- * the call returns when the solve has finished. */
+ * build their factor on the host and in device buffers: CARPIO_GPU_EINVAL).
+ * All arrays must be memory of the current device (or managed memory) that
+ * the caller owns; host memory and another GPU's memory give
+ * CARPIO_GPU_EINVAL. The solver's scratch is a fixed ~3 MiB array compiled
+ * into the library (held by every device that loads it) and n is limited to
+ * 32768 rows (larger n: CARPIO_GPU_EINVAL). The first call on a device looks
+ * up the array's address; make it before any stream capture begins. One
+ * array serves every call on a device: calls that overlap on the GPU race
+ * and must be serialised by the caller. `stream` is a cudaStream_t (NULL =
+ * default); every call reads its result back and synchronises `stream`
+ * before it returns. x is iterated in place: after a negative return it
+ * holds a partial iterate, so a caller that needs x0 afterwards keeps a
+ * copy (carpio_gpu_krylov_csr leaves x untouched on failure). */
 int carpio_gpu_krylov_csr_noalloc(int kind, int n, int nnz,
 		const uint32_t* rowptr, const uint32_t* col, const double* val,
 		const double* b, double* x, int* max_iter, double* tol,
@@ -150,20 +173,26 @@ typedef struct {
 } carpio_gpu_bc;
 
 #define CARPIO_GPU_FP64 0
-#define CARPIO_GPU_MIXED 1   /* FP32 inner CG inside FP64 iterative refinement */
+#define CARPIO_GPU_MIXED 1   /* FP32 inner CG / BiCGSTAB inside FP64 iterative
+                                refinement */
 
 typedef struct {
 	int kind;          /* CARPIO_GPU_CG / JACOBI / DIA_BICGSTAB / BICGSTAB, or
 	                      IC_CGS / IC_CG (FP64, no beta field: the stencil rows
 	                      go to the CSR solver of section 1; synchronous) */
-	int precision;     /* CARPIO_GPU_FP64 or CARPIO_GPU_MIXED (CG only) */
+	int precision;     /* CARPIO_GPU_FP64 or CARPIO_GPU_MIXED (kinds CG,
+	                      DIA_BICGSTAB and BICGSTAB: the inner iterations
+	                      are the kind's own in FP32, the stopping test the
+	                      reference's in FP64 on b - A x) */
 	int max_iter;      /* Solver_::set_max_iter */
 	double tol;        /* Solver_::set_tolerance (relative residual) */
 	int mean_removal;  /* remove the mean of b and x (all-Neumann null space) */
 	double inner_tol;  /* MIXED: residual reduction between two FP64 residual
 	                      replacements (reliable updates; at most 1e-2 is used
 	                      on chip); 0 = 1e-1 on chip with the Chebyshev
-	                      preconditioner, else 3e-2 */
+	                      preconditioner, 3e-2 on chip without it, 1e-4 on
+	                      the global-memory path (BiCGSTAB kinds, non-uniform
+	                      grids, CARPIO_GPU_FLAG_NO_TILE) */
 	int inner_max_iter;/* MIXED, global-memory path: cap on one inner solve */
 	uint32_t flags;    /* CARPIO_GPU_FLAG_* */
 	int poly_degree;   /* MIXED, on-chip path: degree of the band-local
@@ -285,7 +314,9 @@ int carpio_gpu_ns_set_mu_field(carpio_gpu_ns* ns, const double* mu);
 /* Timing of the last carpio_gpu_ns_run, per step (host arrays of length
  * `cap`, any may be NULL): device time of the projection solve launch and of
  * the whole step (CUDA events on the launching stream), inner (FP32) and
- * outer iterations of the solve. *n gets the number of steps recorded. */
+ * outer iterations of the solve (with the learned preconditioner: all
+ * iterations, and those of the flexible CG before any fallback). *n gets the
+ * number of steps recorded. */
 int carpio_gpu_ns_profile(carpio_gpu_ns* ns, int cap, int* n,
 		double* solve_ms, double* step_ms, int* inner_iters, int* outer_iters);
 

@@ -285,6 +285,9 @@ static int cmd_csr(int argc, char** argv) {
 	put_csr(A);
 	put_arr("b", b);
 	put_arr("x0", x);
+	// carpio::Residual (solver_matrix.hpp:583-597) of the start and, below,
+	// of the solution
+	put_scalar("residual_x0", carpio::Residual(A, x, b));
 	std::list<Vt> lr;
 	int ret, mi = max_iter;
 	double t = tol;
@@ -303,6 +306,7 @@ static int cmd_csr(int argc, char** argv) {
 	double ms = std::chrono::duration<double, std::milli>(
 			std::chrono::steady_clock::now() - t0).count();
 	put_arr("x", x);
+	put_scalar("residual_x", carpio::Residual(A, x, b));
 	put_list("lresid", lr);
 	put_scalar("ret", ret);
 	put_scalar("max_iter_in", max_iter);
@@ -476,9 +480,12 @@ static int cmd_cavity(int argc, char** argv) {
 	}
 	ns.initial();
 	if (mufield) put_field("mu", *ns.cs("mu"));
-	std::vector<double> dts, its, ms, res, rets;
+	std::vector<double> dts, its, ms, res, rets, step_ms;
 	for (int s = 0; s < steps; ++s) {
+		auto t0 = std::chrono::steady_clock::now();
 		ns.step_once();
+		step_ms.push_back(std::chrono::duration<double, std::milli>(
+				std::chrono::steady_clock::now() - t0).count());
 		dts.push_back(ns.dt());
 		rets.push_back(rec.back().ret);
 		its.push_back(rec.back().iters);
@@ -510,6 +517,7 @@ static int cmd_cavity(int argc, char** argv) {
 	put_vec("cg_iters", its);
 	put_vec("cg_ret", rets);
 	put_vec("cg_ms", ms);
+	put_vec("step_ms", step_ms);
 	put_vec("cg_resid", res);
 	put_scalar("Re", Re);
 	put_scalar("dt0", dt0);

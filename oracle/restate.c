@@ -85,6 +85,29 @@ static void spmv(int n, const unsigned* rp, const unsigned* ci,
 	}
 }
 
+/* carpio::Residual (solver_matrix.hpp:583-597): nrm2(b - A x) / nrm2(b),
+ * normb = 1 when it is 0, with nrm2's drop-last quirk (full != 0: every
+ * element counted). */
+double rs_residual(int n, const unsigned* rp, const unsigned* ci,
+		const double* va, const double* x, const double* b, int full) {
+	double* r = (double*)malloc(sizeof(double) * (n > 0 ? n : 1));
+	spmv(n, rp, ci, va, x, r, 1);
+	for (int i = 0; i < n; ++i) r[i] = b[i] - r[i];
+	double normb, nr;
+	if (full && n > 1) {
+		double sb = 0.0, sr = 0.0;
+		for (int i = 0; i < n; ++i) { sb += b[i] * b[i]; sr += r[i] * r[i]; }
+		normb = sqrt(sb);
+		nr = sqrt(sr);
+	} else {
+		normb = rs_nrm2(n, b);
+		nr = rs_nrm2(n, r);
+	}
+	free(r);
+	if (normb == 0.0) normb = 1;
+	return nr / normb;
+}
+
 #define VLOOP(n, th) \
 	_Pragma("omp parallel for num_threads(th) if (th > 1) schedule(static)") \
 	for (int i = 0; i < (n); ++i)

@@ -41,6 +41,8 @@ int rs_krylov_csr(int kind, int n, const unsigned* rowptr, const unsigned* col,
 /* lib/algebra/BLAS_Level1.hpp:499-544 and 556-577 */
 double rs_dot(int n, const double* x, const double* y);
 double rs_nrm2(int n, const double* x);
+double rs_residual(int n, const unsigned* rp, const unsigned* ci,
+		const double* va, const double* x, const double* b, int full);
 
 /* Grid_::_set_uniform_grid (lib/structure/s_grid.hpp:372-395): cell sizes
  * s[0..n+2gl) and centres c[0..n+2gl), ghosts included. */

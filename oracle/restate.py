@@ -61,6 +61,8 @@ def lib():
         L.rs_dot.restype = ctypes.c_double
         L.rs_nrm2.argtypes = [ctypes.c_int, _d]
         L.rs_nrm2.restype = ctypes.c_double
+        L.rs_residual.argtypes = [ctypes.c_int, _u, _u, _d, _d, _d, ctypes.c_int]
+        L.rs_residual.restype = ctypes.c_double
         L.rs_grid_uniform.argtypes = [ctypes.c_int, ctypes.c_int,
                                       ctypes.c_double, ctypes.c_double, _d, _d]
         L.rs_grid_sizes.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double,
@@ -157,6 +159,14 @@ class Grid:
     def interior(self, f):
         g = self.gl
         return f[g:g + self.nx, g:g + self.ny]
+
+
+def residual(rowptr, colind, val, x, b, full=False):
+    """carpio::Residual restated: nrm2(b - A x) / nrm2(b)"""
+    rp = np.ascontiguousarray(rowptr, dtype=np.uint32)
+    ci = np.ascontiguousarray(colind, dtype=np.uint32)
+    return lib().rs_residual(len(rp) - 1, _p(rp, _u), _p(ci, _u), _p(_f64(val)),
+                             _p(_f64(x)), _p(_f64(b)), 1 if full else 0)
 
 
 def krylov_csr(kind, rowptr, colind, val, b, x0, max_iter, tol,

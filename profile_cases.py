@@ -1,22 +1,25 @@
 """Small fixed workloads of single kernels, for profilers and timing.
 
-    python -m carpio_gb300.profile_cases unet N
+    python profile_cases.py unet N
         two forwards of the trained U-Net on one N x N field (the tcgen05
         3x3 convolutions and the network's elementwise kernels)
-    python -m carpio_gb300.profile_cases batch COUNT N
+    python profile_cases.py batch COUNT N
         one batched persistent solve of COUNT all-Neumann N x N problems with
         Gaussian sources to 1e-8 (thread-block clusters of 16 CTAs)
 
 Each prints one line with its timing and exits 0 on success.
 """
+import os
 import sys
 
 import numpy as np
 
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+
 
 def unet(n):
     import torch
-    from .unet import load_trained
+    from carpio_gb300.unet import load_trained
     net = load_trained()
     x = torch.randn(1, n, n, device="cuda", generator=torch.Generator("cuda").manual_seed(0))
     z = torch.empty_like(x)
@@ -27,8 +30,8 @@ def unet(n):
 
 
 def batch(count, n):
-    from . import workloads
-    from .batch import BatchedPoisson, Problem, NEUMANN
+    from carpio_gb300 import workloads
+    from carpio_gb300.batch import BatchedPoisson, Problem, NEUMANN
     rng = np.random.default_rng(1)
     probs = [Problem(n, n, bc=[(NEUMANN, 0.0)] * 4) for _ in range(count)]
     srcs = [workloads.gaussian_source(n, n, rng) for _ in probs]

@@ -2,7 +2,7 @@
 reference's own code (oracle/_ref/ref_harness, compiled from the reference's
 headers by `make -C oracle ref`).
 
-    python tests/golden/make_golden.py [--ref /path/to/reference] [--long]
+    python tests/golden/make_golden.py --ref /path/to/reference [--long]
         [--only NAME_PREFIX]
 
 Each fixture is a compressed .npz of the harness's inputs and outputs.
@@ -97,7 +97,7 @@ def save(name, d):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--ref", required=True, help="the reference checkout")
     ap.add_argument("--long", action="store_true")
     ap.add_argument("--long-dir", default=None)
     ap.add_argument("--only-long", action="store_true",

@@ -62,6 +62,13 @@ def test_argument_validation_before_device_work():
                                    None, None, _lib.ptr(z), _lib.ptr(z),
                                    ctypes.byref(mi), ctypes.byref(tol), None,
                                    0, None, 0) == _lib.EINVAL
+    r = ctypes.c_double()
+    assert L.carpio_gpu_residual(0, 0, _lib.ptr(np.zeros(1, np.uint32)), None, None,
+                                 _lib.ptr(z), _lib.ptr(z), 0,
+                                 ctypes.byref(r)) == _lib.EINVAL
+    assert L.carpio_gpu_residual(4, 4, _lib.ptr(np.zeros(5, np.uint32)), None, None,
+                                 _lib.ptr(z), _lib.ptr(z), 0,
+                                 ctypes.byref(r)) == _lib.EINVAL
     h = ctypes.c_void_p()
     assert L.carpio_gpu_grid_create_uniform(0, 4, 2, 0, 1, 0, 1,
                                             ctypes.byref(h)) == _lib.EINVAL

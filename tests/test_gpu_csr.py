@@ -214,3 +214,87 @@ def test_csr_class_jacobi_matches_reference_test(gpu_lib):
     assert abs(s.num_iter() - int(d["max_iter_out"])) <= 60
     assert s.residual() <= 1e-6
     assert rel_l2(x, d["x"]) < 1e-6
+
+
+@pytest.mark.parametrize("name", golden_names("csr_"))
+def test_residual_matches_reference(gpu_lib, name):
+    """carpio_gpu_residual against carpio::Residual as the reference itself
+    evaluated it (solver_matrix.hpp:583-597) on the fixture's start and
+    solution, and against the oracle's restatement. b - A x is bit-exact;
+    the sums of squares are trees instead of a loop: agreement to 1e-13."""
+    from carpio_gb300 import algebra
+    d = golden(name)
+    if "aborted" in d:
+        return
+    A = algebra.MatrixSCR(d["rowptr"], d["colind"], d["val"])
+    for xk, rk in (("x0", "residual_x0"), ("x", "residual_x")):
+        x, b = d[xk].copy(), d["b"].copy()
+        r = algebra.Residual(A, x, b)
+        ref = float(d[rk])
+        orc = R.residual(A.rowptr, A.colind, A.val, x, b)
+        if np.isnan(ref):
+            assert np.isnan(r) and np.isnan(orc)
+            continue
+        assert orc == ref, (name, xk, orc, ref)
+        assert abs(r - ref) <= 1e-13 * ref, (name, xk, r, ref)
+        # the full 2-norm on request
+        rf = algebra.Residual(A, x, b, flags=1)
+        full = np.linalg.norm(b - A @ x) / np.linalg.norm(b)
+        assert abs(rf - full) <= 1e-12 * full
+
+
+def test_residual_edge_cases(gpu_lib):
+    """one row (nrm2 = |x[0]|), zero b (normb taken as 1), device arrays"""
+    torch = pytest.importorskip("torch")
+    from carpio_gb300 import algebra
+    A = algebra.MatrixSCR(np.array([0, 1]), np.array([0]), np.array([2.0]))
+    assert algebra.Residual(A, np.array([3.0]), np.array([1.0])) == 5.0
+    n = 50
+    rp = np.arange(n + 1)
+    A = algebra.MatrixSCR(rp, np.arange(n), np.linspace(1.0, 2.0, n))
+    x = np.linspace(-1.0, 1.0, n)
+    z = np.zeros(n)
+    r = algebra.Residual(A, x, z)
+    assert abs(r - R.residual(A.rowptr, A.colind, A.val, x, z)) <= 1e-14 * r
+    xd = torch.from_numpy(x).cuda()
+    bd = torch.from_numpy(np.ones(n)).cuda()
+    r2 = algebra.Residual(A, xd, bd)
+    assert abs(r2 - R.residual(A.rowptr, A.colind, A.val, x, np.ones(n))) <= 1e-13 * r2
+
+
+@pytest.mark.parametrize("mtx,kind,bar", [("csr_pde225_bicgstab", "bicgstab", 1e-9),
+                                          ("csr_pde225_dia_bicgstab", "dia_bicgstab", 1e-9),
+                                          ("csr_bus685_cg", "cg", 1e-6)])
+def test_csr_mixed_precision_against_oracle(gpu_lib, mtx, kind, bar):
+    """CARPIO_GPU_FLAG_MIXED: the kind's iterations in FP32 inside FP64
+    refinement, to 1e-12 against the oracle's FP64 solve to 1e-13. The bar
+    is the tolerance times the matrix's conditioning: 1e-9 on pde225, 1e-6
+    on 685_bus (kappa ~ 4e5)."""
+    from carpio_gb300 import algebra, _lib
+    d = golden(mtx)
+    A = algebra.MatrixSCR(d["rowptr"], d["colind"], d["val"])
+    x = np.zeros(A.iLen())
+    lr = []
+    code, it, t = algebra.krylov(kind, A, x, d["b"].copy(), 50000, 1e-12, lr,
+                                 flags=_lib.FLAG_MIXED)
+    assert code == 0 and t <= 1e-12
+    assert len(lr) >= 2   # one FP64 residual per refinement
+    c2, x2, it2, t2, _ = R.krylov_csr(kind, A.rowptr, A.colind, A.val, d["b"],
+                                      np.zeros(A.iLen()), 50000, 1e-13)
+    assert c2 == 0
+    err = rel_l2(x, x2)
+    print(f"{mtx} {kind} mixed vs oracle: rel-L2 {err:.2e}, {it} FP32 iterations, "
+          f"{len(lr)} refinements")
+    assert err <= bar, err
+    assert true_resid(A, x, d["b"]) <= 1e-11
+
+
+def test_csr_mixed_rejects_other_kinds(gpu_lib):
+    from carpio_gb300 import algebra, _lib
+    d = golden("csr_bus685_cg")
+    A = algebra.MatrixSCR(d["rowptr"], d["colind"], d["val"])
+    for kind in ("jacobi", "ic_cg", "ic_cgs"):
+        with pytest.raises(_lib.CarpioGpuError) as e:
+            algebra.krylov(kind, A, np.zeros(A.iLen()), d["b"].copy(), 10, 1e-8,
+                           flags=_lib.FLAG_MIXED)
+        assert e.value.code == _lib.EINVAL

@@ -190,3 +190,60 @@ def test_watchdog_expiry_is_reported(gpu_lib):
         L.carpio_gpu_set_watchdog(2000, 600000)
     g, P = make_poisson(64, "c1", "cg", 1000, 1e-10, d["source"])
     assert P.run() == 0
+
+
+# Mixed precision against the FP64 oracle: FP32 inner iterations inside FP64
+# refinement driven to 1e-12 against the oracle's FP64 solve to 1e-13. Both
+# meet their residual tolerances; the solutions then differ by about the
+# tolerance times the conditioning of these small grids (kappa ~ 1e2..1e3):
+# relative L2 <= 1e-9.
+MIXED_RTOL = 1e-9
+
+
+@pytest.mark.parametrize("case,n,kind,name", [
+    ("mixed", 24, "cg", "poisson_mixed_24_cg"),
+    ("mixed", 24, "dia_bicgstab", "poisson_mixed_24_dia_bicgstab"),
+    ("mixed", 24, "bicgstab", "poisson_mixed_24_bicgstab"),
+    ("vbeta", 24, "bicgstab", "poisson_vbeta_24_bicgstab"),
+    ("c1", 64, "bicgstab", "poisson_c1_64_bicgstab"),
+    ("neumann", 48, "cg", "poisson_neumann_48_cg"),
+    ("neumann", 48, "dia_bicgstab", "poisson_neumann_48_cg")])
+def test_mixed_precision_against_oracle(gpu_lib, case, n, kind, name):
+    """CG, Dia_BiCGSTAB and BiCGSTAB with FP32 inner iterations in FP64
+    refinement (the global-memory path for the BiCGSTAB kinds and the beta
+    field, the on-chip path for CG on uniform grids) against the oracle"""
+    d = golden(name)
+    src = d["source"]
+    g, P = make_poisson(n, case, kind, 50000, 1e-12, src, fixture=d, precision="mixed")
+    assert P.run() == 0
+    assert P.stats.tol_out <= 1e-12 and P.stats.outer_iters >= 1
+    og = oracle_grid(d, n, n, 2)
+    rp, ci, va, b = R.assemble_poisson(og, R.make_bc(*BCS[case]), 1.0, src=src,
+                                       bfield=d.get("beta_field"))
+    if case == "neumann":
+        b = b - b.mean()
+    code, x, it, t, _ = R.krylov_csr(kind, rp, ci, va, b, np.zeros(n * n), 50000, 1e-13)
+    if case == "neumann":
+        x = x - x.mean()
+    assert code == 0
+    err = rel_l2(R.field_to_vec(og, P.phi), x)
+    print(f"{name} {kind} mixed vs oracle: rel-L2 {err:.2e}, "
+          f"{P.stats.iters} FP32 iterations, {P.stats.outer_iters} refinements")
+    assert err <= MIXED_RTOL, err
+
+
+def test_mixed_bicgstab_reaches_tolerance_at_1e8(gpu_lib):
+    """the mixed BiCGSTAB kinds at the headline tolerance on a larger
+    all-Neumann problem: code 0, FP64 residual <= 1e-8, and the FP64 solve's
+    answer to the accuracy that tolerance allows"""
+    rng = np.random.default_rng(11)
+    n = 160
+    src = rng.uniform(-1, 1, (n + 4, n + 4))
+    g64, P64 = make_poisson(n, "neumann", "cg", 20000, 1e-12, src)
+    assert P64.run() == 0
+    for kind in ("dia_bicgstab", "bicgstab"):
+        gm, Pm = make_poisson(n, "neumann", kind, 20000, 1e-8, src, precision="mixed")
+        assert Pm.run() == 0
+        assert Pm.stats.tol_out <= 1e-8
+        err = rel_l2(gm.interior(Pm.phi), g64.interior(P64.phi))
+        assert err < 1e-5, (kind, err)

@@ -9,7 +9,17 @@ import pytest
 
 from conftest import ROOT
 
-REF = os.environ.get("CARPIO_REFERENCE", "/root/reference")
+def reference_dir():
+    """CARPIO_REFERENCE, else the location the oracle's build recipe uses"""
+    ref = os.environ.get("CARPIO_REFERENCE")
+    if ref:
+        return ref
+    r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "print-ref"],
+                       capture_output=True, text=True)
+    return r.stdout.strip()
+
+
+REF = reference_dir()
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "lib", "structure")),

@@ -55,6 +55,18 @@ def test_csr_solvers_bitwise(name):
     check_hist(d, hist)
 
 
+@pytest.mark.parametrize("name", golden_names("csr_"))
+def test_residual_bitwise(name):
+    """carpio::Residual (solver_matrix.hpp:583-597) restated, against the
+    reference's own value on the fixture's start and solution"""
+    d = golden(name)
+    if "aborted" in d:
+        return
+    for xk, rk in (("x0", "residual_x0"), ("x", "residual_x")):
+        r = R.residual(d["rowptr"], d["colind"], d["val"], d[xk], d["b"])
+        assert bits_equal(r, float(d[rk])), (xk, r, float(d[rk]))
+
+
 def oracle_grid(d, nx, ny, gl):
     """the fixture's grid: uniform on [0,1]^2, or (stretch) from the normal
     cells' sizes the reference used"""
