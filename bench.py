@@ -66,6 +66,9 @@ def parse():
     ap.add_argument("--poly-degree", type=int, default=0,
                     help="band-local Chebyshev degree of the FP32 CG (0 default, -1 none)")
     ap.add_argument("--poly-ratio", type=float, default=0.0)
+    ap.add_argument("--precond", default="default",
+                    choices=["default", "chebyshev", "multigrid"],
+                    help="preconditioner of the on-chip FP32 CG")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP64 comparison, Poisson, learned, batched, next-row and CPU legs")
     ap.add_argument("--oracle-steps", type=int, default=3,
@@ -98,14 +101,23 @@ def config(n):
 
 def solver_desc(precision, inner_tol):
     """how our arm solves the projection"""
-    return {"precision": precision, "inner_tol": inner_tol,
-            "fp32_preconditioner": (None if precision != "mixed" else "none" if POLY[0] < 0 else
-                                    f"band-local Chebyshev degree {POLY[0] or 5}, "
-                                    f"interval [2/{POLY[1] or 30:g}, 2] of D^-1 A")}
+    if precision != "mixed":
+        pre = None
+    elif PRECOND[0] in ("multigrid", "default"):
+        pre = ("geometric multigrid V(1,1)-cycle (damped Jacobi, bilinear "
+               "prolongation, restriction its transpose)")
+    elif POLY[0] < 0:
+        pre = "none"
+    else:
+        pre = (f"band-local Chebyshev degree {POLY[0] or 5}, "
+               f"interval [2/{POLY[1] or 30:g}, 2] of D^-1 A")
+    return {"precision": precision, "inner_tol": inner_tol, "fp32_preconditioner": pre}
 
 
-# band-local Chebyshev preconditioner of the FP32 CG: (degree, ratio), 0 = defaults
+# preconditioner of the on-chip FP32 CG: band-local Chebyshev (degree, ratio;
+# 0 = defaults) and the choice between it and the multigrid V-cycle
 POLY = [0, 0.0]
+PRECOND = ["default"]
 
 
 def make_cavity(n, precision, inner_tol):
@@ -125,7 +137,8 @@ def make_cavity(n, precision, inner_tol):
     ns.set_uniform_rho(RE)
     ns.set_diffusion_number(0.25, 1.0 / RE)
     ns.set_projection_solver("CG", 200000, TOL, precision=precision,
-                             inner_tol=inner_tol, poly_degree=POLY[0], poly_ratio=POLY[1])
+                             inner_tol=inner_tol, poly_degree=POLY[0], poly_ratio=POLY[1],
+                             precond=PRECOND[0])
     ns.initial()
     return g, ns
 
@@ -196,7 +209,10 @@ def peaks():
 
 
 def poly_degree():
-    """degree of the FP32 CG's band-local Chebyshev preconditioner in use"""
+    """degree of the FP32 CG's band-local Chebyshev preconditioner in use
+    (-1: the multigrid V-cycle)"""
+    if PRECOND[0] in ("multigrid", "default"):
+        return -1
     return 0 if POLY[0] < 0 else (POLY[0] or 5)
 
 
@@ -211,10 +227,18 @@ def solve_bytes(precision, inner, outer, deg=0):
     one more for the first residual; FP64 CG iteration 80 B.
     Preconditioner, per FP32 iteration: first Chebyshev step 20 B (read r,
     D; write d, z, r_k), each further step 28 B (read d, r_k, z, D; write d,
-    r_k, z), the (r, z) dot 8 B."""
+    r_k, z), the (r, z) dot 8 B; the multigrid V-cycle (deg = -1) 32 B per
+    fine cell (write r and the pre-smoothed z; read z and D, write the
+    residual; read it for the restriction; read z and D for the post-
+    smoothing) and a quarter of that again per coarser level (x 4/3)."""
     if precision == "mixed":
         krylov = 40 * inner + 40 * (outer + 1)
-        pre = (20 + 28 * (deg - 1) + 8) * inner if deg > 0 else 0
+        if deg > 0:
+            pre = (20 + 28 * (deg - 1) + 8) * inner
+        elif deg < 0:
+            pre = 32 * 4 / 3 * inner
+        else:
+            pre = 0
         return krylov, pre
     return 80 * inner, 0
 
@@ -323,6 +347,7 @@ def main():
         run_reference(a)
         return
     POLY[0], POLY[1] = a.poly_degree, a.poly_ratio
+    PRECOND[0] = a.precond
     if a.accuracy_steps > 0:
         accuracy_run(a)
         return
@@ -414,7 +439,8 @@ def main():
         out["roofline"]["note"] = (
             "the Krylov vectors stay in shared memory and registers: DRAM "
             "traffic is `traffic`, far below the algorithmic bytes; the kernel "
-            "is bound by grid all-reduce latency, two per FP32 iteration")
+            "is bound by grid synchronisation latency (two all-reduces per FP32 "
+            "iteration, and with the multigrid V-cycle its grid barriers)")
     # e2e through the public API with host buffers: the timed steps again,
     # from the same starting state, each step copying the whole state in
     # from pinned host memory and back out
@@ -649,7 +675,8 @@ def poisson_leg(n, inner_tol):
         P = S.Poisson(g)
         P.set_depend(g.zeros(), None, src)
         P.set_solver("CG", None, 200000, TOL, mean_removal=True, precision=prec,
-                     inner_tol=inner_tol, poly_degree=POLY[0], poly_ratio=POLY[1])
+                     inner_tol=inner_tol, poly_degree=POLY[0], poly_ratio=POLY[1],
+                     precond=PRECOND[0])
         P.run()   # warm-up
         P.set_depend(g.zeros(), None, src)
         rc = P.run()

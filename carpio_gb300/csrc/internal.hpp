@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <atomic>
 #include <mutex>
+#include <utility>
 #include <vector>
 
 #include "../../include/carpio_gpu.h"
@@ -91,11 +92,20 @@ struct StencilCoeffs {
 	bool uniform = true;          // rows described by ax / ay
 	bool bfield_free = true;      // built without a beta field
 	DevBuf cf, cf32;              // otherwise: per-cell coefficients x-, x+, y-, y+
+	// multigrid preconditioner of the on-chip path (uniform grids without the
+	// Helmholtz term): level sizes, the number of global-memory levels (0:
+	// the grid does not coarsen far enough), the interior face coefficients
+	// and every level's diagonal, concatenated
+	std::vector<std::pair<int, int> > mg_dims;
+	int mg_nlev = 0;
+	float mg_cx = 0.f, mg_cy = 0.f;
+	DevBuf mgD;
 };
 
 struct PoissonWs {
 	LaunchWs lw;
 	DevBuf v64, v32, src, phi, hist, out, xbuf;
+	DevBuf mg;   // multigrid level vectors
 };
 
 // bfield: a variable beta (StencilPoisson_ with a beta field, face values

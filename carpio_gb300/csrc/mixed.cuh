@@ -143,6 +143,10 @@ __device__ int inner_bicgstab(const Sp& sp, const MixedT<Op32>& m, int inv,
 		}
 		if (!grid_allreduce<float, 1>(rv, gc, bank)) return -1;
 		alpha = rho_1 / rv[0];
+		// (rt, v) = 0 in FP32: a breakdown the FP64 recurrences would not
+		// meet at these sizes; stop with the iterate so far (the next
+		// refinement restarts from the true residual)
+		if (!isfinite(alpha)) { *brk = 2; break; }
 		float ss[1] = { 0 };
 		KLOOP(sp) {
 			int a = sp.addr(k);
@@ -167,6 +171,12 @@ __device__ int inner_bicgstab(const Sp& sp, const MixedT<Op32>& m, int inv,
 		}
 		if (!grid_allreduce<float, 2>(ts, gc, bank)) return -1;
 		omega = ts[0] / ts[1];
+		if (!isfinite(omega)) {
+			// t = 0: keep the half step x + alpha ph and stop
+			KLOOP(sp) { int a = sp.addr(k); f.x[a] = fmaf(alpha, f.ph[a], f.x[a]); }
+			*brk = 3;
+			break;
+		}
 		float rr[2] = { 0, 0 };
 		KLOOP(sp) {
 			int a = sp.addr(k);
@@ -219,6 +229,7 @@ __device__ void mixed_run(const Sp& sp, const Op64& op,
 		if (!grid_allreduce<double, 3>(rs, gc, bank)) return;
 		resid = sqrt(rs[0]) / normb;
 		hist_push(sc, hl, resid);
+		if (!(resid == resid)) break;   // NaN: code 1 with the NaN residual
 		if (resid <= sc.tol) {
 			if (blockIdx.x == 0 && threadIdx.x == 0) { sc.out->outer = outer; sc.out->inner = total; }
 			finish(sc, 0, total, resid, hl);

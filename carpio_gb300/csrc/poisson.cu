@@ -10,6 +10,7 @@
 #include "internal.hpp"
 #include "poisson_rhs.cuh"
 #include "mixed.cuh"
+#include "mg.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -102,6 +103,7 @@ struct TileArgs {
 	float* xbuf;           // [3][C][2][ny]: band edge rows of r (two iteration
 	                       // parities), then of r after a residual replacement
 	int rows_max;
+	MgArgs mg;             // the multigrid preconditioner (mg.nlev > 0)
 };
 
 __device__ __forceinline__ int band_lo(int c, int C, int nx) {
@@ -139,9 +141,15 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	// rhal); the Chebyshev directions, two buffers in the layout of p with
 	// zero halo rows (one read, one written per step)
 	const int K = m.pdeg;
-	float* zs = K > 0 ? dd + ta.rows_max * ny : rs;
+	const MgArgs& mg = ta.mg;
+	const bool use_mg = mg.nlev > 0;
+	float* zs = (K > 0 || use_mg) ? dd + ta.rows_max * ny : rs;
 	float* dsa = zs + ta.rows_max * ny;    // dsa[1 + (lr + 1) * ny + j]
 	float* dsb = dsa + np;
+	// multigrid (K == 0 then): the corrected fine values of the band and its
+	// halo rows in the place of dsa, then the shared-memory coarse levels
+	float* mgc = dsa;
+	float* mgsm = mgc + np;
 	const bool up = c > 0, down = c < C - 1;
 	const size_t edge = (size_t)2 * C * ny;   // one edge region
 	float* rbuf = ta.xbuf + 2 * edge;         // r edges
@@ -260,6 +268,109 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				}
 			}
 	};
+	// z = M r with M one multigrid V-cycle (mg.cuh); (r, z) and (r, r) of
+	// the band in g. Every CTA passes the same grid barriers.
+	auto precond_mg = [&](float (&g)[2]) -> bool {
+		const float w = mg.omega, cx = mg.cx, cy = mg.cy;
+		const LdL2 gld;
+		const MgLevel& L0 = mg.lev[0];
+		// level 0: R0 = r and the pre-smoothed Z0 = w r / D0 of the band
+#pragma unroll
+		for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+			for (int k = 0; k < NC; ++k) {
+				const int j = tid + k * T;
+				if (lr < rows && j < ny) {
+					const int k0 = (r0 + lr) * ny + j;
+					const float rv = rs[lr * ny + j];
+					__stcg(L0.R + k0, rv);
+					__stcg(L0.Z + k0, w * rv / __ldg(L0.D + k0));
+				}
+			}
+		if (!grid_sync(gc)) return false;
+#pragma unroll
+		for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+			for (int k = 0; k < NC; ++k) {
+				const int j = tid + k * T;
+				if (lr < rows && j < ny) {
+					const int i = r0 + lr;
+					__stcg(L0.S + i * ny + j, rs[lr * ny + j]
+							- mg_apply(gld, L0.Z, L0.D, i, j, nx, ny, cx, cy));
+				}
+			}
+		if (!grid_sync(gc)) return false;
+		const int gt = c * T + tid, G = C * T;
+		for (int l = 1; l < mg.nlev; ++l) {
+			const MgLevel& F = mg.lev[l - 1];
+			const MgLevel& L = mg.lev[l];
+			const int n = L.nx * L.ny;
+			for (int k = gt; k < n; k += G) {
+				const int I = k / L.ny, J = k - I * L.ny;
+				const float rv = mg_restrict(gld, F.S, I, J, F.nx, F.ny);
+				__stcg(L.R + k, rv);
+				__stcg(L.Z + k, w * rv / __ldg(L.D + k));
+			}
+			if (!grid_sync(gc)) return false;
+			for (int k = gt; k < n; k += G) {
+				const int I = k / L.ny, J = k - I * L.ny;
+				__stcg(L.S + k, ldcg(L.R + k) - mg_apply(gld, L.Z, L.D, I, J, L.nx, L.ny, cx, cy));
+			}
+			if (!grid_sync(gc)) return false;
+		}
+		if (c == 0) mg_coarse(mg, mgsm);
+		if (!grid_sync(gc)) return false;
+		for (int l = mg.nlev - 1; l >= 1; --l) {
+			const MgLevel& L = mg.lev[l];
+			const MgLevel& Cl = mg.lev[l + 1];
+			const int n = L.nx * L.ny;
+			for (int k = gt; k < n; k += G) {
+				const int I = k / L.ny, J = k - I * L.ny;
+				__stcg(L.Zp + k, mg_post(gld, L.Z, Cl.Zp, L.R, L.D, I, J, L.nx, L.ny, cx, cy, w));
+			}
+			if (!grid_sync(gc)) return false;
+		}
+		// level 0: c = Z0 + P z1 on the band and its halo rows, then the
+		// post-smoothed z of the band
+		const MgLevel& L1 = mg.lev[1];
+		for (int t = tid; t < (rows + 2) * ny; t += T) {
+			const int lr = t / ny - 1, j = t - (lr + 1) * ny;
+			const int i = r0 + lr;
+			mgc[t] = (i >= 0 && i < nx)
+					? mg_corrected(gld, L0.Z, L1.Zp, i, j, ny, L1.nx, L1.ny) : 0.f;
+		}
+		__syncthreads();
+		g[0] = g[1] = 0.f;
+#pragma unroll
+		for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+			for (int k = 0; k < NC; ++k) {
+				const int j = tid + k * T;
+				if (lr < rows && j < ny) {
+					const int i = r0 + lr, cc = lr * ny + j, pk = (lr + 1) * ny + j;
+					const float cv = mgc[pk];
+					const float d = __ldg(L0.D + i * ny + j);
+					float ac = d * cv;
+					if (i > 0) ac = fmaf(cx, mgc[pk - ny], ac);
+					if (i < nx - 1) ac = fmaf(cx, mgc[pk + ny], ac);
+					if (j > 0) ac = fmaf(cy, mgc[pk - 1], ac);
+					if (j < ny - 1) ac = fmaf(cy, mgc[pk + 1], ac);
+					const float rv = rs[cc];
+					const float z = fmaf(w, (rv - ac) / d, cv);
+					zs[cc] = z;
+					g[0] = fmaf(rv, z, g[0]);
+					g[1] = fmaf(rv, rv, g[1]);
+				}
+			}
+		return true;
+	};
+	// the preconditioner in use: multigrid, the band-local polynomial, or
+	// none (z = r)
+	auto apply_m = [&](float (&g)[2]) -> bool {
+		if (use_mg) return precond_mg(g);
+		if (K > 0) precond(g);
+		return true;
+	};
 	// the neighbours' edge rows of region `src` into the halo rows of z.
 	// Thread t writes entries t and ny + t, the same mapping every reader of
 	// rhal uses, so no barrier is needed between the write and the reads.
@@ -318,7 +429,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				}
 			}
 		float g[2] = { rr, rr };
-		if (K > 0) precond(g);
+		if (!apply_m(g)) return false;
 		__syncthreads();
 		publish_r();
 		if (!grid_allreduce<float, 2>(g, gc, bank)) return false;
@@ -425,7 +536,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				}
 			}
 		float gn[2] = { rr, rr };
-		if (K > 0) precond(gn);
+		if (!apply_m(gn)) return;
 		float* ebuf = ta.xbuf + (size_t)par * edge;
 #pragma unroll
 		for (int k = 0; k < NC; ++k) {
@@ -752,6 +863,45 @@ int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
 		if ((rc = to_device(c.cf, cf.data(), sizeof(double) * cf.size(), s))) return rc;
 		if ((rc = to_device(c.cf32, cf32.data(), sizeof(float) * cf32.size(), s))) return rc;
 	}
+	// multigrid levels (uniform grids, no Helmholtz term): sizes halved
+	// while both sides are even, down to a level of at most kMgGather cells
+	c.mg_nlev = 0;
+	c.mg_dims.clear();
+	std::vector<float> mgd;
+	if (uniform && !helm && g->nx >= 2 && g->ny >= 2) {
+		c.mg_dims.push_back({ g->nx, g->ny });
+		while ((int)c.mg_dims.size() < kMgMaxLev) {
+			const int a = c.mg_dims.back().first, b = c.mg_dims.back().second;
+			if ((a & 1) || (b & 1)) break;
+			c.mg_dims.push_back({ a / 2, b / 2 });
+		}
+		for (size_t l = 1; l < c.mg_dims.size(); ++l)
+			if ((long)c.mg_dims[l].first * c.mg_dims[l].second <= kMgGather) {
+				c.mg_nlev = (int)l;
+				break;
+			}
+		// the interior face coefficients (equal on every face of a uniform
+		// grid up to the rounding of the centre distances)
+		const double cxd = ax[g->nx / 2], cyd = ay[g->ny / 2];
+		c.mg_cx = (float)cxd;
+		c.mg_cy = (float)cyd;
+		// each level's diagonal: every face contributes -c; a boundary face
+		// folds like the fine grid's ghost substitution (Dirichlet: -2c in
+		// all, Neumann: 0)
+		for (const auto& dm : c.mg_dims) {
+			for (int I = 0; I < dm.first; ++I)
+				for (int J = 0; J < dm.second; ++J) {
+					double d = 0.0;
+					d += I > 0 ? -cxd : (bc.type[0] == 1 ? -2.0 * cxd : 0.0);
+					d += I < dm.first - 1 ? -cxd : (bc.type[1] == 1 ? -2.0 * cxd : 0.0);
+					d += J > 0 ? -cyd : (bc.type[2] == 1 ? -2.0 * cyd : 0.0);
+					d += J < dm.second - 1 ? -cyd : (bc.type[3] == 1 ? -2.0 * cyd : 0.0);
+					mgd.push_back((float)d);
+				}
+		}
+		if (c.mg_nlev > 0 && (rc = to_device(c.mgD, mgd.data(), sizeof(float) * mgd.size(), s)))
+			return rc;
+	}
 	CG_CK(cudaStreamSynchronize(s));  // host vectors go out of scope
 	c.uniform = uniform;
 	c.bfield_free = !bfield;
@@ -940,10 +1090,57 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 			                         : (const void*)k_poisson_mixed_tile<SRC_FIELD, NC_, RM_>;
 		TILE_PICK(1, 4) TILE_PICK(1, 16) TILE_PICK(2, 8) TILE_PICK(4, 4)
 #undef TILE_PICK
-		const int pdeg = cfg.poly_degree < 0 ? 0 : (cfg.poly_degree == 0 ? kPolyDegree : cfg.poly_degree);
+		int pdeg = cfg.poly_degree < 0 ? 0 : (cfg.poly_degree == 0 ? kPolyDegree : cfg.poly_degree);
 		const size_t np = (size_t)(rows_max + 2) * g->ny + 2;
-		size_t smem = sizeof(float) * (np + 2 * (size_t)g->ny + (size_t)rows_max * g->ny
+		const size_t base = sizeof(float) * (np + 2 * (size_t)g->ny + (size_t)rows_max * g->ny
 				+ rows_max + 1 + g->ny + 1 + (size_t)rows_max * g->ny);
+		TileArgs ta;
+		std::memset(&ta, 0, sizeof ta);
+		size_t smem = base;
+		// the multigrid V-cycle where asked for and the grid allows it
+		bool mg = false;
+		if (cfg.precond != CARPIO_GPU_PRECOND_CHEBYSHEV && c.mg_nlev > 0) {
+			size_t coarse = 0, work = 0;
+			const int ntot = (int)c.mg_dims.size();
+			for (int l = c.mg_nlev; l < ntot; ++l)
+				coarse += 3 * (size_t)c.mg_dims[l].first * c.mg_dims[l].second;
+			const size_t msmem = base + sizeof(float) * ((size_t)rows_max * g->ny + np + coarse);
+			for (int l = 0; l <= c.mg_nlev; ++l)
+				work += (l == 0 ? 3 : l < c.mg_nlev ? 4 : 1)
+						* (size_t)c.mg_dims[l].first * c.mg_dims[l].second;
+			if (msmem <= 220 * 1024) {
+				if ((rc = w.mg.ensure(sizeof(float) * work))) return rc;
+				MgArgs& m = ta.mg;
+				m.nlev = c.mg_nlev;
+				m.ntot = ntot;
+				m.cx = c.mg_cx;
+				m.cy = c.mg_cy;
+				m.omega = 0.8f;
+				const float* dp = c.mgD.as<float>();
+				float* wp = w.mg.as<float>();
+				for (int l = 0; l < ntot; ++l) {
+					const size_t n = (size_t)c.mg_dims[l].first * c.mg_dims[l].second;
+					MgLevel& L = m.lev[l];
+					L.nx = c.mg_dims[l].first;
+					L.ny = c.mg_dims[l].second;
+					L.D = dp;
+					dp += n;
+					if (l == 0) {
+						L.R = wp; L.Z = wp + n; L.S = wp + 2 * n;
+						wp += 3 * n;
+					} else if (l < c.mg_nlev) {
+						L.R = wp; L.Z = wp + n; L.S = wp + 2 * n; L.Zp = wp + 3 * n;
+						wp += 4 * n;
+					} else if (l == c.mg_nlev) {
+						L.Zp = wp;
+						wp += n;
+					}
+				}
+				smem = msmem;
+				pdeg = 0;
+				mg = true;
+			}
+		}
 		if (pdeg > 0) smem += sizeof(float) * ((size_t)rows_max * g->ny + 2 * np);
 		mx.pdeg = pdeg;
 		mx.pratio = (float)(cfg.poly_ratio > 1.0 ? cfg.poly_ratio : kPolyRatio);
@@ -954,12 +1151,14 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 			if (per_sm >= 1) {
 				if ((rc = w.lw.ensure(C))) return rc;
 				if ((rc = w.xbuf.ensure(sizeof(float) * 6 * (size_t)C * g->ny))) return rc;
-				TileArgs ta;
 				ta.xbuf = w.xbuf.as<float>();
 				ta.rows_max = rows_max;
-				// the preconditioned FP32 CG stops tracking its residual
-				// sooner: replace it after a 1e-1 reduction
-				mx.inner_tol = cfg.inner_tol > 0 ? cfg.inner_tol : (pdeg > 0 ? 1e-1 : 3e-2);
+				// the polynomial-preconditioned FP32 CG stops tracking its
+				// residual sooner: replace it after a 1e-1 reduction; with
+				// the V-cycle each iteration gains about a digit, so after
+				// 1e-2 (the smallest step allowed on chip)
+				mx.inner_tol = cfg.inner_tol > 0 ? cfg.inner_tol
+				                                 : (mg ? 1e-2 : pdeg > 0 ? 1e-1 : 3e-2);
 				GridCtl gc = make_gridctl(w.lw);
 				CG_CK(cudaMemsetAsync(w.lw.ctl.p, 0, sizeof(Ctl), s));
 				CG_CK(cudaMemsetAsync(out_dev, 0, sizeof(cg_dev::SolveOut), s));

@@ -164,10 +164,11 @@ class BoundaryIndex:
 
 def solver_cfg(name="CG", max_iter=1000, tol=1e-3, mean_removal=False,
                precision="fp64", inner_tol=0.0, inner_max_iter=0, flags=0,
-               poly_degree=0, poly_ratio=0.0):
+               poly_degree=0, poly_ratio=0.0, precond="default"):
     c = _lib.SolverCfg()
     c.poly_degree = int(poly_degree)
     c.poly_ratio = float(poly_ratio)
+    c.precond = _lib.PRECOND[precond]
     c.kind = _lib.KINDS[name]
     c.precision = _lib.MIXED if precision == "mixed" else _lib.FP64
     c.max_iter = int(max_iter)
@@ -374,9 +375,10 @@ class NS_explicit:
         """NS_::set_projection_solver (s_ns.hpp:120-130). "CG" is the
         drop-in (with mean removal by default); "IC_CGS" / "IC_CG" are the
         reference's shipped solvers (Solver_IC_CGS_, s_solver.hpp:329-352,
-        removes no mean), FP64 only."""
+        removes no mean), FP64 only; "Dia_BiCGSTAB" / "BiCGSTAB" as the
+        drop-in's other kinds (mean removal by default)."""
         if mean_removal is None:
-            mean_removal = name == "CG"
+            mean_removal = name in ("CG", "Dia_BiCGSTAB", "BiCGSTAB")
         self.proj = solver_cfg(name, max_iter, tol, mean_removal=mean_removal,
                                precision=precision, **kw)
 

@@ -201,7 +201,20 @@ typedef struct {
 	                      < 0 = none (plain CG) */
 	double poly_ratio; /* its eigenvalue interval [2 / ratio, 2] of D^-1 A;
 	                      0 = 30 */
+	int precond;       /* MIXED, on-chip path: preconditioner of the FP32 CG.
+	                      CARPIO_GPU_PRECOND_MULTIGRID: one geometric-
+	                      multigrid V(1,1)-cycle (damped Jacobi smoothing,
+	                      bilinear prolongation, restriction its transpose)
+	                      on grids whose sides halve down to at most 1024
+	                      cells, without the Helmholtz term; other grids take
+	                      the polynomial. CARPIO_GPU_PRECOND_CHEBYSHEV: the
+	                      band-local polynomial above. CARPIO_GPU_PRECOND_DEFAULT
+	                      (0): the multigrid cycle where it applies. */
 } carpio_gpu_solver_cfg;
+
+#define CARPIO_GPU_PRECOND_DEFAULT 0
+#define CARPIO_GPU_PRECOND_CHEBYSHEV 1
+#define CARPIO_GPU_PRECOND_MULTIGRID 2
 
 typedef struct {
 	int code;          /* solver code (0..3) or negative error */

@@ -7,6 +7,14 @@
         one batched persistent solve of COUNT all-Neumann N x N problems with
         Gaussian sources to 1e-8 (thread-block clusters of 16 CTAs)
 
+    python profile_cases.py advect N STEPS
+        STEPS steps of the stand-alone Advection_ on N x N (rotating cone,
+        van Leer): k_advect_band over all SMs (or k_advect on one block)
+    python profile_cases.py ic N KIND
+        one structure-level IC_CGS / IC_CG solve of an N x N Dirichlet-0
+        Poisson problem with a unit source to 1e-8 (level-scheduled factor
+        solves)
+
 Each prints one line with its timing and exits 0 on success.
 """
 import os
@@ -44,12 +52,33 @@ def batch(count, n):
           f"{1000 * st['ms'] / max(st['iters'], 1):.2f} us/iteration")
 
 
+def advect(n, steps):
+    import time
+    import bench
+    g, eq = bench.advection_case(n)
+    t0 = time.perf_counter()
+    eq.run(steps)
+    ms = 1e3 * (time.perf_counter() - t0) / steps
+    print(f"advect {n}x{n}: {ms:.2f} ms per step")
+
+
+def ic(n, kind):
+    import bench
+    g, p = bench.ic_case(n, kind)
+    rc = p.run()
+    print(f"{kind} {n}x{n}: code {rc}, {p.stats.iters} iterations, {p.stats.ms:.2f} ms")
+
+
 def main(argv=None):
     a = list(sys.argv[1:] if argv is None else argv)
     if a[:1] == ["unet"] and len(a) == 2:
         unet(int(a[1]))
     elif a[:1] == ["batch"] and len(a) == 3:
         batch(int(a[1]), int(a[2]))
+    elif a[:1] == ["advect"] and len(a) == 3:
+        advect(int(a[1]), int(a[2]))
+    elif a[:1] == ["ic"] and len(a) == 3:
+        ic(int(a[1]), a[2])
     else:
         sys.exit(__doc__)
 

@@ -84,9 +84,9 @@ def test_ctypes_structs_match_header_layout():
     from carpio_gb300 import _lib
     assert ctypes.sizeof(_lib.BC) == 4 * 4 + 4 * 8
     # int kind, precision, max_iter; double tol; int mean; double inner_tol;
-    # int inner_max; uint32 flags; int poly_degree; double poly_ratio
-    # (natural alignment)
-    assert ctypes.sizeof(_lib.SolverCfg) == 64
+    # int inner_max; uint32 flags; int poly_degree; double poly_ratio;
+    # int precond (natural alignment)
+    assert ctypes.sizeof(_lib.SolverCfg) == 72
     assert ctypes.sizeof(_lib.SolverStats) == 32
 
 

@@ -247,3 +247,71 @@ def test_mixed_bicgstab_reaches_tolerance_at_1e8(gpu_lib):
         assert Pm.stats.tol_out <= 1e-8
         err = rel_l2(gm.interior(Pm.phi), g64.interior(P64.phi))
         assert err < 1e-5, (kind, err)
+
+
+@pytest.mark.parametrize("case,nx,ny", [("neumann", 64, 64), ("c1", 64, 64),
+                                        ("mixed", 32, 32), ("neumann", 64, 32),
+                                        ("mixed", 48, 48), ("neumann", 256, 256),
+                                        ("c1", 128, 64)])
+def test_multigrid_preconditioner_against_oracle(gpu_lib, case, nx, ny):
+    """The on-chip FP32 CG with the geometric-multigrid V-cycle as its
+    preconditioner, in FP64 refinement to 1e-12, against the oracle's FP64
+    CG to 1e-13: relative L2 <= 1e-9 (as the other mixed solves), and a
+    preconditioner that works: a few dozen FP32 iterations where plain CG
+    needs hundreds."""
+    from carpio_gb300 import structure as S
+    rng = np.random.default_rng(nx * 7 + ny)
+    g = S.Grid((0.0, 0.0), (1.0, 1.0), (nx, ny), 2)
+    src = rng.uniform(-1, 1, g.N())
+    P = S.Poisson(g)
+    types, vals = BCS[case]
+    for seg in range(4):
+        bc = S.BoundaryCondition()
+        (bc.set_default_1_bc if types[seg] == 1 else bc.set_default_2_bc)(vals[seg])
+        P.add_bc(0, seg, "phi", bc)
+    P.set_depend(g.zeros(), None, src)
+    P.set_solver("CG", None, 50000, 1e-12, mean_removal=(case == "neumann"),
+                 precision="mixed", precond="multigrid")
+    assert P.run() == 0
+    assert P.stats.tol_out <= 1e-12
+    og = R.Grid(nx, ny, 2)
+    rp, ci, va, b = R.assemble_poisson(og, R.make_bc(types, vals), 1.0, src=src)
+    if case == "neumann":
+        b = b - b.mean()
+    code, x, it, t, _ = R.krylov_csr("cg", rp, ci, va, b, np.zeros(nx * ny), 50000, 1e-13)
+    if case == "neumann":
+        x = x - x.mean()
+    assert code == 0
+    err = rel_l2(R.field_to_vec(og, P.phi), x)
+    print(f"multigrid {case} {nx}x{ny}: rel-L2 {err:.2e}, {P.stats.iters} FP32 "
+          f"iterations, {P.stats.outer_iters} refinements (plain CG: {it})")
+    assert err <= MIXED_RTOL, err
+    assert P.stats.iters <= max(60, it // 5), (P.stats.iters, it)
+
+
+@pytest.mark.parametrize("case,n", [("neumann", 48), ("mixed", 24), ("neumann", 128)])
+def test_chebyshev_preconditioner_against_oracle(gpu_lib, case, n):
+    """the on-chip FP32 CG with the band-local Chebyshev polynomial instead
+    of the V-cycle, in FP64 refinement to 1e-12, against the oracle"""
+    from carpio_gb300 import structure as S
+    rng = np.random.default_rng(n)
+    g = S.Grid((0.0, 0.0), (1.0, 1.0), (n, n), 2)
+    src = rng.uniform(-1, 1, g.N())
+    P = S.Poisson(g)
+    types, vals = BCS[case]
+    for seg in range(4):
+        bc = S.BoundaryCondition()
+        (bc.set_default_1_bc if types[seg] == 1 else bc.set_default_2_bc)(vals[seg])
+        P.add_bc(0, seg, "phi", bc)
+    P.set_depend(g.zeros(), None, src)
+    P.set_solver("CG", None, 50000, 1e-12, mean_removal=(case == "neumann"),
+                 precision="mixed", precond="chebyshev")
+    assert P.run() == 0
+    og = R.Grid(n, n, 2)
+    rp, ci, va, b = R.assemble_poisson(og, R.make_bc(types, vals), 1.0, src=src)
+    if case == "neumann":
+        b = b - b.mean()
+    code, x, it, t, _ = R.krylov_csr("cg", rp, ci, va, b, np.zeros(n * n), 50000, 1e-13)
+    if case == "neumann":
+        x = x - x.mean()
+    assert rel_l2(R.field_to_vec(og, P.phi), x) <= MIXED_RTOL
