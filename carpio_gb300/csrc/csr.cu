@@ -36,7 +36,7 @@ __global__ void k_to_float(const double* a, float* b, int n) {
 		b[i] = (float)a[i];
 }
 
-__global__ void __launch_bounds__(kThreads) k_csr_solve_ic(CsrOp op, IcOp ic,
+__global__ void __launch_bounds__(1024) k_csr_solve_ic(CsrOp op, IcOp ic,
 		Vecs<double> v, SolveCtl sc, GridCtl gc) {
 	gc.start();
 	int bank = 0;
@@ -95,6 +95,7 @@ struct CsrWs {
 	cg_host::LaunchWs lw;
 	cg_host::DevBuf rp, ci, va, vec, hist;
 	cg_host::DevBuf icd, icu[3], icl[3], icf[2], icb[2];   // IC factor, levels
+	cg_host::DevBuf ick[2], icn[2], icc[2], icv[2];         // packed level rows
 	cg_host::DevBuf rx, rb, rpart;   // Residual: staged x, b; partials + result
 	cg_host::DevBuf va32, vec32;     // MIXED: FP32 values and vectors
 };
@@ -298,6 +299,43 @@ extern "C" int carpio_gpu_krylov_csr(int kind, int n, int nnz,
 		const double t1 = nlev * 0.15 + 10.0 * n / kThreads * 0.05;
 		const double tb = nlev * 1.5 + 10.0 * ((double)n / ((double)blocks * kThreads) * 0.05 + 1.5);
 		if (t1 < tb) blocks = 1;
+		// one block whose vector fits in shared memory: the level sweeps
+		// run there on rows packed in level order (ic.cuh ic_apply_smem)
+		if (blocks == 1 && sizeof(double) * (size_t)n <= 200 * 1024) {
+			for (int pass = 0; pass < 2; ++pass) {
+				const std::vector<uint32_t>& rows = pass == 0 ? frows : brows;
+				const std::vector<uint32_t>& ep = pass == 0 ? lp : up;
+				const std::vector<uint32_t>& ec = pass == 0 ? li : ui;
+				const std::vector<double>& ev = pass == 0 ? lv : uv;
+				const size_t np = rows.size();
+				std::vector<uint32_t> pk(np), pc(np * kIcInline, 0);
+				std::vector<int> pn(np);
+				std::vector<double> pv(np * kIcInline, 0.0);
+				for (size_t t = 0; t < np; ++t) {
+					const uint32_t k = rows[t];
+					pk[t] = k;
+					pn[t] = (int)(ep[k + 1] - ep[k]);
+					for (uint32_t e = ep[k], m = 0; e < ep[k + 1] && m < (uint32_t)kIcInline; ++e, ++m) {
+						pc[t * kIcInline + m] = ec[e];
+						pv[t * kIcInline + m] = ev[e];
+					}
+				}
+				if ((rc = put(w.ick[pass], pk.data(), sizeof(uint32_t) * np))) return rc;
+				if ((rc = put(w.icn[pass], pn.data(), sizeof(int) * np))) return rc;
+				if ((rc = put(w.icc[pass], pc.data(), sizeof(uint32_t) * pc.size()))) return rc;
+				if ((rc = put(w.icv[pass], pv.data(), sizeof(double) * pv.size()))) return rc;
+				CG_CK(cudaStreamSynchronize(s));
+			}
+			icop.smem = 1;
+			icop.fk = w.ick[0].as<uint32_t>();
+			icop.bk = w.ick[1].as<uint32_t>();
+			icop.fn = w.icn[0].as<int>();
+			icop.bn = w.icn[1].as<int>();
+			icop.fc = w.icc[0].as<uint32_t>();
+			icop.bc = w.icc[1].as<uint32_t>();
+			icop.fv = w.icv[0].as<double>();
+			icop.bv = w.icv[1].as<double>();
+		}
 	}
 	SolveCtl sc;
 	sc.kind = kind;
@@ -310,8 +348,16 @@ extern "C" int carpio_gpu_krylov_csr(int kind, int n, int nnz,
 	GridCtl gc = make_gridctl(w.lw);
 	if (ic) {
 		void* args[] = { &op, &icop, &v, &sc, &gc };
-		CG_CK(cudaLaunchCooperativeKernel((const void*)k_csr_solve_ic, blocks,
-				kThreads, args, 0, s));
+		if (icop.smem) {
+			// one block of 1024 threads with the vector in shared memory
+			const int sm = (int)(sizeof(double) * (size_t)n);
+			CG_CK(cudaFuncSetAttribute((const void*)k_csr_solve_ic,
+					cudaFuncAttributeMaxDynamicSharedMemorySize, sm));
+			CG_CK(cudaLaunchCooperativeKernel((const void*)k_csr_solve_ic, 1, 1024, args, sm, s));
+		} else {
+			CG_CK(cudaLaunchCooperativeKernel((const void*)k_csr_solve_ic, blocks,
+					kThreads, args, 0, s));
+		}
 	} else if (mixed) {
 		// FP32 copies of the values; 13 FP32 vectors (CG uses four)
 		if ((rc = w.va32.ensure(sizeof(float) * (size_t)(nnz ? nnz : 1)))) return rc;

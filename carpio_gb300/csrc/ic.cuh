@@ -16,6 +16,8 @@ namespace cg_dev {
 // i < k that update k (lp/li/lv, i ascending, i.e. the reference's order of
 // updates); backward solve per row i: its off-diagonal entries (up/ui/uv,
 // columns ascending).
+constexpr int kIcInline = 4;   // entries of a row packed inline (one block)
+
 struct IcOp {
 	int n;
 	const double* d;                                  // val_[pntr_[i]]
@@ -23,7 +25,99 @@ struct IcOp {
 	const uint32_t *up, *ui; const double* uv;
 	const uint32_t *fptr, *frows; int nfl;            // forward levels
 	const uint32_t *bptr, *brows; int nbl;            // backward levels
+	// one-block launches: the solve vector in shared memory, and every
+	// level position's row packed (row, diagonal, entry count, up to
+	// kIcInline (column, value) pairs; longer rows read the lists above)
+	// so that the next level's data loads while the current level runs
+	int smem;                                         // 1: use the path below
+	const uint32_t *fk, *bk;                          // row of each position
+	const int *fn, *bn;                               // its entry count
+	const uint32_t *fc, *bc;                          // [position][kIcInline]
+	const double *fv, *bv;
 };
+
+// One level position's packed row, loaded ahead of its level.
+struct IcRow {
+	uint32_t k;
+	int cnt;
+	double d;
+	uint32_t c[kIcInline];
+	double v[kIcInline];
+};
+
+__device__ __forceinline__ void ic_load_row(const IcOp& ic, bool fwd, uint32_t pos, IcRow& r) {
+	const uint32_t* K = fwd ? ic.fk : ic.bk;
+	const int* N = fwd ? ic.fn : ic.bn;
+	const uint32_t* Cc = fwd ? ic.fc : ic.bc;
+	const double* V = fwd ? ic.fv : ic.bv;
+	r.k = __ldg(K + pos);
+	r.cnt = __ldg(N + pos);
+	r.d = __ldg(ic.d + r.k);
+#pragma unroll
+	for (int m = 0; m < kIcInline; ++m) {
+		r.c[m] = __ldg(Cc + (size_t)pos * kIcInline + m);
+		r.v[m] = __ldg(V + (size_t)pos * kIcInline + m);
+	}
+}
+
+// ic_apply on one block with the vector in shared memory (sm: n doubles).
+// The operations and their order are those of the global-memory path.
+__device__ void ic_apply_smem(const IcOp& ic, const double* in, double* out, double* sm) {
+	const int T = blockDim.x, tid = threadIdx.x;
+	for (int t = tid; t < ic.n; t += T) sm[t] = ldcg(in + t);
+	__syncthreads();
+	for (int pass = 0; pass < 2; ++pass) {
+		const bool fwd = pass == 0;
+		const uint32_t* ptr = fwd ? ic.fptr : ic.bptr;
+		const int nl = fwd ? ic.nfl : ic.nbl;
+		IcRow cur, nxt;
+		uint32_t lo = ptr[0], hi = ptr[nl > 0 ? 1 : 0];
+		if (nl > 0 && lo + tid < hi) ic_load_row(ic, fwd, lo + tid, cur);
+		for (int l = 0; l < nl; ++l) {
+			// rows wider than the block run in several rounds
+			for (uint32_t pos = lo + tid; pos < hi; pos += T) {
+				IcRow r;
+				if (pos == lo + tid) r = cur;
+				else ic_load_row(ic, fwd, pos, r);
+				// the next level's first row for this thread, in flight
+				// while this one computes
+				if (pos == lo + tid && l + 1 < nl) {
+					const uint32_t lo2 = hi, hi2 = ptr[l + 2];
+					if (lo2 + tid < hi2) ic_load_row(ic, fwd, lo2 + tid, nxt);
+				}
+				if (fwd) {
+					double y = sm[r.k];
+					if (r.cnt <= kIcInline) {
+#pragma unroll
+						for (int m = 0; m < kIcInline; ++m)
+							if (m < r.cnt) y = __dsub_rn(y, __dmul_rn(sm[r.c[m]], r.v[m]));
+					} else {
+						for (uint32_t e = ic.lp[r.k]; e < ic.lp[r.k + 1]; ++e)
+							y = __dsub_rn(y, __dmul_rn(sm[ic.li[e]], ic.lv[e]));
+					}
+					sm[r.k] = __ddiv_rn(y, r.d);
+				} else {
+					double z = 0.0;
+					if (r.cnt <= kIcInline) {
+#pragma unroll
+						for (int m = 0; m < kIcInline; ++m)
+							if (m < r.cnt) z = __dadd_rn(z, __dmul_rn(sm[r.c[m]], r.v[m]));
+					} else {
+						for (uint32_t e = ic.up[r.k]; e < ic.up[r.k + 1]; ++e)
+							z = __dadd_rn(z, __dmul_rn(sm[ic.ui[e]], ic.uv[e]));
+					}
+					sm[r.k] = __ddiv_rn(__dsub_rn(sm[r.k], z), r.d);
+				}
+			}
+			__syncthreads();
+			cur = nxt;
+			lo = hi;
+			if (l + 1 < nl) hi = ptr[l + 2];
+		}
+	}
+	for (int t = tid; t < ic.n; t += T) out[t] = sm[t];
+	__syncthreads();
+}
 
 #define GLOOP(cnt)                                                             \
 	for (int t = blockIdx.x * blockDim.x + threadIdx.x, _c = (cnt); t < _c;  \
@@ -33,6 +127,13 @@ struct IcOp {
 // order, so the result does not depend on the level split
 __device__ bool ic_apply(const IcOp& ic, const double* in, double* out,
 		const GridCtl& gc) {
+	if (ic.smem && gridDim.x == 1) {
+		extern __shared__ double ic_sm[];
+		// the block barrier before (the callers' grid_sync<true>) ordered
+		// `in`; the one at the end orders `out` for the next pass
+		ic_apply_smem(ic, in, out, ic_sm);
+		return true;
+	}
 	GLOOP(ic.n) out[t] = in[t];
 	if (!grid_sync<true>(gc)) return false;
 	for (int l = 0; l < ic.nfl; ++l) {

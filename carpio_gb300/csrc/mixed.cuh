@@ -216,6 +216,16 @@ __device__ void mixed_run(const Sp& sp, const Op64& op,
 	double normb = sqrt(acc[0]);
 	if (normb == 0.0) normb = 1;
 	double resid = 0;
+	// The FP32 BiCGSTAB recursion can drift from the true residual and, near a
+	// breakdown, return a correction that makes x worse. Its inner solves are
+	// kept short, x is saved before each one (in v.p, unused here), and a
+	// correction after which the FP64 residual did not drop is undone and
+	// retried with half the cap.
+	const bool bicg = sc.kind != CARPIO_GPU_CG;
+	int bcap = m.inner_max < 100 ? m.inner_max : 100;
+	int rejects = 0;
+	bool restored = false;
+	double best = 0.0;
 	for (;;) {
 		double rs[3] = { 0, 0, 0 };
 		KLOOP(sp) {
@@ -229,20 +239,34 @@ __device__ void mixed_run(const Sp& sp, const Op64& op,
 		if (!grid_allreduce<double, 3>(rs, gc, bank)) return;
 		resid = sqrt(rs[0]) / normb;
 		hist_push(sc, hl, resid);
+		if (bicg && outer > 0 && !restored && !(resid < best)) {
+			if (++rejects > 8 || total >= sc.max_iter) { resid = best; break; }
+			KLOOP(sp) { int a = sp.addr(k); v.x[a] = v.p[a]; }
+			if (!grid_sync(gc)) return;
+			bcap = bcap > 8 ? bcap / 2 : 4;
+			restored = true;
+			continue;
+		}
+		restored = false;
 		if (!(resid == resid)) break;   // NaN: code 1 with the NaN residual
 		if (resid <= sc.tol) {
 			if (blockIdx.x == 0 && threadIdx.x == 0) { sc.out->outer = outer; sc.out->inner = total; }
 			finish(sc, 0, total, resid, hl);
 			return;
 		}
+		best = resid;
 		if (total >= sc.max_iter) break;
 		double mr = mean ? rs[1] / n : 0.0;
 		double rn = sqrt(mean ? fmax(rs[2] - rs[1] * mr, 0.0) : rs[2]);
 		if (!(rn > 0.0)) break;
 		double sc_in = 1.0 / rn;
-		KLOOP(sp) { int a = sp.addr(k); m.f.r[a] = (float)((v.r[a] - mr) * sc_in); }
+		KLOOP(sp) {
+			int a = sp.addr(k);
+			m.f.r[a] = (float)((v.r[a] - mr) * sc_in);
+			if (bicg) v.p[a] = v.x[a];
+		}
 		if (!grid_sync(gc)) return;
-		const int cap = min(m.inner_max, sc.max_iter - total);
+		const int cap = min(bicg ? bcap : m.inner_max, sc.max_iter - total);
 		int brk = 0;
 		int it = sc.kind == CARPIO_GPU_CG
 				? inner_cg(sp, m, cap, gc, bank)

@@ -11,6 +11,7 @@
 // (i + gl) * P + (j + gl).
 #include "internal.hpp"
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -24,6 +25,13 @@ constexpr double kSmall = 1e-10;  // SMALL, lib/type_define.hpp
 struct Geo {
 	int nx, ny, gl, P, NI, NJ;
 	const double *cx, *sx, *cy, *sy;   // incl. ghosts
+	// p2: every cell size along x is hx and along y hy, both powers of two,
+	// and every centre distance (ghosts included) is exactly hx or hy; then
+	// dividing by one of those lengths (or by twice or half of one) equals
+	// multiplying by its reciprocal bit for bit (both round the same exact
+	// real number), and the P2 kernels below do that
+	int p2;
+	double hx, hy, ihx, ihy;
 	__device__ __forceinline__ int at(int i, int j) const { return (i + gl) * P + (j + gl); }
 	__device__ __forceinline__ double CX(int i) const { return cx[i + gl]; }
 	__device__ __forceinline__ double CY(int j) const { return cy[j + gl]; }
@@ -137,9 +145,80 @@ __device__ void bc_fill(const Geo& g, double* f, const BcDev& bc, double* s_old)
 	}
 }
 
-__global__ void __launch_bounds__(1024) k_apply_bc(Geo g, BcFields bf) {
+// The same fill spread over blocks (blockIdx.y: the field). The cells with
+// an order dependency -- the corner ghosts and the y-ghosts of column i = 0
+// whose old values the low-x corners read -- go to block 0, which captures
+// the old values first; every other ghost reads only normal cells, so blocks
+// 1.. fill the rest of the frame in any order.
+__device__ void bc_fill_ordered(const Geo& g, double* f, const BcDev& bc, double* s_old) {
+	const int gl = g.gl, nx = g.nx;
+	const int NI = g.NI, NJ = g.NJ;
+	const int ncorner = 2 * gl * gl;
+	for (int t = threadIdx.x; t < ncorner; t += blockDim.x) {
+		int r = t / gl, c = t - r * gl;
+		int J = r < gl ? r : NJ - 2 * gl + r;
+		int i = c - gl, j = J - gl;
+		int oi, oj;
+		ghost_src(g, i, j, oi, oj);
+		s_old[t] = f[g.at(oi, oj)];
+	}
+	__syncthreads();
+	// the frame rows' cells with I < gl + 1 or I >= NI - gl: 2 gl rows of
+	// 2 gl + 1 cells
+	const int per_row = 2 * gl + 1;
+	for (int t = threadIdx.x; t < 2 * gl * per_row; t += blockDim.x) {
+		const int r = t / per_row, c = t - r * per_row;
+		const int J = r < gl ? r : NJ - 2 * gl + r;
+		const int I = c <= gl ? c : NI - 2 * gl - 1 + c;
+		int i = I - gl, j = J - gl;
+		int oi, oj;
+		ghost_src(g, i, j, oi, oj);
+		double src;
+		if (i < 0) {
+			src = s_old[r * gl + I];
+		} else if (i >= nx) {
+			int oi2, oj2;
+			ghost_src(g, oi, oj, oi2, oj2);
+			src = ghost_value(g, bc, oi, oj, f[g.at(oi2, oj2)], oi2, oj2);
+		} else {
+			src = f[g.at(oi, oj)];
+		}
+		f[(long)I * g.P + J] = ghost_value(g, bc, i, j, src, oi, oj);
+	}
+}
+
+__device__ void bc_fill_rest(const Geo& g, double* f, const BcDev& bc, int part, int nparts) {
+	const int gl = g.gl;
+	const int NI = g.NI, NJ = g.NJ;
+	const long row_cells = NI - 2 * gl - 1;           // I in [gl + 1, NI - gl)
+	const long n_rows = 2L * gl * row_cells;
+	const long n_cols = 2L * gl * (NJ - 2 * gl);     // I < gl or >= NI - gl, J in [gl, NJ - gl)
+	for (long t = part * (long)blockDim.x + threadIdx.x; t < n_rows + n_cols;
+			t += (long)nparts * blockDim.x) {
+		int I, J;
+		if (t < n_rows) {
+			const int r = (int)(t / row_cells);
+			I = gl + 1 + (int)(t - r * row_cells);
+			J = r < gl ? r : NJ - 2 * gl + r;
+		} else {
+			const long u = t - n_rows;
+			const int r = (int)(u / (2 * gl));
+			const int c = (int)(u - (long)r * 2 * gl);
+			J = gl + r;
+			I = c < gl ? c : NI - 2 * gl + c;
+		}
+		int i = I - gl, j = J - gl;
+		int oi, oj;
+		ghost_src(g, i, j, oi, oj);
+		f[(long)I * g.P + J] = ghost_value(g, bc, i, j, f[g.at(oi, oj)], oi, oj);
+	}
+}
+
+__global__ void __launch_bounds__(256) k_apply_bc(Geo g, BcFields bf) {
 	extern __shared__ double s_old[];   // [2 * gl (rows) * gl (cols)]
-	bc_fill(g, bf.f[blockIdx.x], bf.bc[blockIdx.x], s_old);
+	const int fi = blockIdx.y;
+	if (blockIdx.x == 0) bc_fill_ordered(g, bf.f[fi], bf.bc[fi], s_old);
+	else bc_fill_rest(g, bf.f[fi], bf.bc[fi], blockIdx.x - 1, gridDim.x - 1);
 }
 
 // ------------------------------------------------------ advection schemes --
@@ -159,8 +238,11 @@ __device__ __forceinline__ double limiter(int sch, double r, double R) {
 	return 0.0;
 }
 
-// one axis of VdotNabla at cell (i, j); D = 0 x, 1 y
-template<int SCH, int D>
+// one axis of VdotNabla at cell (i, j); D = 0 x, 1 y. P2: the grid's
+// lengths are the powers of two of Geo::p2, so the divisions by them are
+// multiplications by exact reciprocals (the same bits); the divisions by
+// data stay.
+template<int SCH, int D, bool P2 = false>
 __device__ __forceinline__ double adv_axis(const Geo& g, const double* face,
 		const double* f, int i, int j) {
 	const int st = D == 0 ? g.P : 1;
@@ -192,6 +274,18 @@ __device__ __forceinline__ double adv_axis(const Geo& g, const double* face,
 			Dm = Cm = Um = Dp = Cp = Up = 0;
 		}
 		double R, r, fp, fm;
+		if (P2) {
+			// every S is h: R = 2h / h = 2, the sums are 2h
+			const double h = D == 0 ? g.hx : g.hy;
+			const double ih = D == 0 ? g.ihx : g.ihy;
+			const double h2 = h + h, ih2 = 0.5 * ih;
+			R = 2.0;
+			r = (F(Cp) - F(Up)) * h2 / (F(Dp) - F(Cp) + kSmall) * ih2;
+			fp = F(Cp) + limiter(SCH, r, R) * 0.5 * (F(Dp) - F(Cp));
+			r = (F(Cm) - F(Um)) * h2 / (F(Dm) - F(Cm) + kSmall) * ih2;
+			fm = F(Cm) + limiter(SCH, r, R) * 0.5 * (F(Dm) - F(Cm));
+			return (fa0 * fp - fam * fm) * ih;
+		}
 		R = (S(Dp) + S(Cp)) / S(Cp);
 		r = (F(Cp) - F(Up)) * (S(Dp) + S(Cp)) / (F(Dp) - F(Cp) + kSmall) / (S(Cp) + S(Up));
 		fp = F(Cp) + limiter(SCH, r, R) / R * (F(Dp) - F(Cp));
@@ -205,11 +299,11 @@ __device__ __forceinline__ double adv_axis(const Geo& g, const double* face,
 #undef S
 }
 
-template<int SCH>
+template<int SCH, bool P2 = false>
 __device__ __forceinline__ double adv_cell(const Geo& g, const double* uf,
 		const double* vf, const double* f, int i, int j) {
-	double a0 = adv_axis<SCH, 0>(g, uf, f, i, j);
-	double a1 = adv_axis<SCH, 1>(g, vf, f, i, j);
+	double a0 = adv_axis<SCH, 0, P2>(g, uf, f, i, j);
+	double a1 = adv_axis<SCH, 1, P2>(g, vf, f, i, j);
 	double s = 0.0;
 	s += a0;
 	s += a1;
@@ -217,10 +311,28 @@ __device__ __forceinline__ double adv_cell(const Geo& g, const double* uf,
 }
 
 // NablaMuNabla(Vt mu, ...) (s_operation.hpp:664-688)
+template<bool P2 = false>
 __device__ __forceinline__ double diffusion(const Geo& g, double mu,
 		const double* f, int i, int j) {
 	const int a = g.at(i, j);
 	double t0, t1;
+	if (P2) {
+		// centre distances and sizes are hx, hy: multiply by 1 / h
+		{
+			double dm = mu * (f[a] - f[a - g.P]) * g.ihx;
+			double dp = mu * (f[a + g.P] - f[a]) * g.ihx;
+			t0 = (dp - dm) * g.ihx;
+		}
+		{
+			double dm = mu * (f[a] - f[a - 1]) * g.ihy;
+			double dp = mu * (f[a + 1] - f[a]) * g.ihy;
+			t1 = (dp - dm) * g.ihy;
+		}
+		double res = 0.0;
+		res += t0;
+		res += t1;
+		return res;
+	}
 	{
 		double dm = mu * (f[a] - f[a - g.P]) / (g.CX(i) - g.CX(i - 1));
 		double dp = mu * (f[a + g.P] - f[a]) / (g.CX(i + 1) - g.CX(i));
@@ -275,7 +387,7 @@ __device__ __forceinline__ double diffusion_var(const Geo& g, const double* mu,
 // the diagonals in order, the cells of one in parallel, gives the values
 // of the sequential loop. A diagonal holds at most min(nx, ny) cells: one
 // block runs every step, with a block barrier between diagonals.
-template<int SCH>
+template<int SCH, bool P2 = false>
 __global__ void __launch_bounds__(1024) k_advect(Geo g, double* phi, BcDev bc,
 		const double* uf, const double* vf, double dt, int steps) {
 	extern __shared__ double s_old[];
@@ -288,7 +400,7 @@ __global__ void __launch_bounds__(1024) k_advect(Geo g, double* phi, BcDev bc,
 			const int i1 = L < nx - 1 ? L : nx - 1;
 			for (int i = i0 + (int)threadIdx.x; i <= i1; i += blockDim.x) {
 				const int j = L - i;
-				const double adv = adv_cell<SCH>(g, uf, vf, phi, i, j);
+				const double adv = adv_cell<SCH, P2>(g, uf, vf, phi, i, j);
 				const int a = g.at(i, j);
 				const double phin = phi[a];
 				phi[a] = phin - dt * adv;
@@ -311,7 +423,7 @@ __device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
 	asm volatile("st.release.gpu.u32 [%0], %1;" :: "l"(p), "r"(v) : "memory");
 }
 
-template<int SCH>
+template<int SCH, bool P2 = false>
 __global__ void __launch_bounds__(kThreads) k_advect_band(Geo g, double* phi, BcDev bc,
 		const double* uf, const double* vf, double dt, int steps, int R,
 		unsigned* prog, GridCtl gc) {
@@ -359,7 +471,7 @@ __global__ void __launch_bounds__(kThreads) k_advect_band(Geo g, double* phi, Bc
 				const int j = l - k;
 				if (j >= 0 && j < ny) {
 					const int i = r0 + k;
-					const double adv = adv_cell<SCH>(g, uf, vf, phi, i, j);
+					const double adv = adv_cell<SCH, P2>(g, uf, vf, phi, i, j);
 					const int a = g.at(i, j);
 					const double phin = phi[a];
 					phi[a] = phin - dt * adv;
@@ -378,7 +490,7 @@ __global__ void __launch_bounds__(kThreads) k_advect_band(Geo g, double* phi, Bc
 struct StepScalars {
 	double dt;                // current time step (Time_::_dt)
 	double t;                 // current time
-	unsigned long long maxmag_bits;   // max |u_c| of this step (as bits)
+	unsigned long long maxmag_bits;   // max |u_c|^2 of this step (as bits)
 	unsigned done;            // blocks finished with the max reduction
 	unsigned step;            // current step
 };
@@ -402,7 +514,9 @@ __global__ void __launch_bounds__(kThreads) k_restrict_time(Geo g,
 		double s = 0;
 		s += u[a] * u[a];
 		s += v[a] * v[a];
-		m = smax(m, sqrt(s));
+		// max sqrt(s) = sqrt(max s): a correctly rounded sqrt is monotone,
+		// so one sqrt of the largest square gives the same bits
+		m = smax(m, s);
 	}
 	m = block_max(m);
 	__shared__ bool last;
@@ -414,7 +528,7 @@ __global__ void __launch_bounds__(kThreads) k_restrict_time(Geo g,
 	__syncthreads();
 	if (last && threadIdx.x == 0) {
 		__threadfence();
-		double maxmag = __longlong_as_double((long long)atomicAdd(&ss->maxmag_bits, 0ull));
+		double maxmag = sqrt(__longlong_as_double((long long)atomicAdd(&ss->maxmag_bits, 0ull)));
 		double rdt = rule.cfl * rule.mins / maxmag;
 		double dt = ss->dt;
 		double rdt2 = dt;
@@ -452,7 +566,7 @@ __global__ void __launch_bounds__(kThreads) k_maxmag(Geo g, const double* u,
 
 // u* = u + dt (-adv + diff / rho) for both components
 // (NS_explicit_::_veo_star_center, s_ns_explicit.hpp:173-229)
-template<int SCH>
+template<int SCH, bool P2 = false>
 __global__ void __launch_bounds__(kThreads) k_predictor(Geo g, const double* u,
 		const double* v, const double* uf, const double* vf, double* us,
 		double* vs, const StepScalars* ss, double rho, double mu, const double* muf) {
@@ -465,14 +579,14 @@ __global__ void __launch_bounds__(kThreads) k_predictor(Geo g, const double* u,
 		// __diffusion_term (s_ns_explicit.hpp:235-241): the mu field when the
 		// uniform mu was unset
 		{
-			double adv = adv_cell<SCH>(g, uf, vf, u, i, j);
-			double dif = muf ? diffusion_var(g, muf, u, i, j) : diffusion(g, mu, u, i, j);
+			double adv = adv_cell<SCH, P2>(g, uf, vf, u, i, j);
+			double dif = muf ? diffusion_var(g, muf, u, i, j) : diffusion<P2>(g, mu, u, i, j);
 			double src = 0;
 			us[a] = (-adv + (dif + src) / rho) * dt + u[a];
 		}
 		{
-			double adv = adv_cell<SCH>(g, uf, vf, v, i, j);
-			double dif = muf ? diffusion_var(g, muf, v, i, j) : diffusion(g, mu, v, i, j);
+			double adv = adv_cell<SCH, P2>(g, uf, vf, v, i, j);
+			double dif = muf ? diffusion_var(g, muf, v, i, j) : diffusion<P2>(g, mu, v, i, j);
 			double src = 0;
 			vs[a] = (-adv + (dif + src) / rho) * dt + v[a];
 		}
@@ -489,29 +603,41 @@ __global__ void __launch_bounds__(kThreads) k_c2f(Geo g, const double* u,
 		int a = g.at(i, j);
 		double vc = u[a];
 		double hs = g.SX(i) * 0.5, hsp = g.SX(i + 1) * 0.5;
-		fx[a] = (u[a + g.P] * hs + vc * hsp) / (hs + hsp);
+		// (hs + hs') is the cell size: with Geo::p2 a power of two
+		fx[a] = g.p2 ? (u[a + g.P] * hs + vc * hsp) * g.ihx : (u[a + g.P] * hs + vc * hsp) / (hs + hsp);
 		if (i == 0) {
 			double hsm = g.SX(i - 1) * 0.5;
-			fx[a - g.P] = (u[a - g.P] * hs + vc * hsm) / (hs + hsm);
+			fx[a - g.P] = g.p2 ? (u[a - g.P] * hs + vc * hsm) * g.ihx
+			                   : (u[a - g.P] * hs + vc * hsm) / (hs + hsm);
 		}
 		vc = v[a];
 		hs = g.SY(j) * 0.5;
 		hsp = g.SY(j + 1) * 0.5;
-		fy[a] = (v[a + 1] * hs + vc * hsp) / (hs + hsp);
+		fy[a] = g.p2 ? (v[a + 1] * hs + vc * hsp) * g.ihy : (v[a + 1] * hs + vc * hsp) / (hs + hsp);
 		if (j == 0) {
 			double hsm = g.SY(j - 1) * 0.5;
-			fy[a - 1] = (v[a - 1] * hs + vc * hsm) / (hs + hsm);
+			fy[a - 1] = g.p2 ? (v[a - 1] * hs + vc * hsm) * g.ihy
+			                 : (v[a - 1] * hs + vc * hsm) / (hs + hsm);
 		}
 	}
 }
 
 // face gradient of Operation_::Grad (s_operation.hpp:46-72) at x face (i, j)
 // (between i and i+1; i = -1 is the low wall face, computed from cell 0)
+// (with Geo::p2 the centre distance is +-h: multiply by +-1/h)
 __device__ __forceinline__ double gx_at(const Geo& g, const double* phi, int i, int j) {
+	if (g.p2) {
+		if (i >= 0) return (phi[g.at(i + 1, j)] - phi[g.at(i, j)]) * g.ihx;
+		return (phi[g.at(-1, j)] - phi[g.at(0, j)]) * -g.ihx;
+	}
 	if (i >= 0) return (phi[g.at(i + 1, j)] - phi[g.at(i, j)]) / (g.CX(i + 1) - g.CX(i));
 	return (phi[g.at(-1, j)] - phi[g.at(0, j)]) / (g.CX(-1) - g.CX(0));
 }
 __device__ __forceinline__ double gy_at(const Geo& g, const double* phi, int i, int j) {
+	if (g.p2) {
+		if (j >= 0) return (phi[g.at(i, j + 1)] - phi[g.at(i, j)]) * g.ihy;
+		return (phi[g.at(i, -1)] - phi[g.at(i, 0)]) * -g.ihy;
+	}
 	if (j >= 0) return (phi[g.at(i, j + 1)] - phi[g.at(i, j)]) / (g.CY(j + 1) - g.CY(j));
 	return (phi[g.at(i, -1)] - phi[g.at(i, 0)]) / (g.CY(-1) - g.CY(0));
 }
@@ -691,6 +817,24 @@ Geo make_geo(const carpio_gpu_grid* g) {
 	e.sx = g->d_sx;
 	e.cy = g->d_cy;
 	e.sy = g->d_sy;
+	// the power-of-two case (Geo::p2), checked on the host copies of the axes
+	auto pow2 = [](double h) {
+		int ex = 0;
+		return h > 0 && std::frexp(h, &ex) == 0.5;
+	};
+	auto axis_ok = [&](const std::vector<double>& c, const std::vector<double>& sz, double h) {
+		if (!pow2(h)) return false;
+		for (size_t k = 0; k < sz.size(); ++k)
+			if (sz[k] != h) return false;
+		for (size_t k = 0; k + 1 < c.size(); ++k)
+			if (c[k + 1] - c[k] != h) return false;
+		return true;
+	};
+	e.hx = g->sx.empty() ? 0.0 : g->sx[0];
+	e.hy = g->sy.empty() ? 0.0 : g->sy[0];
+	e.p2 = axis_ok(g->cx, g->sx, e.hx) && axis_ok(g->cy, g->sy, e.hy) ? 1 : 0;
+	e.ihx = e.p2 ? 1.0 / e.hx : 0.0;
+	e.ihy = e.p2 ? 1.0 / e.hy : 0.0;
 	return e;
 }
 
@@ -719,7 +863,9 @@ cudaError_t launch_bc(const Geo& geo, double* f0, const carpio_gpu_bc& b0,
 	bf.f[1] = f1;
 	bf.bc[1] = b1 ? to_dev(*b1, gv1) : bf.bc[0];
 	size_t smem = sizeof(double) * 2 * geo.gl * geo.gl;
-	k_apply_bc<<<b1 ? 2 : 1, 1024, smem, s>>>(geo, bf);
+	const long rest = 2L * geo.gl * (geo.NI - 2 * geo.gl - 1) + 2L * geo.gl * (geo.NJ - 2 * geo.gl);
+	const int parts = (int)std::max(1L, std::min(64L, (rest + 255) / 256));
+	k_apply_bc<<<dim3(1 + parts, b1 ? 2 : 1), 256, smem, s>>>(geo, bf);
 	return cudaGetLastError();
 }
 
@@ -728,7 +874,10 @@ cudaError_t launch_pred(const Geo& geo, int blocks, cudaStream_t s,
 		const double* u, const double* v, const double* uf, const double* vf,
 		double* us, double* vs, const StepScalars* ss, double rho, double mu,
 		const double* muf) {
-	k_predictor<SCH><<<blocks, kThreads, 0, s>>>(geo, u, v, uf, vf, us, vs, ss, rho, mu, muf);
+	if (geo.p2)
+		k_predictor<SCH, true><<<blocks, kThreads, 0, s>>>(geo, u, v, uf, vf, us, vs, ss, rho, mu, muf);
+	else
+		k_predictor<SCH, false><<<blocks, kThreads, 0, s>>>(geo, u, v, uf, vf, us, vs, ss, rho, mu, muf);
 	return cudaGetLastError();
 }
 
@@ -775,19 +924,21 @@ cudaError_t launch_kim_source(int sch, const Geo& geo, int blocks, cudaStream_t 
 }
 
 template<int S>
-const void* advect_band_kernel() { return (const void*)k_advect_band<S>; }
+const void* advect_band_kernel(bool p2) {
+	return p2 ? (const void*)k_advect_band<S, true> : (const void*)k_advect_band<S, false>;
+}
 
-const void* pick_advect_band(int sch) {
+const void* pick_advect_band(int sch, bool p2) {
 	switch (sch) {
-	case CARPIO_GPU_UPWIND1: return advect_band_kernel<CARPIO_GPU_UPWIND1>();
-	case CARPIO_GPU_CENTER: return advect_band_kernel<CARPIO_GPU_CENTER>();
-	case CARPIO_GPU_CENTER4: return advect_band_kernel<CARPIO_GPU_CENTER4>();
-	case CARPIO_GPU_UPWIND2: return advect_band_kernel<CARPIO_GPU_UPWIND2>();
-	case CARPIO_GPU_VANLEER: return advect_band_kernel<CARPIO_GPU_VANLEER>();
-	case CARPIO_GPU_SUPERBEE: return advect_band_kernel<CARPIO_GPU_SUPERBEE>();
-	case CARPIO_GPU_WAHYD: return advect_band_kernel<CARPIO_GPU_WAHYD>();
-	case CARPIO_GPU_QUICK: return advect_band_kernel<CARPIO_GPU_QUICK>();
-	case CARPIO_GPU_CUI: return advect_band_kernel<CARPIO_GPU_CUI>();
+	case CARPIO_GPU_UPWIND1: return advect_band_kernel<CARPIO_GPU_UPWIND1>(p2);
+	case CARPIO_GPU_CENTER: return advect_band_kernel<CARPIO_GPU_CENTER>(p2);
+	case CARPIO_GPU_CENTER4: return advect_band_kernel<CARPIO_GPU_CENTER4>(p2);
+	case CARPIO_GPU_UPWIND2: return advect_band_kernel<CARPIO_GPU_UPWIND2>(p2);
+	case CARPIO_GPU_VANLEER: return advect_band_kernel<CARPIO_GPU_VANLEER>(p2);
+	case CARPIO_GPU_SUPERBEE: return advect_band_kernel<CARPIO_GPU_SUPERBEE>(p2);
+	case CARPIO_GPU_WAHYD: return advect_band_kernel<CARPIO_GPU_WAHYD>(p2);
+	case CARPIO_GPU_QUICK: return advect_band_kernel<CARPIO_GPU_QUICK>(p2);
+	case CARPIO_GPU_CUI: return advect_band_kernel<CARPIO_GPU_CUI>(p2);
 	}
 	return nullptr;
 }
@@ -796,7 +947,9 @@ cudaError_t launch_advect(int sch, const Geo& geo, cudaStream_t s, double* phi,
 		const BcDev& bc, const double* uf, const double* vf, double dt, int steps) {
 	const size_t smem = sizeof(double) * 2 * geo.gl * geo.gl;
 	switch (sch) {
-#define CASE(S) case S: k_advect<S><<<1, 1024, smem, s>>>(geo, phi, bc, uf, vf, dt, steps); \
+#define CASE(S) case S: \
+		if (geo.p2) k_advect<S, true><<<1, 1024, smem, s>>>(geo, phi, bc, uf, vf, dt, steps); \
+		else k_advect<S, false><<<1, 1024, smem, s>>>(geo, phi, bc, uf, vf, dt, steps); \
 		return cudaGetLastError();
 	CASE(CARPIO_GPU_UPWIND1) CASE(CARPIO_GPU_CENTER) CASE(CARPIO_GPU_CENTER4)
 	CASE(CARPIO_GPU_UPWIND2) CASE(CARPIO_GPU_VANLEER) CASE(CARPIO_GPU_SUPERBEE)
@@ -1368,7 +1521,7 @@ int carpio_gpu_advection_step(carpio_gpu_advection* a, double dt, int steps) {
 		CG_CK(cudaStreamSynchronize(a->s));
 		return 0;
 	}
-	const void* k = pick_advect_band(a->scheme);
+	const void* k = pick_advect_band(a->scheme, geo.p2 != 0);
 	if (!k) return CARPIO_GPU_EINVAL;
 	// bands of R rows, one block each, at most one per SM (all co-resident)
 	const int maxb = std::min(coop_blocks(k, (long)g->nx * kThreads, 1), sm_count());

@@ -59,8 +59,10 @@ extern "C" {
 /* flags (bitwise OR). 0 = the reference's exact semantics. */
 #define CARPIO_GPU_FLAG_FULL_NRM2 1u   /* use the full 2-norm instead of nrm2's
                                           drop-last-element (BLAS_Level1.hpp:569) */
-#define CARPIO_GPU_FLAG_NO_TILE 2u     /* MIXED: run the inner FP32 CG from global
-                                          memory instead of the on-chip tile kernel */
+#define CARPIO_GPU_FLAG_NO_TILE 2u     /* structure level, CG on a uniform grid:
+                                          run from global memory instead of the
+                                          on-chip tile kernels (the FP64 CG's and
+                                          the MIXED inner CG's) */
 #define CARPIO_GPU_FLAG_MIXED 4u       /* CSR layer: the kind's iterations in FP32
                                           inside FP64 iterative refinement (CG,
                                           DIA_BICGSTAB, BICGSTAB; the stopping
