@@ -20,7 +20,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
 # per-file extra flags: the projection operators must round like the
 # reference's C++ (no FMA contraction)
 EXTRA = {"ns.cu": ["--fmad=false"]}
-SOURCES = ["runtime.cu", "csr.cu", "csr_noalloc.cu", "poisson.cu", "ns.cu", "batch.cu", "batch_k256.cu", "batch_k512.cu", "nn_conv.cu", "nn.cu", "learned.cu"]
+SOURCES = ["runtime.cu", "csr.cu", "csr_noalloc.cu", "poisson.cu", "ns.cu", "batch.cu", "batch_k256.cu", "batch_k512.cu", "batch_mg.cu", "nn_conv.cu", "nn.cu", "learned.cu"]
 
 
 def nvcc():

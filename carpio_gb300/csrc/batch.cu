@@ -17,6 +17,9 @@ namespace cg_batch {
 // k_batch<T> instantiated in its own translation unit per block size
 const void* kernel_256();
 const void* kernel_512();
+// the one-CTA-per-problem multigrid kernel (batch_mg.cu)
+const void* kernel_mg(int T);
+long long mg_scratch_floats(int nx, int ny);
 }  // namespace cg_batch
 
 namespace {
@@ -252,6 +255,11 @@ struct carpio_gpu_batch {
 	long long cells = 0;                // field arena length (doubles)
 	cg_host::DevBuf src, phi, b, r, D, ax, ay, sx, sy, fold, save;
 	cg_host::DevBuf dprob, dteam, dsptr, dslist, dres, dctl;
+	// multigrid kernel: one CTA per problem from a queue (mg), its block
+	// size and grid, FP32 scratch with per-problem offsets, the order
+	bool mg = false;
+	int mg_T = 512, mg_grid = 0;
+	cg_host::DevBuf w32, w32off, order, queue;
 	std::vector<BatchProb> hprob;
 	Plan plan;
 	const void* kern = nullptr;
@@ -303,7 +311,39 @@ int max_clusters(const void* kern, int T, int S, size_t smem, int* out) {
 	return 0;
 }
 
+int launch_mg(carpio_gpu_batch* b, cudaStream_t s) {
+	BatchArgs a;
+	std::memset(&a, 0, sizeof a);
+	a.prob = b->dprob.as<BatchProb>();
+	a.src = b->src.as<double>();
+	a.phi = b->phi.as<double>();
+	a.b = b->b.as<double>();
+	a.r = b->r.as<double>();
+	a.D = b->D.as<double>();
+	a.ax = b->ax.as<double>();
+	a.ay = b->ay.as<double>();
+	a.sx = b->sx.as<double>();
+	a.sy = b->sy.as<double>();
+	a.fold = b->fold.as<double>();
+	a.res = b->dres.as<BatchRes>();
+	a.ctl = b->dctl.as<BatchCtl>();
+	// after a 1e-2 drop of (r, z): with the V-cycle an iteration gains
+	// about a digit
+	a.inner_tol = b->cfg.inner_tol > 0 ? b->cfg.inner_tol : 1e-2;
+	a.queue = b->queue.as<unsigned>();
+	a.order = b->order.as<int>();
+	a.count = b->count;
+	a.w32 = b->w32.as<float>();
+	a.w32off = b->w32off.as<long long>();
+	CG_CK(cudaMemsetAsync(b->dres.p, 0, sizeof(BatchRes) * b->count, s));
+	CG_CK(cudaMemsetAsync(b->queue.p, 0, sizeof(unsigned), s));
+	void* args[] = { &a };
+	CG_CK(cudaLaunchKernel(b->kern, dim3(b->mg_grid), dim3(b->mg_T), args, 0, s));
+	return 0;
+}
+
 int launch(carpio_gpu_batch* b, cudaStream_t s) {
+	if (b->mg) return launch_mg(b, s);
 	const Plan& pl = b->plan;
 	const int T = pl.tiles.threads, S = pl.tiles.cluster;
 	BatchArgs a;
@@ -392,6 +432,50 @@ int configure(carpio_gpu_batch* b, const carpio_gpu_batch_tiles& tiles) {
 	in.smem_bytes = (int)pl.smem;
 	for (int k = 0; k < 5; ++k) in.teams[k] = pl.teams[k];
 	in.est_ms = pl.est_ms;
+	return 0;
+}
+
+// the multigrid kernel with T threads per CTA: as many CTAs as fit (at
+// most four per SM, at most one per problem), the graph captured
+int configure_mg(carpio_gpu_batch* b, int T, int use_graph) {
+	using namespace cg_host;
+	const void* kern = cg_batch::kernel_mg(T);
+	if (!kern) return CARPIO_GPU_EINVAL;
+	int per_sm = 0;
+	CG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, T, 0));
+	if (per_sm < 1) return CARPIO_GPU_EINVAL;
+	per_sm = std::min(per_sm, 4);
+	b->kern = kern;
+	b->mg = true;
+	b->mg_T = T;
+	b->mg_grid = std::max(1, std::min(per_sm * sm_count(), b->count));
+	cudaStream_t s = b->s;
+	CG_CK(cudaStreamSynchronize(s));
+	if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+	if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+	if (use_graph >= 0) {
+		CG_CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+		int rc = launch(b, s);
+		cudaGraph_t g = nullptr;
+		cudaError_t e = cudaStreamEndCapture(s, &g);
+		if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+		if (e != cudaSuccess) { note_cuda_error(e); return CARPIO_GPU_ECUDA; }
+		b->graph = g;
+		CG_CK(cudaGraphInstantiate(&b->exec, g, 0));
+	}
+	carpio_gpu_batch_info& in = b->info;
+	in.tiles.threads = T;
+	in.tiles.cluster = 1;
+	in.tiles.cells_per_cta = 0;
+	in.tiles.use_graph = use_graph;
+	in.clusters = b->mg_grid;
+	in.ctas = b->mg_grid;
+	in.smem_bytes = 0;
+	for (int k = 0; k < 5; ++k) in.teams[k] = 0;
+	in.teams[0] = b->count;
+	in.est_ms = 0.0;
+	b->plan.tiles = in.tiles;
+	b->plan.tiles.cluster = 0;
 	return 0;
 }
 
@@ -586,7 +670,9 @@ int carpio_gpu_batch_create(int count, const carpio_gpu_batch_problem* probs,
 		return fail(CARPIO_GPU_ECUDA);
 	}
 	// configuration: the caller's, else an autotuned one for the same
-	// signature, else the first candidate that fits
+	// signature, else the first candidate that fits. No cluster size asked
+	// for: the multigrid kernel (one CTA per problem); a cluster size: the
+	// cluster-team kernel (plain FP32 CG, teams of CTAs)
 	carpio_gpu_batch_tiles want{};
 	if (tiles) want = *tiles;
 	bool explicit_tiles = tiles && tiles->threads && tiles->cluster && tiles->cells_per_cta;
@@ -600,7 +686,30 @@ int carpio_gpu_batch_create(int count, const carpio_gpu_batch_problem* probs,
 			explicit_tiles = true;
 		}
 	}
-	if (explicit_tiles) {
+	if (want.cluster == 0) {
+		// FP32 scratch of every problem, the problems largest first
+		std::vector<long long> woff(count);
+		long long wtot = 0;
+		for (int i = 0; i < count; ++i) {
+			woff[i] = wtot;
+			wtot += cg_batch::mg_scratch_floats(probs[i].nx, probs[i].ny);
+		}
+		std::vector<int> ord(count);
+		for (int i = 0; i < count; ++i) ord[i] = i;
+		std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) {
+			return (long long)probs[x].nx * probs[x].ny > (long long)probs[y].nx * probs[y].ny;
+		});
+		if ((rc = b->w32.ensure(sizeof(float) * (size_t)wtot))) return fail(rc);
+		if ((rc = to_device(b->w32off, woff.data(), sizeof(long long) * count, s))) return fail(rc);
+		if ((rc = to_device(b->order, ord.data(), sizeof(int) * count, s))) return fail(rc);
+		if ((rc = b->queue.ensure(sizeof(unsigned)))) return fail(rc);
+		if ((rc = to_device(b->dprob, b->hprob.data(), sizeof(BatchProb) * count, s))) return fail(rc);
+		if (cudaStreamSynchronize(s) != cudaSuccess) {
+			note_cuda_error(cudaGetLastError());
+			return fail(CARPIO_GPU_ECUDA);
+		}
+		rc = configure_mg(b, want.threads ? want.threads : 512, want.use_graph);
+	} else if (explicit_tiles) {
 		rc = configure(b, want);
 	} else {
 		rc = CARPIO_GPU_EINVAL;
@@ -709,10 +818,21 @@ int carpio_gpu_batch_autotune(carpio_gpu_batch* b, int max_candidates) {
 	carpio_gpu_batch_tiles best = keep;
 	float best_ms = 0;
 	int tried = 0;
-	for (auto c : candidates(kCellsPerCta)) {
+	// the multigrid kernel's block sizes, or the cluster-team configurations
+	std::vector<carpio_gpu_batch_tiles> cands;
+	if (b->mg) {
+		for (int T : { 512, 256, 1024 }) {
+			carpio_gpu_batch_tiles t{};
+			t.threads = T;
+			cands.push_back(t);
+		}
+	} else {
+		cands = candidates(kCellsPerCta);
+	}
+	for (auto c : cands) {
 		if (tried >= max_candidates) break;
 		c.use_graph = keep.use_graph;
-		rc = configure(b, c);
+		rc = b->mg ? configure_mg(b, c.threads, c.use_graph) : configure(b, c);
 		if (rc == CARPIO_GPU_EINVAL) continue;
 		if (rc) return rc;
 		float ms = 0;
@@ -728,7 +848,7 @@ int carpio_gpu_batch_autotune(carpio_gpu_batch* b, int max_candidates) {
 		}
 	}
 	CG_CK(cudaMemcpyAsync(b->phi.p, b->save.p, fb, cudaMemcpyDeviceToDevice, b->s));
-	if ((rc = configure(b, best))) return rc;
+	if ((rc = b->mg ? configure_mg(b, best.threads, best.use_graph) : configure(b, best))) return rc;
 	b->info.candidates = tried;
 	b->info.tuned_ms = best_ms;
 	std::lock_guard<std::mutex> lk2(tune_mu());

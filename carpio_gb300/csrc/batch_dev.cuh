@@ -80,6 +80,13 @@ struct BatchArgs {
 	const double* fold;
 	BatchRes* res;
 	double inner_tol;
+	// the one-CTA-per-problem multigrid kernel (batch_mg.cu): the queue
+	// counter, the problems largest first, FP32 scratch and its offsets
+	unsigned* queue;
+	const int* order;
+	int count;
+	float* w32;
+	const long long* w32off;
 };
 
 __device__ __forceinline__ int band_of(int m, int t, int nx) {

@@ -74,17 +74,16 @@ __device__ void ic_apply_smem(const IcOp& ic, const double* in, double* out, dou
 		uint32_t lo = ptr[0], hi = ptr[nl > 0 ? 1 : 0];
 		if (nl > 0 && lo + tid < hi) ic_load_row(ic, fwd, lo + tid, cur);
 		for (int l = 0; l < nl; ++l) {
+			// the next level's first row for this thread (every thread that
+			// has one there, whether or not it has a row at this level), in
+			// flight while this level computes
+			const uint32_t lo2 = hi, hi2 = l + 1 < nl ? ptr[l + 2] : hi;
+			if (lo2 + tid < hi2) ic_load_row(ic, fwd, lo2 + tid, nxt);
 			// rows wider than the block run in several rounds
 			for (uint32_t pos = lo + tid; pos < hi; pos += T) {
 				IcRow r;
 				if (pos == lo + tid) r = cur;
 				else ic_load_row(ic, fwd, pos, r);
-				// the next level's first row for this thread, in flight
-				// while this one computes
-				if (pos == lo + tid && l + 1 < nl) {
-					const uint32_t lo2 = hi, hi2 = ptr[l + 2];
-					if (lo2 + tid < hi2) ic_load_row(ic, fwd, lo2 + tid, nxt);
-				}
 				if (fwd) {
 					double y = sm[r.k];
 					if (r.cnt <= kIcInline) {
@@ -111,8 +110,8 @@ __device__ void ic_apply_smem(const IcOp& ic, const double* in, double* out, dou
 			}
 			__syncthreads();
 			cur = nxt;
-			lo = hi;
-			if (l + 1 < nl) hi = ptr[l + 2];
+			lo = lo2;
+			hi = hi2;
 		}
 	}
 	for (int t = tid; t < ic.n; t += T) out[t] = sm[t];

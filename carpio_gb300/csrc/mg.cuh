@@ -11,6 +11,10 @@
 // fine grid's boundary folding (a Dirichlet face doubles its coefficient, a
 // Neumann face cancels it).
 //
+// The smoother scales by a stored reciprocal of D (the same on both sides of
+// the cycle, so M stays symmetric) and the pre-smoothed z = w D^-1 r is never
+// stored: every pass that needs it recomputes it from r.
+//
 // One cycle: pre-smoothing z = w D^-1 r (damped Jacobi from zero), the
 // residual s = r - A z, restriction r_c = P^T s, the cycle on the coarse
 // level, prolongation c = z + P z_c, post-smoothing z = c + w D^-1 (r - A c).
@@ -39,10 +43,10 @@ constexpr int kMgCoarseSweeps = 20; // damped Jacobi sweeps on the coarsest leve
 struct MgLevel {
 	int nx, ny;
 	float* R;          // right-hand side of the level (level 0: the fine r)
-	float* Z;          // pre-smoothed correction
 	float* S;          // residual after pre-smoothing
 	float* Zp;         // the level's final correction (after post-smoothing)
 	const float* D;    // diagonal, nx * ny
+	const float* iD;   // its reciprocal (0 where D is 0): the smoother's scaling
 };
 
 struct MgArgs {
@@ -124,45 +128,88 @@ __device__ __forceinline__ float mg_prolong(const Ld& ld, const float* zc, int i
 	return fmaf(a1, b0 * ld(zc, I1 * nyc + J0) + b1 * ld(zc, I1 * nyc + J1), v);
 }
 
-// the corrected value c = z + P zc at fine cell (i, j)
-template<class Ld>
-__device__ __forceinline__ float mg_corrected(const Ld& ld, const float* z, const float* zc,
-		int i, int j, int nyf, int nxc, int nyc) {
-	return ld(z, i * nyf + j) + mg_prolong(ld, zc, i, j, nxc, nyc);
+// the corrected value c = w iD r + P zc at fine cell (i, j) (the
+// pre-smoothed correction from r, plus the coarse correction); lc reads the
+// constants (iD), lr reads r, lz reads zc
+template<class Lc, class Lr, class Lz>
+__device__ __forceinline__ float mg_corrected(const Lc& lc, const Lr& lr, const Lz& lz,
+		const float* r, const float* iD, const float* zc, int i, int j, int nyf, int nxc,
+		int nyc, float w) {
+	const int k = i * nyf + j;
+	return fmaf(w * lr(r, k), lc(iD, k), mg_prolong(lz, zc, i, j, nxc, nyc));
 }
 
-// post-smoothing at (I, J) of a level: c = z + P zc at the cell and its
-// neighbours, then c + w D^-1 (r - A c)
-template<class Ld>
-__device__ __forceinline__ float mg_post(const Ld& ld, const float* z, const float* zc,
-		const float* r, const float* D, int I, int J, int nx, int ny, float cx, float cy,
-		float w) {
+// post-smoothing at (I, J) of a level: c at the cell and its neighbours,
+// then c + w iD (r - A c)
+template<class Lc, class Lr, class Lz>
+__device__ __forceinline__ float mg_post(const Lc& lc, const Lr& lr, const Lz& lz,
+		const float* r, const float* zc, const float* D, const float* iD, int I, int J,
+		int nx, int ny, float cx, float cy, float w) {
 	const int nxc = nx >> 1, nyc = ny >> 1;
-	const float c = mg_corrected(ld, z, zc, I, J, ny, nxc, nyc);
+	const float c = mg_corrected(lc, lr, lz, r, iD, zc, I, J, ny, nxc, nyc, w);
 	const int k = I * ny + J;
-	const float d = ld(D, k);
-	float ac = d * c;
-	if (I > 0) ac = fmaf(cx, mg_corrected(ld, z, zc, I - 1, J, ny, nxc, nyc), ac);
-	if (I < nx - 1) ac = fmaf(cx, mg_corrected(ld, z, zc, I + 1, J, ny, nxc, nyc), ac);
-	if (J > 0) ac = fmaf(cy, mg_corrected(ld, z, zc, I, J - 1, ny, nxc, nyc), ac);
-	if (J < ny - 1) ac = fmaf(cy, mg_corrected(ld, z, zc, I, J + 1, ny, nxc, nyc), ac);
-	return fmaf(w, (ld(r, k) - ac) / d, c);
+	float ac = lc(D, k) * c;
+	if (I > 0) ac = fmaf(cx, mg_corrected(lc, lr, lz, r, iD, zc, I - 1, J, ny, nxc, nyc, w), ac);
+	if (I < nx - 1) ac = fmaf(cx, mg_corrected(lc, lr, lz, r, iD, zc, I + 1, J, ny, nxc, nyc, w), ac);
+	if (J > 0) ac = fmaf(cy, mg_corrected(lc, lr, lz, r, iD, zc, I, J - 1, ny, nxc, nyc, w), ac);
+	if (J < ny - 1) ac = fmaf(cy, mg_corrected(lc, lr, lz, r, iD, zc, I, J + 1, ny, nxc, nyc, w), ac);
+	return fmaf(w * (lr(r, k) - ac), lc(iD, k), c);
+}
+
+// s = r - A (w iD r) at (I, J): the residual after pre-smoothing, with the
+// pre-smoothed correction recomputed from r. ld reads D and iD, lr reads r.
+template<class Ld, class Lr>
+__device__ __forceinline__ float mg_resid(const Ld& ld, const Lr& lr, const float* r,
+		const float* D, const float* iD, int I, int J, int nx, int ny, float cx, float cy,
+		float w) {
+	const int k = I * ny + J;
+	const float rk = lr(r, k);
+	float v = ld(D, k) * (w * rk * ld(iD, k));
+	if (I > 0) v = fmaf(cx, w * lr(r, k - ny) * ld(iD, k - ny), v);
+	if (I < nx - 1) v = fmaf(cx, w * lr(r, k + ny) * ld(iD, k + ny), v);
+	if (J > 0) v = fmaf(cy, w * lr(r, k - 1) * ld(iD, k - 1), v);
+	if (J < ny - 1) v = fmaf(cy, w * lr(r, k + 1) * ld(iD, k + 1), v);
+	return rk - v;
 }
 
 struct LdL2 {   // data written by other CTAs of the launch
 	__device__ __forceinline__ float operator()(const float* p, int k) const { return ldcg(p + k); }
 };
-struct LdSm {   // this CTA's shared memory (or read-only data)
+struct LdSm {   // this CTA's shared memory (plain loads)
 	__device__ __forceinline__ float operator()(const float* p, int k) const { return p[k]; }
 };
+struct LdRo {   // read-only data of the launch (the diagonals)
+	__device__ __forceinline__ float operator()(const float* p, int k) const { return __ldg(p + k); }
+};
+
+// a distributed pass: every thread of the grid takes cells gt, gt + G, ...
+// of a level, CH at a time, and computes all CH values before storing any,
+// so the loads of the CH cells are in flight together
+template<int CH, class Fn, class St>
+__device__ __forceinline__ void mg_pass(int gt, int G, int n, Fn&& fn, St&& st) {
+	for (int k0 = gt; k0 < n; k0 += CH * G) {
+		float val[CH];
+#pragma unroll
+		for (int u = 0; u < CH; ++u) {
+			const int k = k0 + u * G;
+			val[u] = k < n ? fn(k) : 0.f;
+		}
+#pragma unroll
+		for (int u = 0; u < CH; ++u) {
+			const int k = k0 + u * G;
+			if (k < n) st(k, val[u]);
+		}
+	}
+}
 
 // The levels nlev .. ntot-1 in this CTA's shared memory (called by one CTA):
 // r of level nlev from S of level nlev - 1, the cycle, and level nlev's final
 // correction into lev[nlev].Zp. sm: 3 * (cells of levels nlev .. ntot-1)
 // floats (r, z, s of each level).
-__device__ void mg_coarse(const MgArgs& mg, float* sm) {
+__device__ inline void mg_coarse(const MgArgs& mg, float* sm) {
 	const int T = blockDim.x, tid = threadIdx.x;
 	const LdSm sl;
+	const LdRo ro;
 	const LdL2 gl;
 	// r, z, s of level l at base(l), base(l) + n, base(l) + 2 n
 	auto base = [&](int l) {
@@ -170,35 +217,34 @@ __device__ void mg_coarse(const MgArgs& mg, float* sm) {
 		for (int m = mg.nlev; m < l; ++m) q += 3 * mg.lev[m].nx * mg.lev[m].ny;
 		return q;
 	};
-	auto R = [&](int l) { return base(l); };
-	auto Z = [&](int l) { return base(l) + mg.lev[l].nx * mg.lev[l].ny; };
-	auto S = [&](int l) { return base(l) + 2 * mg.lev[l].nx * mg.lev[l].ny; };
 	const float w = mg.omega, cx = mg.cx, cy = mg.cy;
 	// r of the first shared level from the distributed level above it
 	{
 		const MgLevel& f = mg.lev[mg.nlev - 1];
 		const MgLevel& c = mg.lev[mg.nlev];
-		for (int k = tid; k < c.nx * c.ny; k += T) {
+		float* r = base(mg.nlev);
+		mg_pass<4>(tid, T, c.nx * c.ny, [&](int k) {
 			const int I = k / c.ny, J = k - I * c.ny;
-			R(mg.nlev)[k] = mg_restrict(gl, f.S, I, J, f.nx, f.ny);
-		}
+			return mg_restrict(gl, f.S, I, J, f.nx, f.ny);
+		}, [&](int k, float v) { r[k] = v; });
 	}
 	__syncthreads();
-	// down
+	// down: s = r - A (w iD r), then r of the next level
 	for (int l = mg.nlev; l < mg.ntot - 1; ++l) {
 		const MgLevel& L = mg.lev[l];
 		const int n = L.nx * L.ny;
-		for (int k = tid; k < n; k += T) Z(l)[k] = w * R(l)[k] / __ldg(L.D + k);
-		__syncthreads();
+		float* r = base(l);
+		float* s = r + 2 * n;
 		for (int k = tid; k < n; k += T) {
 			const int I = k / L.ny, J = k - I * L.ny;
-			S(l)[k] = R(l)[k] - mg_apply(sl, Z(l), L.D, I, J, L.nx, L.ny, cx, cy);
+			s[k] = mg_resid(ro, sl, r, L.D, L.iD, I, J, L.nx, L.ny, cx, cy, w);
 		}
 		__syncthreads();
 		const MgLevel& C = mg.lev[l + 1];
+		float* rc = base(l + 1);
 		for (int k = tid; k < C.nx * C.ny; k += T) {
 			const int I = k / C.ny, J = k - I * C.ny;
-			R(l + 1)[k] = mg_restrict(sl, S(l), I, J, L.nx, L.ny);
+			rc[k] = mg_restrict(sl, s, I, J, L.nx, L.ny);
 		}
 		__syncthreads();
 	}
@@ -207,41 +253,45 @@ __device__ void mg_coarse(const MgArgs& mg, float* sm) {
 		const int l = mg.ntot - 1;
 		const MgLevel& L = mg.lev[l];
 		const int n = L.nx * L.ny;
+		float* r = base(l);
+		float* z = r + n;
+		float* s = r + 2 * n;
 		for (int k = tid; k < n; k += T) {
-			const float d = __ldg(L.D + k);
-			Z(l)[k] = d > 0.f ? (n == 1 ? R(l)[k] / d : w * R(l)[k] / d) : 0.f;
+			const float id = __ldg(L.iD + k);
+			z[k] = (n == 1 ? r[k] : w * r[k]) * id;
 		}
 		__syncthreads();
 		if (n > 1) {
 			for (int sweep = 1; sweep < kMgCoarseSweeps; ++sweep) {
 				for (int k = tid; k < n; k += T) {
 					const int I = k / L.ny, J = k - I * L.ny;
-					const float d = __ldg(L.D + k);
-					S(l)[k] = d > 0.f
-							? fmaf(w, (R(l)[k] - mg_apply(sl, Z(l), L.D, I, J, L.nx, L.ny, cx, cy)) / d,
-									Z(l)[k])
-							: 0.f;
+					s[k] = fmaf(w * (r[k] - mg_apply(sl, z, L.D, I, J, L.nx, L.ny, cx, cy)),
+							__ldg(L.iD + k), z[k]);
 				}
 				__syncthreads();
-				for (int k = tid; k < n; k += T) Z(l)[k] = S(l)[k];
+				for (int k = tid; k < n; k += T) z[k] = s[k];
 				__syncthreads();
 			}
 		}
 	}
-	// up: the post-smoothed value goes to s, then back to z
+	// up: the post-smoothed correction into z (this level's z is not read
+	// by the pass: c is recomputed from r and the coarser z)
 	for (int l = mg.ntot - 2; l >= mg.nlev; --l) {
 		const MgLevel& L = mg.lev[l];
+		const MgLevel& C = mg.lev[l + 1];
 		const int n = L.nx * L.ny;
+		float* r = base(l);
+		float* z = r + n;
+		const float* zc = base(l + 1) + C.nx * C.ny;
 		for (int k = tid; k < n; k += T) {
 			const int I = k / L.ny, J = k - I * L.ny;
-			S(l)[k] = mg_post(sl, Z(l), Z(l + 1), R(l), L.D, I, J, L.nx, L.ny, cx, cy, w);
+			z[k] = mg_post(ro, sl, sl, r, zc, L.D, L.iD, I, J, L.nx, L.ny, cx, cy, w);
 		}
-		__syncthreads();
-		for (int k = tid; k < n; k += T) Z(l)[k] = S(l)[k];
 		__syncthreads();
 	}
 	const MgLevel& L = mg.lev[mg.nlev];
-	for (int k = tid; k < L.nx * L.ny; k += T) __stcg(L.Zp + k, Z(mg.nlev)[k]);
+	const float* z = base(mg.nlev) + L.nx * L.ny;
+	for (int k = tid; k < L.nx * L.ny; k += T) __stcg(L.Zp + k, z[k]);
 }
 
 }  // namespace cg_dev

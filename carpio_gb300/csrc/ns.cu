@@ -242,12 +242,15 @@ __device__ __forceinline__ double limiter(int sch, double r, double R) {
 // lengths are the powers of two of Geo::p2, so the divisions by them are
 // multiplications by exact reciprocals (the same bits); the divisions by
 // data stay.
+// The field may sit in another array than the faces (a tile in shared
+// memory): f at index fa with stride fst along the axis; the faces at the
+// grid's index of (i, j).
 template<int SCH, int D, bool P2 = false>
-__device__ __forceinline__ double adv_axis(const Geo& g, const double* face,
-		const double* f, int i, int j) {
+__device__ __forceinline__ double adv_axis_at(const Geo& g, const double* face,
+		const double* f, int fa, int fst, int i, int j) {
 	const int st = D == 0 ? g.P : 1;
 	const int a = g.at(i, j);
-#define F(k) f[a + (k) * st]
+#define F(k) f[fa + (k) * fst]
 #define C(k) (D == 0 ? g.CX(i + (k)) : g.CY(j + (k)))
 #define S(k) (D == 0 ? g.SX(i + (k)) : g.SY(j + (k)))
 	double fa0 = face[a], fam = face[a - st];
@@ -297,6 +300,12 @@ __device__ __forceinline__ double adv_axis(const Geo& g, const double* face,
 #undef F
 #undef C
 #undef S
+}
+
+template<int SCH, int D, bool P2 = false>
+__device__ __forceinline__ double adv_axis(const Geo& g, const double* face,
+		const double* f, int i, int j) {
+	return adv_axis_at<SCH, D, P2>(g, face, f, g.at(i, j), D == 0 ? g.P : 1, i, j);
 }
 
 template<int SCH, bool P2 = false>
@@ -483,6 +492,106 @@ __global__ void __launch_bounds__(kThreads) k_advect_band(Geo g, double* phi, Bc
 			if (threadIdx.x == 0) st_release_gpu(&prog[b], base + (unsigned)l + 1u);
 		}
 		if (!grid_sync(gc)) return;
+	}
+}
+
+// The sweep as a wavefront of tiles: TB x TB tiles of cells, tile (I, J)
+// after (I - 1, J) and (I, J - 1) -- the only tiles holding cells it reads
+// new values of (its axis cross of radius 2 reaches no diagonal tile); the
+// tiles after it are not started, so the old values it reads are still
+// there. A tile is staged in shared memory with a halo of two cells, swept
+// by its own anti-diagonals with block barriers between them (the cell
+// update and its arithmetic are adv_cell's), written back, and published
+// by a release store of the step number; the next tiles acquire it. Tiles
+// are handed out in anti-diagonal order from a counter, so a block waits
+// only on tiles taken earlier by blocks that are running (the launch is
+// cooperative): no deadlock. Per step: block 0 refills phi's ghosts between
+// two grid barriers. Bit for bit the sequential loop's values, like
+// k_advect.
+constexpr int kAdvTile = 32;
+constexpr int kAdvTileThreads = 128;
+
+template<int SCH, bool P2 = false>
+__global__ void __launch_bounds__(kAdvTileThreads) k_advect_tiles(Geo g, double* phi,
+		BcDev bc, const double* uf, const double* vf, double dt, int steps,
+		const int* order, int ntj, int nt, unsigned* done, unsigned* ctr, GridCtl gc) {
+	constexpr int TB = kAdvTile, SP = kAdvTile + 4;
+	__shared__ double tile[SP * SP];
+	__shared__ double s_old[32];
+	__shared__ int s_t, s_ok;
+	gc.start();
+	const int tid = threadIdx.x;
+	for (int st = 0; st < steps; ++st) {
+		if (!grid_sync(gc)) return;
+		if (blockIdx.x == 0) {
+			bc_fill(g, phi, bc, s_old);
+			if (tid == 0) ctr[(st + 1) & 1] = 0u;
+		}
+		if (!grid_sync(gc)) return;
+		for (;;) {
+			if (tid == 0) s_t = (int)atomicAdd(&ctr[st & 1], 1u);
+			__syncthreads();
+			const int t = s_t;
+			__syncthreads();
+			if (t >= nt) break;
+			const int id = order[t];
+			const int I = id / ntj, J = id - I * ntj;
+			const int i0 = I * TB, j0 = J * TB;
+			const int ti = min(TB, g.nx - i0), tj = min(TB, g.ny - j0);
+			// the tiles above and to the left, this step
+			if (tid == 0) {
+				const unsigned need = (unsigned)st + 1u;
+				int ok = 1;
+				unsigned polls = 0;
+				unsigned long long t0 = 0;
+				while ((I > 0 && ld_acquire_gpu(&done[id - ntj]) < need)
+						|| (J > 0 && ld_acquire_gpu(&done[id - 1]) < need)) {
+					if ((++polls & 63u) == 0) {
+						if (*(volatile int*)gc.err) { ok = 0; break; }
+						const unsigned long long tt = globaltimer();
+						if (t0 == 0) t0 = tt;
+						if (tt - t0 > gc.wait_ns || tt > gc.deadline) {
+							set_err(gc, CARPIO_GPU_ETIMEOUT);
+							ok = 0;
+							break;
+						}
+					}
+				}
+				s_ok = ok;
+			}
+			__syncthreads();
+			if (!s_ok) return;
+			// stage the tile and its halo of two (ghosts included)
+			for (int q = tid; q < (ti + 4) * (tj + 4); q += kAdvTileThreads) {
+				const int li = q / (tj + 4), lj = q - li * (tj + 4);
+				tile[li * SP + lj] = ldcg(phi + g.at(i0 + li - 2, j0 + lj - 2));
+			}
+			__syncthreads();
+			// the tile's anti-diagonals
+			for (int L = 0; L <= ti + tj - 2; ++L) {
+				const int li = tid;
+				const int lj = L - tid;
+				if (tid < TB && li < ti && lj >= 0 && lj < tj) {
+					const int i = i0 + li, j = j0 + lj;
+					const int fa = (li + 2) * SP + (lj + 2);
+					double a0 = adv_axis_at<SCH, 0, P2>(g, uf, tile, fa, SP, i, j);
+					double a1 = adv_axis_at<SCH, 1, P2>(g, vf, tile, fa, 1, i, j);
+					double adv = 0.0;
+					adv += a0;
+					adv += a1;
+					const double phin = tile[fa];
+					tile[fa] = phin - dt * adv;
+				}
+				__syncthreads();
+			}
+			for (int q = tid; q < ti * tj; q += kAdvTileThreads) {
+				const int li = q / tj, lj = q - li * tj;
+				phi[g.at(i0 + li, j0 + lj)] = tile[(li + 2) * SP + (lj + 2)];
+			}
+			// the block barrier orders the writes before thread 0's release
+			__syncthreads();
+			if (tid == 0) st_release_gpu(&done[id], (unsigned)st + 1u);
+		}
 	}
 }
 
@@ -943,6 +1052,26 @@ const void* pick_advect_band(int sch, bool p2) {
 	return nullptr;
 }
 
+template<int S>
+const void* advect_tiles_kernel(bool p2) {
+	return p2 ? (const void*)k_advect_tiles<S, true> : (const void*)k_advect_tiles<S, false>;
+}
+
+const void* pick_advect_tiles(int sch, bool p2) {
+	switch (sch) {
+	case CARPIO_GPU_UPWIND1: return advect_tiles_kernel<CARPIO_GPU_UPWIND1>(p2);
+	case CARPIO_GPU_CENTER: return advect_tiles_kernel<CARPIO_GPU_CENTER>(p2);
+	case CARPIO_GPU_CENTER4: return advect_tiles_kernel<CARPIO_GPU_CENTER4>(p2);
+	case CARPIO_GPU_UPWIND2: return advect_tiles_kernel<CARPIO_GPU_UPWIND2>(p2);
+	case CARPIO_GPU_VANLEER: return advect_tiles_kernel<CARPIO_GPU_VANLEER>(p2);
+	case CARPIO_GPU_SUPERBEE: return advect_tiles_kernel<CARPIO_GPU_SUPERBEE>(p2);
+	case CARPIO_GPU_WAHYD: return advect_tiles_kernel<CARPIO_GPU_WAHYD>(p2);
+	case CARPIO_GPU_QUICK: return advect_tiles_kernel<CARPIO_GPU_QUICK>(p2);
+	case CARPIO_GPU_CUI: return advect_tiles_kernel<CARPIO_GPU_CUI>(p2);
+	}
+	return nullptr;
+}
+
 cudaError_t launch_advect(int sch, const Geo& geo, cudaStream_t s, double* phi,
 		const BcDev& bc, const double* uf, const double* vf, double dt, int steps) {
 	const size_t smem = sizeof(double) * 2 * geo.gl * geo.gl;
@@ -1393,6 +1522,7 @@ struct carpio_gpu_advection {
 	carpio_gpu_grid* g;
 	cg_host::LaunchWs lw;     // control words of the band sweep
 	cg_host::DevBuf prog;     // its progress word per band
+	cg_host::DevBuf tord, tdone;   // tile sweep: anti-diagonal order, done words + counters
 	cg_host::DevBuf fields;   // u v uf vf phi, then the ghost values of u v phi
 	double* f[8];
 	carpio_gpu_bc bc[3];      // u v phi
@@ -1513,13 +1643,51 @@ int carpio_gpu_advection_step(carpio_gpu_advection* a, double dt, int steps) {
 	const BcDev bcp = to_dev(a->bc[2], a->has_gv[2] ? a->f[7] : nullptr);
 	// one block while the diagonals are short: it clears ~0.06 us of FP64
 	// work per cell (van Leer: ~20 divisions a cell); longer ones go to the
-	// pipelined bands, one per SM, whose diagonals cost ~20 us (one cell's
-	// dependent FP64 chain plus the hand-off) whatever their length
+	// tile wavefront (two ghost layers or more), else to the pipelined bands
+	// of rows, one per SM, whose diagonals cost ~20 us (a hand-off through
+	// L2 per diagonal) whatever their length
 	const double avg_diag = (double)g->nx * g->ny / (double)(g->nx + g->ny - 1);
 	if (avg_diag < 64.0 || g->nx < 8) {
 		CG_CK(launch_advect(a->scheme, geo, a->s, a->f[4], bcp, a->f[2], a->f[3], dt, steps));
 		CG_CK(cudaStreamSynchronize(a->s));
 		return 0;
+	}
+	if (g->gl >= 2 && g->gl <= 4) {
+		// the tile wavefront (k_advect_tiles)
+		const void* kt = pick_advect_tiles(a->scheme, geo.p2 != 0);
+		if (!kt) return CARPIO_GPU_EINVAL;
+		const int TB = kAdvTile;
+		const int nti = (g->nx + TB - 1) / TB, ntj = (g->ny + TB - 1) / TB;
+		const int nt = nti * ntj;
+		std::vector<int> ord;
+		ord.reserve(nt);
+		for (int d = 0; d <= nti + ntj - 2; ++d)
+			for (int I = std::max(0, d - ntj + 1); I <= std::min(d, nti - 1); ++I)
+				ord.push_back(I * ntj + (d - I));
+		int rc;
+		if ((rc = to_device(a->tord, ord.data(), sizeof(int) * ord.size(), a->s))) return rc;
+		if ((rc = a->tdone.ensure(sizeof(unsigned) * ((size_t)nt + 2)))) return rc;
+		CG_CK(cudaMemsetAsync(a->tdone.p, 0, sizeof(unsigned) * ((size_t)nt + 2), a->s));
+		const int blocks = std::max(1, std::min({ coop_blocks(kt, (long)nt * kAdvTileThreads, 1),
+				sm_count(), nt }));
+		if ((rc = a->lw.ensure(blocks))) return rc;
+		CG_CK(cudaMemsetAsync(a->lw.ctl.p, 0, sizeof(Ctl), a->s));
+		GridCtl gc = make_gridctl(a->lw);
+		double* phi = a->f[4];
+		const double* uf = a->f[2];
+		const double* vf = a->f[3];
+		const int* order = a->tord.as<int>();
+		unsigned* done = a->tdone.as<unsigned>();
+		unsigned* ctr = done + nt;
+		Geo gg = geo;
+		BcDev bb = bcp;
+		int ntj_ = ntj, nt_ = nt;
+		void* args[] = { &gg, &phi, &bb, &uf, &vf, &dt, &steps, &order, &ntj_, &nt_, &done,
+			&ctr, &gc };
+		CG_CK(cudaLaunchCooperativeKernel(kt, blocks, kAdvTileThreads, args, 0, a->s));
+		CG_CK(cudaMemcpyAsync(a->lw.host_ctl, a->lw.ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, a->s));
+		CG_CK(cudaStreamSynchronize(a->s));
+		return a->lw.host_ctl->err;
 	}
 	const void* k = pick_advect_band(a->scheme, geo.p2 != 0);
 	if (!k) return CARPIO_GPU_EINVAL;

@@ -273,21 +273,29 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	auto precond_mg = [&](float (&g)[2]) -> bool {
 		const float w = mg.omega, cx = mg.cx, cy = mg.cy;
 		const LdL2 gld;
+		const LdRo ro;
 		const MgLevel& L0 = mg.lev[0];
-		// level 0: R0 = r and the pre-smoothed Z0 = w r / D0 of the band
+		// level 0's diagonal is the band's own (dd); its reciprocal rounds
+		// like the host-built L0.iD used outside the band
+		auto r0at = [&](int i, int j) -> float {
+			const int lr = i - r0;
+			return (lr >= 0 && lr < rows) ? rs[lr * ny + j] : ldcg(L0.R + i * ny + j);
+		};
+		auto id0at = [&](int i, int j) -> float {
+			const int lr = i - r0;
+			return (lr >= 0 && lr < rows) ? __frcp_rn(dd[lr * ny + j]) : __ldg(L0.iD + i * ny + j);
+		};
+		// level 0: R0 = r of the band, for the neighbours
 #pragma unroll
 		for (int lr = 0; lr < RM; ++lr)
 #pragma unroll
 			for (int k = 0; k < NC; ++k) {
 				const int j = tid + k * T;
-				if (lr < rows && j < ny) {
-					const int k0 = (r0 + lr) * ny + j;
-					const float rv = rs[lr * ny + j];
-					__stcg(L0.R + k0, rv);
-					__stcg(L0.Z + k0, w * rv / __ldg(L0.D + k0));
-				}
+				if (lr < rows && j < ny) __stcg(L0.R + (r0 + lr) * ny + j, rs[lr * ny + j]);
 			}
 		if (!grid_sync(gc)) return false;
+		// S0 = r - A0 (w iD r) on the band (the pre-smoothed correction is
+		// recomputed from r wherever it is needed, never stored)
 #pragma unroll
 		for (int lr = 0; lr < RM; ++lr)
 #pragma unroll
@@ -295,8 +303,14 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				const int j = tid + k * T;
 				if (lr < rows && j < ny) {
 					const int i = r0 + lr;
-					__stcg(L0.S + i * ny + j, rs[lr * ny + j]
-							- mg_apply(gld, L0.Z, L0.D, i, j, nx, ny, cx, cy));
+					const float rk = rs[lr * ny + j];
+					const float dk = dd[lr * ny + j];
+					float v = dk * (w * rk * __frcp_rn(dk));
+					if (i > 0) v = fmaf(cx, w * r0at(i - 1, j) * id0at(i - 1, j), v);
+					if (i < nx - 1) v = fmaf(cx, w * r0at(i + 1, j) * id0at(i + 1, j), v);
+					if (j > 0) v = fmaf(cy, w * rs[lr * ny + j - 1] * __frcp_rn(dd[lr * ny + j - 1]), v);
+					if (j < ny - 1) v = fmaf(cy, w * rs[lr * ny + j + 1] * __frcp_rn(dd[lr * ny + j + 1]), v);
+					__stcg(L0.S + i * ny + j, rk - v);
 				}
 			}
 		if (!grid_sync(gc)) return false;
@@ -305,17 +319,15 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 			const MgLevel& F = mg.lev[l - 1];
 			const MgLevel& L = mg.lev[l];
 			const int n = L.nx * L.ny;
-			for (int k = gt; k < n; k += G) {
+			mg_pass<4>(gt, G, n, [&](int k) {
 				const int I = k / L.ny, J = k - I * L.ny;
-				const float rv = mg_restrict(gld, F.S, I, J, F.nx, F.ny);
-				__stcg(L.R + k, rv);
-				__stcg(L.Z + k, w * rv / __ldg(L.D + k));
-			}
+				return mg_restrict(gld, F.S, I, J, F.nx, F.ny);
+			}, [&](int k, float v) { __stcg(L.R + k, v); });
 			if (!grid_sync(gc)) return false;
-			for (int k = gt; k < n; k += G) {
+			mg_pass<4>(gt, G, n, [&](int k) {
 				const int I = k / L.ny, J = k - I * L.ny;
-				__stcg(L.S + k, ldcg(L.R + k) - mg_apply(gld, L.Z, L.D, I, J, L.nx, L.ny, cx, cy));
-			}
+				return mg_resid(ro, gld, L.R, L.D, L.iD, I, J, L.nx, L.ny, cx, cy, w);
+			}, [&](int k, float v) { __stcg(L.S + k, v); });
 			if (!grid_sync(gc)) return false;
 		}
 		if (c == 0) mg_coarse(mg, mgsm);
@@ -323,22 +335,22 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 		for (int l = mg.nlev - 1; l >= 1; --l) {
 			const MgLevel& L = mg.lev[l];
 			const MgLevel& Cl = mg.lev[l + 1];
-			const int n = L.nx * L.ny;
-			for (int k = gt; k < n; k += G) {
+			mg_pass<2>(gt, G, L.nx * L.ny, [&](int k) {
 				const int I = k / L.ny, J = k - I * L.ny;
-				__stcg(L.Zp + k, mg_post(gld, L.Z, Cl.Zp, L.R, L.D, I, J, L.nx, L.ny, cx, cy, w));
-			}
+				return mg_post(ro, gld, gld, L.R, Cl.Zp, L.D, L.iD, I, J, L.nx, L.ny, cx, cy, w);
+			}, [&](int k, float v) { __stcg(L.Zp + k, v); });
 			if (!grid_sync(gc)) return false;
 		}
-		// level 0: c = Z0 + P z1 on the band and its halo rows, then the
+		// level 0: c = w iD r + P z1 on the band and its halo rows, then the
 		// post-smoothed z of the band
 		const MgLevel& L1 = mg.lev[1];
-		for (int t = tid; t < (rows + 2) * ny; t += T) {
+		mg_pass<4>(tid, T, (rows + 2) * ny, [&](int t) {
 			const int lr = t / ny - 1, j = t - (lr + 1) * ny;
 			const int i = r0 + lr;
-			mgc[t] = (i >= 0 && i < nx)
-					? mg_corrected(gld, L0.Z, L1.Zp, i, j, ny, L1.nx, L1.ny) : 0.f;
-		}
+			return (i >= 0 && i < nx)
+					? fmaf(w * r0at(i, j), id0at(i, j), mg_prolong(gld, L1.Zp, i, j, L1.nx, L1.ny))
+					: 0.f;
+		}, [&](int t, float v) { mgc[t] = v; });
 		__syncthreads();
 		g[0] = g[1] = 0.f;
 #pragma unroll
@@ -349,14 +361,14 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				if (lr < rows && j < ny) {
 					const int i = r0 + lr, cc = lr * ny + j, pk = (lr + 1) * ny + j;
 					const float cv = mgc[pk];
-					const float d = __ldg(L0.D + i * ny + j);
+					const float d = dd[cc];
 					float ac = d * cv;
 					if (i > 0) ac = fmaf(cx, mgc[pk - ny], ac);
 					if (i < nx - 1) ac = fmaf(cx, mgc[pk + ny], ac);
 					if (j > 0) ac = fmaf(cy, mgc[pk - 1], ac);
 					if (j < ny - 1) ac = fmaf(cy, mgc[pk + 1], ac);
 					const float rv = rs[cc];
-					const float z = fmaf(w, (rv - ac) / d, cv);
+					const float z = fmaf(w * (rv - ac), __frcp_rn(d), cv);
 					zs[cc] = z;
 					g[0] = fmaf(rv, z, g[0]);
 					g[1] = fmaf(rv, rv, g[1]);
@@ -1095,9 +1107,17 @@ int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
 		// each level's diagonal: every face contributes -c; a boundary face
 		// folds like the fine grid's ghost substitution (Dirichlet: -2c in
 		// all, Neumann: 0)
-		for (const auto& dm : c.mg_dims) {
+		// level 0 is the fine grid's own FP32 diagonal (the tile kernel's
+		// band copy), the coarser ones follow the rule above; then every
+		// level's reciprocal
+		for (size_t l = 0; l < c.mg_dims.size(); ++l) {
+			const auto& dm = c.mg_dims[l];
 			for (int I = 0; I < dm.first; ++I)
 				for (int J = 0; J < dm.second; ++J) {
+					if (l == 0) {
+						mgd.push_back(D32[(size_t)(I + gl) * g->P + (J + gl)]);
+						continue;
+					}
 					double d = 0.0;
 					d += I > 0 ? -cxd : (bc.type[0] == 1 ? -2.0 * cxd : 0.0);
 					d += I < dm.first - 1 ? -cxd : (bc.type[1] == 1 ? -2.0 * cxd : 0.0);
@@ -1106,6 +1126,8 @@ int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
 					mgd.push_back((float)d);
 				}
 		}
+		const size_t nd = mgd.size();
+		for (size_t k = 0; k < nd; ++k) mgd.push_back(mgd[k] > 0.f ? 1.0f / mgd[k] : 0.f);
 		if (c.mg_nlev > 0 && (rc = to_device(c.mgD, mgd.data(), sizeof(float) * mgd.size(), s)))
 			return rc;
 	}
@@ -1348,7 +1370,7 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 				coarse += 3 * (size_t)c.mg_dims[l].first * c.mg_dims[l].second;
 			const size_t msmem = base + sizeof(float) * ((size_t)rows_max * g->ny + np + coarse);
 			for (int l = 0; l <= c.mg_nlev; ++l)
-				work += (l == 0 ? 3 : l < c.mg_nlev ? 4 : 1)
+				work += (l == 0 ? 2 : l < c.mg_nlev ? 3 : 1)
 						* (size_t)c.mg_dims[l].first * c.mg_dims[l].second;
 			if (msmem <= 220 * 1024) {
 				if ((rc = w.mg.ensure(sizeof(float) * work))) return rc;
@@ -1358,6 +1380,8 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 				m.cx = c.mg_cx;
 				m.cy = c.mg_cy;
 				m.omega = 0.8f;
+				size_t nd = 0;
+				for (int l = 0; l < ntot; ++l) nd += (size_t)c.mg_dims[l].first * c.mg_dims[l].second;
 				const float* dp = c.mgD.as<float>();
 				float* wp = w.mg.as<float>();
 				for (int l = 0; l < ntot; ++l) {
@@ -1366,13 +1390,14 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 					L.nx = c.mg_dims[l].first;
 					L.ny = c.mg_dims[l].second;
 					L.D = dp;
+					L.iD = dp + nd;
 					dp += n;
 					if (l == 0) {
-						L.R = wp; L.Z = wp + n; L.S = wp + 2 * n;
-						wp += 3 * n;
+						L.R = wp; L.S = wp + n;
+						wp += 2 * n;
 					} else if (l < c.mg_nlev) {
-						L.R = wp; L.Z = wp + n; L.S = wp + 2 * n; L.Zp = wp + 3 * n;
-						wp += 4 * n;
+						L.R = wp; L.S = wp + n; L.Zp = wp + 2 * n;
+						wp += 3 * n;
 					} else if (l == c.mg_nlev) {
 						L.Zp = wp;
 						wp += n;

@@ -395,9 +395,12 @@ int carpio_gpu_advection_get(carpio_gpu_advection* a, double* u, double* v,
  * one persistent launch, replayed from a CUDA graph. Each problem is solved as
  * carpio_gpu_poisson_solve solves one grid with the MIXED CG: FP32 inner
  * iterations, FP64 residual, solution and mean removal, the same stopping
- * test. The launch is made of thread-block clusters; a problem is owned by a
- * team of 1..16 CTAs of one cluster (bands of x-rows), whose reductions and
- * halo rows travel through distributed shared memory.
+ * test. Two kernels: by default one CTA per problem, problems taken largest
+ * first from a queue, with the geometric-multigrid V-cycle as the FP32 CG's
+ * preconditioner (block barriers only); when the tiles name a cluster size,
+ * thread-block clusters in which a problem is owned by a team of 1..16 CTAs
+ * (bands of x-rows, plain FP32 CG), whose reductions and halo rows travel
+ * through distributed shared memory.
  *
  * The batch keeps its fields on the device in the layout of a grid with one
  * ghost layer ((nx+2) x (ny+2) doubles, y contiguous, ghosts zero).
@@ -415,8 +418,11 @@ typedef struct {
 
 /* Launch configuration ("tiles"); 0 in a field lets the library choose. */
 typedef struct {
-	int threads;        /* threads per CTA: 256 or 512 */
-	int cluster;        /* CTAs per cluster: 1, 2, 4, 8 or 16 */
+	int threads;        /* threads per CTA: 256 or 512 (cluster teams), 256,
+	                       512 or 1024 (multigrid) */
+	int cluster;        /* CTAs per cluster: 1, 2, 4, 8 or 16 selects the
+	                       cluster-team kernel; 0 the multigrid kernel
+	                       (reported as 1) */
 	int cells_per_cta;  /* target cells per CTA when sizing a problem's team */
 	int use_graph;      /* >= 0: replay a captured CUDA graph; < 0: plain launch */
 } carpio_gpu_batch_tiles;

@@ -1,8 +1,9 @@
 """GPU checks of the batched Poisson solver (carpio_gpu_batch_*): every
 problem of an uneven batch against the oracle (the reference's assembly and
-FP64 CG, with mean removal for all-Neumann problems), on one CTA per problem
-and on teams of up to 16 CTAs that share reductions and halo rows through
-distributed shared memory; repeatability, graph vs plain launch, limits."""
+FP64 CG, with mean removal for all-Neumann problems), with the default
+kernel (one CTA per problem, multigrid-preconditioned) and with the cluster
+kernel (teams of up to 16 CTAs that share reductions and halo rows through
+distributed shared memory); repeatability, graph vs plain launch, limits."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -189,10 +190,15 @@ def test_zero_source_and_warm_start(gpu_lib):
 
 
 def test_rejects_what_does_not_fit(gpu_lib):
+    """the cluster kernel keeps a problem on chip: 1024^2 fits no team of 16
+    CTAs; the block size must be one it is built for"""
     from carpio_gb300 import _lib
     from carpio_gb300.batch import BatchedPoisson, Problem
     with pytest.raises(_lib.CarpioGpuError):
-        BatchedPoisson([Problem(1024, 1024)], tol=TOL)
+        BatchedPoisson([Problem(1024, 1024)], tol=TOL,
+                       tiles=dict(threads=512, cluster=16, cells_per_cta=16384))
+    with pytest.raises(_lib.CarpioGpuError):
+        BatchedPoisson([Problem(64, 64)], tol=TOL, tiles=dict(threads=384))
     with pytest.raises(_lib.CarpioGpuError):
         BatchedPoisson([Problem(64, 64)], tol=TOL,
                        tiles=dict(threads=384, cluster=8, cells_per_cta=4096))
@@ -238,3 +244,46 @@ def test_watchdog_expiry_is_reported(gpu_lib):
         gpu_lib.carpio_gpu_set_watchdog(2000, 600000)
     bp.zero(1)
     assert bp.run() == 0
+
+
+def test_multigrid_kernel_graph_repeatable_and_large(gpu_lib):
+    """the default kernel (one CTA per problem, V-cycle preconditioner):
+    bitwise repeatable, the captured graph equals a plain launch, a few
+    V-cycles per problem, and problems too large for a cluster team (512^2,
+    1024 x 256) solved like carpio_gpu_poisson_solve solves them"""
+    from carpio_gb300 import structure as S
+    from carpio_gb300.batch import BatchedPoisson, NEUMANN, Problem
+    from carpio_gb300.workloads import gaussian_source
+    probs, srcs = problem_set(11, [64, 96, 130, 48, 33, 16])
+    a = BatchedPoisson(probs, tol=TOL)
+    s1 = a.solve(srcs)
+    s2 = a.solve(srcs)
+    b = BatchedPoisson(probs, tol=TOL, tiles=dict(use_graph=-1))
+    s3 = b.solve(srcs)
+    for x, y, z in zip(s1, s2, s3):
+        assert np.array_equal(x, y) and np.array_equal(x, z)
+    assert a.info()["cluster"] == 1 and a.info()["teams"][0] == len(probs)
+    check(probs, srcs, s1, a.stats)
+    for p, st in zip(probs, a.stats):
+        if p.nx % 8 == 0 and p.ny % 8 == 0:
+            assert st["iters"] <= 60, (p.nx, p.ny, st)
+    rng = np.random.default_rng(12)
+    big = [Problem(512, 512, bc=[(NEUMANN, 0.0)] * 4), Problem(1024, 256)]
+    bsrc = [gaussian_source(p.nx, p.ny, rng) for p in big]
+    bp = BatchedPoisson(big, tol=TOL)
+    sols = bp.solve(bsrc)
+    for p, src, sol, st in zip(big, bsrc, sols, bp.stats):
+        assert st["code"] == 0 and st["resid"] <= TOL
+        g = S.Grid(p.box[0], p.box[1], (p.nx, p.ny), 1)
+        P = S.Poisson(g)
+        for seg, (t, v) in enumerate(p.bc):
+            bc = S.BoundaryCondition()
+            (bc.set_default_1_bc if t == 1 else bc.set_default_2_bc)(v)
+            P.add_bc(0, seg, "phi", bc)
+        f = g.zeros()
+        f[1:-1, 1:-1] = src
+        P.set_depend(g.zeros(), None, f)
+        P.set_solver("CG", None, 100000, 1e-10, mean_removal=p.mean_removal,
+                     precision="mixed")
+        assert P.run() == 0
+        assert rel_l2(sol, g.interior(P.phi)) <= 1e-4
