@@ -40,8 +40,17 @@ __global__ void __launch_bounds__(1024) k_csr_solve_ic(CsrOp op, IcOp ic,
 		Vecs<double> v, SolveCtl sc, GridCtl gc) {
 	gc.start();
 	int bank = 0;
-	if (sc.kind == CARPIO_GPU_IC_CGS) ic_cgs_run(ic.n, op, ic, v, sc, gc, bank);
-	else ic_cg_run(ic.n, op, ic, v, sc, gc, bank);
+	if (sc.kind == CARPIO_GPU_IC_CGS) ic_cgs_run<false>(ic.n, op, ic, v, sc, gc, bank);
+	else ic_cg_run<false>(ic.n, op, ic, v, sc, gc, bank);
+}
+
+// the five-point wavefront (ic.grid): block 0 holds one lane per grid row
+__global__ void __launch_bounds__(kIcGridThreads, 1) k_csr_solve_ic_grid(CsrOp op, IcOp ic,
+		Vecs<double> v, SolveCtl sc, GridCtl gc) {
+	gc.start();
+	int bank = 0;
+	if (sc.kind == CARPIO_GPU_IC_CGS) ic_cgs_run<true>(ic.n, op, ic, v, sc, gc, bank);
+	else ic_cg_run<true>(ic.n, op, ic, v, sc, gc, bank);
 }
 
 // carpio::Residual (solver_matrix.hpp:583-597), first part: r = b - A x per
@@ -96,6 +105,7 @@ struct CsrWs {
 	cg_host::DevBuf rp, ci, va, vec, hist;
 	cg_host::DevBuf icd, icu[3], icl[3], icf[2], icb[2];   // IC factor, levels
 	cg_host::DevBuf ick[2], icn[2], icc[2], icv[2];         // packed level rows
+	cg_host::DevBuf icg[3];                                 // five-point factor
 	cg_host::DevBuf rx, rb, rpart;   // Residual: staged x, b; partials + result
 	cg_host::DevBuf va32, vec32;     // MIXED: FP32 values and vectors
 };
@@ -291,6 +301,53 @@ extern "C" int carpio_gpu_krylov_csr(int kind, int n, int nnz,
 		icop.bptr = w.icb[0].as<uint32_t>();
 		icop.brows = w.icb[1].as<uint32_t>();
 		icop.nbl = (int)bptr.size() - 1;
+		// a five-point factor in natural order (every upper entry of row i at
+		// i + 1 within a grid row, or at i + m, one m for all rows): the
+		// wavefront sweeps of ic_sweep_grid, one lane per grid row
+		int gm = 0;
+		bool grid = !(flags & CARPIO_GPU_FLAG_NO_TILE);
+		for (int i = 0; i < n && grid; ++i)
+			for (uint32_t e = up[i]; e < up[i + 1]; ++e) {
+				const long d = (long)ui[e] - i;
+				if (d == 1) continue;
+				if (!gm) gm = (int)d;
+				else if (d != gm) { grid = false; break; }
+			}
+		grid = grid && gm >= 2 && n % gm == 0 && n / gm <= kIcGridThreads;
+		for (int i = 0; i < n && grid; ++i) {
+			int near = 0, far = 0;
+			for (uint32_t e = up[i]; e < up[i + 1]; ++e) {
+				if (ui[e] == (uint32_t)i + 1) ++near;
+				else ++far;
+			}
+			if (near > 1 || far > 1 || (near && (i + 1) % gm == 0)) grid = false;
+		}
+		if (grid) {
+			std::vector<double> gf(2 * (size_t)n, 0.0), gb(2 * (size_t)n, 0.0), rd(n);
+			for (int i = 0; i < n; ++i) {
+				rd[i] = 1.0 / dg[i];
+				for (uint32_t e = up[i]; e < up[i + 1]; ++e) {
+					const uint32_t c = ui[e];
+					if (c == (uint32_t)i + 1) {
+						gf[2 * (size_t)c + 1] = uv[e];
+						gb[2 * (size_t)i] = uv[e];
+					} else {
+						gf[2 * (size_t)c] = uv[e];
+						gb[2 * (size_t)i + 1] = uv[e];
+					}
+				}
+			}
+			if ((rc = put(w.icg[0], gf.data(), sizeof(double) * gf.size()))) return rc;
+			if ((rc = put(w.icg[1], gb.data(), sizeof(double) * gb.size()))) return rc;
+			if ((rc = put(w.icg[2], rd.data(), sizeof(double) * rd.size()))) return rc;
+			CG_CK(cudaStreamSynchronize(s));
+			icop.grid = 1;
+			icop.gm = gm;
+			icop.gR = n / gm;
+			icop.gf = w.icg[0].as<double2>();
+			icop.gb = w.icg[1].as<double2>();
+			icop.grd = w.icg[2].as<double>();
+		}
 		// every level ends in a barrier: one block (block barriers, ~0.15 us)
 		// when that beats the grid (grid barriers, ~1.5 us, but all SMs on
 		// the ~10 vector passes of an iteration); a rough cost model, it
@@ -298,7 +355,7 @@ extern "C" int carpio_gpu_krylov_csr(int kind, int n, int nnz,
 		const double nlev = (double)icop.nfl + icop.nbl;
 		const double t1 = nlev * 0.15 + 10.0 * n / kThreads * 0.05;
 		const double tb = nlev * 1.5 + 10.0 * ((double)n / ((double)blocks * kThreads) * 0.05 + 1.5);
-		if (t1 < tb) blocks = 1;
+		if (t1 < tb && !grid) blocks = 1;
 		// one block whose vector fits in shared memory: the level sweeps
 		// run there on rows packed in level order (ic.cuh ic_apply_smem)
 		if (blocks == 1 && sizeof(double) * (size_t)n <= 200 * 1024) {
@@ -348,7 +405,18 @@ extern "C" int carpio_gpu_krylov_csr(int kind, int n, int nnz,
 	GridCtl gc = make_gridctl(w.lw);
 	if (ic) {
 		void* args[] = { &op, &icop, &v, &sc, &gc };
-		if (icop.smem) {
+		if (icop.grid) {
+			// block 0 runs the sweeps with one lane per grid row; the vector
+			// passes spread over blocks of the same size
+			const void* gk = (const void*)k_csr_solve_ic_grid;
+			int per_sm = 0;
+			CG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, gk, kIcGridThreads, 0));
+			const int gb = (int)std::max(1L, std::min((long)std::max(per_sm, 1) * sm_count(),
+					((long)n + kIcGridThreads - 1) / kIcGridThreads));
+			if ((rc = w.lw.ensure(gb))) return rc;
+			gc = make_gridctl(w.lw);
+			CG_CK(cudaLaunchCooperativeKernel(gk, gb, kIcGridThreads, args, 0, s));
+		} else if (icop.smem) {
 			// one block of 1024 threads with the vector in shared memory
 			const int sm = (int)(sizeof(double) * (size_t)n);
 			CG_CK(cudaFuncSetAttribute((const void*)k_csr_solve_ic,

@@ -34,6 +34,15 @@ struct IcOp {
 	const int *fn, *bn;                               // its entry count
 	const uint32_t *fc, *bc;                          // [position][kIcInline]
 	const double *fv, *bv;
+	// five-point factors in natural order (row k = j m + i coupled to k - 1
+	// and k + 1 within a grid row of length m, to k - m and k + m across
+	// rows, nothing wrapping around a row end): the two triangular solves run
+	// as a skewed wavefront in block 0 (ic_sweep_grid)
+	int grid;                                         // 1: use that path
+	int gm, gR;                                       // row length m, rows R
+	const double2* gf;      // forward {U(k-m, k), U(k-1, k)}, 0 where absent
+	const double2* gb;      // backward {U(k, k+1), U(k, k+m)}, 0 where absent
+	const double* grd;      // 1 / d_k
 };
 
 // One level position's packed row, loaded ahead of its level.
@@ -118,14 +127,169 @@ __device__ void ic_apply_smem(const IcOp& ic, const double* in, double* out, dou
 	__syncthreads();
 }
 
+// ------------------------------------------------- five-point wavefront --
+// The triangular solves of a factor with the five-point pattern, in one
+// block: lane l of warp w owns grid row j = 32 w + l and walks its m cells in
+// order, skewed one step behind lane l - 1 (forward; ahead of it backward),
+// so that the row neighbour's value is in the lane's own register and the
+// value across rows arrives by one warp shuffle from the previous step. Lane
+// 0 (forward) / 31 (backward) takes that value from the neighbouring warp
+// through a shared-memory ring with release/acquire counters. No block
+// barrier per level: a step is a shuffle and three FP64 operations.
+// The arithmetic is the reference's sequence of updates in its order
+// (ICPre::solve, preconditioner.hpp:143-161) with two relaxations: each
+// update is one fused multiply-add, and the division by d_k is a
+// multiplication by its reciprocal (both within a rounding of the
+// reference's per operation).
+constexpr int kIcRing = 64;        // columns in flight per warp boundary
+constexpr int kIcAhead = 8;        // steps between a cell's input load and its use
+constexpr int kIcGridThreads = 512; // block size of the wavefront launch: rows <= 512
+
+__device__ __forceinline__ int ic_ld_acquire(const int* p) {
+	int v;
+	asm volatile("ld.acquire.cta.shared.b32 %0, [%1];" : "=r"(v)
+			: "r"((uint32_t)__cvta_generic_to_shared(p)) : "memory");
+	return v;
+}
+__device__ __forceinline__ void ic_st_release(int* p, int v) {
+	asm volatile("st.release.cta.shared.b32 [%0], %1;"
+			:: "r"((uint32_t)__cvta_generic_to_shared(p)), "r"(v) : "memory");
+}
+__device__ __forceinline__ void ic_prefetch(const void* p) {
+	asm volatile("prefetch.global.L1 [%0];" :: "l"(p));
+}
+
+// Wait until *p >= want (cache keeps the last value read). Bounded: after
+// the launch's per-wait limit the error word is set, *abort raised and the
+// caller carries on without the value (the solve then ends with the error).
+__device__ __forceinline__ void ic_wait(const int* p, int want, int& cache,
+		volatile int* abort, const GridCtl& gc) {
+	if (cache >= want) return;
+	unsigned long long t0 = 0;
+	for (unsigned spin = 0;; ++spin) {
+		cache = ic_ld_acquire(p);
+		if (cache >= want || *abort) return;
+		if ((spin & 255u) == 255u) {
+			const unsigned long long t = globaltimer();
+			if (!t0) t0 = t;
+			else if (t - t0 > gc.wait_ns) {
+				set_err(gc, CARPIO_GPU_ETIMEOUT);
+				*abort = 1;
+				return;
+			}
+		}
+	}
+}
+
+// out = M^-1 in for a five-point factor (ic.grid), run by one block of at
+// least 32 * ceil(R / 32) threads; `in` and `out` in global memory
+// (distinct arrays). Ends with a block barrier.
+__device__ void ic_sweep_grid(const IcOp& ic, const double* in, double* out,
+		const GridCtl& gc) {
+	__shared__ double ring[kIcGridThreads / 32][kIcRing];   // [boundary][column mod ring]
+	__shared__ int prog[32], cons[32];       // per boundary: columns published / consumed
+	__shared__ int abort_flag;
+	const int m = ic.gm, R = ic.gR, W = (R + 31) >> 5;
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int j = warp * 32 + lane;
+	const bool act = warp < W && j < R;
+	volatile int* abort = &abort_flag;
+	for (int pass = 0; pass < 2; ++pass) {
+		if (threadIdx.x < 32) { prog[threadIdx.x] = 0; cons[threadIdx.x] = 0; }
+		if (threadIdx.x == 0 && pass == 0) abort_flag = 0;
+		__syncthreads();
+		if (warp < W) {
+			const bool fwd = pass == 0;
+			// forward: boundary `warp` feeds lane 0 from warp - 1's lane 31,
+			// and this warp's lane 31 feeds boundary warp + 1; backward:
+			// boundary warp + 1 feeds lane 31 from warp + 1's lane 0, and this
+			// warp's lane 0 feeds boundary `warp`
+			const int skew = fwd ? lane : 31 - lane;
+			const bool edge_lane = fwd ? lane == 0 : lane == 31;
+			const bool cons_lane = fwd ? (lane == 0 && warp > 0) : (lane == 31 && warp + 1 < W);
+			const bool prod_lane = fwd ? (lane == 31 && warp + 1 < W) : (lane == 0 && warp > 0);
+			const int cb = fwd ? warp : warp + 1;     // boundary consumed
+			const int pb = fwd ? warp + 1 : warp;     // boundary produced
+			const double* src = fwd ? in : out;
+			const double2* cf = fwd ? ic.gf : ic.gb;
+			const size_t row = (size_t)j * m;
+			// the input of cell t: kIcAhead steps ahead in registers (it
+			// comes from L2: other blocks wrote it), coefficients through L1
+			auto cell = [&](int t) { return row + (fwd ? t : m - 1 - t); };
+			double pre[kIcAhead];
+#pragma unroll
+			for (int u = 0; u < kIcAhead; ++u) {
+				const int t = u - skew;
+				pre[u] = act && t >= 0 && t < m ? ldcg(src + cell(t)) : 0.0;
+			}
+			int have = 0, room = 0;
+			double res = 0.0;                          // the previous step's value
+			for (int s0 = 0; s0 < m + 31; s0 += kIcAhead) {
+#pragma unroll
+				for (int u = 0; u < kIcAhead; ++u) {
+					const int s = s0 + u;              // warp-uniform
+					if (s >= m + 31) break;
+					double nb = fwd ? __shfl_up_sync(0xffffffffu, res, 1)
+					                : __shfl_down_sync(0xffffffffu, res, 1);
+					const int t = s - skew;            // cells done before this one
+					const bool on = act && t >= 0 && t < m;
+					const double in_t = pre[u];
+					const int tn = t + kIcAhead;
+					pre[u] = act && tn >= 0 && tn < m ? ldcg(src + cell(tn)) : 0.0;
+					if (edge_lane) nb = 0.0;           // no row beyond the edge
+					if (cons_lane && on) {
+						ic_wait(&prog[cb], t + 1, have, abort, gc);
+						nb = ring[cb][t & (kIcRing - 1)];
+						ic_st_release(&cons[cb], t + 1);
+					}
+					if (on) {
+						const size_t k = cell(t);
+						if ((t & 7) == 0 && t + 16 < m) {
+							const size_t kp = cell(t + 16);
+							ic_prefetch(cf + kp);
+							ic_prefetch(ic.grd + kp);
+						}
+						const double2 c = __ldg(cf + k);
+						const double own = t > 0 ? res : 0.0;   // the row neighbour
+						double y = in_t;
+						if (fwd) {
+							y = fma(-c.x, nb, y);         // U(k-m, k) z_{k-m}
+							y = fma(-c.y, own, y);        // U(k-1, k) z_{k-1}
+						} else {
+							y = fma(-c.x, own, y);        // U(k, k+1) z_{k+1}
+							y = fma(-c.y, nb, y);         // U(k, k+m) z_{k+m}
+						}
+						y *= __ldg(ic.grd + k);
+						out[k] = y;
+						res = y;
+						if (prod_lane) {
+							ic_wait(&cons[pb], t + 1 - kIcRing, room, abort, gc);
+							ring[pb][t & (kIcRing - 1)] = y;
+							ic_st_release(&prog[pb], t + 1);
+						}
+					}
+				}
+			}
+		}
+		__syncthreads();
+	}
+}
+
 #define GLOOP(cnt)                                                             \
 	for (int t = blockIdx.x * blockDim.x + threadIdx.x, _c = (cnt); t < _c;  \
 			t += gridDim.x * blockDim.x)
 
 // out = M^-1 in (ICPre::solve); exact IEEE operations in the reference's
 // order, so the result does not depend on the level split
+// GRID: the launch uses the five-point wavefront (ic.grid set)
+template<bool GRID>
 __device__ bool ic_apply(const IcOp& ic, const double* in, double* out,
 		const GridCtl& gc) {
+	if constexpr (GRID) {
+		// block 0 sweeps; the callers' grid barrier before ordered `in`
+		if (blockIdx.x == 0) ic_sweep_grid(ic, in, out, gc);
+		return grid_sync<true>(gc);
+	}
 	if (ic.smem && gridDim.x == 1) {
 		extern __shared__ double ic_sm[];
 		// the block barrier before (the callers' grid_sync<true>) ordered
@@ -209,7 +373,7 @@ __device__ bool ic_start(const Op& op, const Vecs<double>& v, int n, bool full,
 }
 
 // carpio::IC_CG (solver_matrix.hpp:318-374)
-template<class Op>
+template<bool GRID, class Op>
 __device__ void ic_cg_run(int n, const Op& op, const IcOp& ic, const Vecs<double>& v,
 		const SolveCtl& sc, const GridCtl& gc, int& bank) {
 	const bool full = (sc.flags & CARPIO_GPU_FLAG_FULL_NRM2) || n == 1;
@@ -220,7 +384,7 @@ __device__ void ic_cg_run(int n, const Op& op, const IcOp& ic, const Vecs<double
 	double rho_1 = 0.0;
 	for (int it = 1; it <= sc.max_iter; ++it) {
 		if (!grid_sync<true>(gc)) return;
-		if (!ic_apply(ic, v.r, v.z, gc)) return;           // z = M^-1 r
+		if (!ic_apply<GRID>(ic, v.r, v.z, gc)) return;           // z = M^-1 r
 		double rz[1];
 		{
 			const double* a[1] = { v.r };
@@ -255,7 +419,7 @@ __device__ void ic_cg_run(int n, const Op& op, const IcOp& ic, const Vecs<double
 
 // carpio::IC_CGS (solver_matrix.hpp:376-438); rtilde = rt, u = s, phat = ph,
 // vhat = v, uhat = sh, qhat = t, u + q = d
-template<class Op>
+template<bool GRID, class Op>
 __device__ void ic_cgs_run(int n, const Op& op, const IcOp& ic, const Vecs<double>& v,
 		const SolveCtl& sc, const GridCtl& gc, int& bank) {
 	const bool full = (sc.flags & CARPIO_GPU_FLAG_FULL_NRM2) || n == 1;
@@ -291,7 +455,7 @@ __device__ void ic_cgs_run(int n, const Op& op, const IcOp& ic, const Vecs<doubl
 			}
 		}
 		if (!grid_sync<true>(gc)) return;
-		if (!ic_apply(ic, v.p, v.ph, gc)) return;          // phat = M^-1 p
+		if (!ic_apply<GRID>(ic, v.p, v.ph, gc)) return;          // phat = M^-1 p
 		GLOOP(n) v.v[t] = op.apply(v.ph, t, t);            // vhat = A phat
 		if (!grid_sync<true>(gc)) return;
 		double rv[1];
@@ -307,7 +471,7 @@ __device__ void ic_cgs_run(int n, const Op& op, const IcOp& ic, const Vecs<doubl
 			v.d[t] = v.s[t] + q;                           // u + q
 		}
 		if (!grid_sync<true>(gc)) return;
-		if (!ic_apply(ic, v.d, v.sh, gc)) return;          // uhat = M^-1 (u + q)
+		if (!ic_apply<GRID>(ic, v.d, v.sh, gc)) return;          // uhat = M^-1 (u + q)
 		GLOOP(n) {
 			v.x[t] = fma(alpha, v.sh[t], v.x[t]);
 			v.t[t] = op.apply(v.sh, t, t);                 // qhat = A uhat

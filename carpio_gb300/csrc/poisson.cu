@@ -657,213 +657,6 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_poisson_mixed_tile(
 	KLOOP(sp) { int a = sp.addr(k); ra.phi[a] = ra.mean ? v.x[a] - mx0 : v.x[a]; }
 }
 
-// ---------------------------------------------- tile-resident FP64 CG --
-// carpio::CG (solver_matrix.hpp:264-316) exactly as cg_run states it (the
-// same recurrences, nrm2 stopping test, codes, history and max_iter/tol
-// out values), with the Krylov state on chip: one CTA per SM owns a band of
-// x-rows as in tile_solve; r and p (with one halo row above and below) live
-// in shared memory, A p in registers, x in global memory (read and written
-// once per iteration, L2-resident). p's halo rows are advanced locally from
-// the neighbours' edge rows of r, which cross CTAs once per iteration with
-// the second all-reduce (double-buffered by parity), so an iteration is two
-// grid all-reduces and three on-chip passes. The FP64 pipe (GB300: about 2
-// FMA per clock per SM) bounds the passes: ten FP64 operations a cell.
-template<int NC, int RM>
-__device__ void tile_cg64(const GridSpace& sp, const StencilOp<double>& op,
-		const Vecs<double>& v, const TileArgs& ta, const SolveCtl& sc,
-		const GridCtl& gc, int& bank) {
-	extern __shared__ double smem64[];
-	const int C = gridDim.x, c = blockIdx.x, T = blockDim.x, tid = threadIdx.x;
-	const int nx = sp.nx, ny = sp.ny, gl = sp.gl, P = sp.P;
-	const int r0 = band_lo(c, C, nx), r1 = band_lo(c + 1, C, nx);
-	const int rows = r1 - r0;
-	const int np = (ta.rows_max + 2) * ny + 2;
-	const bool full = (sc.flags & CARPIO_GPU_FLAG_FULL_NRM2) || sp.count() == 1;
-	const bool has_last = r1 == nx;      // the reference's last element (nx-1, ny-1)
-	double* p = smem64;                  // p[1 + (lr + 1) * ny + j], lr = -1 .. rows
-	double* rhal = p + np;               // neighbours' edge rows of r
-	double* rs = rhal + 2 * ny;          // the band's r
-	double* axs = rs + ta.rows_max * ny; // x-face coefficients of faces r0 .. r1
-	double* ays = axs + ta.rows_max + 1;
-	const bool up = c > 0, down = c < C - 1;
-	double* ebuf64 = reinterpret_cast<double*>(ta.xbuf);
-	const size_t edge = (size_t)2 * C * ny;   // one parity's region (doubles)
-	for (int t = tid; t < np; t += T) p[t] = 0.0;
-	for (int t = tid; t < 2 * ny; t += T) rhal[t] = 0.0;
-	for (int t = tid; t <= rows; t += T) axs[t] = op.ax[r0 + t];
-	for (int t = tid; t <= ny; t += T) ays[t] = op.ay[t];
-	__syncthreads();
-	double ayl[NC], ayr[NC];
-#pragma unroll
-	for (int k = 0; k < NC; ++k) {
-		const int j = tid + k * T;
-		ayl[k] = j < ny ? ays[j] : 0.0;
-		ayr[k] = j < ny ? ays[j + 1] : 0.0;
-	}
-	double q[RM][NC];
-	int hl = 0, par = 0;
-	// publish the band's edge rows of r into parity region `pr`
-	auto publish = [&](int pr) {
-		double* pub = ebuf64 + (size_t)pr * edge + (size_t)(2 * c) * ny;
-#pragma unroll
-		for (int k = 0; k < NC; ++k) {
-			const int j = tid + k * T;
-			if (j < ny && rows > 0) {
-				pub[j] = rs[j];
-				pub[ny + j] = rs[(rows - 1) * ny + j];
-			}
-		}
-	};
-	auto read_halo = [&](int pr) {
-		const double* src = ebuf64 + (size_t)pr * edge;
-		for (int t = tid; t < ny; t += T) {
-			if (up) rhal[t] = ldcg(src + (size_t)(2 * (c - 1) + 1) * ny + t);
-			if (down) rhal[ny + t] = ldcg(src + (size_t)(2 * (c + 1)) * ny + t);
-		}
-	};
-	// r = b - A x; nrm2(b), nrm2(r), and the last element's share of (r, r)
-	double acc[3] = { 0, 0, 0 };
-#pragma unroll
-	for (int lr = 0; lr < RM; ++lr)
-#pragma unroll
-		for (int k = 0; k < NC; ++k) {
-			const int j = tid + k * T;
-			if (lr < rows && j < ny) {
-				const int kk = (r0 + lr) * ny + j;
-				const int a = (r0 + lr + gl) * P + j + gl;
-				const double bb = v.b[a];
-				const double rr = bb - op.apply(v.x, kk, a);
-				rs[lr * ny + j] = rr;
-				if (has_last && lr == rows - 1 && j == ny - 1 && !full) acc[2] = rr * rr;
-				else { acc[0] = fma(bb, bb, acc[0]); acc[1] = fma(rr, rr, acc[1]); }
-			}
-		}
-	publish(par);
-	if (!grid_allreduce<double, 3>(acc, gc, bank)) return;
-	read_halo(par);
-	par ^= 1;
-	double normb = sqrt(acc[0]);
-	if (normb == 0.0) normb = 1;
-	double resid = sqrt(acc[1]) / normb;
-	if (resid <= sc.tol) { finish(sc, 0, 0, resid, hl); return; }
-	double rho = acc[1] + acc[2], beta = 0.0;
-	for (int it = 1; it <= sc.max_iter; ++it) {
-		// p = r + beta p over the band and its halo rows
-#pragma unroll
-		for (int lr = 0; lr < RM; ++lr)
-#pragma unroll
-			for (int k = 0; k < NC; ++k) {
-				const int j = tid + k * T;
-				if (lr < rows && j < ny) {
-					const int pk = 1 + (lr + 1) * ny + j;
-					p[pk] = it == 1 ? rs[lr * ny + j] : fma(beta, p[pk], rs[lr * ny + j]);
-				}
-			}
-		for (int t = tid; t < ny; t += T) {
-			if (up) p[1 + t] = it == 1 ? rhal[t] : fma(beta, p[1 + t], rhal[t]);
-			if (down) {
-				double* pp = p + 1 + (rows + 1) * ny + t;
-				*pp = it == 1 ? rhal[ny + t] : fma(beta, *pp, rhal[ny + t]);
-			}
-		}
-		__syncthreads();
-		// q = A p, (p, q)
-		double pq[1] = { 0.0 };
-#pragma unroll
-		for (int lr = 0; lr < RM; ++lr) {
-			const double ax0 = axs[lr], ax1 = axs[lr + 1];
-#pragma unroll
-			for (int k = 0; k < NC; ++k) {
-				const int j = tid + k * T;
-				if (lr < rows && j < ny) {
-					const int pk = 1 + (lr + 1) * ny + j;
-					const double pc = p[pk];
-					double vv = __ldg(op.D + (r0 + lr + gl) * P + j + gl) * pc;
-					vv = fma(ax0, p[pk - ny], vv);
-					vv = fma(ax1, p[pk + ny], vv);
-					vv = fma(ayl[k], p[pk - 1], vv);
-					vv = fma(ayr[k], p[pk + 1], vv);
-					q[lr][k] = vv;
-					pq[0] = fma(pc, vv, pq[0]);
-				}
-			}
-		}
-		if (!grid_allreduce<double, 1>(pq, gc, bank)) return;
-		const double alpha = rho / pq[0];
-		// x += alpha p, r -= alpha q; nrm2(r) and the last element's share
-		double rr[2] = { 0.0, 0.0 };
-#pragma unroll
-		for (int lr = 0; lr < RM; ++lr)
-#pragma unroll
-			for (int k = 0; k < NC; ++k) {
-				const int j = tid + k * T;
-				if (lr < rows && j < ny) {
-					const int pk = 1 + (lr + 1) * ny + j;
-					const int a = (r0 + lr + gl) * P + j + gl;
-					v.x[a] = fma(alpha, p[pk], v.x[a]);
-					const double r2 = fma(-alpha, q[lr][k], rs[lr * ny + j]);
-					rs[lr * ny + j] = r2;
-					if (has_last && lr == rows - 1 && j == ny - 1 && !full) rr[1] = r2 * r2;
-					else rr[0] = fma(r2, r2, rr[0]);
-				}
-			}
-		__syncthreads();
-		publish(par);
-		if (!grid_allreduce<double, 2>(rr, gc, bank)) return;
-		read_halo(par);
-		par ^= 1;
-		resid = sqrt(rr[0]) / normb;
-		hist_push(sc, hl, resid);
-		if (resid <= sc.tol) { finish(sc, 0, it, resid, hl); return; }
-		const double rho_new = rr[0] + rr[1];
-		beta = rho_new / rho;
-		rho = rho_new;
-	}
-	finish(sc, 1, sc.max_iter, resid, hl);
-}
-
-template<int SRC, int NC, int RM>
-__global__ void __launch_bounds__(kTileThreads, 1) k_poisson_cg64_tile(
-		StencilOp<double> op, Vecs<double> v, RhsArgs ra, TileArgs ta, SolveCtl sc,
-		GridCtl gc) {
-	gc.start();
-	int bank = 0;
-	const GridSpace& sp = op.sp;
-	double s[1] = { 0 };
-	KLOOP(sp) {
-		int i, j;
-		sp.ij(k, i, j);
-		int a = sp.addr(k);
-		double bb = rhs_at<SRC>(sp, ra, i, j, a);
-		v.b[a] = bb;
-		v.x[a] = ra.phi[a];
-		s[0] += bb;
-	}
-	if (ra.mean) {
-		if (!grid_allreduce<double, 1>(s, gc, bank)) return;
-		double mm = s[0] / (double)sp.count();
-		KLOOP(sp) { int a = sp.addr(k); v.b[a] = v.b[a] - mm; }
-	}
-	if (!grid_sync(gc)) return;
-	tile_cg64<NC, RM>(sp, op, v, ta, sc, gc, bank);
-	if (read_err(gc)) {
-		if (blockIdx.x == 0 && threadIdx.x == 0) sc.out->code = read_err(gc);
-		return;
-	}
-	if (!grid_sync(gc)) return;
-	double mx0 = 0.0;
-	if (ra.mean) {
-		double t[1] = { 0 };
-		KLOOP(sp) { int a = sp.addr(k); t[0] += v.x[a]; }
-		if (!grid_allreduce<double, 1>(t, gc, bank)) {
-			if (blockIdx.x == 0 && threadIdx.x == 0) sc.out->code = read_err(gc);
-			return;
-		}
-		mx0 = t[0] / (double)sp.count();
-	}
-	KLOOP(sp) { int a = sp.addr(k); ra.phi[a] = ra.mean ? v.x[a] - mx0 : v.x[a]; }
-}
-
 // b and x0 as vectors in the reference's numbering (x fastest: i + j nx),
 // for the solvers that run on an assembled CSR matrix
 template<int SRC>
@@ -1305,41 +1098,6 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 	sc.hist = hist_dev;
 	sc.hist_cap = hist_dev ? hist_cap : 0;
 	sc.out = out_dev;
-	// FP64 CG on a uniform grid: the tile-resident kernel when its band fits
-	if (!mixed && cfg.kind == CARPIO_GPU_CG && c.uniform && !(cfg.flags & CARPIO_GPU_FLAG_NO_TILE)) {
-		const int C = std::min(sm_count(), g->nx);
-		const int rows_max = (g->nx + C - 1) / C;
-		const int nc = (g->ny + kTileThreads - 1) / kTileThreads;
-		const void* tk = nullptr;
-#define TILE64_PICK(NC_, RM_)                                                       \
-		if (!tk && nc <= NC_ && rows_max <= RM_)                                    \
-			tk = src_mode == SRC_DIV ? (const void*)k_poisson_cg64_tile<SRC_DIV, NC_, RM_>      \
-			                         : (const void*)k_poisson_cg64_tile<SRC_FIELD, NC_, RM_>;
-		TILE64_PICK(1, 4) TILE64_PICK(1, 16) TILE64_PICK(2, 8) TILE64_PICK(4, 4)
-#undef TILE64_PICK
-		const size_t np = (size_t)(rows_max + 2) * g->ny + 2;
-		const size_t smem = sizeof(double) * (np + 2 * (size_t)g->ny + (size_t)rows_max * g->ny
-				+ rows_max + 1 + g->ny + 1);
-		if (tk && smem <= 220 * 1024) {
-			CG_CK(cudaFuncSetAttribute(tk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-			int per_sm = 0;
-			CG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tk, kTileThreads, smem));
-			if (per_sm >= 1) {
-				if ((rc = w.lw.ensure(C))) return rc;
-				if ((rc = w.xbuf.ensure(sizeof(double) * 4 * (size_t)C * g->ny))) return rc;
-				TileArgs ta;
-				std::memset(&ta, 0, sizeof ta);
-				ta.xbuf = w.xbuf.as<float>();
-				ta.rows_max = rows_max;
-				GridCtl gc = make_gridctl(w.lw);
-				CG_CK(cudaMemsetAsync(w.lw.ctl.p, 0, sizeof(Ctl), s));
-				CG_CK(cudaMemsetAsync(out_dev, 0, sizeof(cg_dev::SolveOut), s));
-				void* args[] = { &op, &v, &ra, &ta, &sc, &gc };
-				CG_CK(cudaLaunchCooperativeKernel(tk, C, kTileThreads, args, smem, s));
-				return 0;
-			}
-		}
-	}
 	// mixed solves whose bands fit the tile kernel run on chip
 	// the on-chip kernel keeps one coefficient per face row / column: uniform
 	// grids only (non-uniform ones run the global-memory FP32 inner CG)

@@ -59,10 +59,13 @@ extern "C" {
 /* flags (bitwise OR). 0 = the reference's exact semantics. */
 #define CARPIO_GPU_FLAG_FULL_NRM2 1u   /* use the full 2-norm instead of nrm2's
                                           drop-last-element (BLAS_Level1.hpp:569) */
-#define CARPIO_GPU_FLAG_NO_TILE 2u     /* structure level, CG on a uniform grid:
-                                          run from global memory instead of the
-                                          on-chip tile kernels (the FP64 CG's and
-                                          the MIXED inner CG's) */
+#define CARPIO_GPU_FLAG_NO_TILE 2u     /* structure level, MIXED CG on a uniform
+                                          grid: run the inner FP32 CG from global
+                                          memory instead of the on-chip tile
+                                          kernel; IC_CGS / IC_CG: level-scheduled
+                                          triangular solves (IEEE divisions in the
+                                          reference's order) instead of the
+                                          five-point wavefront */
 #define CARPIO_GPU_FLAG_MIXED 4u       /* CSR layer: the kind's iterations in FP32
                                           inside FP64 iterative refinement (CG,
                                           DIA_BICGSTAB, BICGSTAB; the stopping

@@ -9,11 +9,11 @@
 
     python profile_cases.py advect N STEPS
         STEPS steps of the stand-alone Advection_ on N x N (rotating cone,
-        van Leer): k_advect_band over all SMs (or k_advect on one block)
+        van Leer): the tile wavefront k_advect_tiles
     python profile_cases.py ic N KIND
         one structure-level IC_CGS / IC_CG solve of an N x N Dirichlet-0
-        Poisson problem with a unit source to 1e-8 (level-scheduled factor
-        solves)
+        Poisson problem with a unit source to 1e-8 (the factor's triangular
+        solves as the five-point wavefront)
 
 Each prints one line with its timing and exits 0 on success.
 """
