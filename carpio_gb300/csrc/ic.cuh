@@ -132,147 +132,113 @@ __device__ void ic_apply_smem(const IcOp& ic, const double* in, double* out, dou
 // block: lane l of warp w owns grid row j = 32 w + l and walks its m cells in
 // order, skewed one step behind lane l - 1 (forward; ahead of it backward),
 // so that the row neighbour's value is in the lane's own register and the
-// value across rows arrives by one warp shuffle from the previous step. Lane
-// 0 (forward) / 31 (backward) takes that value from the neighbouring warp
-// through a shared-memory ring with release/acquire counters. No block
-// barrier per level: a step is a shuffle and three FP64 operations.
+// value across rows arrives by one warp shuffle from the previous step. The
+// warps run in lockstep over global steps, warp w kIcLag steps behind warp
+// w - 1, with a barrier of the sweeping warps every kIcSync steps: lane 31's
+// value of column t (forward) goes into a shared-memory ring at one step and
+// the next warp's lane 0 reads it kIcSync steps later, after that barrier.
+// No flags, no per-step fences. Inputs, coefficients and reciprocals of the
+// next kIcAhead cells wait in registers.
 // The arithmetic is the reference's sequence of updates in its order
 // (ICPre::solve, preconditioner.hpp:143-161) with two relaxations: each
 // update is one fused multiply-add, and the division by d_k is a
 // multiplication by its reciprocal (both within a rounding of the
 // reference's per operation).
-constexpr int kIcRing = 64;        // columns in flight per warp boundary
-constexpr int kIcAhead = 8;        // steps between a cell's input load and its use
-constexpr int kIcGridThreads = 512; // block size of the wavefront launch: rows <= 512
+constexpr int kIcRing = 64;          // ring columns per warp boundary
+constexpr int kIcAhead = 8;          // cells loaded ahead of their step
+constexpr int kIcSync = 4;           // steps between barriers (divides kIcAhead)
+constexpr int kIcLag = 31 + kIcSync; // steps between neighbouring warps
+constexpr int kIcGridThreads = 512;  // block size of the wavefront launch: rows <= 512
+static_assert(kIcAhead % kIcSync == 0 && 2 * kIcSync <= kIcRing, "ring");
 
-__device__ __forceinline__ int ic_ld_acquire(const int* p) {
-	int v;
-	asm volatile("ld.acquire.cta.shared.b32 %0, [%1];" : "=r"(v)
-			: "r"((uint32_t)__cvta_generic_to_shared(p)) : "memory");
-	return v;
-}
-__device__ __forceinline__ void ic_st_release(int* p, int v) {
-	asm volatile("st.release.cta.shared.b32 [%0], %1;"
-			:: "r"((uint32_t)__cvta_generic_to_shared(p)), "r"(v) : "memory");
-}
-__device__ __forceinline__ void ic_prefetch(const void* p) {
-	asm volatile("prefetch.global.L1 [%0];" :: "l"(p));
-}
-
-// Wait until *p >= want (cache keeps the last value read). Bounded: after
-// the launch's per-wait limit the error word is set, *abort raised and the
-// caller carries on without the value (the solve then ends with the error).
-__device__ __forceinline__ void ic_wait(const int* p, int want, int& cache,
-		volatile int* abort, const GridCtl& gc) {
-	if (cache >= want) return;
-	unsigned long long t0 = 0;
-	for (unsigned spin = 0;; ++spin) {
-		cache = ic_ld_acquire(p);
-		if (cache >= want || *abort) return;
-		if ((spin & 255u) == 255u) {
-			const unsigned long long t = globaltimer();
-			if (!t0) t0 = t;
-			else if (t - t0 > gc.wait_ns) {
-				set_err(gc, CARPIO_GPU_ETIMEOUT);
-				*abort = 1;
-				return;
-			}
-		}
-	}
+__device__ __forceinline__ void ic_bar(int threads) {
+	asm volatile("bar.sync 1, %0;" :: "r"(threads) : "memory");
 }
 
 // out = M^-1 in for a five-point factor (ic.grid), run by one block of at
 // least 32 * ceil(R / 32) threads; `in` and `out` in global memory
 // (distinct arrays). Ends with a block barrier.
-__device__ void ic_sweep_grid(const IcOp& ic, const double* in, double* out,
-		const GridCtl& gc) {
+__device__ void ic_sweep_grid(const IcOp& ic, const double* in, double* out) {
 	__shared__ double ring[kIcGridThreads / 32][kIcRing];   // [boundary][column mod ring]
-	__shared__ int prog[32], cons[32];       // per boundary: columns published / consumed
-	__shared__ int abort_flag;
 	const int m = ic.gm, R = ic.gR, W = (R + 31) >> 5;
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-	const int j = warp * 32 + lane;
-	const bool act = warp < W && j < R;
-	volatile int* abort = &abort_flag;
-	for (int pass = 0; pass < 2; ++pass) {
-		if (threadIdx.x < 32) { prog[threadIdx.x] = 0; cons[threadIdx.x] = 0; }
-		if (threadIdx.x == 0 && pass == 0) abort_flag = 0;
-		__syncthreads();
-		if (warp < W) {
+	if (warp < W) {
+		const int j = warp * 32 + lane;
+		const bool act = j < R;
+		const int nsteps = (W - 1) * kIcLag + m + 31;
+		for (int pass = 0; pass < 2; ++pass) {
 			const bool fwd = pass == 0;
-			// forward: boundary `warp` feeds lane 0 from warp - 1's lane 31,
-			// and this warp's lane 31 feeds boundary warp + 1; backward:
-			// boundary warp + 1 feeds lane 31 from warp + 1's lane 0, and this
-			// warp's lane 0 feeds boundary `warp`
+			// forward: lane 0 takes row j - 1 from warp - 1's lane 31 through
+			// ring `warp`, lane 31 feeds ring warp + 1; backward: lane 31 takes
+			// row j + 1 from warp + 1's lane 0 through ring warp + 1, lane 0
+			// feeds ring `warp`
 			const int skew = fwd ? lane : 31 - lane;
+			const int off = (fwd ? warp : W - 1 - warp) * kIcLag + skew;
 			const bool edge_lane = fwd ? lane == 0 : lane == 31;
 			const bool cons_lane = fwd ? (lane == 0 && warp > 0) : (lane == 31 && warp + 1 < W);
 			const bool prod_lane = fwd ? (lane == 31 && warp + 1 < W) : (lane == 0 && warp > 0);
-			const int cb = fwd ? warp : warp + 1;     // boundary consumed
-			const int pb = fwd ? warp + 1 : warp;     // boundary produced
+			const int cb = fwd ? warp : warp + 1;     // ring read
+			const int pb = fwd ? warp + 1 : warp;     // ring written
 			const double* src = fwd ? in : out;
 			const double2* cf = fwd ? ic.gf : ic.gb;
 			const size_t row = (size_t)j * m;
-			// the input of cell t: kIcAhead steps ahead in registers (it
-			// comes from L2: other blocks wrote it), coefficients through L1
-			auto cell = [&](int t) { return row + (fwd ? t : m - 1 - t); };
-			double pre[kIcAhead];
+			auto cell = [&](int t) { return row + (size_t)(fwd ? t : m - 1 - t); };
+			double pin[kIcAhead], pc0[kIcAhead], pc1[kIcAhead], prd[kIcAhead];
 #pragma unroll
 			for (int u = 0; u < kIcAhead; ++u) {
-				const int t = u - skew;
-				pre[u] = act && t >= 0 && t < m ? ldcg(src + cell(t)) : 0.0;
-			}
-			int have = 0, room = 0;
-			double res = 0.0;                          // the previous step's value
-			for (int s0 = 0; s0 < m + 31; s0 += kIcAhead) {
-#pragma unroll
-				for (int u = 0; u < kIcAhead; ++u) {
-					const int s = s0 + u;              // warp-uniform
-					if (s >= m + 31) break;
-					double nb = fwd ? __shfl_up_sync(0xffffffffu, res, 1)
-					                : __shfl_down_sync(0xffffffffu, res, 1);
-					const int t = s - skew;            // cells done before this one
-					const bool on = act && t >= 0 && t < m;
-					const double in_t = pre[u];
-					const int tn = t + kIcAhead;
-					pre[u] = act && tn >= 0 && tn < m ? ldcg(src + cell(tn)) : 0.0;
-					if (edge_lane) nb = 0.0;           // no row beyond the edge
-					if (cons_lane && on) {
-						ic_wait(&prog[cb], t + 1, have, abort, gc);
-						nb = ring[cb][t & (kIcRing - 1)];
-						ic_st_release(&cons[cb], t + 1);
-					}
-					if (on) {
-						const size_t k = cell(t);
-						if ((t & 7) == 0 && t + 16 < m) {
-							const size_t kp = cell(t + 16);
-							ic_prefetch(cf + kp);
-							ic_prefetch(ic.grd + kp);
-						}
-						const double2 c = __ldg(cf + k);
-						const double own = t > 0 ? res : 0.0;   // the row neighbour
-						double y = in_t;
-						if (fwd) {
-							y = fma(-c.x, nb, y);         // U(k-m, k) z_{k-m}
-							y = fma(-c.y, own, y);        // U(k-1, k) z_{k-1}
-						} else {
-							y = fma(-c.x, own, y);        // U(k, k+1) z_{k+1}
-							y = fma(-c.y, nb, y);         // U(k, k+m) z_{k+m}
-						}
-						y *= __ldg(ic.grd + k);
-						out[k] = y;
-						res = y;
-						if (prod_lane) {
-							ic_wait(&cons[pb], t + 1 - kIcRing, room, abort, gc);
-							ring[pb][t & (kIcRing - 1)] = y;
-							ic_st_release(&prog[pb], t + 1);
-						}
-					}
+				const int t = u - off;
+				pin[u] = pc0[u] = pc1[u] = prd[u] = 0.0;
+				if (act && t >= 0 && t < m) {
+					const size_t k = cell(t);
+					const double2 c = __ldg(cf + k);
+					pin[u] = ldcg(src + k);
+					pc0[u] = c.x;
+					pc1[u] = c.y;
+					prd[u] = __ldg(ic.grd + k);
 				}
 			}
+			double res = 0.0;                          // the previous step's value
+			for (int S0 = 0; S0 < nsteps; S0 += kIcAhead) {
+#pragma unroll
+				for (int u = 0; u < kIcAhead; ++u) {
+					const int t = S0 + u - off;        // this lane's cell
+					double nb = fwd ? __shfl_up_sync(0xffffffffu, res, 1)
+					                : __shfl_down_sync(0xffffffffu, res, 1);
+					if (edge_lane) nb = 0.0;           // no row beyond the edge
+					const bool on = act && t >= 0 && t < m;
+					if (on) {
+						if (cons_lane) nb = ring[cb][t & (kIcRing - 1)];
+						const double own = t > 0 ? res : 0.0;   // the row neighbour
+						double y = pin[u];
+						if (fwd) {
+							y = fma(-pc0[u], nb, y);      // U(k-m, k) z_{k-m}
+							y = fma(-pc1[u], own, y);     // U(k-1, k) z_{k-1}
+						} else {
+							y = fma(-pc0[u], own, y);     // U(k, k+1) z_{k+1}
+							y = fma(-pc1[u], nb, y);      // U(k, k+m) z_{k+m}
+						}
+						y *= prd[u];
+						out[cell(t)] = y;
+						res = y;
+						if (prod_lane) ring[pb][t & (kIcRing - 1)] = y;
+					}
+					// the slot's next cell: kIcAhead steps on
+					const int tn = t + kIcAhead;
+					if (act && tn >= 0 && tn < m) {
+						const size_t k = cell(tn);
+						const double2 c = __ldg(cf + k);
+						pin[u] = ldcg(src + k);
+						pc0[u] = c.x;
+						pc1[u] = c.y;
+						prd[u] = __ldg(ic.grd + k);
+					}
+					if ((u % kIcSync) == kIcSync - 1) ic_bar(W * 32);
+				}
+			}
+			ic_bar(W * 32);   // the forward's writes before the backward's reads
 		}
-		__syncthreads();
 	}
+	__syncthreads();
 }
 
 #define GLOOP(cnt)                                                             \
@@ -287,7 +253,7 @@ __device__ bool ic_apply(const IcOp& ic, const double* in, double* out,
 		const GridCtl& gc) {
 	if constexpr (GRID) {
 		// block 0 sweeps; the callers' grid barrier before ordered `in`
-		if (blockIdx.x == 0) ic_sweep_grid(ic, in, out, gc);
+		if (blockIdx.x == 0) ic_sweep_grid(ic, in, out);
 		return grid_sync<true>(gc);
 	}
 	if (ic.smem && gridDim.x == 1) {

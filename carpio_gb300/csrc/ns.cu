@@ -595,6 +595,184 @@ __global__ void __launch_bounds__(kAdvTileThreads) k_advect_tiles(Geo g, double*
 	}
 }
 
+// Row-pipelined sweep: lane l of warp b owns grid row i = 32 b + l and walks
+// its columns j in order, one step behind lane l - 1, so that at every step
+// the lanes of a warp hold one anti-diagonal of the in-place sweep. A cell
+// reads, as the reference's loop does, the new values of (i-1, j), (i-2, j),
+// (i, j-1), (i, j-2) and the old values of (i+1, j), (i+2, j), (i, j+1),
+// (i, j+2): the rows above come from lanes l - 1 and l - 2 (their last two
+// results, by shuffle), the own row's new values are the lane's last two
+// results, and the old values come from a three-cell window that each lane
+// keeps of its own row ahead of its column (lanes l + 1 and l + 2, by
+// shuffle). There is no barrier per diagonal. Only the two rows across a
+// band edge go through memory: the next band's first lanes read the two
+// rows above from L2 once this band's lane 31 has published its column
+// (release/acquire progress word, every kAdvPub columns), and this band's
+// last lanes read the two old rows below before they publish.
+// One band per block: the FP64 pipe is shared by an SM's warps (16 cycles
+// per warp instruction), so bands on separate SMs run their FP64 work side
+// by side.
+constexpr int kAdvRowWarps = 1;     // bands (warps) per block
+constexpr int kAdvPub = 8;          // columns per progress publication
+
+template<int SCH, bool P2 = false>
+__global__ void __launch_bounds__(kAdvRowWarps * 32, 1) k_advect_rows(Geo g, double* phi,
+		BcDev bc, const double* uf, const double* vf, double dt, int steps,
+		unsigned* prog, GridCtl gc) {
+	__shared__ double scr[kAdvRowWarps][10][32];   // a lane's two stencils, [k][lane]
+	__shared__ double s_old[32];
+	gc.start();
+	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int nx = g.nx, ny = g.ny, gl = g.gl;
+	const int nb = (nx + 31) >> 5;
+	const int band = blockIdx.x * kAdvRowWarps + warp;
+	const int i0 = band * 32, i = i0 + lane;
+	const bool act = band < nb && i < nx;         // the lane computes cells
+	double* F = &scr[warp][0][0];
+	// phi at (r, c) inside the ghost ring, else 0 (never used)
+	auto at = [&](int r, int c) -> double {
+		return (r >= -gl && r < nx + gl && c >= -gl && c < ny + gl) ? ldcg(phi + g.at(r, c)) : 0.0;
+	};
+	for (int st = 0; st < steps; ++st) {
+		if (!grid_sync(gc)) return;
+		if (blockIdx.x == 0) {
+			bc_fill(g, phi, bc, s_old);
+			for (int t = threadIdx.x; t < nb; t += blockDim.x) prog[t] = 0u;
+		}
+		if (!grid_sync(gc)) return;
+		if (band >= nb) continue;
+		const bool upper = band > 0;                  // rows above from band - 1
+		const bool lower = band + 1 < nb;             // band + 1 reads this band
+		// own row: the last two new values (the ghosts left of column 0
+		// before the first cell) and the old window at columns t .. t + 3
+		double res1 = at(i, -1), res2 = at(i, -2);
+		const int tz = -lane;                         // column at step 0
+		double o0 = at(i, tz), o1 = at(i, tz + 1), o2 = at(i, tz + 2), o3 = at(i, tz + 3);
+		// rows i0 - 1, i0 - 2 at column s (lane 0) and i0 - 1 at s - 1
+		double aC = 0.0, bC = 0.0, aP = 0.0, aN = 0.0, bN = 0.0;
+		// rows i0 + 32, i0 + 33 (old) at columns s - 31 (and i0 + 32 at s - 30)
+		double cC = 0.0, cN = 0.0, dC = 0.0, cNN = 0.0, dN = 0.0;
+		unsigned have = 0;
+		bool ok = true;
+		// lane 0: wait until band - 1 has published `need` columns
+		auto wait_up = [&](unsigned need) {
+			if (!upper || have >= need || !ok) return;
+			unsigned polls = 0;
+			unsigned long long t0 = 0;
+			for (;;) {
+				have = ld_acquire_gpu(&prog[band - 1]);
+				if (have >= need) return;
+				if ((++polls & 63u) == 0) {
+					if (*(volatile int*)gc.err) { ok = false; return; }
+					const unsigned long long tt = globaltimer();
+					if (t0 == 0) t0 = tt;
+					if (tt - t0 > gc.wait_ns || tt > gc.deadline) {
+						set_err(gc, CARPIO_GPU_ETIMEOUT);
+						ok = false;
+						return;
+					}
+				}
+			}
+		};
+		if (lane == 0) {
+			wait_up(1u);
+			aC = at(i0 - 1, 0);
+			bC = at(i0 - 2, 0);
+			aP = at(i0 - 1, -1);
+			if (ny > 1) {
+				wait_up(2u);
+				aN = at(i0 - 1, 1);
+				bN = at(i0 - 2, 1);
+			}
+		}
+		if (lane == 31) {
+			cC = at(i0 + 32, -31);
+			cN = at(i0 + 32, -30);
+			dC = at(i0 + 33, -31);
+			cNN = at(i0 + 32, -29);
+			dN = at(i0 + 33, -30);
+		}
+		for (int s = 0; s < ny + 31; ++s) {
+			const int t = s - lane;                   // this lane's column
+			const bool on = act && t >= 0 && t < ny;
+			// new values of the rows above at column t, old values below
+			double up1 = __shfl_up_sync(0xffffffffu, res1, 1);
+			double up2 = __shfl_up_sync(0xffffffffu, res2, 2);
+			double dn1 = __shfl_down_sync(0xffffffffu, o1, 1);
+			double dn2 = __shfl_down_sync(0xffffffffu, o2, 2);
+			const double aPl = __shfl_sync(0xffffffffu, aP, 0);
+			const double cNl = __shfl_sync(0xffffffffu, cN, 31);
+			if (lane == 0) { up1 = aC; up2 = bC; }
+			if (lane == 1) up2 = aPl;
+			if (lane == 30) dn2 = cNl;
+			if (lane == 31) { dn1 = cC; dn2 = dC; }
+			if (on && (t & 7) == 0 && t + 16 < ny) {
+				// the face velocities' next lines into L1 (read-only here)
+				const int ap = g.at(i, t + 16);
+				asm volatile("prefetch.global.L1 [%0];" :: "l"(uf + ap));
+				asm volatile("prefetch.global.L1 [%0];" :: "l"(uf + ap - g.P));
+				asm volatile("prefetch.global.L1 [%0];" :: "l"(vf + ap));
+			}
+			if (on) {
+				F[0 * 32 + lane] = up2;
+				F[1 * 32 + lane] = up1;
+				F[2 * 32 + lane] = o0;
+				F[3 * 32 + lane] = dn1;
+				F[4 * 32 + lane] = dn2;
+				F[5 * 32 + lane] = res2;
+				F[6 * 32 + lane] = res1;
+				F[7 * 32 + lane] = o0;
+				F[8 * 32 + lane] = o1;
+				F[9 * 32 + lane] = o2;
+				const int fa = 2 * 32 + lane;
+				const double a0 = adv_axis_at<SCH, 0, P2>(g, uf, F, fa, 32, i, t);
+				const double a1 = adv_axis_at<SCH, 1, P2>(g, vf, F + 5 * 32, fa, 32, i, t);
+				double adv = 0.0;
+				adv += a0;
+				adv += a1;
+				const double nv = o0 - dt * adv;
+				phi[g.at(i, t)] = nv;
+				res2 = res1;
+				res1 = nv;
+			} else if (t >= ny) {
+				res2 = res1;                          // past the row end: keep the last two
+			}
+			// advance the window (old values of the own row, loaded ahead)
+			o0 = o1;
+			o1 = o2;
+			o2 = o3;
+			o3 = at(i, t + 4);
+			// lane 0: the rows above at columns s + 1 (ready) and s + 2 (loaded)
+			if (lane == 0) {
+				aP = aC;
+				aC = aN;
+				bC = bN;
+				if (s + 2 < ny) {
+					wait_up((unsigned)(s + 3));
+					aN = at(i0 - 1, s + 2);
+					bN = at(i0 - 2, s + 2);
+				}
+			}
+			// lane 31: the old rows below at columns s - 30 and s - 29
+			if (lane == 31) {
+				cC = cN;
+				cN = cNN;
+				dC = dN;
+				cNN = at(i0 + 32, s - 28);
+				dN = at(i0 + 33, s - 29);
+			}
+			// publish lane 31's progress (lane 30's column is one ahead)
+			const int t31 = s - 31;
+			if (lower && t31 >= 0 && t31 < ny && ((t31 + 1) % kAdvPub == 0 || t31 == ny - 1)) {
+				if (lane >= 30) __threadfence();
+				__syncwarp();
+				if (lane == 31) st_release_gpu(&prog[band], (unsigned)(t31 + 1));
+			}
+		}
+		// lane 0 may have stopped on an error: the grid barrier returns it
+	}
+}
+
 // ------------------------------------------------------------- NS kernels --
 struct StepScalars {
 	double dt;                // current time step (Time_::_dt)
@@ -1048,6 +1226,26 @@ const void* pick_advect_band(int sch, bool p2) {
 	case CARPIO_GPU_WAHYD: return advect_band_kernel<CARPIO_GPU_WAHYD>(p2);
 	case CARPIO_GPU_QUICK: return advect_band_kernel<CARPIO_GPU_QUICK>(p2);
 	case CARPIO_GPU_CUI: return advect_band_kernel<CARPIO_GPU_CUI>(p2);
+	}
+	return nullptr;
+}
+
+template<int S>
+const void* advect_rows_kernel(bool p2) {
+	return p2 ? (const void*)k_advect_rows<S, true> : (const void*)k_advect_rows<S, false>;
+}
+
+const void* pick_advect_rows(int sch, bool p2) {
+	switch (sch) {
+	case CARPIO_GPU_UPWIND1: return advect_rows_kernel<CARPIO_GPU_UPWIND1>(p2);
+	case CARPIO_GPU_CENTER: return advect_rows_kernel<CARPIO_GPU_CENTER>(p2);
+	case CARPIO_GPU_CENTER4: return advect_rows_kernel<CARPIO_GPU_CENTER4>(p2);
+	case CARPIO_GPU_UPWIND2: return advect_rows_kernel<CARPIO_GPU_UPWIND2>(p2);
+	case CARPIO_GPU_VANLEER: return advect_rows_kernel<CARPIO_GPU_VANLEER>(p2);
+	case CARPIO_GPU_SUPERBEE: return advect_rows_kernel<CARPIO_GPU_SUPERBEE>(p2);
+	case CARPIO_GPU_WAHYD: return advect_rows_kernel<CARPIO_GPU_WAHYD>(p2);
+	case CARPIO_GPU_QUICK: return advect_rows_kernel<CARPIO_GPU_QUICK>(p2);
+	case CARPIO_GPU_CUI: return advect_rows_kernel<CARPIO_GPU_CUI>(p2);
 	}
 	return nullptr;
 }
@@ -1641,50 +1839,38 @@ int carpio_gpu_advection_step(carpio_gpu_advection* a, double dt, int steps) {
 	CG_CK(launch_bc(geo, a->f[0], a->bc[0], a->f[1], &a->bc[1], a->s,
 			a->has_gv[0] ? a->f[5] : nullptr, a->has_gv[1] ? a->f[6] : nullptr));
 	const BcDev bcp = to_dev(a->bc[2], a->has_gv[2] ? a->f[7] : nullptr);
-	// one block while the diagonals are short: it clears ~0.06 us of FP64
-	// work per cell (van Leer: ~20 divisions a cell); longer ones go to the
-	// tile wavefront (two ghost layers or more), else to the pipelined bands
-	// of rows, one per SM, whose diagonals cost ~20 us (a hand-off through
-	// L2 per diagonal) whatever their length
+	// one block while the diagonals are short (van Leer: ~20 FP64 divisions
+	// a cell); longer ones go to the row-pipelined sweep (two ghost layers
+	// or more), else to the pipelined bands of rows, one per SM, whose
+	// diagonals cost ~20 us (a hand-off through L2 per diagonal)
 	const double avg_diag = (double)g->nx * g->ny / (double)(g->nx + g->ny - 1);
 	if (avg_diag < 64.0 || g->nx < 8) {
 		CG_CK(launch_advect(a->scheme, geo, a->s, a->f[4], bcp, a->f[2], a->f[3], dt, steps));
 		CG_CK(cudaStreamSynchronize(a->s));
 		return 0;
 	}
-	if (g->gl >= 2 && g->gl <= 4) {
-		// the tile wavefront (k_advect_tiles)
-		const void* kt = pick_advect_tiles(a->scheme, geo.p2 != 0);
-		if (!kt) return CARPIO_GPU_EINVAL;
-		const int TB = kAdvTile;
-		const int nti = (g->nx + TB - 1) / TB, ntj = (g->ny + TB - 1) / TB;
-		const int nt = nti * ntj;
-		std::vector<int> ord;
-		ord.reserve(nt);
-		for (int d = 0; d <= nti + ntj - 2; ++d)
-			for (int I = std::max(0, d - ntj + 1); I <= std::min(d, nti - 1); ++I)
-				ord.push_back(I * ntj + (d - I));
+	if (g->gl >= 2) {
+		// the row-pipelined sweep (k_advect_rows): one lane per grid row
+		const void* kr = pick_advect_rows(a->scheme, geo.p2 != 0);
+		if (!kr) return CARPIO_GPU_EINVAL;
+		const int nb = (g->nx + 31) / 32;
+		const int blocks = (nb + kAdvRowWarps - 1) / kAdvRowWarps;
+		int per_sm = 0;
+		CG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kr, kAdvRowWarps * 32, 0));
+		if ((long)per_sm * sm_count() < blocks) return CARPIO_GPU_EINVAL;
 		int rc;
-		if ((rc = to_device(a->tord, ord.data(), sizeof(int) * ord.size(), a->s))) return rc;
-		if ((rc = a->tdone.ensure(sizeof(unsigned) * ((size_t)nt + 2)))) return rc;
-		CG_CK(cudaMemsetAsync(a->tdone.p, 0, sizeof(unsigned) * ((size_t)nt + 2), a->s));
-		const int blocks = std::max(1, std::min({ coop_blocks(kt, (long)nt * kAdvTileThreads, 1),
-				sm_count(), nt }));
 		if ((rc = a->lw.ensure(blocks))) return rc;
+		if ((rc = a->prog.ensure(sizeof(unsigned) * (size_t)nb))) return rc;
 		CG_CK(cudaMemsetAsync(a->lw.ctl.p, 0, sizeof(Ctl), a->s));
 		GridCtl gc = make_gridctl(a->lw);
 		double* phi = a->f[4];
 		const double* uf = a->f[2];
 		const double* vf = a->f[3];
-		const int* order = a->tord.as<int>();
-		unsigned* done = a->tdone.as<unsigned>();
-		unsigned* ctr = done + nt;
+		unsigned* prog = a->prog.as<unsigned>();
 		Geo gg = geo;
 		BcDev bb = bcp;
-		int ntj_ = ntj, nt_ = nt;
-		void* args[] = { &gg, &phi, &bb, &uf, &vf, &dt, &steps, &order, &ntj_, &nt_, &done,
-			&ctr, &gc };
-		CG_CK(cudaLaunchCooperativeKernel(kt, blocks, kAdvTileThreads, args, 0, a->s));
+		void* args[] = { &gg, &phi, &bb, &uf, &vf, &dt, &steps, &prog, &gc };
+		CG_CK(cudaLaunchCooperativeKernel(kr, blocks, kAdvRowWarps * 32, args, 0, a->s));
 		CG_CK(cudaMemcpyAsync(a->lw.host_ctl, a->lw.ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, a->s));
 		CG_CK(cudaStreamSynchronize(a->s));
 		return a->lw.host_ctl->err;

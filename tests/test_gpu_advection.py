@@ -83,20 +83,28 @@ def oracle_bc(c):
     return o
 
 
-@pytest.mark.parametrize("nx,ny,scheme", [(7, 19, "VanLeer"), (1, 9, "QUICK"),
-                                          (13, 2, "upwind1"), (16, 16, "center4")])
-def test_advection_ragged_grids_match_oracle(nx, ny, scheme):
+@pytest.mark.parametrize("nx,ny,scheme,ly,dt", [(7, 19, "VanLeer", 0.7, 0.01),
+                                                (1, 9, "QUICK", 0.7, 0.01),
+                                                (13, 2, "upwind1", 0.7, 0.01),
+                                                (16, 16, "center4", 0.7, 0.01),
+                                                (161, 130, "VanLeer", 0.7, 1e-3),
+                                                (190, 100, "superbee", 0.7, 1e-3),
+                                                (256, 128, "VanLeer", 0.5, 1e-3),
+                                                (96, 300, "WAHYD", 0.7, 1e-3)])
+def test_advection_ragged_grids_match_oracle(nx, ny, scheme, ly, dt):
     """ragged and one-cell-wide grids, random velocity and phi fields, a
     Dirichlet function BC and Neumann values: the GPU sweep against the
-    oracle's sequential loop, bit for bit"""
+    oracle's sequential loop, bit for bit. The larger grids run the row-
+    pipelined sweep: a last band of one row (161) and of 30 rows (190),
+    power-of-two spacings (256 x 128 on 1 x 0.5), three full bands (96)."""
     from carpio_gb300 import structure as S
     from oracle import restate as R
     rng = np.random.default_rng(nx * 100 + ny)
-    g = S.Grid((0.0, 0.0), (1.0, 0.7), (nx, ny), 2)
-    og = R.Grid(nx, ny, 2, 0.0, 1.0, 0.0, 0.7)
+    g = S.Grid((0.0, 0.0), (1.0, ly), (nx, ny), 2)
+    og = R.Grid(nx, ny, 2, 0.0, 1.0, 0.0, ly)
     assert bits_equal(og.cx, g.cx) and bits_equal(og.sy, g.sy)
     eq = S.Advection(g)
-    eq.set_time(11, 0.01)
+    eq.set_time(11, dt)
     u0, v0, p0 = (rng.uniform(-1, 1, g.N()) for _ in range(3))
     eq.initial_CS("u", 0.0)
     bi = S.BoundaryIndex()
@@ -118,7 +126,7 @@ def test_advection_ragged_grids_match_oracle(nx, ny, scheme):
     uf, vf = R.c2f(og, u, v)
     gv = bi.ghost_values(g, "phi", 0.0)
     phi = R.advect_run(og, scheme.lower(), oracle_bc(bi.to_c("phi", functions=True)),
-                       uf, vf, 0.01, 12, p0, gv)
+                       uf, vf, dt, 12, p0, gv)
     assert bits_equal(eq.get_CS("uf"), uf) and bits_equal(eq.get_CS("vf"), vf)
     assert bits_equal(eq.get_CS("phi"), phi)
 
