@@ -20,7 +20,7 @@ FP64, MIXED = 0, 1
 FLAG_FULL_NRM2 = 1
 FLAG_NO_TILE = 2
 FLAG_MIXED = 4
-PRECOND = {"default": 0, "chebyshev": 1, "multigrid": 2}
+PRECOND = {"default": 0, "chebyshev": 1, "multigrid": 2, "spectral": 3}
 SCHEMES = {"upwind1": 0, "center": 1, "center4": 2, "upwind2": 3,
            "VanLeer": 4, "vanleer": 4, "superbee": 5, "WAHYD": 6, "wahyd": 6,
            "QUICK": 7, "quick": 7, "CUI": 8, "cui": 8, "minmod": 9}

@@ -1,0 +1,138 @@
+// Spectral preconditioner of the on-chip FP32 CG: on a uniform grid with a
+// uniform coefficient, and the same boundary type on both sides of each
+// axis, the five-point operator (with the ghost substitution folded into its
+// diagonal) is separable, A = cx L_x (x) I + cy I (x) L_y, and L is
+// diagonalised by the DCT-II (Neumann: mirrored ghosts) or the DST-II
+// (Dirichlet: antisymmetric ghosts). M^-1 = C^-1 diag(1 / lambda) C applies
+// A^-1 up to FP32 rounding (lambda = 0, the all-Neumann mean, maps to 0).
+//
+// A length-N DCT-II is one N-point complex FFT of the reordered sequence
+// v[n] = x[2n], v[N-1-n] = x[2n+1] followed by X[k] = Re(e^{-i pi k / 2N} V[k])
+// (Makhoul 1980); its inverse runs the same steps backwards, and the DST-II
+// is the DCT-II of (-1)^n x read in reverse order (the order reversal lives
+// in the eigenvalue table). The FFT is an in-place radix-2 decimation in
+// time on bit-reversed input in shared memory, one block barrier per stage,
+// a batch of sequences at a time. Lengths are powers of two, N >= 2.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace cg_dev {
+
+struct DctArgs {
+	int on;              // 1: the spectral preconditioner
+	int lx, ly;          // log2 nx, log2 ny
+	int fx, fy;          // 1: Dirichlet sides on the axis (sign flip)
+	const float* lamx;   // [nx] eigenvalue parts, DCT index order
+	const float* lamy;   // [ny]
+	const float2* twx;   // FFT twiddles e^{-2 pi i t / nx}, t < nx / 2
+	const float2* twy;
+	const float2* ex;    // e^{-i pi k / (2 nx)}, k < nx
+	const float2* ey;
+	float* G;            // [nx][ny] spectral workspace (global memory, L2)
+};
+
+__device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
+	return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+
+__device__ __forceinline__ int bitrev(int m, int logN) {
+	return (int)(__brev((unsigned)m) >> (32 - logN));
+}
+
+// element m of the reordered sequence comes from x[src]
+__device__ __forceinline__ int dct_src(int m, int N) {
+	return m < (N >> 1) ? 2 * m : 2 * (N - 1 - m) + 1;
+}
+
+// B sequences of N = 2^logN complex values in buf (bit-reversed order) ->
+// their DFTs in natural order. Begins after the caller's barrier, ends with
+// one.
+__device__ __forceinline__ void fft_stages(float2* buf, int B, int logN, const float2* tw) {
+	const int N = 1 << logN, halfN = N >> 1, nb = B * halfN;
+	for (int s = 1; s <= logN; ++s) {
+		const int h = 1 << (s - 1);
+		for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+			const int seq = b >> (logN - 1);
+			const int w = b & (halfN - 1);
+			const int pos = w & (h - 1);
+			const int i1 = seq * N + ((w - pos) << 1) + pos, i2 = i1 + h;
+			const float2 t = cmulf(__ldg(tw + (pos << (logN - s))), buf[i2]);
+			const float2 a = buf[i1];
+			buf[i1] = make_float2(a.x + t.x, a.y + t.y);
+			buf[i2] = make_float2(a.x - t.x, a.y - t.y);
+		}
+		__syncthreads();
+	}
+}
+
+// Thread t of the block takes element m of sequence seq: seq-major
+// (t = seq N + m) or, SM, seq-minor (t = m B + seq: neighbouring threads on
+// neighbouring sequences, for sequences that are columns in memory).
+template<bool SM>
+__device__ __forceinline__ void dct_index(int t, int B, int logN, int& seq, int& m) {
+	if (SM) {
+		m = t / B;
+		seq = t - m * B;
+	} else {
+		seq = t >> logN;
+		m = t & ((1 << logN) - 1);
+	}
+}
+
+// Forward transform of B real sequences: in(seq, n) -> out(seq, k, X[k]).
+// `flip`: the DST through the DCT of (-1)^n x.
+template<bool SM, class IN, class OUT>
+__device__ __forceinline__ void dct_forward(float2* buf, int B, int logN, const float2* tw,
+		const float2* E, bool flip, IN in, OUT out) {
+	const int N = 1 << logN;
+	for (int t = threadIdx.x; t < B * N; t += blockDim.x) {
+		int seq, m;
+		dct_index<SM>(t, B, logN, seq, m);
+		const int n = dct_src(m, N);
+		float val = in(seq, n);
+		if (flip && (n & 1)) val = -val;
+		buf[seq * N + bitrev(m, logN)] = make_float2(val, 0.f);
+	}
+	__syncthreads();
+	fft_stages(buf, B, logN, tw);
+	for (int t = threadIdx.x; t < B * N; t += blockDim.x) {
+		int seq, k;
+		dct_index<SM>(t, B, logN, seq, k);
+		const float2 V = buf[seq * N + k];
+		const float2 e = __ldg(E + k);
+		out(seq, k, e.x * V.x - e.y * V.y);
+	}
+	__syncthreads();
+}
+
+// Inverse of dct_forward: in(seq, k) = X[k] -> out(seq, n, x[n]).
+template<bool SM, class IN, class OUT>
+__device__ __forceinline__ void dct_inverse(float2* buf, int B, int logN, const float2* tw,
+		const float2* E, bool flip, IN in, OUT out) {
+	const int N = 1 << logN;
+	for (int t = threadIdx.x; t < B * N; t += blockDim.x) {
+		int seq, k;
+		dct_index<SM>(t, B, logN, seq, k);
+		const float xk = in(seq, k);
+		const float xr = k > 0 ? in(seq, N - k) : 0.f;
+		// conj(V[k]) = e^{-i pi k / 2N} (X[k] + i X[N-k]); the FFT of conj(V)
+		// is N conj(v), v real
+		buf[seq * N + bitrev(k, logN)] = cmulf(__ldg(E + k), make_float2(xk, xr));
+	}
+	__syncthreads();
+	fft_stages(buf, B, logN, tw);
+	const float invN = 1.f / (float)N;
+	for (int t = threadIdx.x; t < B * N; t += blockDim.x) {
+		int seq, m;
+		dct_index<SM>(t, B, logN, seq, m);
+		const int n = dct_src(m, N);
+		float val = buf[seq * N + m].x * invN;
+		if (flip && (n & 1)) val = -val;
+		out(seq, n, val);
+	}
+	__syncthreads();
+}
+
+}  // namespace cg_dev

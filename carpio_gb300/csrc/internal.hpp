@@ -100,12 +100,20 @@ struct StencilCoeffs {
 	int mg_nlev = 0;
 	float mg_cx = 0.f, mg_cy = 0.f;
 	DevBuf mgD;
+	// spectral preconditioner (separable operator, power-of-two sides, the
+	// same boundary type on both sides of an axis): log2 of the sides, the
+	// Dirichlet flags and the tables (eigenvalue parts [nx], [ny]; FFT
+	// twiddles [nx/2], [ny/2]; DCT factors [nx], [ny] as float2), packed
+	bool dct_ok = false;
+	int dct_lx = 0, dct_ly = 0, dct_fx = 0, dct_fy = 0;
+	DevBuf dctT;
 };
 
 struct PoissonWs {
 	LaunchWs lw;
 	DevBuf v64, v32, src, phi, hist, out, xbuf;
 	DevBuf mg;   // multigrid level vectors
+	DevBuf dct;  // spectral workspace [nx][ny] (FP32)
 };
 
 // bfield: a variable beta (StencilPoisson_ with a beta field, face values

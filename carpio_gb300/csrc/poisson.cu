@@ -11,6 +11,7 @@
 #include "poisson_rhs.cuh"
 #include "mixed.cuh"
 #include "mg.cuh"
+#include "dct.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -104,6 +105,7 @@ struct TileArgs {
 	                       // parities), then of r after a residual replacement
 	int rows_max;
 	MgArgs mg;             // the multigrid preconditioner (mg.nlev > 0)
+	DctArgs dct;           // the spectral preconditioner (dct.on)
 };
 
 __device__ __forceinline__ int band_lo(int c, int C, int nx) {
@@ -143,7 +145,12 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	const int K = m.pdeg;
 	const MgArgs& mg = ta.mg;
 	const bool use_mg = mg.nlev > 0;
-	float* zs = (K > 0 || use_mg) ? dd + ta.rows_max * ny : rs;
+	const DctArgs& dc = ta.dct;
+	const bool use_dct = dc.on != 0;
+	float* zs = (K > 0 || use_mg || use_dct) ? dd + ta.rows_max * ny : rs;
+	// spectral: the FFT buffer after zs, rounded up to 8 bytes
+	float2* dbuf = reinterpret_cast<float2*>(
+			(reinterpret_cast<uintptr_t>(zs + ta.rows_max * ny) + 7) & ~(uintptr_t)7);
 	float* dsa = zs + ta.rows_max * ny;    // dsa[1 + (lr + 1) * ny + j]
 	float* dsb = dsa + np;
 	// multigrid (K == 0 then): the corrected fine values of the band and its
@@ -376,9 +383,49 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 			}
 		return true;
 	};
-	// the preconditioner in use: multigrid, the band-local polynomial, or
-	// none (z = r)
+	// z = M r with M = A^-1 through the separable transforms (dct.cuh):
+	// the band's rows along y, a grid barrier, this CTA's block of columns
+	// along x with the division by the eigenvalues and back, a grid barrier,
+	// the band's rows back along y. (r, z) and (r, r) of the band in g.
+	auto precond_dct = [&](float (&g)[2]) -> bool {
+		float* G = dc.G;
+		dct_forward<false>(dbuf, rows, dc.ly, dc.twy, dc.ey, dc.fy != 0,
+				[&](int sq, int n) { return rs[sq * ny + n]; },
+				[&](int sq, int k, float val) { __stcg(G + (size_t)(r0 + sq) * ny + k, val); });
+		if (!grid_sync(gc)) return false;
+		const int l0 = band_lo(c, C, ny), B = band_lo(c + 1, C, ny) - l0;
+		dct_forward<true>(dbuf, B, dc.lx, dc.twx, dc.ex, dc.fx != 0,
+				[&](int sq, int n) { return ldcg(G + (size_t)n * ny + l0 + sq); },
+				[&](int sq, int k, float val) {
+					const float lam = __ldg(dc.lamx + k) + __ldg(dc.lamy + l0 + sq);
+					__stcg(G + (size_t)k * ny + l0 + sq, lam > 0.f ? val / lam : 0.f);
+				});
+		dct_inverse<true>(dbuf, B, dc.lx, dc.twx, dc.ex, dc.fx != 0,
+				[&](int sq, int k) { return ldcg(G + (size_t)k * ny + l0 + sq); },
+				[&](int sq, int n, float val) { __stcg(G + (size_t)n * ny + l0 + sq, val); });
+		if (!grid_sync(gc)) return false;
+		dct_inverse<false>(dbuf, rows, dc.ly, dc.twy, dc.ey, dc.fy != 0,
+				[&](int sq, int k) { return ldcg(G + (size_t)(r0 + sq) * ny + k); },
+				[&](int sq, int n, float val) { zs[sq * ny + n] = val; });
+		g[0] = g[1] = 0.f;
+#pragma unroll
+		for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+			for (int k = 0; k < NC; ++k) {
+				const int j = tid + k * T;
+				if (lr < rows && j < ny) {
+					const int cc = lr * ny + j;
+					const float rv = rs[cc];
+					g[0] = fmaf(rv, zs[cc], g[0]);
+					g[1] = fmaf(rv, rv, g[1]);
+				}
+			}
+		return true;
+	};
+	// the preconditioner in use: spectral, multigrid, the band-local
+	// polynomial, or none (z = r)
 	auto apply_m = [&](float (&g)[2]) -> bool {
+		if (use_dct) return precond_dct(g);
 		if (use_mg) return precond_mg(g);
 		if (K > 0) precond(g);
 		return true;
@@ -422,6 +469,8 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 		}
 		__syncthreads();
 		to.resid = s_sc[0];
+		// converged: the caller stops, no FP32 residual or preconditioner
+		if (to.resid <= sc.tol) return true;
 		const double mr = s_sc[1];
 		if (first) {
 			rn0 = s_sc[2];
@@ -924,6 +973,61 @@ int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
 		if (c.mg_nlev > 0 && (rc = to_device(c.mgD, mgd.data(), sizeof(float) * mgd.size(), s)))
 			return rc;
 	}
+	// the spectral preconditioner: power-of-two sides, Neumann or Dirichlet
+	// on both sides of each axis, and an operator that is the separable
+	// five-point one (uniform interior faces, the diagonal folded as above)
+	c.dct_ok = false;
+	auto pow2 = [](int n, int& lg) {
+		lg = 0;
+		while ((1 << lg) < n) ++lg;
+		return n >= 2 && (1 << lg) == n && n <= 4096;
+	};
+	int lgx = 0, lgy = 0;
+	if (uniform && !helm && pow2(g->nx, lgx) && pow2(g->ny, lgy) && bc.type[0] == bc.type[1]
+			&& bc.type[2] == bc.type[3] && (bc.type[0] == 1 || bc.type[0] == 2)
+			&& (bc.type[2] == 1 || bc.type[2] == 2)) {
+		const int nx = g->nx, ny = g->ny;
+		const double cxd = ax[nx / 2], cyd = ay[ny / 2];
+		bool ok = cxd < 0.0 && cyd < 0.0;
+		auto near = [](double a, double b) { return std::fabs(a - b) <= 1e-10 * std::fabs(b); };
+		for (int i = 1; i < nx && ok; ++i) ok = near(ax[i], cxd);
+		for (int j = 1; j < ny && ok; ++j) ok = near(ay[j], cyd);
+		for (int i = 0; i < nx && ok; ++i)
+			for (int j = 0; j < ny && ok; ++j) {
+				double d = 0.0;
+				d += i > 0 ? -cxd : (bc.type[0] == 1 ? -2.0 * cxd : 0.0);
+				d += i < nx - 1 ? -cxd : (bc.type[1] == 1 ? -2.0 * cxd : 0.0);
+				d += j > 0 ? -cyd : (bc.type[2] == 1 ? -2.0 * cyd : 0.0);
+				d += j < ny - 1 ? -cyd : (bc.type[3] == 1 ? -2.0 * cyd : 0.0);
+				ok = near(D[(size_t)(i + gl) * g->P + (j + gl)], d);
+			}
+		if (ok) {
+			const double pi = 3.14159265358979323846;
+			std::vector<float> t;
+			auto lam = [&](int N, double cc, bool dir) {
+				for (int m = 0; m < N; ++m) {
+					const double th = pi * (dir ? N - m : m) / N;
+					t.push_back((float)(-cc * (2.0 - 2.0 * std::cos(th))));
+				}
+			};
+			auto cplx = [&](double a) {
+				t.push_back((float)std::cos(a));
+				t.push_back((float)std::sin(a));
+			};
+			lam(nx, cxd, bc.type[0] == 1);
+			lam(ny, cyd, bc.type[2] == 1);
+			for (int q = 0; q < nx / 2; ++q) cplx(-2.0 * pi * q / nx);
+			for (int q = 0; q < ny / 2; ++q) cplx(-2.0 * pi * q / ny);
+			for (int k = 0; k < nx; ++k) cplx(-pi * k / (2.0 * nx));
+			for (int k = 0; k < ny; ++k) cplx(-pi * k / (2.0 * ny));
+			if ((rc = to_device(c.dctT, t.data(), sizeof(float) * t.size(), s))) return rc;
+			c.dct_ok = true;
+			c.dct_lx = lgx;
+			c.dct_ly = lgy;
+			c.dct_fx = bc.type[0] == 1;
+			c.dct_fy = bc.type[2] == 1;
+		}
+	}
 	CG_CK(cudaStreamSynchronize(s));  // host vectors go out of scope
 	c.uniform = uniform;
 	c.bfield_free = !bfield;
@@ -1119,9 +1223,41 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 		TileArgs ta;
 		std::memset(&ta, 0, sizeof ta);
 		size_t smem = base;
+		// the spectral preconditioner where asked for (or by default) and the
+		// operator allows it: zs, then the FFT buffer of the band's rows or
+		// of a CTA's block of columns, whichever is longer
+		bool mg = false, spec = false;
+		if ((cfg.precond == CARPIO_GPU_PRECOND_DEFAULT || cfg.precond == CARPIO_GPU_PRECOND_SPECTRAL)
+				&& c.dct_ok) {
+			const size_t zsn = (size_t)rows_max * g->ny;
+			const size_t cmax = ((size_t)g->ny + C - 1) / C;
+			const size_t fb = std::max(zsn, cmax * (size_t)g->nx);
+			const size_t ssmem = base + sizeof(float) * (zsn + 1) + sizeof(float2) * fb;
+			if (ssmem <= 220 * 1024) {
+				if ((rc = w.dct.ensure(sizeof(float) * (size_t)g->nx * g->ny))) return rc;
+				DctArgs& d = ta.dct;
+				const float* tp = c.dctT.as<float>();
+				const int nx = g->nx, ny = g->ny;
+				d.on = 1;
+				d.lx = c.dct_lx;
+				d.ly = c.dct_ly;
+				d.fx = c.dct_fx;
+				d.fy = c.dct_fy;
+				d.lamx = tp;
+				d.lamy = tp + nx;
+				const float2* cp = reinterpret_cast<const float2*>(tp + nx + ny);
+				d.twx = cp;
+				d.twy = cp + nx / 2;
+				d.ex = cp + nx / 2 + ny / 2;
+				d.ey = cp + nx / 2 + ny / 2 + nx;
+				d.G = w.dct.as<float>();
+				smem = ssmem;
+				pdeg = 0;
+				spec = true;
+			}
+		}
 		// the multigrid V-cycle where asked for and the grid allows it
-		bool mg = false;
-		if (cfg.precond != CARPIO_GPU_PRECOND_CHEBYSHEV && c.mg_nlev > 0) {
+		if (!spec && cfg.precond != CARPIO_GPU_PRECOND_CHEBYSHEV && c.mg_nlev > 0) {
 			size_t coarse = 0, work = 0;
 			const int ntot = (int)c.mg_dims.size();
 			for (int l = c.mg_nlev; l < ntot; ++l)
@@ -1183,7 +1319,7 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 				// the V-cycle each iteration gains about a digit, so after
 				// 1e-2 (the smallest step allowed on chip)
 				mx.inner_tol = cfg.inner_tol > 0 ? cfg.inner_tol
-				                                 : (mg ? 1e-2 : pdeg > 0 ? 1e-1 : 3e-2);
+				                                 : ((mg || spec) ? 1e-2 : pdeg > 0 ? 1e-1 : 3e-2);
 				GridCtl gc = make_gridctl(w.lw);
 				CG_CK(cudaMemsetAsync(w.lw.ctl.p, 0, sizeof(Ctl), s));
 				CG_CK(cudaMemsetAsync(out_dev, 0, sizeof(cg_dev::SolveOut), s));

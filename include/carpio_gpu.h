@@ -213,13 +213,22 @@ typedef struct {
 	                      on grids whose sides halve down to at most 1024
 	                      cells, without the Helmholtz term; other grids take
 	                      the polynomial. CARPIO_GPU_PRECOND_CHEBYSHEV: the
-	                      band-local polynomial above. CARPIO_GPU_PRECOND_DEFAULT
-	                      (0): the multigrid cycle where it applies. */
+	                      band-local polynomial above.
+	                      CARPIO_GPU_PRECOND_SPECTRAL: M = A^-1 through the
+	                      DCT-II / DST-II of both axes (FP32 FFTs on chip) on
+	                      grids with power-of-two sides, a uniform
+	                      coefficient and the same boundary type (Neumann or
+	                      Dirichlet) on both sides of each axis; other grids
+	                      as DEFAULT. CARPIO_GPU_PRECOND_DEFAULT (0): the
+	                      spectral preconditioner where it applies, else the
+	                      multigrid cycle where it applies, else the
+	                      polynomial. */
 } carpio_gpu_solver_cfg;
 
 #define CARPIO_GPU_PRECOND_DEFAULT 0
 #define CARPIO_GPU_PRECOND_CHEBYSHEV 1
 #define CARPIO_GPU_PRECOND_MULTIGRID 2
+#define CARPIO_GPU_PRECOND_SPECTRAL 3
 
 typedef struct {
 	int code;          /* solver code (0..3) or negative error */
