@@ -329,11 +329,11 @@ extern "C" int carpio_gpu_krylov_csr(int kind, int n, int nnz,
 				for (uint32_t e = up[i]; e < up[i + 1]; ++e) {
 					const uint32_t c = ui[e];
 					if (c == (uint32_t)i + 1) {
-						gf[2 * (size_t)c + 1] = uv[e];
-						gb[2 * (size_t)i] = uv[e];
+						gf[2 * (size_t)c + 1] = uv[e] / dg[c];
+						gb[2 * (size_t)i] = uv[e] / dg[i];
 					} else {
-						gf[2 * (size_t)c] = uv[e];
-						gb[2 * (size_t)i + 1] = uv[e];
+						gf[2 * (size_t)c] = uv[e] / dg[c];
+						gb[2 * (size_t)i + 1] = uv[e] / dg[i];
 					}
 				}
 			}

@@ -40,8 +40,8 @@ struct IcOp {
 	// as a skewed wavefront in block 0 (ic_sweep_grid)
 	int grid;                                         // 1: use that path
 	int gm, gR;                                       // row length m, rows R
-	const double2* gf;      // forward {U(k-m, k), U(k-1, k)}, 0 where absent
-	const double2* gb;      // backward {U(k, k+1), U(k, k+m)}, 0 where absent
+	const double2* gf;      // forward {U(k-m, k), U(k-1, k)} / d_k, 0 where absent
+	const double2* gb;      // backward {U(k, k+1), U(k, k+m)} / d_k, 0 where absent
 	const double* grd;      // 1 / d_k
 };
 
@@ -139,14 +139,15 @@ __device__ void ic_apply_smem(const IcOp& ic, const double* in, double* out, dou
 // the next warp's lane 0 reads it kIcSync steps later, after that barrier.
 // No flags, no per-step fences. Inputs, coefficients and reciprocals of the
 // next kIcAhead cells wait in registers.
-// The arithmetic is the reference's sequence of updates in its order
-// (ICPre::solve, preconditioner.hpp:143-161) with two relaxations: each
-// update is one fused multiply-add, and the division by d_k is a
-// multiplication by its reciprocal (both within a rounding of the
-// reference's per operation).
+// The arithmetic is the reference's update (ICPre::solve,
+// preconditioner.hpp:143-161), y_k = (x_k - sum_i U(i, k) y_i) / d_k, with
+// the division distributed: the host scales each coefficient by 1 / d_k and
+// the lane forms x_k / d_k while it waits, so that a step's dependent chain
+// is two fused multiply-adds (the row neighbour's, then the shuffled one);
+// the result is within a few roundings of the reference's.
 constexpr int kIcRing = 64;          // ring columns per warp boundary
 constexpr int kIcAhead = 8;          // cells loaded ahead of their step
-constexpr int kIcSync = 4;           // steps between barriers (divides kIcAhead)
+constexpr int kIcSync = 8;           // steps between barriers (divides kIcAhead)
 constexpr int kIcLag = 31 + kIcSync; // steps between neighbouring warps
 constexpr int kIcGridThreads = 512;  // block size of the wavefront launch: rows <= 512
 static_assert(kIcAhead % kIcSync == 0 && 2 * kIcSync <= kIcRing, "ring");
@@ -209,15 +210,14 @@ __device__ void ic_sweep_grid(const IcOp& ic, const double* in, double* out) {
 					if (on) {
 						if (cons_lane) nb = ring[cb][t & (kIcRing - 1)];
 						const double own = t > 0 ? res : 0.0;   // the row neighbour
-						double y = pin[u];
+						double y = pin[u] * prd[u];
 						if (fwd) {
-							y = fma(-pc0[u], nb, y);      // U(k-m, k) z_{k-m}
-							y = fma(-pc1[u], own, y);     // U(k-1, k) z_{k-1}
+							y = fma(-pc1[u], own, y);     // U(k-1, k) / d_k z_{k-1}
+							y = fma(-pc0[u], nb, y);      // U(k-m, k) / d_k z_{k-m}
 						} else {
-							y = fma(-pc0[u], own, y);     // U(k, k+1) z_{k+1}
-							y = fma(-pc1[u], nb, y);      // U(k, k+m) z_{k+m}
+							y = fma(-pc0[u], own, y);     // U(k, k+1) / d_k z_{k+1}
+							y = fma(-pc1[u], nb, y);      // U(k, k+m) / d_k z_{k+m}
 						}
-						y *= prd[u];
 						out[cell(t)] = y;
 						res = y;
 						if (prod_lane) ring[pb][t & (kIcRing - 1)] = y;

@@ -495,107 +495,7 @@ __global__ void __launch_bounds__(kThreads) k_advect_band(Geo g, double* phi, Bc
 	}
 }
 
-// The sweep as a wavefront of tiles: TB x TB tiles of cells, tile (I, J)
-// after (I - 1, J) and (I, J - 1) -- the only tiles holding cells it reads
-// new values of (its axis cross of radius 2 reaches no diagonal tile); the
-// tiles after it are not started, so the old values it reads are still
-// there. A tile is staged in shared memory with a halo of two cells, swept
-// by its own anti-diagonals with block barriers between them (the cell
-// update and its arithmetic are adv_cell's), written back, and published
-// by a release store of the step number; the next tiles acquire it. Tiles
-// are handed out in anti-diagonal order from a counter, so a block waits
-// only on tiles taken earlier by blocks that are running (the launch is
-// cooperative): no deadlock. Per step: block 0 refills phi's ghosts between
-// two grid barriers. Bit for bit the sequential loop's values, like
-// k_advect.
-constexpr int kAdvTile = 32;
-constexpr int kAdvTileThreads = 128;
-
-template<int SCH, bool P2 = false>
-__global__ void __launch_bounds__(kAdvTileThreads) k_advect_tiles(Geo g, double* phi,
-		BcDev bc, const double* uf, const double* vf, double dt, int steps,
-		const int* order, int ntj, int nt, unsigned* done, unsigned* ctr, GridCtl gc) {
-	constexpr int TB = kAdvTile, SP = kAdvTile + 4;
-	__shared__ double tile[SP * SP];
-	__shared__ double s_old[32];
-	__shared__ int s_t, s_ok;
-	gc.start();
-	const int tid = threadIdx.x;
-	for (int st = 0; st < steps; ++st) {
-		if (!grid_sync(gc)) return;
-		if (blockIdx.x == 0) {
-			bc_fill(g, phi, bc, s_old);
-			if (tid == 0) ctr[(st + 1) & 1] = 0u;
-		}
-		if (!grid_sync(gc)) return;
-		for (;;) {
-			if (tid == 0) s_t = (int)atomicAdd(&ctr[st & 1], 1u);
-			__syncthreads();
-			const int t = s_t;
-			__syncthreads();
-			if (t >= nt) break;
-			const int id = order[t];
-			const int I = id / ntj, J = id - I * ntj;
-			const int i0 = I * TB, j0 = J * TB;
-			const int ti = min(TB, g.nx - i0), tj = min(TB, g.ny - j0);
-			// the tiles above and to the left, this step
-			if (tid == 0) {
-				const unsigned need = (unsigned)st + 1u;
-				int ok = 1;
-				unsigned polls = 0;
-				unsigned long long t0 = 0;
-				while ((I > 0 && ld_acquire_gpu(&done[id - ntj]) < need)
-						|| (J > 0 && ld_acquire_gpu(&done[id - 1]) < need)) {
-					if ((++polls & 63u) == 0) {
-						if (*(volatile int*)gc.err) { ok = 0; break; }
-						const unsigned long long tt = globaltimer();
-						if (t0 == 0) t0 = tt;
-						if (tt - t0 > gc.wait_ns || tt > gc.deadline) {
-							set_err(gc, CARPIO_GPU_ETIMEOUT);
-							ok = 0;
-							break;
-						}
-					}
-				}
-				s_ok = ok;
-			}
-			__syncthreads();
-			if (!s_ok) return;
-			// stage the tile and its halo of two (ghosts included)
-			for (int q = tid; q < (ti + 4) * (tj + 4); q += kAdvTileThreads) {
-				const int li = q / (tj + 4), lj = q - li * (tj + 4);
-				tile[li * SP + lj] = ldcg(phi + g.at(i0 + li - 2, j0 + lj - 2));
-			}
-			__syncthreads();
-			// the tile's anti-diagonals
-			for (int L = 0; L <= ti + tj - 2; ++L) {
-				const int li = tid;
-				const int lj = L - tid;
-				if (tid < TB && li < ti && lj >= 0 && lj < tj) {
-					const int i = i0 + li, j = j0 + lj;
-					const int fa = (li + 2) * SP + (lj + 2);
-					double a0 = adv_axis_at<SCH, 0, P2>(g, uf, tile, fa, SP, i, j);
-					double a1 = adv_axis_at<SCH, 1, P2>(g, vf, tile, fa, 1, i, j);
-					double adv = 0.0;
-					adv += a0;
-					adv += a1;
-					const double phin = tile[fa];
-					tile[fa] = phin - dt * adv;
-				}
-				__syncthreads();
-			}
-			for (int q = tid; q < ti * tj; q += kAdvTileThreads) {
-				const int li = q / tj, lj = q - li * tj;
-				phi[g.at(i0 + li, j0 + lj)] = tile[(li + 2) * SP + (lj + 2)];
-			}
-			// the block barrier orders the writes before thread 0's release
-			__syncthreads();
-			if (tid == 0) st_release_gpu(&done[id], (unsigned)st + 1u);
-		}
-	}
-}
-
-// Row-pipelined sweep: lane l of warp b owns grid row i = 32 b + l and walks
+// Row-pipelined sweep: lane l < RPW of band b owns grid row i = RPW b + l and walks
 // its columns j in order, one step behind lane l - 1, so that at every step
 // the lanes of a warp hold one anti-diagonal of the in-place sweep. A cell
 // reads, as the reference's loop does, the new values of (i-1, j), (i-2, j),
@@ -606,28 +506,31 @@ __global__ void __launch_bounds__(kAdvTileThreads) k_advect_tiles(Geo g, double*
 // keeps of its own row ahead of its column (lanes l + 1 and l + 2, by
 // shuffle). There is no barrier per diagonal. Only the two rows across a
 // band edge go through memory: the next band's first lanes read the two
-// rows above from L2 once this band's lane 31 has published its column
+// rows above from L2 once this band's last lane has published its column
 // (release/acquire progress word, every kAdvPub columns), and this band's
-// last lanes read the two old rows below before they publish.
-// One band per block: the FP64 pipe is shared by an SM's warps (16 cycles
-// per warp instruction), so bands on separate SMs run their FP64 work side
-// by side.
-constexpr int kAdvRowWarps = 1;     // bands (warps) per block
+// last lanes read the two old rows below before they publish. A band is
+// one warp (RPW rows, lanes beyond RPW idle); NW bands share a block.
 constexpr int kAdvPub = 8;          // columns per progress publication
+constexpr int kAdvRows = 32;        // rows per band (one warp)
+constexpr int kAdvBands = 1;        // bands per block
 
-template<int SCH, bool P2 = false>
-__global__ void __launch_bounds__(kAdvRowWarps * 32, 1) k_advect_rows(Geo g, double* phi,
+template<int SCH, bool P2, int RPW, int NW>
+__global__ void __launch_bounds__(NW * 32, 1) k_advect_rows(Geo g, double* phi,
 		BcDev bc, const double* uf, const double* vf, double dt, int steps,
 		unsigned* prog, GridCtl gc) {
-	__shared__ double scr[kAdvRowWarps][10][32];   // a lane's two stencils, [k][lane]
+	static_assert(RPW >= 4 && RPW <= 32, "band rows");
+	__shared__ double scr[NW][10][32];             // a lane's two stencils, [k][lane]
 	__shared__ double s_old[32];
 	gc.start();
 	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const int nx = g.nx, ny = g.ny, gl = g.gl;
-	const int nb = (nx + 31) >> 5;
-	const int band = blockIdx.x * kAdvRowWarps + warp;
-	const int i0 = band * 32, i = i0 + lane;
-	const bool act = band < nb && i < nx;         // the lane computes cells
+	const int nb = (nx + RPW - 1) / RPW;
+	const int band = blockIdx.x * NW + warp;
+	const int i0 = band * RPW;
+	// idle lanes get a row outside the ghost ring: `at` gives them 0
+	const int i = lane < RPW ? i0 + lane : -4 * (gl + 1);
+	const bool act = lane < RPW && band < nb && i < nx;   // the lane computes cells
+	constexpr int LB = RPW - 1;                   // the band's last lane
 	double* F = &scr[warp][0][0];
 	// phi at (r, c) inside the ghost ring, else 0 (never used)
 	auto at = [&](int r, int c) -> double {
@@ -650,7 +553,8 @@ __global__ void __launch_bounds__(kAdvRowWarps * 32, 1) k_advect_rows(Geo g, dou
 		double o0 = at(i, tz), o1 = at(i, tz + 1), o2 = at(i, tz + 2), o3 = at(i, tz + 3);
 		// rows i0 - 1, i0 - 2 at column s (lane 0) and i0 - 1 at s - 1
 		double aC = 0.0, bC = 0.0, aP = 0.0, aN = 0.0, bN = 0.0;
-		// rows i0 + 32, i0 + 33 (old) at columns s - 31 (and i0 + 32 at s - 30)
+		// rows i0 + RPW, i0 + RPW + 1 (old) at columns s - LB (and i0 + RPW
+		// at s - LB + 1), for the last two lanes
 		double cC = 0.0, cN = 0.0, dC = 0.0, cNN = 0.0, dN = 0.0;
 		unsigned have = 0;
 		bool ok = true;
@@ -685,14 +589,14 @@ __global__ void __launch_bounds__(kAdvRowWarps * 32, 1) k_advect_rows(Geo g, dou
 				bN = at(i0 - 2, 1);
 			}
 		}
-		if (lane == 31) {
-			cC = at(i0 + 32, -31);
-			cN = at(i0 + 32, -30);
-			dC = at(i0 + 33, -31);
-			cNN = at(i0 + 32, -29);
-			dN = at(i0 + 33, -30);
+		if (lane == LB) {
+			cC = at(i0 + RPW, -LB);
+			cN = at(i0 + RPW, -LB + 1);
+			dC = at(i0 + RPW + 1, -LB);
+			cNN = at(i0 + RPW, -LB + 2);
+			dN = at(i0 + RPW + 1, -LB + 1);
 		}
-		for (int s = 0; s < ny + 31; ++s) {
+		for (int s = 0; s < ny + LB; ++s) {
 			const int t = s - lane;                   // this lane's column
 			const bool on = act && t >= 0 && t < ny;
 			// new values of the rows above at column t, old values below
@@ -701,11 +605,11 @@ __global__ void __launch_bounds__(kAdvRowWarps * 32, 1) k_advect_rows(Geo g, dou
 			double dn1 = __shfl_down_sync(0xffffffffu, o1, 1);
 			double dn2 = __shfl_down_sync(0xffffffffu, o2, 2);
 			const double aPl = __shfl_sync(0xffffffffu, aP, 0);
-			const double cNl = __shfl_sync(0xffffffffu, cN, 31);
+			const double cNl = __shfl_sync(0xffffffffu, cN, LB);
 			if (lane == 0) { up1 = aC; up2 = bC; }
 			if (lane == 1) up2 = aPl;
-			if (lane == 30) dn2 = cNl;
-			if (lane == 31) { dn1 = cC; dn2 = dC; }
+			if (lane == LB - 1) dn2 = cNl;
+			if (lane == LB) { dn1 = cC; dn2 = dC; }
 			if (on && (t & 7) == 0 && t + 16 < ny) {
 				// the face velocities' next lines into L1 (read-only here)
 				const int ap = g.at(i, t + 16);
@@ -753,20 +657,21 @@ __global__ void __launch_bounds__(kAdvRowWarps * 32, 1) k_advect_rows(Geo g, dou
 					bN = at(i0 - 2, s + 2);
 				}
 			}
-			// lane 31: the old rows below at columns s - 30 and s - 29
-			if (lane == 31) {
+			// the last lane: the old rows below at columns s - LB + 1 and
+			// s - LB + 2 for the next steps
+			if (lane == LB) {
 				cC = cN;
 				cN = cNN;
 				dC = dN;
-				cNN = at(i0 + 32, s - 28);
-				dN = at(i0 + 33, s - 29);
+				cNN = at(i0 + RPW, s - LB + 3);
+				dN = at(i0 + RPW + 1, s - LB + 2);
 			}
-			// publish lane 31's progress (lane 30's column is one ahead)
-			const int t31 = s - 31;
-			if (lower && t31 >= 0 && t31 < ny && ((t31 + 1) % kAdvPub == 0 || t31 == ny - 1)) {
-				if (lane >= 30) __threadfence();
+			// publish the last lane's progress (the lane before is one ahead)
+			const int tl = s - LB;
+			if (lower && tl >= 0 && tl < ny && ((tl + 1) % kAdvPub == 0 || tl == ny - 1)) {
+				if (lane == LB - 1 || lane == LB) __threadfence();
 				__syncwarp();
-				if (lane == 31) st_release_gpu(&prog[band], (unsigned)(t31 + 1));
+				if (lane == LB) st_release_gpu(&prog[band], (unsigned)(tl + 1));
 			}
 		}
 		// lane 0 may have stopped on an error: the grid barrier returns it
@@ -1232,7 +1137,8 @@ const void* pick_advect_band(int sch, bool p2) {
 
 template<int S>
 const void* advect_rows_kernel(bool p2) {
-	return p2 ? (const void*)k_advect_rows<S, true> : (const void*)k_advect_rows<S, false>;
+	return p2 ? (const void*)k_advect_rows<S, true, kAdvRows, kAdvBands>
+	          : (const void*)k_advect_rows<S, false, kAdvRows, kAdvBands>;
 }
 
 const void* pick_advect_rows(int sch, bool p2) {
@@ -1246,26 +1152,6 @@ const void* pick_advect_rows(int sch, bool p2) {
 	case CARPIO_GPU_WAHYD: return advect_rows_kernel<CARPIO_GPU_WAHYD>(p2);
 	case CARPIO_GPU_QUICK: return advect_rows_kernel<CARPIO_GPU_QUICK>(p2);
 	case CARPIO_GPU_CUI: return advect_rows_kernel<CARPIO_GPU_CUI>(p2);
-	}
-	return nullptr;
-}
-
-template<int S>
-const void* advect_tiles_kernel(bool p2) {
-	return p2 ? (const void*)k_advect_tiles<S, true> : (const void*)k_advect_tiles<S, false>;
-}
-
-const void* pick_advect_tiles(int sch, bool p2) {
-	switch (sch) {
-	case CARPIO_GPU_UPWIND1: return advect_tiles_kernel<CARPIO_GPU_UPWIND1>(p2);
-	case CARPIO_GPU_CENTER: return advect_tiles_kernel<CARPIO_GPU_CENTER>(p2);
-	case CARPIO_GPU_CENTER4: return advect_tiles_kernel<CARPIO_GPU_CENTER4>(p2);
-	case CARPIO_GPU_UPWIND2: return advect_tiles_kernel<CARPIO_GPU_UPWIND2>(p2);
-	case CARPIO_GPU_VANLEER: return advect_tiles_kernel<CARPIO_GPU_VANLEER>(p2);
-	case CARPIO_GPU_SUPERBEE: return advect_tiles_kernel<CARPIO_GPU_SUPERBEE>(p2);
-	case CARPIO_GPU_WAHYD: return advect_tiles_kernel<CARPIO_GPU_WAHYD>(p2);
-	case CARPIO_GPU_QUICK: return advect_tiles_kernel<CARPIO_GPU_QUICK>(p2);
-	case CARPIO_GPU_CUI: return advect_tiles_kernel<CARPIO_GPU_CUI>(p2);
 	}
 	return nullptr;
 }
@@ -1720,7 +1606,6 @@ struct carpio_gpu_advection {
 	carpio_gpu_grid* g;
 	cg_host::LaunchWs lw;     // control words of the band sweep
 	cg_host::DevBuf prog;     // its progress word per band
-	cg_host::DevBuf tord, tdone;   // tile sweep: anti-diagonal order, done words + counters
 	cg_host::DevBuf fields;   // u v uf vf phi, then the ghost values of u v phi
 	double* f[8];
 	carpio_gpu_bc bc[3];      // u v phi
@@ -1853,10 +1738,10 @@ int carpio_gpu_advection_step(carpio_gpu_advection* a, double dt, int steps) {
 		// the row-pipelined sweep (k_advect_rows): one lane per grid row
 		const void* kr = pick_advect_rows(a->scheme, geo.p2 != 0);
 		if (!kr) return CARPIO_GPU_EINVAL;
-		const int nb = (g->nx + 31) / 32;
-		const int blocks = (nb + kAdvRowWarps - 1) / kAdvRowWarps;
+		const int nb = (g->nx + kAdvRows - 1) / kAdvRows;
+		const int blocks = (nb + kAdvBands - 1) / kAdvBands;
 		int per_sm = 0;
-		CG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kr, kAdvRowWarps * 32, 0));
+		CG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kr, kAdvBands * 32, 0));
 		if ((long)per_sm * sm_count() < blocks) return CARPIO_GPU_EINVAL;
 		int rc;
 		if ((rc = a->lw.ensure(blocks))) return rc;
@@ -1870,7 +1755,7 @@ int carpio_gpu_advection_step(carpio_gpu_advection* a, double dt, int steps) {
 		Geo gg = geo;
 		BcDev bb = bcp;
 		void* args[] = { &gg, &phi, &bb, &uf, &vf, &dt, &steps, &prog, &gc };
-		CG_CK(cudaLaunchCooperativeKernel(kr, blocks, kAdvRowWarps * 32, args, 0, a->s));
+		CG_CK(cudaLaunchCooperativeKernel(kr, blocks, kAdvBands * 32, args, 0, a->s));
 		CG_CK(cudaMemcpyAsync(a->lw.host_ctl, a->lw.ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, a->s));
 		CG_CK(cudaStreamSynchronize(a->s));
 		return a->lw.host_ctl->err;
