@@ -389,6 +389,9 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	// the band's rows back along y. (r, z) and (r, r) of the band in g.
 	auto precond_dct = [&](float (&g)[2]) -> bool {
 		float* G = dc.G;
+		// the transform reads every cell of the band's r, which the callers
+		// wrote thread by thread
+		__syncthreads();
 		dct_forward<false>(dbuf, rows, dc.ly, dc.twy, dc.ey, dc.fy != 0,
 				[&](int sq, int n) { return rs[sq * ny + n]; },
 				[&](int sq, int k, float val) { __stcg(G + (size_t)(r0 + sq) * ny + k, val); });
