@@ -238,68 +238,93 @@ __device__ __forceinline__ double limiter(int sch, double r, double R) {
 	return 0.0;
 }
 
-// one axis of VdotNabla at cell (i, j); D = 0 x, 1 y. P2: the grid's
-// lengths are the powers of two of Geo::p2, so the divisions by them are
+// The TVD schemes (upwind2, van Leer, superbee, WAHYD, QUICK, CUI) build
+// each face value from an upwind-biased stencil of three cells; the others
+// (upwind1, center, center4) are single expressions.
+template<int SCH>
+constexpr bool kTvdScheme = SCH != CARPIO_GPU_UPWIND1 && SCH != CARPIO_GPU_CENTER
+		&& SCH != CARPIO_GPU_CENTER4;
+
+// One face value of a TVD scheme at cell (i, j) along axis D (0 x, 1 y):
+// `plus` the face at +1/2 (fp), else the face at -1/2 (fm), the stencil
+// chosen by the sign of the cell's velocity veo. P2: the grid's lengths are
+// the powers of two of Geo::p2, so the divisions by them are
 // multiplications by exact reciprocals (the same bits); the divisions by
-// data stay.
-// The field may sit in another array than the faces (a tile in shared
-// memory): f at index fa with stride fst along the axis; the faces at the
-// grid's index of (i, j).
+// data stay. The field may sit in another array than the faces (a tile in
+// shared memory, a lane's registers): f at index fa with stride fst along
+// the axis; the faces at the grid's index of (i, j).
+template<int SCH, int D, bool P2>
+__device__ __forceinline__ double tvd_half(const Geo& g, const double* face,
+		const double* f, int fa, int fst, int i, int j, bool plus) {
+	const int st = D == 0 ? g.P : 1;
+	const int a = g.at(i, j);
+#define F(k) f[fa + (k) * fst]
+#define S(k) (D == 0 ? g.SX(i + (k)) : g.SY(j + (k)))
+	const double fa0 = face[a], fam = face[a - st];
+	const double veo = (fa0 + fam) * 0.5;
+	int C_, U_, D_;
+	if (veo >= 0.0) {
+		if (plus) { D_ = 1; C_ = 0; U_ = -1; } else { D_ = 0; C_ = -1; U_ = -2; }
+	} else if (veo < 0.0) {
+		if (plus) { D_ = 0; C_ = 1; U_ = 2; } else { D_ = -1; C_ = 0; U_ = 1; }
+	} else {
+		D_ = C_ = U_ = 0;
+	}
+	if (P2) {
+		// every S is h: R = 2h / h = 2, the sums are 2h
+		const double h = D == 0 ? g.hx : g.hy;
+		const double ih = D == 0 ? g.ihx : g.ihy;
+		const double h2 = h + h, ih2 = 0.5 * ih;
+		const double R = 2.0;
+		const double r = (F(C_) - F(U_)) * h2 / (F(D_) - F(C_) + kSmall) * ih2;
+		return F(C_) + limiter(SCH, r, R) * 0.5 * (F(D_) - F(C_));
+	}
+	const double R = (S(D_) + S(C_)) / S(C_);
+	const double r = (F(C_) - F(U_)) * (S(D_) + S(C_)) / (F(D_) - F(C_) + kSmall) / (S(C_) + S(U_));
+	return F(C_) + limiter(SCH, r, R) / R * (F(D_) - F(C_));
+#undef F
+#undef S
+}
+
+// the TVD axis term from its two face values: (u+ fp - u- fm) / S(0)
+template<int D, bool P2>
+__device__ __forceinline__ double tvd_combine(const Geo& g, const double* face,
+		int i, int j, double fp, double fm) {
+	const int st = D == 0 ? g.P : 1;
+	const int a = g.at(i, j);
+	const double fa0 = face[a], fam = face[a - st];
+	if (P2) return (fa0 * fp - fam * fm) * (D == 0 ? g.ihx : g.ihy);
+	return (fa0 * fp - fam * fm) / (D == 0 ? g.SX(i) : g.SY(j));
+}
+
+// one axis of VdotNabla at cell (i, j); D = 0 x, 1 y (field addressing as
+// tvd_half)
 template<int SCH, int D, bool P2 = false>
 __device__ __forceinline__ double adv_axis_at(const Geo& g, const double* face,
 		const double* f, int fa, int fst, int i, int j) {
+	if constexpr (kTvdScheme<SCH>) {
+		const double fp = tvd_half<SCH, D, P2>(g, face, f, fa, fst, i, j, true);
+		const double fm = tvd_half<SCH, D, P2>(g, face, f, fa, fst, i, j, false);
+		return tvd_combine<D, P2>(g, face, i, j, fp, fm);
+	}
 	const int st = D == 0 ? g.P : 1;
 	const int a = g.at(i, j);
 #define F(k) f[fa + (k) * fst]
 #define C(k) (D == 0 ? g.CX(i + (k)) : g.CY(j + (k)))
-#define S(k) (D == 0 ? g.SX(i + (k)) : g.SY(j + (k)))
-	double fa0 = face[a], fam = face[a - st];
-	double veo = (fa0 + fam) * 0.5;
+	const double fa0 = face[a], fam = face[a - st];
+	const double veo = (fa0 + fam) * 0.5;
 	if (SCH == CARPIO_GPU_UPWIND1) {
 		if (veo > 0.0) return veo * (F(0) - F(-1)) / (C(0) - C(-1));
 		if (veo < 0.0) return veo * (F(1) - F(0)) / (C(1) - C(0));
 		return 0.0;
 	} else if (SCH == CARPIO_GPU_CENTER) {
 		return veo * (F(1) - F(-1)) / (C(1) - C(-1));
-	} else if (SCH == CARPIO_GPU_CENTER4) {
-		double din = (F(1) - F(-1)) / (C(1) - C(-1));
-		double dout = (F(2) - F(-2)) / (C(2) - C(-2));
-		return (4.0 * din - dout) / 3.0;
-	} else {
-		int Cm, Um, Dm, Cp, Up, Dp;
-		if (veo >= 0.0) {
-			Dm = 0; Cm = -1; Um = -2;
-			Dp = 1; Cp = 0; Up = -1;
-		} else if (veo < 0.0) {
-			Dm = -1; Cm = 0; Um = 1;
-			Dp = 0; Cp = 1; Up = 2;
-		} else {
-			Dm = Cm = Um = Dp = Cp = Up = 0;
-		}
-		double R, r, fp, fm;
-		if (P2) {
-			// every S is h: R = 2h / h = 2, the sums are 2h
-			const double h = D == 0 ? g.hx : g.hy;
-			const double ih = D == 0 ? g.ihx : g.ihy;
-			const double h2 = h + h, ih2 = 0.5 * ih;
-			R = 2.0;
-			r = (F(Cp) - F(Up)) * h2 / (F(Dp) - F(Cp) + kSmall) * ih2;
-			fp = F(Cp) + limiter(SCH, r, R) * 0.5 * (F(Dp) - F(Cp));
-			r = (F(Cm) - F(Um)) * h2 / (F(Dm) - F(Cm) + kSmall) * ih2;
-			fm = F(Cm) + limiter(SCH, r, R) * 0.5 * (F(Dm) - F(Cm));
-			return (fa0 * fp - fam * fm) * ih;
-		}
-		R = (S(Dp) + S(Cp)) / S(Cp);
-		r = (F(Cp) - F(Up)) * (S(Dp) + S(Cp)) / (F(Dp) - F(Cp) + kSmall) / (S(Cp) + S(Up));
-		fp = F(Cp) + limiter(SCH, r, R) / R * (F(Dp) - F(Cp));
-		R = (S(Dm) + S(Cm)) / S(Cm);
-		r = (F(Cm) - F(Um)) * (S(Dm) + S(Cm)) / (F(Dm) - F(Cm) + kSmall) / (S(Cm) + S(Um));
-		fm = F(Cm) + limiter(SCH, r, R) / R * (F(Dm) - F(Cm));
-		return (fa0 * fp - fam * fm) / S(0);
 	}
+	double din = (F(1) - F(-1)) / (C(1) - C(-1));
+	double dout = (F(2) - F(-2)) / (C(2) - C(-2));
+	return (4.0 * din - dout) / 3.0;
 #undef F
 #undef C
-#undef S
 }
 
 template<int SCH, int D, bool P2 = false>
@@ -514,15 +539,25 @@ constexpr int kAdvPub = 8;          // columns per progress publication
 constexpr int kAdvRows = 32;        // rows per band (one warp)
 constexpr int kAdvBands = 1;        // bands per block
 
-template<int SCH, bool P2, int RPW, int NW>
-__global__ void __launch_bounds__(NW * 32, 1) k_advect_rows(Geo g, double* phi,
+// NF = 4 (TVD schemes): four warps per band, warp q computing one of the
+// cell's four face values (x at +1/2 and -1/2, y at +1/2 and -1/2) on its
+// own SMSP -- a warp issues one FP64 instruction per 64 cycles, so a face's
+// ~50 instead of a cell's ~200 per step -- with identical lane state in all
+// four; the faces meet in shared memory behind one barrier of the band's
+// warps per step (double-buffered by step parity), every warp combines
+// them, and warp 0 alone stores and publishes.
+template<int SCH, bool P2, int RPW, int NW, int NF>
+__global__ void __launch_bounds__(NW * NF * 32, 1) k_advect_rows(Geo g, double* phi,
 		BcDev bc, const double* uf, const double* vf, double dt, int steps,
 		unsigned* prog, GridCtl gc) {
 	static_assert(RPW >= 4 && RPW <= 32, "band rows");
-	__shared__ double scr[NW][10][32];             // a lane's two stencils, [k][lane]
+	static_assert(NF == 1 || (NF == 4 && kTvdScheme<SCH> && NW == 1), "face split");
+	__shared__ double scr[NW * NF][10][32];        // a lane's two stencils, [k][lane]
+	__shared__ double sfc[2][NW][NF][32];          // face values by step parity
 	__shared__ double s_old[32];
 	gc.start();
-	const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int wq = threadIdx.x >> 5, lane = threadIdx.x & 31;
+	const int warp = wq / NF, q = wq - warp * NF;  // band in the block, face
 	const int nx = g.nx, ny = g.ny, gl = g.gl;
 	const int nb = (nx + RPW - 1) / RPW;
 	const int band = blockIdx.x * NW + warp;
@@ -531,7 +566,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_advect_rows(Geo g, double* phi,
 	const int i = lane < RPW ? i0 + lane : -4 * (gl + 1);
 	const bool act = lane < RPW && band < nb && i < nx;   // the lane computes cells
 	constexpr int LB = RPW - 1;                   // the band's last lane
-	double* F = &scr[warp][0][0];
+	double* F = &scr[wq][0][0];
 	// phi at (r, c) inside the ghost ring, else 0 (never used)
 	auto at = [&](int r, int c) -> double {
 		return (r >= -gl && r < nx + gl && c >= -gl && c < ny + gl) ? ldcg(phi + g.at(r, c)) : 0.0;
@@ -617,6 +652,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_advect_rows(Geo g, double* phi,
 				asm volatile("prefetch.global.L1 [%0];" :: "l"(uf + ap - g.P));
 				asm volatile("prefetch.global.L1 [%0];" :: "l"(vf + ap));
 			}
+			double a0 = 0.0, a1 = 0.0;   // the two axis terms
 			if (on) {
 				F[0 * 32 + lane] = up2;
 				F[1 * 32 + lane] = up1;
@@ -629,13 +665,35 @@ __global__ void __launch_bounds__(NW * 32, 1) k_advect_rows(Geo g, double* phi,
 				F[8 * 32 + lane] = o1;
 				F[9 * 32 + lane] = o2;
 				const int fa = 2 * 32 + lane;
-				const double a0 = adv_axis_at<SCH, 0, P2>(g, uf, F, fa, 32, i, t);
-				const double a1 = adv_axis_at<SCH, 1, P2>(g, vf, F + 5 * 32, fa, 32, i, t);
+				if constexpr (NF == 4) {
+					double fv;
+					switch (q) {
+					case 0: fv = tvd_half<SCH, 0, P2>(g, uf, F, fa, 32, i, t, true); break;
+					case 1: fv = tvd_half<SCH, 0, P2>(g, uf, F, fa, 32, i, t, false); break;
+					case 2: fv = tvd_half<SCH, 1, P2>(g, vf, F + 5 * 32, fa, 32, i, t, true); break;
+					default: fv = tvd_half<SCH, 1, P2>(g, vf, F + 5 * 32, fa, 32, i, t, false); break;
+					}
+					sfc[s & 1][warp][q][lane] = fv;
+				} else {
+					a0 = adv_axis_at<SCH, 0, P2>(g, uf, F, fa, 32, i, t);
+					a1 = adv_axis_at<SCH, 1, P2>(g, vf, F + 5 * 32, fa, 32, i, t);
+				}
+			}
+			if constexpr (NF == 4) {
+				// every warp of the band, every step
+				asm volatile("bar.sync %0, %1;" :: "r"(1 + warp), "r"(NF * 32) : "memory");
+			}
+			if (on) {
+				if constexpr (NF == 4) {
+					const double (*fv)[32] = sfc[s & 1][warp];
+					a0 = tvd_combine<0, P2>(g, uf, i, t, fv[0][lane], fv[1][lane]);
+					a1 = tvd_combine<1, P2>(g, vf, i, t, fv[2][lane], fv[3][lane]);
+				}
 				double adv = 0.0;
 				adv += a0;
 				adv += a1;
 				const double nv = o0 - dt * adv;
-				phi[g.at(i, t)] = nv;
+				if (q == 0) phi[g.at(i, t)] = nv;
 				res2 = res1;
 				res1 = nv;
 			} else if (t >= ny) {
@@ -668,7 +726,7 @@ __global__ void __launch_bounds__(NW * 32, 1) k_advect_rows(Geo g, double* phi,
 			}
 			// publish the last lane's progress (the lane before is one ahead)
 			const int tl = s - LB;
-			if (lower && tl >= 0 && tl < ny && ((tl + 1) % kAdvPub == 0 || tl == ny - 1)) {
+			if (q == 0 && lower && tl >= 0 && tl < ny && ((tl + 1) % kAdvPub == 0 || tl == ny - 1)) {
 				if (lane == LB - 1 || lane == LB) __threadfence();
 				__syncwarp();
 				if (lane == LB) st_release_gpu(&prog[band], (unsigned)(tl + 1));
@@ -1137,8 +1195,9 @@ const void* pick_advect_band(int sch, bool p2) {
 
 template<int S>
 const void* advect_rows_kernel(bool p2) {
-	return p2 ? (const void*)k_advect_rows<S, true, kAdvRows, kAdvBands>
-	          : (const void*)k_advect_rows<S, false, kAdvRows, kAdvBands>;
+	constexpr int nf = kTvdScheme<S> ? 4 : 1;
+	return p2 ? (const void*)k_advect_rows<S, true, kAdvRows, kAdvBands, nf>
+	          : (const void*)k_advect_rows<S, false, kAdvRows, kAdvBands, nf>;
 }
 
 const void* pick_advect_rows(int sch, bool p2) {
