@@ -99,11 +99,21 @@ def config(n):
             "parallelism": "replicas"}
 
 
-def solver_desc(precision, inner_tol):
+def spectral_applies(n):
+    """the cavity's pressure operator (uniform grid and coefficient, all
+    Neumann) takes the spectral preconditioner when its side is a power of
+    two"""
+    return PRECOND[0] in ("default", "spectral") and n >= 2 and (n & (n - 1)) == 0
+
+
+def solver_desc(precision, inner_tol, n=1024):
     """how our arm solves the projection"""
     if precision != "mixed":
         pre = None
-    elif PRECOND[0] in ("multigrid", "default"):
+    elif spectral_applies(n):
+        pre = ("spectral: M = A^-1 through the DCT-II of both axes (FP32 FFTs "
+               "in shared memory, two grid barriers per application)")
+    elif PRECOND[0] in ("multigrid", "default", "spectral"):
         pre = ("geometric multigrid V(1,1)-cycle (damped Jacobi, bilinear "
                "prolongation, restriction its transpose)")
     elif POLY[0] < 0:
@@ -208,10 +218,12 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def poly_degree():
+def poly_degree(n=1024):
     """degree of the FP32 CG's band-local Chebyshev preconditioner in use
-    (-1: the multigrid V-cycle)"""
-    if PRECOND[0] in ("multigrid", "default"):
+    (-1: the multigrid V-cycle, -2: the spectral preconditioner)"""
+    if spectral_applies(n):
+        return -2
+    if PRECOND[0] in ("multigrid", "default", "spectral"):
         return -1
     return 0 if POLY[0] < 0 else (POLY[0] or 5)
 
@@ -230,11 +242,17 @@ def solve_bytes(precision, inner, outer, deg=0):
     r_k, z), the (r, z) dot 8 B; the multigrid V-cycle (deg = -1) 32 B per
     fine cell (write r and the pre-smoothed z; read z and D, write the
     residual; read it for the restriction; read z and D for the post-
-    smoothing) and a quarter of that again per coarser level (x 4/3)."""
+    smoothing) and a quarter of that again per coarser level (x 4/3); the
+    spectral preconditioner (deg = -2) 32 B per cell and application (rows:
+    read r, write the workspace; columns: read and write it twice; rows back:
+    read it, write z), applied once per FP32 iteration and once per
+    refinement that does not converge (the first residual's included)."""
     if precision == "mixed":
         krylov = 40 * inner + 40 * (outer + 1)
         if deg > 0:
             pre = (20 + 28 * (deg - 1) + 8) * inner
+        elif deg == -2:
+            pre = 32 * (inner + outer)
         elif deg < 0:
             pre = 32 * 4 / 3 * inner
         else:
@@ -408,7 +426,7 @@ def main():
         "dtype": "f32+f64" if a.precision == "mixed" else "f64",
         "data": "synthetic (cavity from rest)",
         "config": config(n),
-        "solver": solver_desc(a.precision, a.inner_tol),
+        "solver": solver_desc(a.precision, a.inner_tol, n),
         "gpu_launches": LAUNCHES_PER_STEP * a.steps,
         "clocks": clk,
         "wall_ms_per_step": 1e3 * wall / a.steps,
@@ -422,7 +440,7 @@ def main():
     # passes are reported beside it
     peak, how = peaks()
     kry, pre = solve_bytes(a.precision, inner, outer,
-                           poly_degree() if a.precision == "mixed" else 0)
+                           poly_degree(n) if a.precision == "mixed" else 0)
     achieved = kry * n * n / (solve_ms / 1e3) / 1e9
     out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak,
                        "unit": "GB/s", "frac": achieved / peak,
@@ -439,8 +457,9 @@ def main():
         out["roofline"]["note"] = (
             "the Krylov vectors stay in shared memory and registers: DRAM "
             "traffic is `traffic`, far below the algorithmic bytes; the kernel "
-            "is bound by grid synchronisation latency (two all-reduces per FP32 "
-            "iteration, and with the multigrid V-cycle its grid barriers)")
+            "is bound by grid synchronisation latency and by its FP64 residual "
+            "passes (two all-reduces per FP32 iteration, the preconditioner's "
+            "grid barriers, three FP64 residuals and the prologue per solve)")
     # e2e through the public API with host buffers: the timed steps again,
     # from the same starting state, each step copying the whole state in
     # from pinned host memory and back out
@@ -570,7 +589,8 @@ def next_rows_leg(steps=5):
     ms = 1e3 * (time.perf_counter() - t0) / steps
     out["advection_1024"] = {"ms_per_step": ms, "mcell_steps_per_s": n * n / ms / 1e3,
                              "steps": steps, "scheme": "VanLeer",
-                             "kernel": "k_advect_band (pipelined bands of rows, one per SM)"}
+                             "kernel": "k_advect_rows (one lane per grid row, four warps "
+                                       "per band computing one TVD face each)"}
     del eq
     from carpio_gb300 import structure as S
     m = 256

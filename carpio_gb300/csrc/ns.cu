@@ -555,6 +555,12 @@ __global__ void __launch_bounds__(NW * NF * 32, 1) k_advect_rows(Geo g, double* 
 	__shared__ double scr[NW * NF][10][32];        // a lane's two stencils, [k][lane]
 	__shared__ double sfc[2][NW][NF][32];          // face values by step parity
 	__shared__ double s_old[32];
+	// the per-step barrier counts NF warps per band: any other block size
+	// is refused before the first barrier (uniform over the grid)
+	if (blockDim.x != NW * NF * 32) {
+		if (threadIdx.x == 0 && blockIdx.x == 0) set_err(gc, CARPIO_GPU_EINVAL);
+		return;
+	}
 	gc.start();
 	const int wq = threadIdx.x >> 5, lane = threadIdx.x & 31;
 	const int warp = wq / NF, q = wq - warp * NF;  // band in the block, face
@@ -1193,24 +1199,26 @@ const void* pick_advect_band(int sch, bool p2) {
 	return nullptr;
 }
 
+// the row sweep's kernel for a scheme and its block size (threads)
 template<int S>
-const void* advect_rows_kernel(bool p2) {
+const void* advect_rows_kernel(bool p2, int& threads) {
 	constexpr int nf = kTvdScheme<S> ? 4 : 1;
+	threads = kAdvBands * nf * 32;
 	return p2 ? (const void*)k_advect_rows<S, true, kAdvRows, kAdvBands, nf>
 	          : (const void*)k_advect_rows<S, false, kAdvRows, kAdvBands, nf>;
 }
 
-const void* pick_advect_rows(int sch, bool p2) {
+const void* pick_advect_rows(int sch, bool p2, int& threads) {
 	switch (sch) {
-	case CARPIO_GPU_UPWIND1: return advect_rows_kernel<CARPIO_GPU_UPWIND1>(p2);
-	case CARPIO_GPU_CENTER: return advect_rows_kernel<CARPIO_GPU_CENTER>(p2);
-	case CARPIO_GPU_CENTER4: return advect_rows_kernel<CARPIO_GPU_CENTER4>(p2);
-	case CARPIO_GPU_UPWIND2: return advect_rows_kernel<CARPIO_GPU_UPWIND2>(p2);
-	case CARPIO_GPU_VANLEER: return advect_rows_kernel<CARPIO_GPU_VANLEER>(p2);
-	case CARPIO_GPU_SUPERBEE: return advect_rows_kernel<CARPIO_GPU_SUPERBEE>(p2);
-	case CARPIO_GPU_WAHYD: return advect_rows_kernel<CARPIO_GPU_WAHYD>(p2);
-	case CARPIO_GPU_QUICK: return advect_rows_kernel<CARPIO_GPU_QUICK>(p2);
-	case CARPIO_GPU_CUI: return advect_rows_kernel<CARPIO_GPU_CUI>(p2);
+	case CARPIO_GPU_UPWIND1: return advect_rows_kernel<CARPIO_GPU_UPWIND1>(p2, threads);
+	case CARPIO_GPU_CENTER: return advect_rows_kernel<CARPIO_GPU_CENTER>(p2, threads);
+	case CARPIO_GPU_CENTER4: return advect_rows_kernel<CARPIO_GPU_CENTER4>(p2, threads);
+	case CARPIO_GPU_UPWIND2: return advect_rows_kernel<CARPIO_GPU_UPWIND2>(p2, threads);
+	case CARPIO_GPU_VANLEER: return advect_rows_kernel<CARPIO_GPU_VANLEER>(p2, threads);
+	case CARPIO_GPU_SUPERBEE: return advect_rows_kernel<CARPIO_GPU_SUPERBEE>(p2, threads);
+	case CARPIO_GPU_WAHYD: return advect_rows_kernel<CARPIO_GPU_WAHYD>(p2, threads);
+	case CARPIO_GPU_QUICK: return advect_rows_kernel<CARPIO_GPU_QUICK>(p2, threads);
+	case CARPIO_GPU_CUI: return advect_rows_kernel<CARPIO_GPU_CUI>(p2, threads);
 	}
 	return nullptr;
 }
@@ -1795,12 +1803,13 @@ int carpio_gpu_advection_step(carpio_gpu_advection* a, double dt, int steps) {
 	}
 	if (g->gl >= 2) {
 		// the row-pipelined sweep (k_advect_rows): one lane per grid row
-		const void* kr = pick_advect_rows(a->scheme, geo.p2 != 0);
+		int threads = 0;
+		const void* kr = pick_advect_rows(a->scheme, geo.p2 != 0, threads);
 		if (!kr) return CARPIO_GPU_EINVAL;
 		const int nb = (g->nx + kAdvRows - 1) / kAdvRows;
 		const int blocks = (nb + kAdvBands - 1) / kAdvBands;
 		int per_sm = 0;
-		CG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kr, kAdvBands * 32, 0));
+		CG_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kr, threads, 0));
 		if ((long)per_sm * sm_count() < blocks) return CARPIO_GPU_EINVAL;
 		int rc;
 		if ((rc = a->lw.ensure(blocks))) return rc;
@@ -1814,7 +1823,7 @@ int carpio_gpu_advection_step(carpio_gpu_advection* a, double dt, int steps) {
 		Geo gg = geo;
 		BcDev bb = bcp;
 		void* args[] = { &gg, &phi, &bb, &uf, &vf, &dt, &steps, &prog, &gc };
-		CG_CK(cudaLaunchCooperativeKernel(kr, blocks, kAdvBands * 32, args, 0, a->s));
+		CG_CK(cudaLaunchCooperativeKernel(kr, blocks, threads, args, 0, a->s));
 		CG_CK(cudaMemcpyAsync(a->lw.host_ctl, a->lw.ctl.p, sizeof(Ctl), cudaMemcpyDeviceToHost, a->s));
 		CG_CK(cudaStreamSynchronize(a->s));
 		return a->lw.host_ctl->err;
