@@ -253,23 +253,13 @@ constexpr bool kTvdScheme = SCH != CARPIO_GPU_UPWIND1 && SCH != CARPIO_GPU_CENTE
 // data stay. The field may sit in another array than the faces (a tile in
 // shared memory, a lane's registers): f at index fa with stride fst along
 // the axis; the faces at the grid's index of (i, j).
+// The face value from its three stencil cells at offsets D_, C_, U_
+// (downwind, central, upwind) of cell (i, j) along axis D.
 template<int SCH, int D, bool P2>
-__device__ __forceinline__ double tvd_half(const Geo& g, const double* face,
-		const double* f, int fa, int fst, int i, int j, bool plus) {
-	const int st = D == 0 ? g.P : 1;
-	const int a = g.at(i, j);
+__device__ __forceinline__ double tvd_value(const Geo& g, const double* f, int fa,
+		int fst, int i, int j, int D_, int C_, int U_) {
 #define F(k) f[fa + (k) * fst]
 #define S(k) (D == 0 ? g.SX(i + (k)) : g.SY(j + (k)))
-	const double fa0 = face[a], fam = face[a - st];
-	const double veo = (fa0 + fam) * 0.5;
-	int C_, U_, D_;
-	if (veo >= 0.0) {
-		if (plus) { D_ = 1; C_ = 0; U_ = -1; } else { D_ = 0; C_ = -1; U_ = -2; }
-	} else if (veo < 0.0) {
-		if (plus) { D_ = 0; C_ = 1; U_ = 2; } else { D_ = -1; C_ = 0; U_ = 1; }
-	} else {
-		D_ = C_ = U_ = 0;
-	}
 	if (P2) {
 		// every S is h: R = 2h / h = 2, the sums are 2h
 		const double h = D == 0 ? g.hx : g.hy;
@@ -284,6 +274,34 @@ __device__ __forceinline__ double tvd_half(const Geo& g, const double* face,
 	return F(C_) + limiter(SCH, r, R) / R * (F(D_) - F(C_));
 #undef F
 #undef S
+}
+
+// the stencil orientation of a cell from its velocity veo: 1 (veo >= 0), -1
+// (veo < 0), 0 (NaN: every offset 0)
+__device__ __forceinline__ int tvd_orient(double veo) {
+	return veo >= 0.0 ? 1 : (veo < 0.0 ? -1 : 0);
+}
+
+// the +1/2 face of a cell in its own frame: the same value as the -1/2
+// face of the next cell with the same orientation (the same three cells)
+template<int SCH, int D, bool P2>
+__device__ __forceinline__ double tvd_plus(const Geo& g, const double* f, int fa,
+		int fst, int i, int j, int o) {
+	return o > 0 ? tvd_value<SCH, D, P2>(g, f, fa, fst, i, j, 1, 0, -1)
+	     : o < 0 ? tvd_value<SCH, D, P2>(g, f, fa, fst, i, j, 0, 1, 2)
+	             : tvd_value<SCH, D, P2>(g, f, fa, fst, i, j, 0, 0, 0);
+}
+
+template<int SCH, int D, bool P2>
+__device__ __forceinline__ double tvd_half(const Geo& g, const double* face,
+		const double* f, int fa, int fst, int i, int j, bool plus) {
+	const int st = D == 0 ? g.P : 1;
+	const int a = g.at(i, j);
+	const double veo = (face[a] + face[a - st]) * 0.5;
+	const int o = tvd_orient(veo);
+	if (plus || o == 0) return tvd_plus<SCH, D, P2>(g, f, fa, fst, i, j, o);
+	return o > 0 ? tvd_value<SCH, D, P2>(g, f, fa, fst, i, j, 0, -1, -2)
+	             : tvd_value<SCH, D, P2>(g, f, fa, fst, i, j, -1, 0, 1);
 }
 
 // the TVD axis term from its two face values: (u+ fp - u- fm) / S(0)
@@ -849,6 +867,96 @@ __global__ void __launch_bounds__(kThreads) k_predictor(Geo g, const double* u,
 	}
 }
 
+// The predictor for the TVD schemes, by tiles of kPredTI x kPredTJ cells:
+// a face's value depends only on the face and the upwind orientation, so
+// the +1/2 face of a cell and the -1/2 face of the next cell are the same
+// bits whenever the two cells' velocities have the same sign. Each tile
+// stages the component with two halo cells in shared memory, evaluates
+// every face it needs once per orientation its cells ask for (once where
+// they agree, the usual case), then combines them per cell exactly as
+// adv_cell does. The per-cell arithmetic is k_predictor's.
+constexpr int kPredTI = 8, kPredTJ = 64, kPredThreads = 512;
+
+template<int SCH, bool P2>
+__global__ void __launch_bounds__(kPredThreads) k_predictor_tiles(Geo g, const double* u,
+		const double* v, const double* uf, const double* vf, double* us,
+		double* vs, const StepScalars* ss, double rho, double mu, const double* muf) {
+	constexpr int TI = kPredTI, TJ = kPredTJ, SJ = TJ + 4;
+	__shared__ double tile[(TI + 4) * SJ];   // the component, two halo cells
+	__shared__ double fpx[TI * TJ], fmx[TI * TJ], fpy[TI * TJ], fmy[TI * TJ];
+	__shared__ signed char ox[TI * TJ], oy[TI * TJ];   // the cells' orientations
+	const double dt = ss->dt;
+	const int i0 = blockIdx.y * TI, j0 = blockIdx.x * TJ;
+	const int ti = min(TI, g.nx - i0), tj = min(TJ, g.ny - j0);
+	const int tid = threadIdx.x, T = blockDim.x;
+	for (int q = tid; q < ti * tj; q += T) {
+		const int li = q / tj, lj = q - li * tj;
+		const int a = g.at(i0 + li, j0 + lj);
+		ox[li * TJ + lj] = (signed char)tvd_orient((uf[a] + uf[a - g.P]) * 0.5);
+		oy[li * TJ + lj] = (signed char)tvd_orient((vf[a] + vf[a - 1]) * 0.5);
+	}
+	const int nxf = (ti + 1) * tj, nyf = ti * (tj + 1);
+	for (int comp = 0; comp < 2; ++comp) {
+		const double* f = comp == 0 ? u : v;
+		__syncthreads();   // the previous component's readers are done
+		for (int q = tid; q < (ti + 4) * (tj + 4); q += T) {
+			const int li = q / (tj + 4), lj = q - li * (tj + 4);
+			tile[li * SJ + lj] = f[g.at(i0 + li - 2, j0 + lj - 2)];
+		}
+		__syncthreads();
+		for (int q = tid; q < nxf + nyf; q += T) {
+			if (q < nxf) {
+				// x face between local rows r and r + 1, frame cell r
+				const int r = q / tj - 1, lj = q - (r + 1) * tj;
+				const bool L = r >= 0, R = r + 1 < ti;
+				const int oL = L ? ox[r * TJ + lj] : 0, oR = R ? ox[(r + 1) * TJ + lj] : 0;
+				const int fa = (r + 2) * SJ + (lj + 2), i = i0 + r, j = j0 + lj;
+				if (L && R && oL == oR && oL != 0) {
+					const double val = tvd_plus<SCH, 0, P2>(g, tile, fa, SJ, i, j, oL);
+					fpx[r * TJ + lj] = val;
+					fmx[(r + 1) * TJ + lj] = val;
+				} else {
+					if (L) fpx[r * TJ + lj] = tvd_plus<SCH, 0, P2>(g, tile, fa, SJ, i, j, oL);
+					if (R) fmx[(r + 1) * TJ + lj] = oR != 0
+							? tvd_plus<SCH, 0, P2>(g, tile, fa, SJ, i, j, oR)
+							: tvd_value<SCH, 0, P2>(g, tile, fa + SJ, SJ, i + 1, j, 0, 0, 0);
+				}
+			} else {
+				// y face between local columns c and c + 1, frame cell c
+				const int qq = q - nxf;
+				const int li = qq / (tj + 1), c = qq - li * (tj + 1) - 1;
+				const bool L = c >= 0, R = c + 1 < tj;
+				const int oL = L ? oy[li * TJ + c] : 0, oR = R ? oy[li * TJ + c + 1] : 0;
+				const int fa = (li + 2) * SJ + (c + 2), i = i0 + li, j = j0 + c;
+				if (L && R && oL == oR && oL != 0) {
+					const double val = tvd_plus<SCH, 1, P2>(g, tile, fa, 1, i, j, oL);
+					fpy[li * TJ + c] = val;
+					fmy[li * TJ + c + 1] = val;
+				} else {
+					if (L) fpy[li * TJ + c] = tvd_plus<SCH, 1, P2>(g, tile, fa, 1, i, j, oL);
+					if (R) fmy[li * TJ + c + 1] = oR != 0
+							? tvd_plus<SCH, 1, P2>(g, tile, fa, 1, i, j, oR)
+							: tvd_value<SCH, 1, P2>(g, tile, fa + 1, 1, i, j + 1, 0, 0, 0);
+				}
+			}
+		}
+		__syncthreads();
+		double* out = comp == 0 ? us : vs;
+		for (int q = tid; q < ti * tj; q += T) {
+			const int li = q / tj, lj = q - li * tj;
+			const int i = i0 + li, j = j0 + lj, a = g.at(i, j), e = li * TJ + lj;
+			const double a0 = tvd_combine<0, P2>(g, uf, i, j, fpx[e], fmx[e]);
+			const double a1 = tvd_combine<1, P2>(g, vf, i, j, fpy[e], fmy[e]);
+			double adv = 0.0;
+			adv += a0;
+			adv += a1;
+			const double dif = muf ? diffusion_var(g, muf, f, i, j) : diffusion<P2>(g, mu, f, i, j);
+			const double src = 0;
+			out[a] = (-adv + (dif + src) / rho) * dt + f[a];
+		}
+	}
+}
+
 // Operation_::InterpolateC2F(VecC, VecF) (s_operation.hpp:166-187)
 __global__ void __launch_bounds__(kThreads) k_c2f(Geo g, const double* u,
 		const double* v, double* fx, double* fy) {
@@ -1130,6 +1238,17 @@ cudaError_t launch_pred(const Geo& geo, int blocks, cudaStream_t s,
 		const double* u, const double* v, const double* uf, const double* vf,
 		double* us, double* vs, const StepScalars* ss, double rho, double mu,
 		const double* muf) {
+	if (kTvdScheme<SCH> && geo.gl >= 2) {
+		// the face-sharing tiles (k_predictor_tiles, whose stencils reach
+		// two cells into the ghost ring); `blocks` sizes the one-cell-per-
+		// thread kernel of the other cases
+		const dim3 grid((geo.ny + kPredTJ - 1) / kPredTJ, (geo.nx + kPredTI - 1) / kPredTI);
+		if (geo.p2)
+			k_predictor_tiles<SCH, true><<<grid, kPredThreads, 0, s>>>(geo, u, v, uf, vf, us, vs, ss, rho, mu, muf);
+		else
+			k_predictor_tiles<SCH, false><<<grid, kPredThreads, 0, s>>>(geo, u, v, uf, vf, us, vs, ss, rho, mu, muf);
+		return cudaGetLastError();
+	}
 	if (geo.p2)
 		k_predictor<SCH, true><<<blocks, kThreads, 0, s>>>(geo, u, v, uf, vf, us, vs, ss, rho, mu, muf);
 	else
@@ -1613,10 +1732,11 @@ int carpio_gpu_operator(carpio_gpu_grid* g, int which, int scheme,
 		const double* b, const double* c, double* out1, double* out2,
 		double* scalar) {
 	using namespace cg_host;
-	if (!g || which < 0 || which > 8) return CARPIO_GPU_EINVAL;
+	if (!g || which < 0 || which > 9) return CARPIO_GPU_EINVAL;
 	if (which == 8 && (!a || !c)) return CARPIO_GPU_EINVAL;
-	if (which == 4 && (scheme < 0 || scheme > 9 || g->gl < (scheme >= 2 ? 2 : 1)))
+	if ((which == 4 || which == 9) && (scheme < 0 || scheme > 9 || g->gl < (scheme >= 2 ? 2 : 1)))
 		return CARPIO_GPU_EINVAL;
+	if (which == 9 && (!a || !b || !c || !out1)) return CARPIO_GPU_EINVAL;
 	if (which == 6 && (!bc || !valid_bc(*bc) || !out1)) return CARPIO_GPU_EINVAL;
 	std::lock_guard<std::mutex> lock(g->mu);
 	cudaStream_t s = g->stream;
@@ -1654,12 +1774,23 @@ int carpio_gpu_operator(carpio_gpu_grid* g, int which, int scheme,
 		std::memcpy(&mxm, &bits, sizeof mxm);
 		if (scalar) *scalar = mxm;
 		return 0;
+	} else if (which == 9) {
+		// the projection step's predictor on one field, dt = rho = 1: the
+		// kernel of the step itself (both components of it given the field)
+		StepScalars hs{};
+		hs.dt = 1.0;
+		DevBuf sb;
+		if ((rc = sb.ensure(sizeof(StepScalars)))) return rc;
+		CG_CK(cudaMemcpyAsync(sb.p, &hs, sizeof hs, cudaMemcpyHostToDevice, s));
+		CG_CK(launch_predictor(scheme, geo, nb, s, d[2], d[2], d[0], d[1], d[3], d[4],
+				sb.as<StepScalars>(), 1.0, coef, nullptr));
+		CG_CK(cudaStreamSynchronize(s));
 	} else {
 		k_op<<<nb, kThreads, 0, s>>>(geo, which, scheme, coef, d[0], d[1], d[2], d[3], d[4]);
 	}
 	CG_CK(cudaGetLastError());
 	if (out1 && (rc = copy_field(g, out1, d[3], false, s))) return rc;
-	if (out2 && which != 1 && which != 4 && which != 5 && which != 6 && which != 8
+	if (out2 && which != 1 && which != 4 && which != 5 && which != 6 && which != 8 && which != 9
 			&& (rc = copy_field(g, out2, d[4], false, s)))
 		return rc;
 	CG_CK(cudaStreamSynchronize(s));
