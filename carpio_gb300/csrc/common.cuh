@@ -190,6 +190,34 @@ __device__ __forceinline__ void block_sum_light(R (&v)[NV], int buf) {
 	}
 }
 
+// The same sum for thread 0 alone (the other threads' v is left
+// unspecified): the warp values added in the same fixed order by one thread
+// instead of by every thread of the block -- FP64 adds cost a warp
+// instruction each on the FP64 pipe, whose throughput bounds the kernels
+// that reduce in FP64.
+template<class R, int NV>
+__device__ __forceinline__ void block_sum_to0(R (&v)[NV], int buf) {
+	__shared__ R s_w0[2][NV][32];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const int nwarps = blockDim.x >> 5;
+#pragma unroll
+	for (int m = 0; m < NV; ++m) {
+		R x = v[m];
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+		if (lane == 0) s_w0[buf][m][warp] = x;
+	}
+	__syncthreads();
+	if (threadIdx.x == 0) {
+#pragma unroll
+		for (int m = 0; m < NV; ++m) {
+			R x = 0;
+			for (int w = 0; w < nwarps; ++w) x += s_w0[buf][m][w];
+			v[m] = x;
+		}
+	}
+}
+
 __device__ __forceinline__ unsigned atom_add_release_gpu(unsigned* p, unsigned v) {
 	unsigned old;
 	asm volatile("atom.add.release.gpu.u32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
@@ -230,7 +258,7 @@ __device__ __forceinline__ bool grid_allreduce(R (&v)[NV], const GridCtl& c,
 		bank ^= 1;
 		return ok1;
 	}
-	block_sum_light<R, NV>(v, 0);
+	block_sum_to0<R, NV>(v, 0);
 	double* part = c.partials + (size_t)bank * kMaxReduce * gridDim.x;
 	const int lane = threadIdx.x & 31;
 	if (threadIdx.x < 32) {
