@@ -20,6 +20,8 @@
 
 namespace cg_dev {
 
+constexpr int kDctBatch = 4;   // loads per thread in flight in the fill passes
+
 struct DctArgs {
 	int on;              // 1: the spectral preconditioner
 	int lx, ly;          // log2 nx, log2 ny
@@ -31,6 +33,7 @@ struct DctArgs {
 	const float2* ex;    // e^{-i pi k / (2 nx)}, k < nx
 	const float2* ey;
 	float* G;            // [nx][ny] spectral workspace (global memory, L2)
+	int fb;              // float2 elements of the shared FFT buffer
 };
 
 __device__ __forceinline__ float2 cmulf(float2 a, float2 b) {
@@ -84,16 +87,29 @@ __device__ __forceinline__ void dct_index(int t, int B, int logN, int& seq, int&
 // Forward transform of B real sequences: in(seq, n) -> out(seq, k, X[k]).
 // `flip`: the DST through the DCT of (-1)^n x.
 template<bool SM, class IN, class OUT>
-__device__ __forceinline__ void dct_forward(float2* buf, int B, int logN, const float2* tw,
+__device__ __noinline__ void dct_forward(float2* buf, int B, int logN, const float2* tw,
 		const float2* E, bool flip, IN in, OUT out) {
-	const int N = 1 << logN;
-	for (int t = threadIdx.x; t < B * N; t += blockDim.x) {
-		int seq, m;
-		dct_index<SM>(t, B, logN, seq, m);
-		const int n = dct_src(m, N);
-		float val = in(seq, n);
-		if (flip && (n & 1)) val = -val;
-		buf[seq * N + bitrev(m, logN)] = make_float2(val, 0.f);
+	const int N = 1 << logN, tot = B * N, T = blockDim.x;
+	// kDctBatch inputs per thread in flight before their stores
+	for (int t0 = 0; t0 < tot; t0 += kDctBatch * T) {
+		float val[kDctBatch];
+		int pos[kDctBatch];
+#pragma unroll
+		for (int e = 0; e < kDctBatch; ++e) {
+			const int t = t0 + e * T + threadIdx.x;
+			pos[e] = -1;
+			if (t < tot) {
+				int seq, m;
+				dct_index<SM>(t, B, logN, seq, m);
+				const int n = dct_src(m, N);
+				float x = in(seq, n);
+				val[e] = (flip && (n & 1)) ? -x : x;
+				pos[e] = seq * N + bitrev(m, logN);
+			}
+		}
+#pragma unroll
+		for (int e = 0; e < kDctBatch; ++e)
+			if (pos[e] >= 0) buf[pos[e]] = make_float2(val[e], 0.f);
 	}
 	__syncthreads();
 	fft_stages(buf, B, logN, tw);
@@ -109,17 +125,30 @@ __device__ __forceinline__ void dct_forward(float2* buf, int B, int logN, const 
 
 // Inverse of dct_forward: in(seq, k) = X[k] -> out(seq, n, x[n]).
 template<bool SM, class IN, class OUT>
-__device__ __forceinline__ void dct_inverse(float2* buf, int B, int logN, const float2* tw,
+__device__ __noinline__ void dct_inverse(float2* buf, int B, int logN, const float2* tw,
 		const float2* E, bool flip, IN in, OUT out) {
-	const int N = 1 << logN;
-	for (int t = threadIdx.x; t < B * N; t += blockDim.x) {
-		int seq, k;
-		dct_index<SM>(t, B, logN, seq, k);
-		const float xk = in(seq, k);
-		const float xr = k > 0 ? in(seq, N - k) : 0.f;
-		// conj(V[k]) = e^{-i pi k / 2N} (X[k] + i X[N-k]); the FFT of conj(V)
-		// is N conj(v), v real
-		buf[seq * N + bitrev(k, logN)] = cmulf(__ldg(E + k), make_float2(xk, xr));
+	const int N = 1 << logN, tot = B * N, T = blockDim.x;
+	for (int t0 = 0; t0 < tot; t0 += kDctBatch * T) {
+		float2 val[kDctBatch];
+		int pos[kDctBatch];
+#pragma unroll
+		for (int e = 0; e < kDctBatch; ++e) {
+			const int t = t0 + e * T + threadIdx.x;
+			pos[e] = -1;
+			if (t < tot) {
+				int seq, k;
+				dct_index<SM>(t, B, logN, seq, k);
+				val[e].x = in(seq, k);
+				val[e].y = k > 0 ? in(seq, N - k) : 0.f;
+				// conj(V[k]) = e^{-i pi k / 2N} (X[k] + i X[N-k]); the FFT
+				// of conj(V) is N conj(v), v real
+				val[e] = cmulf(__ldg(E + k), val[e]);
+				pos[e] = seq * N + bitrev(k, logN);
+			}
+		}
+#pragma unroll
+		for (int e = 0; e < kDctBatch; ++e)
+			if (pos[e] >= 0) buf[pos[e]] = val[e];
 	}
 	__syncthreads();
 	fft_stages(buf, B, logN, tw);

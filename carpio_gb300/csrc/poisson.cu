@@ -123,7 +123,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 		const Vecs<double>& v, const MixedArgs& m, const TileArgs& ta,
 		const SolveCtl& sc, bool mean, double normb, const GridCtl& gc,
 		int& bank, TileOut& to) {
-	extern __shared__ float smem[];
+	extern __shared__ __align__(16) float smem[];
 	__shared__ double s_sc[4];
 	const int C = gridDim.x, c = blockIdx.x, T = blockDim.x, tid = threadIdx.x;
 	const int nx = sp.nx, ny = sp.ny, gl = sp.gl, P = sp.P;
@@ -148,9 +148,11 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	const DctArgs& dc = ta.dct;
 	const bool use_dct = dc.on != 0;
 	float* zs = (K > 0 || use_mg || use_dct) ? dd + ta.rows_max * ny : rs;
-	// spectral: the FFT buffer after zs, rounded up to 8 bytes
-	float2* dbuf = reinterpret_cast<float2*>(
-			(reinterpret_cast<uintptr_t>(zs + ta.rows_max * ny) + 7) & ~(uintptr_t)7);
+	// spectral: the FFT buffer after zs at an even float offset (8 bytes),
+	// then the column phase's spectrum (B columns x nx, real)
+	const int zs_end = (int)(zs - smem) + ta.rows_max * ny;
+	float2* dbuf = reinterpret_cast<float2*>(smem + ((zs_end + 1) & ~1));
+	float* dspec = reinterpret_cast<float*>(dbuf + ta.dct.fb);
 	float* dsa = zs + ta.rows_max * ny;    // dsa[1 + (lr + 1) * ny + j]
 	float* dsb = dsa + np;
 	// multigrid (K == 0 then): the corrected fine values of the band and its
@@ -397,14 +399,16 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				[&](int sq, int k, float val) { __stcg(G + (size_t)(r0 + sq) * ny + k, val); });
 		if (!grid_sync(gc)) return false;
 		const int l0 = band_lo(c, C, ny), B = band_lo(c + 1, C, ny) - l0;
+		const int nxc = 1 << dc.lx;
+		// the scaled spectrum stays in shared memory between the two passes
 		dct_forward<true>(dbuf, B, dc.lx, dc.twx, dc.ex, dc.fx != 0,
 				[&](int sq, int n) { return ldcg(G + (size_t)n * ny + l0 + sq); },
 				[&](int sq, int k, float val) {
 					const float lam = __ldg(dc.lamx + k) + __ldg(dc.lamy + l0 + sq);
-					__stcg(G + (size_t)k * ny + l0 + sq, lam > 0.f ? val / lam : 0.f);
+					dspec[sq * nxc + k] = lam > 0.f ? val / lam : 0.f;
 				});
 		dct_inverse<true>(dbuf, B, dc.lx, dc.twx, dc.ex, dc.fx != 0,
-				[&](int sq, int k) { return ldcg(G + (size_t)k * ny + l0 + sq); },
+				[&](int sq, int k) { return dspec[sq * nxc + k]; },
 				[&](int sq, int n, float val) { __stcg(G + (size_t)n * ny + l0 + sq, val); });
 		if (!grid_sync(gc)) return false;
 		dct_inverse<false>(dbuf, rows, dc.ly, dc.twy, dc.ey, dc.fy != 0,
@@ -1235,7 +1239,8 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 			const size_t zsn = (size_t)rows_max * g->ny;
 			const size_t cmax = ((size_t)g->ny + C - 1) / C;
 			const size_t fb = std::max(zsn, cmax * (size_t)g->nx);
-			const size_t ssmem = base + sizeof(float) * (zsn + 1) + sizeof(float2) * fb;
+			const size_t ssmem = base + sizeof(float) * (zsn + 1) + sizeof(float2) * fb
+					+ sizeof(float) * cmax * (size_t)g->nx;
 			if (ssmem <= 220 * 1024) {
 				if ((rc = w.dct.ensure(sizeof(float) * (size_t)g->nx * g->ny))) return rc;
 				DctArgs& d = ta.dct;
@@ -1254,6 +1259,7 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 				d.ex = cp + nx / 2 + ny / 2;
 				d.ey = cp + nx / 2 + ny / 2 + nx;
 				d.G = w.dct.as<float>();
+				d.fb = (int)fb;
 				smem = ssmem;
 				pdeg = 0;
 				spec = true;
