@@ -44,6 +44,15 @@ __device__ __forceinline__ int bitrev(int m, int logN) {
 	return (int)(__brev((unsigned)m) >> (32 - logN));
 }
 
+// Physical slot of element e of a sequence in the shared FFT buffer: the
+// low five bits XORed with the next five, so that the bit-reversed scatter
+// of the fill passes (consecutive m, addresses N/32 apart) lands on
+// distinct banks. A permutation of every aligned block of 32 elements
+// (and the identity below 32), applied to every access of the buffer.
+__device__ __forceinline__ int dswz(int e) {
+	return e ^ ((e >> 5) & 31);
+}
+
 // element m of the reordered sequence comes from x[src]
 __device__ __forceinline__ int dct_src(int m, int N) {
 	return m < (N >> 1) ? 2 * m : 2 * (N - 1 - m) + 1;
@@ -60,7 +69,8 @@ __device__ __forceinline__ void fft_stages(float2* buf, int B, int logN, const f
 			const int seq = b >> (logN - 1);
 			const int w = b & (halfN - 1);
 			const int pos = w & (h - 1);
-			const int i1 = seq * N + ((w - pos) << 1) + pos, i2 = i1 + h;
+			const int e1 = ((w - pos) << 1) + pos, e2 = e1 + h;
+			const int i1 = seq * N + dswz(e1), i2 = seq * N + dswz(e2);
 			const float2 t = cmulf(__ldg(tw + (pos << (logN - s))), buf[i2]);
 			const float2 a = buf[i1];
 			buf[i1] = make_float2(a.x + t.x, a.y + t.y);
@@ -104,7 +114,7 @@ __device__ __noinline__ void dct_forward(float2* buf, int B, int logN, const flo
 				const int n = dct_src(m, N);
 				float x = in(seq, n);
 				val[e] = (flip && (n & 1)) ? -x : x;
-				pos[e] = seq * N + bitrev(m, logN);
+				pos[e] = seq * N + dswz(bitrev(m, logN));
 			}
 		}
 #pragma unroll
@@ -116,7 +126,7 @@ __device__ __noinline__ void dct_forward(float2* buf, int B, int logN, const flo
 	for (int t = threadIdx.x; t < B * N; t += blockDim.x) {
 		int seq, k;
 		dct_index<SM>(t, B, logN, seq, k);
-		const float2 V = buf[seq * N + k];
+		const float2 V = buf[seq * N + dswz(k)];
 		const float2 e = __ldg(E + k);
 		out(seq, k, e.x * V.x - e.y * V.y);
 	}
@@ -143,7 +153,7 @@ __device__ __noinline__ void dct_inverse(float2* buf, int B, int logN, const flo
 				// conj(V[k]) = e^{-i pi k / 2N} (X[k] + i X[N-k]); the FFT
 				// of conj(V) is N conj(v), v real
 				val[e] = cmulf(__ldg(E + k), val[e]);
-				pos[e] = seq * N + bitrev(k, logN);
+				pos[e] = seq * N + dswz(bitrev(k, logN));
 			}
 		}
 #pragma unroll
@@ -157,7 +167,7 @@ __device__ __noinline__ void dct_inverse(float2* buf, int B, int logN, const flo
 		int seq, m;
 		dct_index<SM>(t, B, logN, seq, m);
 		const int n = dct_src(m, N);
-		float val = buf[seq * N + m].x * invN;
+		float val = buf[seq * N + dswz(m)].x * invN;
 		if (flip && (n & 1)) val = -val;
 		out(seq, n, val);
 	}

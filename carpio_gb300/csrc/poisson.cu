@@ -603,6 +603,23 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 					rr = fmaf(rv, rv, rr);
 				}
 			}
+		if (use_dct) {
+			// M is A^-1 to FP32 rounding: this step is the whole correction,
+			// so the FP64 residual replaces r at once (it carries the next z),
+			// instead of a preconditioner application whose z the drop test
+			// would discard
+			++it;
+			fold_x();
+			if (!grid_sync(gc)) return;
+			float gnew;
+			if (!true_residual(false, gnew)) return;
+			++to.updates;
+			if (to.resid <= sc.tol) { to.done = 1; break; }
+			gamma_ref = gnew;
+			gamma_old = gamma;
+			gamma = gnew;
+			continue;
+		}
 		float gn[2] = { rr, rr };
 		if (!apply_m(gn)) return;
 		float* ebuf = ta.xbuf + (size_t)par * edge;
