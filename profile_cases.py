@@ -3,9 +3,11 @@
     python profile_cases.py unet N
         two forwards of the trained U-Net on one N x N field (the tcgen05
         3x3 convolutions and the network's elementwise kernels)
-    python profile_cases.py batch COUNT N
+    python profile_cases.py batch COUNT N [cluster]
         one batched persistent solve of COUNT all-Neumann N x N problems with
-        Gaussian sources to 1e-8 (thread-block clusters of 16 CTAs)
+        Gaussian sources to 1e-8 (the default kernel, one CTA per problem
+        with the multigrid preconditioner; `cluster`: thread-block clusters
+        of 16 CTAs)
 
     python profile_cases.py advect N STEPS
         STEPS steps of the stand-alone Advection_ on N x N (rotating cone,
@@ -37,13 +39,14 @@ def unet(n):
     print(f"unet {n}x{n}: mean |z| {float(z.abs().mean()):.4e}")
 
 
-def batch(count, n):
+def batch(count, n, cluster=False):
     from carpio_gb300 import workloads
     from carpio_gb300.batch import BatchedPoisson, Problem, NEUMANN
     rng = np.random.default_rng(1)
     probs = [Problem(n, n, bc=[(NEUMANN, 0.0)] * 4) for _ in range(count)]
     srcs = [workloads.gaussian_source(n, n, rng) for _ in probs]
-    bp = BatchedPoisson(probs, tol=1e-8, tiles=dict(threads=512, cluster=16))
+    bp = BatchedPoisson(probs, tol=1e-8,
+                        tiles=dict(threads=512, cluster=16) if cluster else None)
     bp.upload(0, srcs)
     bp.zero(1)
     bp.run()
@@ -73,8 +76,8 @@ def main(argv=None):
     a = list(sys.argv[1:] if argv is None else argv)
     if a[:1] == ["unet"] and len(a) == 2:
         unet(int(a[1]))
-    elif a[:1] == ["batch"] and len(a) == 3:
-        batch(int(a[1]), int(a[2]))
+    elif a[:1] == ["batch"] and len(a) in (3, 4):
+        batch(int(a[1]), int(a[2]), len(a) > 3 and a[3] == "cluster")
     elif a[:1] == ["advect"] and len(a) == 3:
         advect(int(a[1]), int(a[2]))
     elif a[:1] == ["ic"] and len(a) == 3:
