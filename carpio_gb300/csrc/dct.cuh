@@ -7,6 +7,7 @@
 // A^-1 up to FP32 rounding (lambda = 0, the all-Neumann mean, maps to 0).
 //
 // A length-N DCT-II is one N-point complex FFT of the reordered sequence
+// (two real sequences share one complex FFT)
 // v[n] = x[2n], v[N-1-n] = x[2n+1] followed by X[k] = Re(e^{-i pi k / 2N} V[k])
 // (Makhoul 1980); its inverse runs the same steps backwards, and the DST-II
 // is the DCT-II of (-1)^n x read in reverse order (the order reversal lives
@@ -95,49 +96,14 @@ __device__ __forceinline__ void dct_index(int t, int B, int logN, int& seq, int&
 }
 
 // Forward transform of B real sequences: in(seq, n) -> out(seq, k, X[k]).
-// `flip`: the DST through the DCT of (-1)^n x.
+// `flip`: the DST through the DCT of (-1)^n x. Two real sequences share one
+// complex FFT (z = v0 + i v1): V0[k] = (Z[k] + conj Z[N-k]) / 2 and
+// V1[k] = (Z[k] - conj Z[N-k]) / 2i, so B sequences take ceil(B / 2) FFTs.
 template<bool SM, class IN, class OUT>
-__device__ __noinline__ void dct_forward(float2* buf, int B, int logN, const float2* tw,
+__device__ __forceinline__ void dct_forward(float2* buf, int B, int logN, const float2* tw,
 		const float2* E, bool flip, IN in, OUT out) {
-	const int N = 1 << logN, tot = B * N, T = blockDim.x;
-	// kDctBatch inputs per thread in flight before their stores
-	for (int t0 = 0; t0 < tot; t0 += kDctBatch * T) {
-		float val[kDctBatch];
-		int pos[kDctBatch];
-#pragma unroll
-		for (int e = 0; e < kDctBatch; ++e) {
-			const int t = t0 + e * T + threadIdx.x;
-			pos[e] = -1;
-			if (t < tot) {
-				int seq, m;
-				dct_index<SM>(t, B, logN, seq, m);
-				const int n = dct_src(m, N);
-				float x = in(seq, n);
-				val[e] = (flip && (n & 1)) ? -x : x;
-				pos[e] = seq * N + dswz(bitrev(m, logN));
-			}
-		}
-#pragma unroll
-		for (int e = 0; e < kDctBatch; ++e)
-			if (pos[e] >= 0) buf[pos[e]] = make_float2(val[e], 0.f);
-	}
-	__syncthreads();
-	fft_stages(buf, B, logN, tw);
-	for (int t = threadIdx.x; t < B * N; t += blockDim.x) {
-		int seq, k;
-		dct_index<SM>(t, B, logN, seq, k);
-		const float2 V = buf[seq * N + dswz(k)];
-		const float2 e = __ldg(E + k);
-		out(seq, k, e.x * V.x - e.y * V.y);
-	}
-	__syncthreads();
-}
-
-// Inverse of dct_forward: in(seq, k) = X[k] -> out(seq, n, x[n]).
-template<bool SM, class IN, class OUT>
-__device__ __noinline__ void dct_inverse(float2* buf, int B, int logN, const float2* tw,
-		const float2* E, bool flip, IN in, OUT out) {
-	const int N = 1 << logN, tot = B * N, T = blockDim.x;
+	const int N = 1 << logN, P = (B + 1) >> 1, tot = P * N, T = blockDim.x;
+	// kDctBatch elements per thread in flight before their stores
 	for (int t0 = 0; t0 < tot; t0 += kDctBatch * T) {
 		float2 val[kDctBatch];
 		int pos[kDctBatch];
@@ -146,14 +112,14 @@ __device__ __noinline__ void dct_inverse(float2* buf, int B, int logN, const flo
 			const int t = t0 + e * T + threadIdx.x;
 			pos[e] = -1;
 			if (t < tot) {
-				int seq, k;
-				dct_index<SM>(t, B, logN, seq, k);
-				val[e].x = in(seq, k);
-				val[e].y = k > 0 ? in(seq, N - k) : 0.f;
-				// conj(V[k]) = e^{-i pi k / 2N} (X[k] + i X[N-k]); the FFT
-				// of conj(V) is N conj(v), v real
-				val[e] = cmulf(__ldg(E + k), val[e]);
-				pos[e] = seq * N + dswz(bitrev(k, logN));
+				int p, m;
+				dct_index<SM>(t, P, logN, p, m);
+				const int n = dct_src(m, N);
+				float x0 = in(2 * p, n);
+				float x1 = 2 * p + 1 < B ? in(2 * p + 1, n) : 0.f;
+				if (flip && (n & 1)) { x0 = -x0; x1 = -x1; }
+				val[e] = make_float2(x0, x1);
+				pos[e] = p * N + dswz(bitrev(m, logN));
 			}
 		}
 #pragma unroll
@@ -161,15 +127,67 @@ __device__ __noinline__ void dct_inverse(float2* buf, int B, int logN, const flo
 			if (pos[e] >= 0) buf[pos[e]] = val[e];
 	}
 	__syncthreads();
-	fft_stages(buf, B, logN, tw);
+	fft_stages(buf, P, logN, tw);
+	for (int t = threadIdx.x; t < tot; t += T) {
+		int p, k;
+		dct_index<SM>(t, P, logN, p, k);
+		const float2 zk = buf[p * N + dswz(k)];
+		const float2 zn = buf[p * N + dswz((N - k) & (N - 1))];
+		const float2 e = __ldg(E + k);
+		const float2 v0 = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
+		out(2 * p, k, e.x * v0.x - e.y * v0.y);
+		if (2 * p + 1 < B) {
+			const float2 v1 = make_float2(0.5f * (zk.y + zn.y), 0.5f * (zn.x - zk.x));
+			out(2 * p + 1, k, e.x * v1.x - e.y * v1.y);
+		}
+	}
+	__syncthreads();
+}
+
+// Inverse of dct_forward: in(seq, k) = X[k] -> out(seq, n, x[n]). With
+// Y[k] = e^{-i pi k / 2N} (X[k] + i X[N-k]) = conj(V[k]), the FFT of
+// Y0 + i Y1 is N (v0 + i v1) (v0, v1 real): two sequences per FFT, no
+// separation step.
+template<bool SM, class IN, class OUT>
+__device__ __forceinline__ void dct_inverse(float2* buf, int B, int logN, const float2* tw,
+		const float2* E, bool flip, IN in, OUT out) {
+	const int N = 1 << logN, P = (B + 1) >> 1, tot = P * N, T = blockDim.x;
+	for (int t0 = 0; t0 < tot; t0 += kDctBatch * T) {
+		float2 val[kDctBatch];
+		int pos[kDctBatch];
+#pragma unroll
+		for (int e = 0; e < kDctBatch; ++e) {
+			const int t = t0 + e * T + threadIdx.x;
+			pos[e] = -1;
+			if (t < tot) {
+				int p, k;
+				dct_index<SM>(t, P, logN, p, k);
+				const bool two = 2 * p + 1 < B;
+				const float2 ek = __ldg(E + k);
+				const float2 y0 = cmulf(ek, make_float2(in(2 * p, k), k > 0 ? in(2 * p, N - k) : 0.f));
+				const float2 y1 = two ? cmulf(ek, make_float2(in(2 * p + 1, k),
+				                                          k > 0 ? in(2 * p + 1, N - k) : 0.f))
+				                      : make_float2(0.f, 0.f);
+				val[e] = make_float2(y0.x - y1.y, y0.y + y1.x);
+				pos[e] = p * N + dswz(bitrev(k, logN));
+			}
+		}
+#pragma unroll
+		for (int e = 0; e < kDctBatch; ++e)
+			if (pos[e] >= 0) buf[pos[e]] = val[e];
+	}
+	__syncthreads();
+	fft_stages(buf, P, logN, tw);
 	const float invN = 1.f / (float)N;
-	for (int t = threadIdx.x; t < B * N; t += blockDim.x) {
-		int seq, m;
-		dct_index<SM>(t, B, logN, seq, m);
+	for (int t = threadIdx.x; t < tot; t += T) {
+		int p, m;
+		dct_index<SM>(t, P, logN, p, m);
 		const int n = dct_src(m, N);
-		float val = buf[seq * N + dswz(m)].x * invN;
-		if (flip && (n & 1)) val = -val;
-		out(seq, n, val);
+		const float2 w = buf[p * N + dswz(m)];
+		float v0 = w.x * invN, v1 = w.y * invN;
+		if (flip && (n & 1)) { v0 = -v0; v1 = -v1; }
+		out(2 * p, n, v0);
+		if (2 * p + 1 < B) out(2 * p + 1, n, v1);
 	}
 	__syncthreads();
 }

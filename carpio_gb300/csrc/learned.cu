@@ -326,6 +326,7 @@ int learned_solve(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& pws, LearnedW
 	ra.fold = c.fold.as<double>();
 	ra.src_a = src_a;
 	ra.src_b = src_b;
+	rhs_set_p2(ra, g->sx, g->sy);
 	ra.phi = phi;
 	ra.mean = mean ? 1 : 0;
 	if (src_mode == SRC_DIV) k_rhs<SRC_DIV><<<nb, kLT, 0, s>>>(sp, ra, b, x, part);

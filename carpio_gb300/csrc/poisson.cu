@@ -1104,6 +1104,7 @@ static int ic_structured(carpio_gpu_grid* g, StencilCoeffs& c, int src_mode,
 	ra.fold = c.fold.as<double>();
 	ra.src_a = src_a;
 	ra.src_b = src_b;
+	rhs_set_p2(ra, g->sx, g->sy);
 	ra.phi = phi;
 	ra.mean = 0;
 	ra.helm = c.helm ? 1 : 0;
@@ -1215,6 +1216,7 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 	ra.fold = c.fold.as<double>();
 	ra.src_a = src_a;
 	ra.src_b = src_b;
+	rhs_set_p2(ra, g->sx, g->sy);
 	ra.phi = phi;
 	ra.mean = cfg.mean_removal ? 1 : 0;
 	ra.helm = c.helm ? 1 : 0;

@@ -4,6 +4,9 @@
 
 #include "internal.hpp"
 
+#include <cmath>
+#include <vector>
+
 namespace cg_dev {
 
 struct RhsArgs {
@@ -18,7 +21,30 @@ struct RhsArgs {
 	// the source scales by the cell volume sx sy; StencilPoisson_::src
 	// (:75-83) multiplies sx by itself (it indexes the size by `dim`)
 	int helm = 0;
+	// every cell size a power of two, the same along each axis: the divisions
+	// of Div by them are multiplications by their exact reciprocals (the
+	// same bits)
+	int p2 = 0;
+	double ihx = 0.0, ihy = 0.0;
 };
+
+// RhsArgs::p2 and its reciprocals from the host copies of the cell sizes
+inline void rhs_set_p2(RhsArgs& ra, const std::vector<double>& sx,
+		const std::vector<double>& sy) {
+	auto uniform_pow2 = [](const std::vector<double>& s, double& inv) {
+		if (s.empty()) return false;
+		int ex = 0;
+		if (!(s[0] > 0.0) || std::frexp(s[0], &ex) != 0.5) return false;
+		for (double v : s)
+			if (v != s[0]) return false;
+		inv = 1.0 / s[0];
+		return true;
+	};
+	double ix = 0.0, iy = 0.0;
+	ra.p2 = uniform_pow2(sx, ix) && uniform_pow2(sy, iy) ? 1 : 0;
+	ra.ihx = ra.p2 ? ix : 0.0;
+	ra.ihy = ra.p2 ? iy : 0.0;
+}
 
 // Row constant of StencilPoisson_::coe_row + ghost folds, then b = -constant
 // (trimmed to +0 when the constant is exactly zero, s_solver.hpp:110-127).
@@ -34,8 +60,13 @@ __device__ __forceinline__ double rhs_at(const GridSpace& sp, const RhsArgs& ra,
 	} else {
 		// Operation_::Div(VecF) (s_operation.hpp:100-120)
 		double d = 0.0;
-		d = __dadd_rn(d, __ddiv_rn(__dsub_rn(ra.src_a[a], ra.src_a[a - sp.P]), sxi));
-		d = __dadd_rn(d, __ddiv_rn(__dsub_rn(ra.src_b[a], ra.src_b[a - 1]), ra.sy[j + gl]));
+		if (ra.p2) {
+			d = __dadd_rn(d, __dmul_rn(__dsub_rn(ra.src_a[a], ra.src_a[a - sp.P]), ra.ihx));
+			d = __dadd_rn(d, __dmul_rn(__dsub_rn(ra.src_b[a], ra.src_b[a - 1]), ra.ihy));
+		} else {
+			d = __dadd_rn(d, __ddiv_rn(__dsub_rn(ra.src_a[a], ra.src_a[a - sp.P]), sxi));
+			d = __dadd_rn(d, __ddiv_rn(__dsub_rn(ra.src_b[a], ra.src_b[a - 1]), ra.sy[j + gl]));
+		}
 		f = d;
 	}
 	double val = __dmul_rn(__dmul_rn(1.0, sxi), ra.helm ? ra.sy[j + gl] : sxi);
