@@ -21,7 +21,7 @@
 
 namespace cg_dev {
 
-constexpr int kDctBatch = 4;   // loads per thread in flight in the fill passes
+constexpr int kDctBatch = 2;   // loads per thread in flight in the fill passes
 
 struct DctArgs {
 	int on;              // 1: the spectral preconditioner
@@ -59,11 +59,12 @@ __device__ __forceinline__ int dct_src(int m, int N) {
 	return m < (N >> 1) ? 2 * m : 2 * (N - 1 - m) + 1;
 }
 
-// B sequences of N = 2^logN complex values in buf (bit-reversed order) ->
-// their DFTs in natural order. Begins after the caller's barrier, ends with
-// one.
-__device__ __forceinline__ void fft_stages(float2* buf, int B, int logN, const float2* tw) {
-	const int N = 1 << logN, halfN = N >> 1, nb = B * halfN;
+// B sequences of N = 2^logN complex values in buf, NS apart (bit-reversed
+// order) -> their DFTs in natural order. Begins after the caller's barrier,
+// ends with one.
+__device__ __forceinline__ void fft_stages(float2* buf, int B, int logN, const float2* tw,
+		int NS) {
+	const int halfN = 1 << (logN - 1), nb = B * halfN;
 	for (int s = 1; s <= logN; ++s) {
 		const int h = 1 << (s - 1);
 		for (int b = threadIdx.x; b < nb; b += blockDim.x) {
@@ -71,7 +72,7 @@ __device__ __forceinline__ void fft_stages(float2* buf, int B, int logN, const f
 			const int w = b & (halfN - 1);
 			const int pos = w & (h - 1);
 			const int e1 = ((w - pos) << 1) + pos, e2 = e1 + h;
-			const int i1 = seq * N + dswz(e1), i2 = seq * N + dswz(e2);
+			const int i1 = seq * NS + dswz(e1), i2 = seq * NS + dswz(e2);
 			const float2 t = cmulf(__ldg(tw + (pos << (logN - s))), buf[i2]);
 			const float2 a = buf[i1];
 			buf[i1] = make_float2(a.x + t.x, a.y + t.y);
@@ -103,6 +104,9 @@ template<bool SM, class IN, class OUT>
 __device__ __forceinline__ void dct_forward(float2* buf, int B, int logN, const float2* tw,
 		const float2* E, bool flip, IN in, OUT out) {
 	const int N = 1 << logN, P = (B + 1) >> 1, tot = P * N, T = blockDim.x;
+	// sequences one element apart more than their length when neighbouring
+	// threads take neighbouring sequences (SM): distinct banks
+	const int NS = SM ? N + 1 : N;
 	// kDctBatch elements per thread in flight before their stores
 	for (int t0 = 0; t0 < tot; t0 += kDctBatch * T) {
 		float2 val[kDctBatch];
@@ -119,7 +123,7 @@ __device__ __forceinline__ void dct_forward(float2* buf, int B, int logN, const 
 				float x1 = 2 * p + 1 < B ? in(2 * p + 1, n) : 0.f;
 				if (flip && (n & 1)) { x0 = -x0; x1 = -x1; }
 				val[e] = make_float2(x0, x1);
-				pos[e] = p * N + dswz(bitrev(m, logN));
+				pos[e] = p * NS + dswz(bitrev(m, logN));
 			}
 		}
 #pragma unroll
@@ -127,12 +131,12 @@ __device__ __forceinline__ void dct_forward(float2* buf, int B, int logN, const 
 			if (pos[e] >= 0) buf[pos[e]] = val[e];
 	}
 	__syncthreads();
-	fft_stages(buf, P, logN, tw);
+	fft_stages(buf, P, logN, tw, NS);
 	for (int t = threadIdx.x; t < tot; t += T) {
 		int p, k;
 		dct_index<SM>(t, P, logN, p, k);
-		const float2 zk = buf[p * N + dswz(k)];
-		const float2 zn = buf[p * N + dswz((N - k) & (N - 1))];
+		const float2 zk = buf[p * NS + dswz(k)];
+		const float2 zn = buf[p * NS + dswz((N - k) & (N - 1))];
 		const float2 e = __ldg(E + k);
 		const float2 v0 = make_float2(0.5f * (zk.x + zn.x), 0.5f * (zk.y - zn.y));
 		out(2 * p, k, e.x * v0.x - e.y * v0.y);
@@ -152,6 +156,7 @@ template<bool SM, class IN, class OUT>
 __device__ __forceinline__ void dct_inverse(float2* buf, int B, int logN, const float2* tw,
 		const float2* E, bool flip, IN in, OUT out) {
 	const int N = 1 << logN, P = (B + 1) >> 1, tot = P * N, T = blockDim.x;
+	const int NS = SM ? N + 1 : N;
 	for (int t0 = 0; t0 < tot; t0 += kDctBatch * T) {
 		float2 val[kDctBatch];
 		int pos[kDctBatch];
@@ -169,7 +174,7 @@ __device__ __forceinline__ void dct_inverse(float2* buf, int B, int logN, const 
 				                                          k > 0 ? in(2 * p + 1, N - k) : 0.f))
 				                      : make_float2(0.f, 0.f);
 				val[e] = make_float2(y0.x - y1.y, y0.y + y1.x);
-				pos[e] = p * N + dswz(bitrev(k, logN));
+				pos[e] = p * NS + dswz(bitrev(k, logN));
 			}
 		}
 #pragma unroll
@@ -177,13 +182,13 @@ __device__ __forceinline__ void dct_inverse(float2* buf, int B, int logN, const 
 			if (pos[e] >= 0) buf[pos[e]] = val[e];
 	}
 	__syncthreads();
-	fft_stages(buf, P, logN, tw);
+	fft_stages(buf, P, logN, tw, NS);
 	const float invN = 1.f / (float)N;
 	for (int t = threadIdx.x; t < tot; t += T) {
 		int p, m;
 		dct_index<SM>(t, P, logN, p, m);
 		const int n = dct_src(m, N);
-		const float2 w = buf[p * N + dswz(m)];
+		const float2 w = buf[p * NS + dswz(m)];
 		float v0 = w.x * invN, v1 = w.y * invN;
 		if (flip && (n & 1)) { v0 = -v0; v1 = -v1; }
 		out(2 * p, n, v0);

@@ -405,10 +405,10 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				[&](int sq, int n) { return ldcg(G + (size_t)n * ny + l0 + sq); },
 				[&](int sq, int k, float val) {
 					const float lam = __ldg(dc.lamx + k) + __ldg(dc.lamy + l0 + sq);
-					dspec[sq * nxc + k] = lam > 0.f ? val / lam : 0.f;
+					dspec[sq * (nxc + 1) + k] = lam > 0.f ? val / lam : 0.f;
 				});
 		dct_inverse<true>(dbuf, B, dc.lx, dc.twx, dc.ex, dc.fx != 0,
-				[&](int sq, int k) { return dspec[sq * nxc + k]; },
+				[&](int sq, int k) { return dspec[sq * (nxc + 1) + k]; },
 				[&](int sq, int n, float val) { __stcg(G + (size_t)n * ny + l0 + sq, val); });
 		if (!grid_sync(gc)) return false;
 		dct_inverse<false>(dbuf, rows, dc.ly, dc.twy, dc.ey, dc.fy != 0,
@@ -1257,9 +1257,12 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 				&& c.dct_ok) {
 			const size_t zsn = (size_t)rows_max * g->ny;
 			const size_t cmax = ((size_t)g->ny + C - 1) / C;
-			const size_t fb = std::max(zsn, cmax * (size_t)g->nx);
+			// the FFT buffer: ceil(B / 2) sequences per pass (two real ones
+			// share one), the column passes' sequences one element apart
+			const size_t fb = std::max((zsn / g->ny + 1) / 2 * (size_t)g->ny,
+					(cmax + 1) / 2 * ((size_t)g->nx + 1));
 			const size_t ssmem = base + sizeof(float) * (zsn + 1) + sizeof(float2) * fb
-					+ sizeof(float) * cmax * (size_t)g->nx;
+					+ sizeof(float) * cmax * ((size_t)g->nx + 1);
 			if (ssmem <= 220 * 1024) {
 				if ((rc = w.dct.ensure(sizeof(float) * (size_t)g->nx * g->ny))) return rc;
 				DctArgs& d = ta.dct;
