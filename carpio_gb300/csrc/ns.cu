@@ -50,6 +50,57 @@ struct BcDev {
 __host__ __device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
 __host__ __device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
 
+// GB300 issues one FP64 instruction per warp every 64 cycles, so the
+// helpers below replace FP64 operations by integer ones where the result is
+// the same bits.
+
+// 0.0 + x: x, with -0 turned into +0 (the reference's `s = 0; s += x`)
+__device__ __forceinline__ double plus_zero(double x) {
+	const long long b = __double_as_longlong(x);
+	return b == (long long)0x8000000000000000ull ? 0.0 : x;
+}
+
+// biased exponent field of x (0 zero or subnormal, 2047 inf or NaN)
+__device__ __forceinline__ int exp_field(double x) {
+	return (int)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ff;
+}
+
+// x / d rounded to nearest, for a divisor fixed per launch, with y =
+// RN(1 / d): q = RN(x y) is within one ulp of x / d, r = x - d q is exact
+// by the FMA, and RN(q + r y) = RN(x / d) (Markstein, IBM J. Res. Dev.
+// 34(1), 1990: correction of a faithful quotient with the correctly
+// rounded reciprocal). Valid without under- or overflow: `on` is set on
+// the host for |d| within 2^+-100, and x here within 2^+-800; zeros,
+// subnormals, infinities and NaNs divide.
+struct FixedDiv {
+	double d, y;
+	int on;
+};
+
+inline FixedDiv make_fixed_div(double d) {
+	FixedDiv f;
+	f.d = d;
+	f.y = 1.0 / d;
+	int ex = 0;
+	const double m = std::frexp(std::fabs(d), &ex);
+	f.on = std::isfinite(d) && m != 0.0 && ex >= -100 && ex <= 100 ? 1 : 0;
+	return f;
+}
+
+__device__ __noinline__ double div_slow(double x, double d) {
+	return __ddiv_rn(x, d);
+}
+
+__device__ __forceinline__ double fixed_div(double x, const FixedDiv& f) {
+	const int e = exp_field(x);
+	if (f.on && e >= 1023 - 800 && e <= 1023 + 800) {
+		const double q = __dmul_rn(x, f.y);
+		const double r = __fma_rn(-f.d, q, x);
+		return __fma_rn(r, f.y, q);
+	}
+	return div_slow(x, f.d);
+}
+
 // ------------------------------------------------------------ ghost fill --
 // Value Equation_::apply_bc (s_equation.hpp:340-378) gives ghost (i, j) when
 // its source cell (oi, oj) holds `src`.
@@ -238,6 +289,25 @@ __device__ __forceinline__ double limiter(int sch, double r, double R) {
 	return 0.0;
 }
 
+// The stencil ratio of a TVD face on a P2 grid, ((a 2h) / b) / (2h) with the
+// reciprocal of 2h: both scalings are exact while a 2h and the quotients
+// stay normal, and then the value is RN(a / b). The exponent fields are
+// checked with a margin of 100 (|log2 2h| <= 91 on a P2 grid); a zero a
+// gives the same signed zero (or NaN) either way, an infinite quotient the
+// same infinity; anything else takes the reference's three operations.
+__device__ __noinline__ double tvd_ratio_slow(double a, double b, double h2, double ih2) {
+	return __dmul_rn(__ddiv_rn(__dmul_rn(a, h2), b), ih2);
+}
+
+__device__ __forceinline__ double tvd_ratio(double a, double b, double h2, double ih2) {
+	const double r = __ddiv_rn(a, b);
+	const int ea = exp_field(a), er = exp_field(r);
+	const bool a0 = (__double_as_longlong(a) << 1) == 0;
+	if (a0 || (ea >= 100 && ea <= 1947 && ((er >= 100 && er <= 1947) || er == 2047)))
+		return r;
+	return tvd_ratio_slow(a, b, h2, ih2);
+}
+
 // The TVD schemes (upwind2, van Leer, superbee, WAHYD, QUICK, CUI) build
 // each face value from an upwind-biased stencil of three cells; the others
 // (upwind1, center, center4) are single expressions.
@@ -266,7 +336,7 @@ __device__ __forceinline__ double tvd_value(const Geo& g, const double* f, int f
 		const double ih = D == 0 ? g.ihx : g.ihy;
 		const double h2 = h + h, ih2 = 0.5 * ih;
 		const double R = 2.0;
-		const double r = (F(C_) - F(U_)) * h2 / (F(D_) - F(C_) + kSmall) * ih2;
+		const double r = tvd_ratio(F(C_) - F(U_), F(D_) - F(C_) + kSmall, h2, ih2);
 		return F(C_) + limiter(SCH, r, R) * 0.5 * (F(D_) - F(C_));
 	}
 	const double R = (S(D_) + S(C_)) / S(C_);
@@ -284,12 +354,15 @@ __device__ __forceinline__ int tvd_orient(double veo) {
 
 // the +1/2 face of a cell in its own frame: the same value as the -1/2
 // face of the next cell with the same orientation (the same three cells)
+// The stencil offsets are chosen first and the face evaluated once: with
+// one tvd_value per orientation the compiler may predicate them, and a
+// predicated-off FP64 instruction still takes its issue slot.
 template<int SCH, int D, bool P2>
 __device__ __forceinline__ double tvd_plus(const Geo& g, const double* f, int fa,
 		int fst, int i, int j, int o) {
-	return o > 0 ? tvd_value<SCH, D, P2>(g, f, fa, fst, i, j, 1, 0, -1)
-	     : o < 0 ? tvd_value<SCH, D, P2>(g, f, fa, fst, i, j, 0, 1, 2)
-	             : tvd_value<SCH, D, P2>(g, f, fa, fst, i, j, 0, 0, 0);
+	// o > 0: (1, 0, -1); o < 0: (0, 1, 2); o == 0: (0, 0, 0)
+	const int d_ = o > 0 ? 1 : 0, c_ = o < 0 ? 1 : 0, u_ = o > 0 ? -1 : (o < 0 ? 2 : 0);
+	return tvd_value<SCH, D, P2>(g, f, fa, fst, i, j, d_, c_, u_);
 }
 
 template<int SCH, int D, bool P2>
@@ -299,9 +372,31 @@ __device__ __forceinline__ double tvd_half(const Geo& g, const double* face,
 	const int a = g.at(i, j);
 	const double veo = (face[a] + face[a - st]) * 0.5;
 	const int o = tvd_orient(veo);
-	if (plus || o == 0) return tvd_plus<SCH, D, P2>(g, f, fa, fst, i, j, o);
-	return o > 0 ? tvd_value<SCH, D, P2>(g, f, fa, fst, i, j, 0, -1, -2)
-	             : tvd_value<SCH, D, P2>(g, f, fa, fst, i, j, -1, 0, 1);
+	if (plus) return tvd_plus<SCH, D, P2>(g, f, fa, fst, i, j, o);
+	// the -1/2 face: o > 0: (0, -1, -2); o < 0: (-1, 0, 1); o == 0: (0, 0, 0)
+	const int d_ = o < 0 ? -1 : 0, c_ = o > 0 ? -1 : 0, u_ = o > 0 ? -2 : (o < 0 ? 1 : 0);
+	return tvd_value<SCH, D, P2>(g, f, fa, fst, i, j, d_, c_, u_);
+}
+
+// The stencil offsets (D, C, U) from frame cell c of the face between c and
+// c + 1 for the orientation o of the cell that owns it: the same cells
+// whether that is c (own, the +1/2 face) or c + 1 (the -1/2 face), except
+// for o == 0 (NaN velocity), whose stencil is the owning cell alone.
+__device__ __forceinline__ void face_offsets(int o, bool own, int& d_, int& c_, int& u_) {
+	if (o > 0) { d_ = 1; c_ = 0; u_ = -1; }
+	else if (o < 0) { d_ = 0; c_ = 1; u_ = 2; }
+	else { d_ = c_ = u_ = own ? 0 : 1; }
+}
+
+// the -1/2 face of cell c + 1 where it differs from the +1/2 face of c (the
+// orientations differ): out of line, so that the common path carries one
+// face evaluation
+template<int SCH, int D, bool P2>
+__device__ __noinline__ double tvd_face_next(const Geo& g, const double* f, int fa,
+		int fst, int i, int j, int o) {
+	int d_, c_, u_;
+	face_offsets(o, false, d_, c_, u_);
+	return tvd_value<SCH, D, P2>(g, f, fa, fst, i, j, d_, c_, u_);
 }
 
 // the TVD axis term from its two face values: (u+ fp - u- fm) / S(0)
@@ -362,28 +457,29 @@ __device__ __forceinline__ double adv_cell(const Geo& g, const double* uf,
 	return s;
 }
 
-// NablaMuNabla(Vt mu, ...) (s_operation.hpp:664-688)
-template<bool P2 = false>
+// NablaMuNabla(Vt mu, ...) (s_operation.hpp:664-688). MU1: mu is 1.0, and
+// mu * x is x (the same bits)
+template<bool P2 = false, bool MU1 = false>
 __device__ __forceinline__ double diffusion(const Geo& g, double mu,
 		const double* f, int i, int j) {
 	const int a = g.at(i, j);
 	double t0, t1;
 	if (P2) {
 		// centre distances and sizes are hx, hy: multiply by 1 / h
+#define MUX(x) (MU1 ? (x) : mu * (x))
 		{
-			double dm = mu * (f[a] - f[a - g.P]) * g.ihx;
-			double dp = mu * (f[a + g.P] - f[a]) * g.ihx;
+			double dm = MUX(f[a] - f[a - g.P]) * g.ihx;
+			double dp = MUX(f[a + g.P] - f[a]) * g.ihx;
 			t0 = (dp - dm) * g.ihx;
 		}
 		{
-			double dm = mu * (f[a] - f[a - 1]) * g.ihy;
-			double dp = mu * (f[a + 1] - f[a]) * g.ihy;
+			double dm = MUX(f[a] - f[a - 1]) * g.ihy;
+			double dp = MUX(f[a + 1] - f[a]) * g.ihy;
 			t1 = (dp - dm) * g.ihy;
 		}
-		double res = 0.0;
-		res += t0;
-		res += t1;
-		return res;
+#undef MUX
+		// res = 0; res += t0; res += t1
+		return plus_zero(t0 + t1);
 	}
 	{
 		double dm = mu * (f[a] - f[a - g.P]) / (g.CX(i) - g.CX(i - 1));
@@ -877,10 +973,11 @@ __global__ void __launch_bounds__(kThreads) k_predictor(Geo g, const double* u,
 // adv_cell does. The per-cell arithmetic is k_predictor's.
 constexpr int kPredTI = 8, kPredTJ = 64, kPredThreads = 512;
 
-template<int SCH, bool P2>
+// DIFF: 0 the mu field muf, 1 the uniform mu, 2 the uniform mu 1.0.
+template<int SCH, bool P2, int DIFF>
 __global__ void __launch_bounds__(kPredThreads) k_predictor_tiles(Geo g, const double* u,
 		const double* v, const double* uf, const double* vf, double* us,
-		double* vs, const StepScalars* ss, double rho, double mu, const double* muf) {
+		double* vs, const StepScalars* ss, FixedDiv rho, double mu, const double* muf) {
 	constexpr int TI = kPredTI, TJ = kPredTJ, SJ = TJ + 4;
 	__shared__ double tile[(TI + 4) * SJ];   // the component, two halo cells
 	__shared__ double fpx[TI * TJ], fmx[TI * TJ], fpy[TI * TJ], fmy[TI * TJ];
@@ -911,16 +1008,14 @@ __global__ void __launch_bounds__(kPredThreads) k_predictor_tiles(Geo g, const d
 				const bool L = r >= 0, R = r + 1 < ti;
 				const int oL = L ? ox[r * TJ + lj] : 0, oR = R ? ox[(r + 1) * TJ + lj] : 0;
 				const int fa = (r + 2) * SJ + (lj + 2), i = i0 + r, j = j0 + lj;
-				if (L && R && oL == oR && oL != 0) {
-					const double val = tvd_plus<SCH, 0, P2>(g, tile, fa, SJ, i, j, oL);
-					fpx[r * TJ + lj] = val;
-					fmx[(r + 1) * TJ + lj] = val;
-				} else {
-					if (L) fpx[r * TJ + lj] = tvd_plus<SCH, 0, P2>(g, tile, fa, SJ, i, j, oL);
-					if (R) fmx[(r + 1) * TJ + lj] = oR != 0
-							? tvd_plus<SCH, 0, P2>(g, tile, fa, SJ, i, j, oR)
-							: tvd_value<SCH, 0, P2>(g, tile, fa + SJ, SJ, i + 1, j, 0, 0, 0);
-				}
+				const bool shared = L && R && oL == oR && oL != 0;
+				int d_, c_, u_;
+				face_offsets(L ? oL : oR, L, d_, c_, u_);
+				const double val = tvd_value<SCH, 0, P2>(g, tile, fa, SJ, i, j, d_, c_, u_);
+				if (L) fpx[r * TJ + lj] = val;
+				if (R && (shared || !L)) fmx[(r + 1) * TJ + lj] = val;
+				if (L && R && !shared)
+					fmx[(r + 1) * TJ + lj] = tvd_face_next<SCH, 0, P2>(g, tile, fa, SJ, i, j, oR);
 			} else {
 				// y face between local columns c and c + 1, frame cell c
 				const int qq = q - nxf;
@@ -928,16 +1023,14 @@ __global__ void __launch_bounds__(kPredThreads) k_predictor_tiles(Geo g, const d
 				const bool L = c >= 0, R = c + 1 < tj;
 				const int oL = L ? oy[li * TJ + c] : 0, oR = R ? oy[li * TJ + c + 1] : 0;
 				const int fa = (li + 2) * SJ + (c + 2), i = i0 + li, j = j0 + c;
-				if (L && R && oL == oR && oL != 0) {
-					const double val = tvd_plus<SCH, 1, P2>(g, tile, fa, 1, i, j, oL);
-					fpy[li * TJ + c] = val;
-					fmy[li * TJ + c + 1] = val;
-				} else {
-					if (L) fpy[li * TJ + c] = tvd_plus<SCH, 1, P2>(g, tile, fa, 1, i, j, oL);
-					if (R) fmy[li * TJ + c + 1] = oR != 0
-							? tvd_plus<SCH, 1, P2>(g, tile, fa, 1, i, j, oR)
-							: tvd_value<SCH, 1, P2>(g, tile, fa + 1, 1, i, j + 1, 0, 0, 0);
-				}
+				const bool shared = L && R && oL == oR && oL != 0;
+				int d_, c_, u_;
+				face_offsets(L ? oL : oR, L, d_, c_, u_);
+				const double val = tvd_value<SCH, 1, P2>(g, tile, fa, 1, i, j, d_, c_, u_);
+				if (L) fpy[li * TJ + c] = val;
+				if (R && (shared || !L)) fmy[li * TJ + c + 1] = val;
+				if (L && R && !shared)
+					fmy[li * TJ + c + 1] = tvd_face_next<SCH, 1, P2>(g, tile, fa, 1, i, j, oR);
 			}
 		}
 		__syncthreads();
@@ -947,41 +1040,52 @@ __global__ void __launch_bounds__(kPredThreads) k_predictor_tiles(Geo g, const d
 			const int i = i0 + li, j = j0 + lj, a = g.at(i, j), e = li * TJ + lj;
 			const double a0 = tvd_combine<0, P2>(g, uf, i, j, fpx[e], fmx[e]);
 			const double a1 = tvd_combine<1, P2>(g, vf, i, j, fpy[e], fmy[e]);
-			double adv = 0.0;
-			adv += a0;
-			adv += a1;
-			const double dif = muf ? diffusion_var(g, muf, f, i, j) : diffusion<P2>(g, mu, f, i, j);
-			const double src = 0;
-			out[a] = (-adv + (dif + src) / rho) * dt + f[a];
+			// adv = 0; adv += a0; adv += a1
+			const double adv = plus_zero(a0 + a1);
+			const double dif = DIFF == 0 ? diffusion_var(g, muf, f, i, j)
+			                             : diffusion<P2, DIFF == 2>(g, mu, f, i, j);
+			// (dif + src) / rho with src = 0
+			out[a] = (-adv + fixed_div(plus_zero(dif), rho)) * dt + f[a];
 		}
 	}
 }
 
-// Operation_::InterpolateC2F(VecC, VecF) (s_operation.hpp:166-187)
+// Operation_::InterpolateC2F(VecC, VecF) (s_operation.hpp:166-187). The
+// low wall faces (i = 0: the x face at -1/2, j = 0: the y face) come after
+// the main loop, not inside it: a branch there gets predicated, and its
+// FP64 instructions then take issue slots in every cell.
+template<int PM = -1>
 __global__ void __launch_bounds__(kThreads) k_c2f(Geo g, const double* u,
 		const double* v, double* fx, double* fy) {
+	const bool p2 = PM == 1 || (PM < 0 && g.p2);
 	const long n = (long)g.nx * g.ny;
-	for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n;
-			k += (long)gridDim.x * blockDim.x) {
+	const long t0 = blockIdx.x * (long)blockDim.x + threadIdx.x;
+	const long stride = (long)gridDim.x * blockDim.x;
+	for (long k = t0; k < n; k += stride) {
 		int i = (int)(k / g.ny), j = (int)(k - (long)i * g.ny);
 		int a = g.at(i, j);
 		double vc = u[a];
 		double hs = g.SX(i) * 0.5, hsp = g.SX(i + 1) * 0.5;
 		// (hs + hs') is the cell size: with Geo::p2 a power of two
-		fx[a] = g.p2 ? (u[a + g.P] * hs + vc * hsp) * g.ihx : (u[a + g.P] * hs + vc * hsp) / (hs + hsp);
-		if (i == 0) {
-			double hsm = g.SX(i - 1) * 0.5;
-			fx[a - g.P] = g.p2 ? (u[a - g.P] * hs + vc * hsm) * g.ihx
-			                   : (u[a - g.P] * hs + vc * hsm) / (hs + hsm);
-		}
+		fx[a] = p2 ? (u[a + g.P] * hs + vc * hsp) * g.ihx : (u[a + g.P] * hs + vc * hsp) / (hs + hsp);
 		vc = v[a];
 		hs = g.SY(j) * 0.5;
 		hsp = g.SY(j + 1) * 0.5;
-		fy[a] = g.p2 ? (v[a + 1] * hs + vc * hsp) * g.ihy : (v[a + 1] * hs + vc * hsp) / (hs + hsp);
-		if (j == 0) {
-			double hsm = g.SY(j - 1) * 0.5;
-			fy[a - 1] = g.p2 ? (v[a - 1] * hs + vc * hsm) * g.ihy
-			                 : (v[a - 1] * hs + vc * hsm) / (hs + hsm);
+		fy[a] = p2 ? (v[a + 1] * hs + vc * hsp) * g.ihy : (v[a + 1] * hs + vc * hsp) / (hs + hsp);
+	}
+	for (long k = t0; k < (long)g.ny + g.nx; k += stride) {
+		if (k < g.ny) {
+			const int j = (int)k, a = g.at(0, j);
+			const double vc = u[a];
+			const double hs = g.SX(0) * 0.5, hsm = g.SX(-1) * 0.5;
+			fx[a - g.P] = p2 ? (u[a - g.P] * hs + vc * hsm) * g.ihx
+			                 : (u[a - g.P] * hs + vc * hsm) / (hs + hsm);
+		} else {
+			const int i = (int)(k - g.ny), a = g.at(i, 0);
+			const double vc = v[a];
+			const double hs = g.SY(0) * 0.5, hsm = g.SY(-1) * 0.5;
+			fy[a - 1] = p2 ? (v[a - 1] * hs + vc * hsm) * g.ihy
+			               : (v[a - 1] * hs + vc * hsm) / (hs + hsm);
 		}
 	}
 }
@@ -989,46 +1093,91 @@ __global__ void __launch_bounds__(kThreads) k_c2f(Geo g, const double* u,
 // face gradient of Operation_::Grad (s_operation.hpp:46-72) at x face (i, j)
 // (between i and i+1; i = -1 is the low wall face, computed from cell 0)
 // (with Geo::p2 the centre distance is +-h: multiply by +-1/h)
+// PM: 1 a P2 grid, 0 not, -1 read Geo::p2 (the compile-time forms keep the
+// other branch's divisions out of the FP64 pipe). gx_in / gy_in: the
+// interior faces (i >= 0, j >= 0).
+template<int PM = -1>
+__device__ __forceinline__ double gx_in(const Geo& g, const double* phi, int i, int j) {
+	if (PM == 1 || (PM < 0 && g.p2)) return (phi[g.at(i + 1, j)] - phi[g.at(i, j)]) * g.ihx;
+	return (phi[g.at(i + 1, j)] - phi[g.at(i, j)]) / (g.CX(i + 1) - g.CX(i));
+}
+template<int PM = -1>
+__device__ __forceinline__ double gy_in(const Geo& g, const double* phi, int i, int j) {
+	if (PM == 1 || (PM < 0 && g.p2)) return (phi[g.at(i, j + 1)] - phi[g.at(i, j)]) * g.ihy;
+	return (phi[g.at(i, j + 1)] - phi[g.at(i, j)]) / (g.CY(j + 1) - g.CY(j));
+}
+template<int PM = -1>
 __device__ __forceinline__ double gx_at(const Geo& g, const double* phi, int i, int j) {
-	if (g.p2) {
-		if (i >= 0) return (phi[g.at(i + 1, j)] - phi[g.at(i, j)]) * g.ihx;
-		return (phi[g.at(-1, j)] - phi[g.at(0, j)]) * -g.ihx;
-	}
-	if (i >= 0) return (phi[g.at(i + 1, j)] - phi[g.at(i, j)]) / (g.CX(i + 1) - g.CX(i));
+	if (i >= 0) return gx_in<PM>(g, phi, i, j);
+	if (PM == 1 || (PM < 0 && g.p2)) return (phi[g.at(-1, j)] - phi[g.at(0, j)]) * -g.ihx;
 	return (phi[g.at(-1, j)] - phi[g.at(0, j)]) / (g.CX(-1) - g.CX(0));
 }
+template<int PM = -1>
 __device__ __forceinline__ double gy_at(const Geo& g, const double* phi, int i, int j) {
-	if (g.p2) {
-		if (j >= 0) return (phi[g.at(i, j + 1)] - phi[g.at(i, j)]) * g.ihy;
-		return (phi[g.at(i, -1)] - phi[g.at(i, 0)]) * -g.ihy;
-	}
-	if (j >= 0) return (phi[g.at(i, j + 1)] - phi[g.at(i, j)]) / (g.CY(j + 1) - g.CY(j));
+	if (j >= 0) return gy_in<PM>(g, phi, i, j);
+	if (PM == 1 || (PM < 0 && g.p2)) return (phi[g.at(i, -1)] - phi[g.at(i, 0)]) * -g.ihy;
 	return (phi[g.at(i, -1)] - phi[g.at(i, 0)]) / (g.CY(-1) - g.CY(0));
 }
 
 // The end of run_one_step (s_ns_explicit.hpp:140-153) over every array
 // element: gradphi = Grad(phi); p = phi, p *= 1/dt on normal cells;
-// uf = us_f - gradphi; u = us - InterpolateF2C(gradphi).
+// uf = us_f - gradphi; u = us - InterpolateF2C(gradphi). The cells with
+// i >= 1 and j >= 1 (every face gradient they read an interior one) run
+// first without a branch; the rest of the array (ghost frame, row 0,
+// column 0) after them in the general form, so that no predicated branch
+// costs FP64 issue slots in the bulk.
+template<int PM = -1>
 __global__ void __launch_bounds__(kThreads) k_correct(Geo g, const double* phi,
 		const double* us, const double* vs, const double* usf,
 		const double* vsf, double* u, double* v, double* uf, double* vf,
 		double* p, const StepScalars* ss) {
 	const double inv = 1.0 / ss->dt;
-	const long n = (long)g.NI * g.NJ;
-	for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n;
-			k += (long)gridDim.x * blockDim.x) {
-		int I = (int)(k / g.NJ), J = (int)(k - (long)I * g.NJ);
+	const long t0 = blockIdx.x * (long)blockDim.x + threadIdx.x;
+	const long stride = (long)gridDim.x * blockDim.x;
+	const int mx = g.nx - 1, my = g.ny - 1;
+	const long nin = (long)mx * my;
+	for (long k = t0; k < nin; k += stride) {
+		const int i = 1 + (int)(k / my), j = 1 + (int)(k - (long)(i - 1) * my);
+		const int a = g.at(i, j);
+		const double gx = gx_in<PM>(g, phi, i, j), gy = gy_in<PM>(g, phi, i, j);
+		uf[a] = usf[a] - gx;
+		vf[a] = vsf[a] - gy;
+		const double gcx = (gx + gx_in<PM>(g, phi, i - 1, j)) * 0.5;
+		const double gcy = (gy + gy_in<PM>(g, phi, i, j - 1)) * 0.5;
+		u[a] = us[a] - gcx;
+		v[a] = vs[a] - gcy;
+		p[a] = phi[a] * inv;
+	}
+	// the rest: full rows I <= gl and I >= gl + nx, then in the rows between
+	// the columns J <= gl and J >= gl + ny
+	const int gl = g.gl, NJ = g.NJ;
+	const int top = gl + 1, bot = g.NI - gl - g.nx, left = gl + 1, right = NJ - gl - g.ny;
+	const long full = (long)(top + bot) * NJ;
+	const int W = left + right;
+	const long rest = full + (long)mx * W;
+	for (long k = t0; k < rest; k += stride) {
+		int I, J;
+		if (k < full) {
+			const int r = (int)(k / NJ);
+			J = (int)(k - (long)r * NJ);
+			I = r < top ? r : gl + g.nx + (r - top);
+		} else {
+			const long t = k - full;
+			const int m = (int)(t / W), c = (int)(t - (long)m * W);
+			I = gl + 1 + m;
+			J = c < left ? c : gl + g.ny + (c - left);
+		}
 		int i = I - g.gl, j = J - g.gl;
 		int a = I * g.P + J;
 		bool jin = j >= 0 && j < g.ny, iin = i >= 0 && i < g.nx;
-		double gx = (jin && i >= -1 && i < g.nx) ? gx_at(g, phi, i, j) : 0.0;
-		double gy = (iin && j >= -1 && j < g.ny) ? gy_at(g, phi, i, j) : 0.0;
+		double gx = (jin && i >= -1 && i < g.nx) ? gx_at<PM>(g, phi, i, j) : 0.0;
+		double gy = (iin && j >= -1 && j < g.ny) ? gy_at<PM>(g, phi, i, j) : 0.0;
 		uf[a] = usf[a] - gx;
 		vf[a] = vsf[a] - gy;
 		double gcx = 0.0, gcy = 0.0;
 		if (iin && jin) {
-			gcx = (gx + gx_at(g, phi, i - 1, j)) * 0.5;
-			gcy = (gy + gy_at(g, phi, i, j - 1)) * 0.5;
+			gcx = (gx + gx_at<PM>(g, phi, i - 1, j)) * 0.5;
+			gcy = (gy + gy_at<PM>(g, phi, i, j - 1)) * 0.5;
 		}
 		u[a] = us[a] - gcx;
 		v[a] = vs[a] - gcy;
@@ -1181,10 +1330,12 @@ Geo make_geo(const carpio_gpu_grid* g) {
 	e.sx = g->d_sx;
 	e.cy = g->d_cy;
 	e.sy = g->d_sy;
-	// the power-of-two case (Geo::p2), checked on the host copies of the axes
+	// the power-of-two case (Geo::p2), checked on the host copies of the axes;
+	// h within 2^+-90, so that scaling by 2h never leaves the exponent range
+	// that tvd_ratio's shortcut checks
 	auto pow2 = [](double h) {
 		int ex = 0;
-		return h > 0 && std::frexp(h, &ex) == 0.5;
+		return h > 0 && std::frexp(h, &ex) == 0.5 && ex >= -90 && ex <= 90;
 	};
 	auto axis_ok = [&](const std::vector<double>& c, const std::vector<double>& sz, double h) {
 		if (!pow2(h)) return false;
@@ -1243,10 +1394,19 @@ cudaError_t launch_pred(const Geo& geo, int blocks, cudaStream_t s,
 		// two cells into the ghost ring); `blocks` sizes the one-cell-per-
 		// thread kernel of the other cases
 		const dim3 grid((geo.ny + kPredTJ - 1) / kPredTJ, (geo.nx + kPredTI - 1) / kPredTI);
-		if (geo.p2)
-			k_predictor_tiles<SCH, true><<<grid, kPredThreads, 0, s>>>(geo, u, v, uf, vf, us, vs, ss, rho, mu, muf);
-		else
-			k_predictor_tiles<SCH, false><<<grid, kPredThreads, 0, s>>>(geo, u, v, uf, vf, us, vs, ss, rho, mu, muf);
+		const FixedDiv rd = make_fixed_div(rho);
+		const int diff = muf ? 0 : (mu == 1.0 ? 2 : 1);
+#define PT(P, D) k_predictor_tiles<SCH, P, D><<<grid, kPredThreads, 0, s>>>(geo, u, v, uf, vf, \
+		us, vs, ss, rd, mu, muf)
+		if (geo.p2) {
+			if (diff == 0) PT(true, 0);
+			else if (diff == 1) PT(true, 1);
+			else PT(true, 2);
+		} else {
+			if (diff == 0) PT(false, 0);
+			else PT(false, 1);
+		}
+#undef PT
 		return cudaGetLastError();
 	}
 	if (geo.p2)
@@ -1605,7 +1765,8 @@ int carpio_gpu_ns_run(carpio_gpu_ns* ns, int steps, double* step_dt,
 		CG_CK(launch_predictor(c.scheme, geo, nb, s, u, v, uf, vf, us, vs, ss, c.rho, c.mu,
 				ns->has_mu ? ns->muf.as<double>() : nullptr));
 		CG_CK(launch_bc(geo, us, c.bc_u, vs, &c.bc_v, s));
-		k_c2f<<<nb, kThreads, 0, s>>>(geo, us, vs, usf, vsf);
+		if (geo.p2) k_c2f<1><<<nb, kThreads, 0, s>>>(geo, us, vs, usf, vsf);
+		else k_c2f<0><<<nb, kThreads, 0, s>>>(geo, us, vs, usf, vsf);
 		CG_CK(cudaGetLastError());
 		CG_CK(cudaEventRecord(ns->ev[3 * st + 1], s));
 		if (ns->learned) {
@@ -1620,8 +1781,10 @@ int carpio_gpu_ns_run(carpio_gpu_ns* ns, int steps, double* step_dt,
 		}
 		CG_CK(cudaEventRecord(ns->ev[3 * st + 2], s));
 		CG_CK(launch_bc(geo, phi, bc_phi, nullptr, nullptr, s));
-		k_correct<<<nbf, kThreads, 0, s>>>(geo, phi, us, vs, usf, vsf, u, v, uf,
-				vf, p, ss);
+		if (geo.p2)
+			k_correct<1><<<nbf, kThreads, 0, s>>>(geo, phi, us, vs, usf, vsf, u, v, uf, vf, p, ss);
+		else
+			k_correct<0><<<nbf, kThreads, 0, s>>>(geo, phi, us, vs, usf, vsf, u, v, uf, vf, p, ss);
 		CG_CK(cudaGetLastError());
 		++ns->steps_done;
 	}
@@ -1775,15 +1938,17 @@ int carpio_gpu_operator(carpio_gpu_grid* g, int which, int scheme,
 		if (scalar) *scalar = mxm;
 		return 0;
 	} else if (which == 9) {
-		// the projection step's predictor on one field, dt = rho = 1: the
-		// kernel of the step itself (both components of it given the field)
+		// the projection step's predictor on one field, dt = 1, rho from
+		// *scalar (default 1): the kernel of the step itself (both
+		// components of it given the field)
+		const double rho = scalar && *scalar != 0.0 ? *scalar : 1.0;
 		StepScalars hs{};
 		hs.dt = 1.0;
 		DevBuf sb;
 		if ((rc = sb.ensure(sizeof(StepScalars)))) return rc;
 		CG_CK(cudaMemcpyAsync(sb.p, &hs, sizeof hs, cudaMemcpyHostToDevice, s));
 		CG_CK(launch_predictor(scheme, geo, nb, s, d[2], d[2], d[0], d[1], d[3], d[4],
-				sb.as<StepScalars>(), 1.0, coef, nullptr));
+				sb.as<StepScalars>(), rho, coef, nullptr));
 		CG_CK(cudaStreamSynchronize(s));
 	} else {
 		k_op<<<nb, kThreads, 0, s>>>(geo, which, scheme, coef, d[0], d[1], d[2], d[3], d[4]);

@@ -618,12 +618,13 @@ class NS_kim(NS_explicit):
 
 
 def operator(grid, which, a=None, b=None, c=None, scheme=0, coef=0.0,
-             bc=None, out1=None, out2=None):
-    """carpio_gpu_operator on host fields; returns (out1, out2, scalar)."""
+             bc=None, out1=None, out2=None, rho=None):
+    """carpio_gpu_operator on host fields; returns (out1, out2, scalar).
+    `rho`: the density of operator 9 (default 1)."""
     L = _lib.load()
     o1 = grid.zeros() if out1 is None else np.array(out1, dtype=np.float64)
     o2 = grid.zeros() if out2 is None else np.array(out2, dtype=np.float64)
-    s = ctypes.c_double(0.0)
+    s = ctypes.c_double(0.0 if rho is None else float(rho))
     sch = _lib.SCHEMES[scheme] if isinstance(scheme, str) else int(scheme)
     keep = [None if x is None else np.ascontiguousarray(x, dtype=np.float64)
             for x in (a, b, c)]

@@ -361,8 +361,9 @@ int carpio_gpu_ns_profile(carpio_gpu_ns* ns, int cap, int* n,
  *          8 NablaMuNabla(mu field) (:630-662) mu a, in c -> out1
  *          9 the projection step's predictor (_veo_star_center, s_ns_explicit.hpp:173-213,
  *            the kernel NS_explicit_ stepping runs) on one field with
- *            dt = rho = 1 and mu = coef: faces a, b, field c ->
- *            out1 = (-VdotNabla + NablaMuNabla(mu) / 1) * 1 + c
+ *            dt = 1, mu = coef and rho = *scalar (in; 1 when scalar is
+ *            NULL or *scalar is 0): faces a, b, field c ->
+ *            out1 = (-VdotNabla + NablaMuNabla(mu) / rho) * 1 + c
  * Outputs of 0, 1, 2, 4, 5, 8, 9 are zero outside the cells the reference writes. */
 int carpio_gpu_operator(carpio_gpu_grid* g, int which, int scheme,
 		double coef, const carpio_gpu_bc* bc, const double* a,

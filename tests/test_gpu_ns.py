@@ -93,6 +93,56 @@ def test_predictor_tiles_bitwise_large(gpu_lib, nx, ny, ly):
         assert bits_equal(got[inner], want[inner]), s
 
 
+def nan_aware_bits_equal(a, b):
+    """bit for bit, with NaN in the same cells (payloads aside)"""
+    a, b = np.asarray(a, dtype=np.float64), np.asarray(b, dtype=np.float64)
+    na, nb = np.isnan(a), np.isnan(b)
+    return np.array_equal(na, nb) and bits_equal(np.where(na, 0.0, a), np.where(nb, 0.0, b))
+
+
+def mixed_scale_field(rng, shape):
+    """uniform(-1, 1) with cells set to +0, -0, ~1e-300 and ~1e250: ratios
+    and quotients outside the exponent ranges of the predictor's integer
+    shortcuts, so that their fallbacks run too"""
+    f = rng.uniform(-1, 1, shape)
+    k = rng.integers(0, 10, shape)
+    f[k == 6] = 0.0
+    f[k == 7] = -0.0
+    f[k == 8] *= 1e-300
+    f[k == 9] *= 1e250
+    return f
+
+
+@pytest.mark.parametrize("nx,ny,ly", [(256, 128, 0.5), (150, 200, 1.3)])
+def test_predictor_shortcuts_bitwise(gpu_lib, nx, ny, ly):
+    """The predictor's integer shortcuts (the TVD ratio without its two
+    power-of-two scalings, 0 + x without an add, mu = 1 without its
+    multiplications, the division by rho through the correctly rounded
+    reciprocal) on fields mixing zeros, signed zeros, tiny and huge values:
+    VdotNabla and NablaMuNabla bit for bit against the oracle, and
+    operator 9 with mu in {0.37, 1} and rho in {1, 1000, 3, 0.7} bit for bit
+    against them composed on the host in the reference's order."""
+    from carpio_gb300 import structure as S
+    from oracle import restate as R
+    rng = np.random.default_rng(7 * nx + ny)
+    g = S.Grid((0.0, 0.0), (1.0, ly), (nx, ny), 2)
+    og = R.Grid(nx, ny, 2, 0.0, 1.0, 0.0, ly)
+    a = mixed_scale_field(rng, g.zeros().shape)
+    uf, vf = (rng.uniform(-1, 1, g.zeros().shape) for _ in range(2))
+    inner = (slice(2, 2 + nx), slice(2, 2 + ny))
+    for s in ("vanleer", "superbee", "upwind2", "quick"):
+        adv, _, _ = S.operator(g, 4, a=uf, b=vf, c=a, scheme=s)
+        want_adv = R.advection(og, s, uf, vf, a)
+        assert nan_aware_bits_equal(adv[inner], want_adv[inner]), s
+        for mu in (0.37, 1.0):
+            dif, _, _ = S.operator(g, 5, c=a, coef=mu)
+            assert nan_aware_bits_equal(dif[inner], R.diffusion(og, mu, a)[inner]), (s, mu)
+            for rho in (1.0, 1000.0, 3.0, 0.7):
+                got, _, _ = S.operator(g, 9, a=uf, b=vf, c=a, scheme=s, coef=mu, rho=rho)
+                want = (-want_adv + (dif + 0.0) / rho) * 1.0 + a
+                assert nan_aware_bits_equal(got[inner], want[inner]), (s, mu, rho)
+
+
 def fixture_proj(d):
     """the projection solver of a cavity fixture: (name, mean removal)"""
     for x in d.get("case_args", []):
