@@ -115,6 +115,7 @@ __device__ __forceinline__ int band_lo(int c, int C, int nx) {
 struct TileOut {
 	int iters, updates, done;
 	double resid;
+	double xmean;   // fused: the mean of the final x (for the epilogue)
 };
 
 // NC columns per thread, RM rows per band at most.
@@ -122,9 +123,10 @@ template<int NC, int RM>
 __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 		const Vecs<double>& v, const MixedArgs& m, const TileArgs& ta,
 		const SolveCtl& sc, bool mean, double normb, const GridCtl& gc,
-		int& bank, TileOut& to) {
+		int& bank, TileOut& to, bool fused = false, double bmean = 0.0) {
 	extern __shared__ __align__(16) float smem[];
 	__shared__ double s_sc[4];
+	__shared__ double s_xm;
 	const int C = gridDim.x, c = blockIdx.x, T = blockDim.x, tid = threadIdx.x;
 	const int nx = sp.nx, ny = sp.ny, gl = sp.gl, P = sp.P;
 	const int r0 = band_lo(c, C, nx), r1 = band_lo(c + 1, C, nx);
@@ -190,6 +192,9 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	// r (FP32) = (r64 - mean) * scale0 with scale0 fixed for the whole solve
 	double scale0 = 1.0, rn0 = 1.0;
 	float rrn = 0.f;   // (r, r) of the current FP32 residual
+	double nrmb = normb;   // ||b|| (fused: from the first residual's reduction)
+	float rr_band = 0.f;   // (r, r) of the band's newest FP32 residual
+	to.xmean = 0.0;
 
 	auto publish_r = [&]() {
 		float* pub = rbuf + (size_t)(2 * c) * ny;
@@ -388,8 +393,8 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	// z = M r with M = A^-1 through the separable transforms (dct.cuh):
 	// the band's rows along y, a grid barrier, this CTA's block of columns
 	// along x with the division by the eigenvalues and back, a grid barrier,
-	// the band's rows back along y. (r, z) and (r, r) of the band in g.
-	auto precond_dct = [&](float (&g)[2]) -> bool {
+	// the band's rows back along y, each z value handed to out(row, col, z).
+	auto dct_apply = [&](auto out) -> bool {
 		float* G = dc.G;
 		// the transform reads every cell of the band's r, which the callers
 		// wrote thread by thread
@@ -413,7 +418,13 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 		if (!grid_sync(gc)) return false;
 		dct_inverse<false>(dbuf, rows, dc.ly, dc.twy, dc.ey, dc.fy != 0,
 				[&](int sq, int k) { return ldcg(G + (size_t)(r0 + sq) * ny + k); },
-				[&](int sq, int n, float val) { zs[sq * ny + n] = val; });
+				out);
+		return true;
+	};
+	// the spectral preconditioner of the CG: z into zs, (r, z) and (r, r) of
+	// the band in g
+	auto precond_dct = [&](float (&g)[2]) -> bool {
+		if (!dct_apply([&](int sq, int n, float val) { zs[sq * ny + n] = val; })) return false;
 		g[0] = g[1] = 0.f;
 #pragma unroll
 		for (int lr = 0; lr < RM; ++lr)
@@ -446,12 +457,20 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 			if (down) rhal[ny + t] = ldcg(src + (size_t)(2 * (c + 1)) * ny + t);
 		}
 	};
-	// FP64 residual of the band (x64 complete on entry), into rs (FP32),
-	// edges exchanged; returns gamma = (r, r) of the new FP32 residual
-	auto true_residual = [&](bool first, float& gamma) -> bool {
-		double sums[3] = { 0, 0, 0 };
-		// the FP64 residual goes through v.r (each thread re-reads only
-		// its own cells) rather than registers
+	// FP64 residual of the band (x64 complete on entry) and its norms; unless
+	// it meets the tolerance, the scaled FP32 residual into rs. One FMA per
+	// cell for the squares (the reference's nrm2 leaves the last element
+	// out: its square is taken off once, by the thread that holds it), the
+	// residual kept in FP32 (the scaling then costs no FP64 operation).
+	// fused (the first call of the spectral path): b's mean bmean is taken
+	// off here and ||b|| summed, in place of two separate passes; with
+	// `mean` the sum of x rides along for the epilogue's mean removal.
+	auto resid64 = [&](bool first) -> bool {
+		const bool fb = fused && first;
+		const bool sx = fused && mean;
+		double sums[5] = { 0, 0, 0, 0, 0 };   // (r, r), sum r, (b, b), sum x, last r^2
+		double rla = 0.0, bla = 0.0;
+		float* r32 = reinterpret_cast<float*>(v.r);
 #pragma unroll
 		for (int lr = 0; lr < RM; ++lr)
 #pragma unroll
@@ -460,29 +479,48 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				if (lr < rows && j < ny) {
 					const int kk = (r0 + lr) * ny + j;
 					const int a = (r0 + lr + gl) * P + j + gl;
-					const double rv = v.b[a] - op.apply(v.x, kk, a);
-					v.r[a] = rv;
-					if (a != la || full) sums[0] = fma(rv, rv, sums[0]);
+					double bb = v.b[a];
+					if (fb) {
+						bb = bb - bmean;
+						v.b[a] = bb;
+						sums[2] = fma(bb, bb, sums[2]);
+					}
+					if (sx) sums[3] += ldcg(v.x + a);
+					const double rv = bb - op.apply(v.x, kk, a);
+					r32[a] = (float)rv;
+					sums[0] = fma(rv, rv, sums[0]);
 					sums[1] += rv;
-					sums[2] = fma(rv, rv, sums[2]);
+					if (a == la) { rla = rv; bla = bb; }
 				}
 			}
-		if (!grid_allreduce<double, 3>(sums, gc, bank)) return false;
+		if (!full) {
+			sums[4] = rla * rla;
+			if (fb) sums[2] -= bla * bla;
+		}
+		if (!grid_allreduce<double, 5>(sums, gc, bank)) return false;
 		if (tid == 0) {
+			if (fb) {
+				const double nb = sqrt(fmax(sums[2], 0.0));
+				s_sc[3] = nb == 0.0 ? 1.0 : nb;
+			}
+			const double nrm = fb ? s_sc[3] : nrmb;
 			double mr = mean ? sums[1] / ncell : 0.0;
-			s_sc[0] = sqrt(sums[0]) / normb;
+			s_sc[0] = sqrt(fmax(sums[0] - sums[4], 0.0)) / nrm;
 			s_sc[1] = mr;
-			s_sc[2] = sqrt(mean ? fmax(sums[2] - sums[1] * mr, 0.0) : sums[2]);
+			s_sc[2] = sqrt(mean ? fmax(sums[0] - sums[1] * mr, 0.0) : sums[0]);
+			s_xm = sums[3] / ncell;
 		}
 		__syncthreads();
+		if (fb) nrmb = s_sc[3];
 		to.resid = s_sc[0];
+		to.xmean = s_xm;
 		// converged: the caller stops, no FP32 residual or preconditioner
 		if (to.resid <= sc.tol) return true;
-		const double mr = s_sc[1];
 		if (first) {
 			rn0 = s_sc[2];
 			scale0 = rn0 > 0.0 ? 1.0 / rn0 : 1.0;
 		}
+		const float mr = (float)s_sc[1], sc32 = (float)scale0;
 		float rr = 0.f;
 #pragma unroll
 		for (int lr = 0; lr < RM; ++lr)
@@ -491,12 +529,21 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				const int j = tid + k * T;
 				if (lr < rows && j < ny) {
 					const int a = (r0 + lr + gl) * P + j + gl;
-					const float rv = (float)((v.r[a] - mr) * scale0);
+					const float rv = (r32[a] - mr) * sc32;
 					rs[lr * ny + j] = rv;
 					rr = fmaf(rv, rv, rr);
 				}
 			}
-		float g[2] = { rr, rr };
+		rr_band = rr;
+		return true;
+	};
+	// resid64, then (unless converged) z = M r with the edges exchanged;
+	// returns gamma = (r, z) and rrn = (r, r) of the new FP32 residual
+	auto true_residual = [&](bool first, float& gamma) -> bool {
+		if (!resid64(first)) return false;
+		if (to.resid <= sc.tol) return true;
+		// (r, z) and (r, r) of the band: z = r without a preconditioner
+		float g[2] = { rr_band, rr_band };
 		if (!apply_m(g)) return false;
 		__syncthreads();
 		publish_r();
@@ -524,6 +571,29 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	to.iters = 0;
 	to.updates = 0;
 	to.done = 0;
+	if (use_dct) {
+		// Iterative refinement with M = A^-1 to FP32 rounding: x += rn0 M r
+		// (r scaled by 1 / rn0), then the FP64 residual, until it meets the
+		// tolerance. The CG step of the other preconditioners would take
+		// alpha = 1 up to FP32 rounding here; it is left out, with its two
+		// reductions and its halo exchange.
+		if (!resid64(true)) return;
+		int it = 0;
+		while (!(to.resid <= sc.tol) && it < sc.max_iter) {
+			if (!dct_apply([&](int sq, int n, float val) {
+					const int a = (r0 + sq + gl) * P + n + gl;
+					v.x[a] = fma(rn0, (double)val, v.x[a]);
+				}))
+				return;
+			++it;
+			if (!grid_sync(gc)) return;
+			if (!resid64(false)) return;
+			++to.updates;
+		}
+		to.iters = it;
+		to.done = to.resid <= sc.tol ? 1 : 0;
+		return;
+	}
 	float gamma = 0.f;   // (r, z)
 	if (!true_residual(true, gamma)) return;
 	if (to.resid <= sc.tol) { to.done = 1; return; }
@@ -538,7 +608,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	constexpr int kStall = 1000;
 	int since = 0;
 	// iterated-residual level at which the FP64 residual is worth checking
-	const double tol_scaled = sc.tol * normb * scale0;
+	const double tol_scaled = sc.tol * nrmb * scale0;
 	const float near = (float)(0.25 * tol_scaled * tol_scaled);
 	int it = 0;
 	bool first = true;
@@ -603,23 +673,6 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 					rr = fmaf(rv, rv, rr);
 				}
 			}
-		if (use_dct) {
-			// M is A^-1 to FP32 rounding: this step is the whole correction,
-			// so the FP64 residual replaces r at once (it carries the next z),
-			// instead of a preconditioner application whose z the drop test
-			// would discard
-			++it;
-			fold_x();
-			if (!grid_sync(gc)) return;
-			float gnew;
-			if (!true_residual(false, gnew)) return;
-			++to.updates;
-			if (to.resid <= sc.tol) { to.done = 1; break; }
-			gamma_ref = gnew;
-			gamma_old = gamma;
-			gamma = gnew;
-			continue;
-		}
 		float gn[2] = { rr, rr };
 		if (!apply_m(gn)) return;
 		float* ebuf = ta.xbuf + (size_t)par * edge;
@@ -658,37 +711,15 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	}
 }
 
-// mixed solve with the Krylov state on chip (tile_solve)
-template<int NC, int RM>
-__device__ void mixed_tile_run(const GridSpace& sp, const StencilOp<double>& op,
-		const Vecs<double>& v, const MixedArgs& m, const TileArgs& ta,
-		const SolveCtl& sc, bool mean, const GridCtl& gc, int& bank) {
-	const bool full = (sc.flags & CARPIO_GPU_FLAG_FULL_NRM2) || sp.count() == 1;
-	const int la = sp.last_addr();
-	__shared__ double s_nb;
-	double acc[1] = { 0 };
-	KLOOP(sp) {
-		int a = sp.addr(k);
-		double bb = v.b[a];
-		if (a != la || full) acc[0] = fma(bb, bb, acc[0]);
-	}
-	if (!grid_allreduce<double, 1>(acc, gc, bank)) return;
-	if (threadIdx.x == 0) {
-		double nb = sqrt(acc[0]);
-		s_nb = nb == 0.0 ? 1.0 : nb;
-	}
-	__syncthreads();
-	const double normb = s_nb;
-	TileOut to;
-	tile_solve<NC, RM>(sp, op, v, m, ta, sc, mean, normb, gc, bank, to);
-	if (read_err(gc)) return;
-	if (blockIdx.x == 0 && threadIdx.x == 0) {
-		sc.out->outer = to.updates;
-		sc.out->inner = to.iters;
-	}
-	finish(sc, to.done ? 0 : 1, to.iters, to.resid, to.updates + 1);
-}
-
+// The mixed solve with the Krylov state on chip (tile_solve), one call site
+// per instantiation. Spectral path (fused): b of the CTA's band (the row
+// constant's folds only at the boundary cells, which take the general form
+// out of line) with x0, one reduction for b's mean (also the barrier that
+// completes x0); tile_solve then centres b, sums ||b|| and takes the first
+// residual in one pass, and returns x's mean from its last residual; the
+// epilogue writes the band's phi. Other preconditioners: b and x0 over
+// the grid, b centred, ||b|| (the reference's nrm2), and the mean of x
+// after the solve.
 template<int SRC, int NC, int RM>
 __global__ void __launch_bounds__(kTileThreads, 1) k_poisson_mixed_tile(
 		StencilOp<double> op, Vecs<double> v, RhsArgs ra, MixedArgs mx,
@@ -696,25 +727,76 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_poisson_mixed_tile(
 	gc.start();
 	int bank = 0;
 	const GridSpace& sp = op.sp;
-	double s[1] = { 0 };
-	KLOOP(sp) {
-		int i, j;
-		sp.ij(k, i, j);
-		int a = sp.addr(k);
-		double bb = rhs_at<SRC>(sp, ra, i, j, a);
-		v.b[a] = bb;
-		v.x[a] = ra.phi[a];
-		s[0] += bb;
-	}
-	if (ra.mean) {
+	const bool fused = ta.dct.on != 0;
+	const int C = gridDim.x, c = blockIdx.x, T = blockDim.x, tid = threadIdx.x;
+	const int nx = sp.nx, ny = sp.ny, gl = sp.gl, P = sp.P;
+	const int r0 = band_lo(c, C, nx), rows = band_lo(c + 1, C, nx) - r0;
+	__shared__ double s_nb;
+	double bm = 0.0, normb = 1.0;
+	if (fused) {
+		double s[1] = { 0 };
+		for (int t = tid; t < rows * ny; t += T) {
+			const int lr = t / ny, j = t - lr * ny, i = r0 + lr;
+			const int a = (i + gl) * P + j + gl;
+			const bool in = i > 0 && i < nx - 1 && j > 0 && j < ny - 1;
+			const double bb = in ? rhs_in<SRC>(sp, ra, i, j, a) : rhs_at_call<SRC>(sp, ra, i, j, a);
+			v.b[a] = bb;
+			v.x[a] = ra.phi[a];
+			s[0] += bb;
+		}
 		if (!grid_allreduce<double, 1>(s, gc, bank)) return;
-		double mm = s[0] / (double)sp.count();
-		KLOOP(sp) { int a = sp.addr(k); v.b[a] = v.b[a] - mm; }
+		bm = ra.mean ? s[0] / (double)sp.count() : 0.0;
+	} else {
+		double s[1] = { 0 };
+		KLOOP(sp) {
+			int i, j;
+			sp.ij(k, i, j);
+			int a = sp.addr(k);
+			double bb = rhs_at<SRC>(sp, ra, i, j, a);
+			v.b[a] = bb;
+			v.x[a] = ra.phi[a];
+			s[0] += bb;
+		}
+		if (ra.mean) {
+			if (!grid_allreduce<double, 1>(s, gc, bank)) return;
+			double mm = s[0] / (double)sp.count();
+			KLOOP(sp) { int a = sp.addr(k); v.b[a] = v.b[a] - mm; }
+		}
+		if (!grid_sync(gc)) return;
+		const bool full = (sc.flags & CARPIO_GPU_FLAG_FULL_NRM2) || sp.count() == 1;
+		const int la = sp.last_addr();
+		double acc[1] = { 0 };
+		KLOOP(sp) {
+			int a = sp.addr(k);
+			double bb = v.b[a];
+			if (a != la || full) acc[0] = fma(bb, bb, acc[0]);
+		}
+		if (!grid_allreduce<double, 1>(acc, gc, bank)) return;
+		if (threadIdx.x == 0) {
+			double nb = sqrt(acc[0]);
+			s_nb = nb == 0.0 ? 1.0 : nb;
+		}
+		__syncthreads();
+		normb = s_nb;
 	}
-	if (!grid_sync(gc)) return;
-	mixed_tile_run<NC, RM>(sp, op, v, mx, ta, sc, ra.mean != 0, gc, bank);
+	TileOut to;
+	tile_solve<NC, RM>(sp, op, v, mx, ta, sc, ra.mean != 0, normb, gc, bank, to, fused, bm);
 	if (read_err(gc)) {
 		if (blockIdx.x == 0 && threadIdx.x == 0) sc.out->code = read_err(gc);
+		return;
+	}
+	if (blockIdx.x == 0 && threadIdx.x == 0) {
+		sc.out->outer = to.updates;
+		sc.out->inner = to.iters;
+	}
+	finish(sc, to.done ? 0 : 1, to.iters, to.resid, to.updates + 1);
+	if (fused) {
+		const double xm = ra.mean ? to.xmean : 0.0;
+		for (int t = tid; t < rows * ny; t += T) {
+			const int lr = t / ny, j = t - lr * ny;
+			const int a = (r0 + lr + gl) * P + j + gl;
+			ra.phi[a] = ra.mean ? v.x[a] - xm : v.x[a];
+		}
 		return;
 	}
 	double mx0 = 0.0;
