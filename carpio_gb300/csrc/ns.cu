@@ -32,6 +32,7 @@ struct Geo {
 	// real number), and the P2 kernels below do that
 	int p2;
 	double hx, hy, ihx, ihy;
+	int kx, ky;   // p2: ihx = 2^kx, ihy = 2^ky
 	__device__ __forceinline__ int at(int i, int j) const { return (i + gl) * P + (j + gl); }
 	__device__ __forceinline__ double CX(int i) const { return cx[i + gl]; }
 	__device__ __forceinline__ double CY(int j) const { return cy[j + gl]; }
@@ -89,6 +90,42 @@ inline FixedDiv make_fixed_div(double d) {
 
 __device__ __noinline__ double div_slow(double x, double d) {
 	return __ddiv_rn(x, d);
+}
+
+// x * s for s = 2^k: the exponent field moved by k where x and the product
+// are normal, x itself where x is +-0 (the product's sign is x's);
+// subnormals, infinities, NaNs and products outside the normal range take
+// the FPU multiply, out of line. The same bits as x * s in every case.
+__device__ __noinline__ double mul_p2_slow(double x, double s) {
+	return __dmul_rn(x, s);
+}
+
+__device__ __forceinline__ double mul_p2(double x, int k, double s) {
+	const long long b = __double_as_longlong(x);
+	if ((b << 1) == 0) return x;
+	const int e = exp_field(x), en = e + k;
+	if (e >= 1 && e <= 2046 && en >= 1 && en <= 2046)
+		return __longlong_as_double(b + ((long long)k << 52));
+	return mul_p2_slow(x, s);
+}
+
+// r + |r| by the bits: +0 for finite r <= 0, 2r (the exponent field + 1)
+// for normal r > 0 below 2^1023; subnormals, infinities and NaNs by the FPU
+__device__ __noinline__ double r_plus_abs_slow(double r) {
+	return __dadd_rn(r, fabs(r));
+}
+
+__device__ __forceinline__ double r_plus_abs(double r) {
+	const long long b = __double_as_longlong(r);
+	const int e = exp_field(r);
+	if (e < 2047 && (b < 0 || b == 0)) return 0.0;
+	if (b > 0 && e >= 1 && e <= 2045) return __longlong_as_double(b + (1ll << 52));
+	return r_plus_abs_slow(r);
+}
+
+// -x by the sign bit
+__device__ __forceinline__ double neg_bits(double x) {
+	return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
 }
 
 __device__ __forceinline__ double fixed_div(double x, const FixedDiv& f) {
@@ -336,8 +373,13 @@ __device__ __forceinline__ double tvd_value(const Geo& g, const double* f, int f
 		const double ih = D == 0 ? g.ihx : g.ihy;
 		const double h2 = h + h, ih2 = 0.5 * ih;
 		const double R = 2.0;
-		const double r = tvd_ratio(F(C_) - F(U_), F(D_) - F(C_) + kSmall, h2, ih2);
-		return F(C_) + limiter(SCH, r, R) * 0.5 * (F(D_) - F(C_));
+		const double dc = F(D_) - F(C_);
+		const double r = tvd_ratio(F(C_) - F(U_), dc + kSmall, h2, ih2);
+		// van Leer's 0.5 R (r + |r|) / (R - 1 + r) is (r + |r|) / (1 + r)
+		// at R = 2 (0.5 R = 1 exactly)
+		const double lim = SCH == CARPIO_GPU_VANLEER ? r_plus_abs(r) / (1.0 + r)
+		                                             : limiter(SCH, r, R);
+		return F(C_) + mul_p2(lim, -1, 0.5) * dc;
 	}
 	const double R = (S(D_) + S(C_)) / S(C_);
 	const double r = (F(C_) - F(U_)) * (S(D_) + S(C_)) / (F(D_) - F(C_) + kSmall) / (S(C_) + S(U_));
@@ -350,6 +392,16 @@ __device__ __forceinline__ double tvd_value(const Geo& g, const double* f, int f
 // (veo < 0), 0 (NaN: every offset 0)
 __device__ __forceinline__ int tvd_orient(double veo) {
 	return veo >= 0.0 ? 1 : (veo < 0.0 ? -1 : 0);
+}
+
+// tvd_orient((x + y) * 0.5) from s = x + y by its bits: the halving keeps
+// the sign and turns only -2^-1074 into -0 (round to nearest even), which
+// orients like a positive value
+__device__ __forceinline__ int tvd_orient_sum(double s) {
+	const long long b = __double_as_longlong(s);
+	if (exp_field(s) == 2047 && (b & 0x000fffffffffffffll) != 0) return 0;   // NaN
+	if (b >= 0) return 1;
+	return (b & 0x7fffffffffffffffll) <= 1 ? 1 : -1;
 }
 
 // the +1/2 face of a cell in its own frame: the same value as the -1/2
@@ -370,8 +422,8 @@ __device__ __forceinline__ double tvd_half(const Geo& g, const double* face,
 		const double* f, int fa, int fst, int i, int j, bool plus) {
 	const int st = D == 0 ? g.P : 1;
 	const int a = g.at(i, j);
-	const double veo = (face[a] + face[a - st]) * 0.5;
-	const int o = tvd_orient(veo);
+	// veo = (face[a] + face[a - st]) * 0.5
+	const int o = tvd_orient_sum(face[a] + face[a - st]);
 	if (plus) return tvd_plus<SCH, D, P2>(g, f, fa, fst, i, j, o);
 	// the -1/2 face: o > 0: (0, -1, -2); o < 0: (-1, 0, 1); o == 0: (0, 0, 0)
 	const int d_ = o < 0 ? -1 : 0, c_ = o > 0 ? -1 : 0, u_ = o > 0 ? -2 : (o < 0 ? 1 : 0);
@@ -406,7 +458,7 @@ __device__ __forceinline__ double tvd_combine(const Geo& g, const double* face,
 	const int st = D == 0 ? g.P : 1;
 	const int a = g.at(i, j);
 	const double fa0 = face[a], fam = face[a - st];
-	if (P2) return (fa0 * fp - fam * fm) * (D == 0 ? g.ihx : g.ihy);
+	if (P2) return mul_p2(fa0 * fp - fam * fm, D == 0 ? g.kx : g.ky, D == 0 ? g.ihx : g.ihy);
 	return (fa0 * fp - fam * fm) / (D == 0 ? g.SX(i) : g.SY(j));
 }
 
@@ -468,14 +520,14 @@ __device__ __forceinline__ double diffusion(const Geo& g, double mu,
 		// centre distances and sizes are hx, hy: multiply by 1 / h
 #define MUX(x) (MU1 ? (x) : mu * (x))
 		{
-			double dm = MUX(f[a] - f[a - g.P]) * g.ihx;
-			double dp = MUX(f[a + g.P] - f[a]) * g.ihx;
-			t0 = (dp - dm) * g.ihx;
+			double dm = mul_p2(MUX(f[a] - f[a - g.P]), g.kx, g.ihx);
+			double dp = mul_p2(MUX(f[a + g.P] - f[a]), g.kx, g.ihx);
+			t0 = mul_p2(dp - dm, g.kx, g.ihx);
 		}
 		{
-			double dm = MUX(f[a] - f[a - 1]) * g.ihy;
-			double dp = MUX(f[a + 1] - f[a]) * g.ihy;
-			t1 = (dp - dm) * g.ihy;
+			double dm = mul_p2(MUX(f[a] - f[a - 1]), g.ky, g.ihy);
+			double dp = mul_p2(MUX(f[a + 1] - f[a]), g.ky, g.ihy);
+			t1 = mul_p2(dp - dm, g.ky, g.ihy);
 		}
 #undef MUX
 		// res = 0; res += t0; res += t1
@@ -989,8 +1041,8 @@ __global__ void __launch_bounds__(kPredThreads) k_predictor_tiles(Geo g, const d
 	for (int q = tid; q < ti * tj; q += T) {
 		const int li = q / tj, lj = q - li * tj;
 		const int a = g.at(i0 + li, j0 + lj);
-		ox[li * TJ + lj] = (signed char)tvd_orient((uf[a] + uf[a - g.P]) * 0.5);
-		oy[li * TJ + lj] = (signed char)tvd_orient((vf[a] + vf[a - 1]) * 0.5);
+		ox[li * TJ + lj] = (signed char)tvd_orient_sum(uf[a] + uf[a - g.P]);
+		oy[li * TJ + lj] = (signed char)tvd_orient_sum(vf[a] + vf[a - 1]);
 	}
 	const int nxf = (ti + 1) * tj, nyf = ti * (tj + 1);
 	for (int comp = 0; comp < 2; ++comp) {
@@ -1061,17 +1113,26 @@ __global__ void __launch_bounds__(kThreads) k_c2f(Geo g, const double* u,
 	const long n = (long)g.nx * g.ny;
 	const long t0 = blockIdx.x * (long)blockDim.x + threadIdx.x;
 	const long stride = (long)gridDim.x * blockDim.x;
+	// Geo::p2: every half size is h / 2 = 2^(-k - 1) and (hs + hs') = h, so
+	// both products and the division are exponent moves (mul_p2)
+	const double hsx = g.hx * 0.5, hsy = g.hy * 0.5;
 	for (long k = t0; k < n; k += stride) {
 		int i = (int)(k / g.ny), j = (int)(k - (long)i * g.ny);
 		int a = g.at(i, j);
+		if (p2) {
+			fx[a] = mul_p2(mul_p2(u[a + g.P], -g.kx - 1, hsx) + mul_p2(u[a], -g.kx - 1, hsx),
+					g.kx, g.ihx);
+			fy[a] = mul_p2(mul_p2(v[a + 1], -g.ky - 1, hsy) + mul_p2(v[a], -g.ky - 1, hsy),
+					g.ky, g.ihy);
+			continue;
+		}
 		double vc = u[a];
 		double hs = g.SX(i) * 0.5, hsp = g.SX(i + 1) * 0.5;
-		// (hs + hs') is the cell size: with Geo::p2 a power of two
-		fx[a] = p2 ? (u[a + g.P] * hs + vc * hsp) * g.ihx : (u[a + g.P] * hs + vc * hsp) / (hs + hsp);
+		fx[a] = (u[a + g.P] * hs + vc * hsp) / (hs + hsp);
 		vc = v[a];
 		hs = g.SY(j) * 0.5;
 		hsp = g.SY(j + 1) * 0.5;
-		fy[a] = p2 ? (v[a + 1] * hs + vc * hsp) * g.ihy : (v[a + 1] * hs + vc * hsp) / (hs + hsp);
+		fy[a] = (v[a + 1] * hs + vc * hsp) / (hs + hsp);
 	}
 	for (long k = t0; k < (long)g.ny + g.nx; k += stride) {
 		if (k < g.ny) {
@@ -1096,26 +1157,32 @@ __global__ void __launch_bounds__(kThreads) k_c2f(Geo g, const double* u,
 // PM: 1 a P2 grid, 0 not, -1 read Geo::p2 (the compile-time forms keep the
 // other branch's divisions out of the FP64 pipe). gx_in / gy_in: the
 // interior faces (i >= 0, j >= 0).
+// (the multiplications by +-1/h as exponent moves, mul_p2; x * -s is
+// -(x * s))
 template<int PM = -1>
 __device__ __forceinline__ double gx_in(const Geo& g, const double* phi, int i, int j) {
-	if (PM == 1 || (PM < 0 && g.p2)) return (phi[g.at(i + 1, j)] - phi[g.at(i, j)]) * g.ihx;
+	if (PM == 1 || (PM < 0 && g.p2))
+		return mul_p2(phi[g.at(i + 1, j)] - phi[g.at(i, j)], g.kx, g.ihx);
 	return (phi[g.at(i + 1, j)] - phi[g.at(i, j)]) / (g.CX(i + 1) - g.CX(i));
 }
 template<int PM = -1>
 __device__ __forceinline__ double gy_in(const Geo& g, const double* phi, int i, int j) {
-	if (PM == 1 || (PM < 0 && g.p2)) return (phi[g.at(i, j + 1)] - phi[g.at(i, j)]) * g.ihy;
+	if (PM == 1 || (PM < 0 && g.p2))
+		return mul_p2(phi[g.at(i, j + 1)] - phi[g.at(i, j)], g.ky, g.ihy);
 	return (phi[g.at(i, j + 1)] - phi[g.at(i, j)]) / (g.CY(j + 1) - g.CY(j));
 }
 template<int PM = -1>
 __device__ __forceinline__ double gx_at(const Geo& g, const double* phi, int i, int j) {
 	if (i >= 0) return gx_in<PM>(g, phi, i, j);
-	if (PM == 1 || (PM < 0 && g.p2)) return (phi[g.at(-1, j)] - phi[g.at(0, j)]) * -g.ihx;
+	if (PM == 1 || (PM < 0 && g.p2))
+		return neg_bits(mul_p2(phi[g.at(-1, j)] - phi[g.at(0, j)], g.kx, g.ihx));
 	return (phi[g.at(-1, j)] - phi[g.at(0, j)]) / (g.CX(-1) - g.CX(0));
 }
 template<int PM = -1>
 __device__ __forceinline__ double gy_at(const Geo& g, const double* phi, int i, int j) {
 	if (j >= 0) return gy_in<PM>(g, phi, i, j);
-	if (PM == 1 || (PM < 0 && g.p2)) return (phi[g.at(i, -1)] - phi[g.at(i, 0)]) * -g.ihy;
+	if (PM == 1 || (PM < 0 && g.p2))
+		return neg_bits(mul_p2(phi[g.at(i, -1)] - phi[g.at(i, 0)], g.ky, g.ihy));
 	return (phi[g.at(i, -1)] - phi[g.at(i, 0)]) / (g.CY(-1) - g.CY(0));
 }
 
@@ -1142,8 +1209,8 @@ __global__ void __launch_bounds__(kThreads) k_correct(Geo g, const double* phi,
 		const double gx = gx_in<PM>(g, phi, i, j), gy = gy_in<PM>(g, phi, i, j);
 		uf[a] = usf[a] - gx;
 		vf[a] = vsf[a] - gy;
-		const double gcx = (gx + gx_in<PM>(g, phi, i - 1, j)) * 0.5;
-		const double gcy = (gy + gy_in<PM>(g, phi, i, j - 1)) * 0.5;
+		const double gcx = mul_p2(gx + gx_in<PM>(g, phi, i - 1, j), -1, 0.5);
+		const double gcy = mul_p2(gy + gy_in<PM>(g, phi, i, j - 1), -1, 0.5);
 		u[a] = us[a] - gcx;
 		v[a] = vs[a] - gcy;
 		p[a] = phi[a] * inv;
@@ -1350,6 +1417,9 @@ Geo make_geo(const carpio_gpu_grid* g) {
 	e.p2 = axis_ok(g->cx, g->sx, e.hx) && axis_ok(g->cy, g->sy, e.hy) ? 1 : 0;
 	e.ihx = e.p2 ? 1.0 / e.hx : 0.0;
 	e.ihy = e.p2 ? 1.0 / e.hy : 0.0;
+	int ex = 0;
+	e.kx = e.p2 ? (std::frexp(e.ihx, &ex), ex - 1) : 0;
+	e.ky = e.p2 ? (std::frexp(e.ihy, &ex), ex - 1) : 0;
 	return e;
 }
 

@@ -17,6 +17,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 namespace {
@@ -123,7 +124,7 @@ template<int NC, int RM>
 __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 		const Vecs<double>& v, const MixedArgs& m, const TileArgs& ta,
 		const SolveCtl& sc, bool mean, double normb, const GridCtl& gc,
-		int& bank, TileOut& to, bool fused = false, double bmean = 0.0) {
+		int& bank, TileOut& to, double bmean = 0.0) {
 	extern __shared__ __align__(16) float smem[];
 	__shared__ double s_sc[4];
 	__shared__ double s_xm;
@@ -462,12 +463,15 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	// cell for the squares (the reference's nrm2 leaves the last element
 	// out: its square is taken off once, by the thread that holds it), the
 	// residual kept in FP32 (the scaling then costs no FP64 operation).
-	// fused (the first call of the spectral path): b's mean bmean is taken
-	// off here and ||b|| summed, in place of two separate passes; with
-	// `mean` the sum of x rides along for the epilogue's mean removal.
-	auto resid64 = [&](bool first) -> bool {
-		const bool fb = fused && first;
-		const bool sx = fused && mean;
+	// fb (the first call of the spectral path, whose prologue leaves b
+	// uncentred): b's mean bmean is taken off here and ||b|| summed, in
+	// place of two separate passes; sx: the sum of x rides along for the
+	// epilogue's mean removal. Both are std::integral_constant tags, so that
+	// the optional terms are compiled in or out rather than issued
+	// predicated.
+	auto resid64 = [&](auto fbt, auto sxt, bool first) -> bool {
+		constexpr bool fb = decltype(fbt)::value;   // the fused first pass
+		constexpr bool sx = decltype(sxt)::value;   // sum x for the epilogue
 		double sums[5] = { 0, 0, 0, 0, 0 };   // (r, r), sum r, (b, b), sum x, last r^2
 		double rla = 0.0, bla = 0.0;
 		float* r32 = reinterpret_cast<float*>(v.r);
@@ -540,7 +544,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	// resid64, then (unless converged) z = M r with the edges exchanged;
 	// returns gamma = (r, z) and rrn = (r, r) of the new FP32 residual
 	auto true_residual = [&](bool first, float& gamma) -> bool {
-		if (!resid64(first)) return false;
+		if (!resid64(std::false_type{}, std::false_type{}, first)) return false;
 		if (to.resid <= sc.tol) return true;
 		// (r, z) and (r, r) of the band: z = r without a preconditioner
 		float g[2] = { rr_band, rr_band };
@@ -577,7 +581,8 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 		// tolerance. The CG step of the other preconditioners would take
 		// alpha = 1 up to FP32 rounding here; it is left out, with its two
 		// reductions and its halo exchange.
-		if (!resid64(true)) return;
+		// (every call here is fused: the sum of x always rides along)
+		if (!resid64(std::true_type{}, std::true_type{}, true)) return;
 		int it = 0;
 		while (!(to.resid <= sc.tol) && it < sc.max_iter) {
 			if (!dct_apply([&](int sq, int n, float val) {
@@ -587,7 +592,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				return;
 			++it;
 			if (!grid_sync(gc)) return;
-			if (!resid64(false)) return;
+			if (!resid64(std::false_type{}, std::true_type{}, false)) return;
 			++to.updates;
 		}
 		to.iters = it;
@@ -780,7 +785,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_poisson_mixed_tile(
 		normb = s_nb;
 	}
 	TileOut to;
-	tile_solve<NC, RM>(sp, op, v, mx, ta, sc, ra.mean != 0, normb, gc, bank, to, fused, bm);
+	tile_solve<NC, RM>(sp, op, v, mx, ta, sc, ra.mean != 0, normb, gc, bank, to, bm);
 	if (read_err(gc)) {
 		if (blockIdx.x == 0 && threadIdx.x == 0) sc.out->code = read_err(gc);
 		return;
