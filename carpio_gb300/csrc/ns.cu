@@ -10,6 +10,7 @@
 // layout of the grid: cell (i, j), i, j in normal-cell coordinates, at
 // (i + gl) * P + (j + gl).
 #include "internal.hpp"
+#include "bits.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -55,17 +56,6 @@ __host__ __device__ __forceinline__ double smax(double a, double b) { return (a 
 // helpers below replace FP64 operations by integer ones where the result is
 // the same bits.
 
-// 0.0 + x: x, with -0 turned into +0 (the reference's `s = 0; s += x`)
-__device__ __forceinline__ double plus_zero(double x) {
-	const long long b = __double_as_longlong(x);
-	return b == (long long)0x8000000000000000ull ? 0.0 : x;
-}
-
-// biased exponent field of x (0 zero or subnormal, 2047 inf or NaN)
-__device__ __forceinline__ int exp_field(double x) {
-	return (int)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ff;
-}
-
 // x / d rounded to nearest, for a divisor fixed per launch, with y =
 // RN(1 / d): q = RN(x y) is within one ulp of x / d, r = x - d q is exact
 // by the FMA, and RN(q + r y) = RN(x / d) (Markstein, IBM J. Res. Dev.
@@ -92,23 +82,6 @@ __device__ __noinline__ double div_slow(double x, double d) {
 	return __ddiv_rn(x, d);
 }
 
-// x * s for s = 2^k: the exponent field moved by k where x and the product
-// are normal, x itself where x is +-0 (the product's sign is x's);
-// subnormals, infinities, NaNs and products outside the normal range take
-// the FPU multiply, out of line. The same bits as x * s in every case.
-__device__ __noinline__ double mul_p2_slow(double x, double s) {
-	return __dmul_rn(x, s);
-}
-
-__device__ __forceinline__ double mul_p2(double x, int k, double s) {
-	const long long b = __double_as_longlong(x);
-	if ((b << 1) == 0) return x;
-	const int e = exp_field(x), en = e + k;
-	if (e >= 1 && e <= 2046 && en >= 1 && en <= 2046)
-		return __longlong_as_double(b + ((long long)k << 52));
-	return mul_p2_slow(x, s);
-}
-
 // r + |r| by the bits: +0 for finite r <= 0, 2r (the exponent field + 1)
 // for normal r > 0 below 2^1023; subnormals, infinities and NaNs by the FPU
 __device__ __noinline__ double r_plus_abs_slow(double r) {
@@ -116,16 +89,12 @@ __device__ __noinline__ double r_plus_abs_slow(double r) {
 }
 
 __device__ __forceinline__ double r_plus_abs(double r) {
-	const long long b = __double_as_longlong(r);
-	const int e = exp_field(r);
-	if (e < 2047 && (b < 0 || b == 0)) return 0.0;
-	if (b > 0 && e >= 1 && e <= 2045) return __longlong_as_double(b + (1ll << 52));
+	unsigned lo, hi;
+	split_bits(r, lo, hi);
+	const int e = (int)((hi >> 20) & 0x7ffu);
+	if (e < 2047 && ((hi >> 31) != 0u || (hi | lo) == 0u)) return join_bits(0u, 0u);
+	if ((hi >> 31) == 0u && e >= 1 && e <= 2045) return join_bits(lo, hi + (1u << 20));
 	return r_plus_abs_slow(r);
-}
-
-// -x by the sign bit
-__device__ __forceinline__ double neg_bits(double x) {
-	return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
 }
 
 __device__ __forceinline__ double fixed_div(double x, const FixedDiv& f) {
@@ -339,7 +308,7 @@ __device__ __noinline__ double tvd_ratio_slow(double a, double b, double h2, dou
 __device__ __forceinline__ double tvd_ratio(double a, double b, double h2, double ih2) {
 	const double r = __ddiv_rn(a, b);
 	const int ea = exp_field(a), er = exp_field(r);
-	const bool a0 = (__double_as_longlong(a) << 1) == 0;
+	const bool a0 = is_zero_bits(a);
 	if (a0 || (ea >= 100 && ea <= 1947 && ((er >= 100 && er <= 1947) || er == 2047)))
 		return r;
 	return tvd_ratio_slow(a, b, h2, ih2);
@@ -398,10 +367,12 @@ __device__ __forceinline__ int tvd_orient(double veo) {
 // the sign and turns only -2^-1074 into -0 (round to nearest even), which
 // orients like a positive value
 __device__ __forceinline__ int tvd_orient_sum(double s) {
-	const long long b = __double_as_longlong(s);
-	if (exp_field(s) == 2047 && (b & 0x000fffffffffffffll) != 0) return 0;   // NaN
-	if (b >= 0) return 1;
-	return (b & 0x7fffffffffffffffll) <= 1 ? 1 : -1;
+	unsigned lo, hi;
+	split_bits(s, lo, hi);
+	const unsigned mag = hi & 0x7fffffffu;
+	if (mag > 0x7ff00000u || (mag == 0x7ff00000u && lo != 0u)) return 0;   // NaN
+	if ((hi >> 31) == 0u) return 1;
+	return (mag == 0u && lo <= 1u) ? 1 : -1;
 }
 
 // the +1/2 face of a cell in its own frame: the same value as the -1/2

@@ -3,6 +3,7 @@
 #pragma once
 
 #include "internal.hpp"
+#include "bits.cuh"
 
 #include <cmath>
 #include <vector>
@@ -102,13 +103,11 @@ __device__ __forceinline__ double rhs_in(const GridSpace& sp, const RhsArgs& ra,
 		const double t1 = __dmul_rn(__dsub_rn(ra.src_a[a], ra.src_a[a - sp.P]), ra.ihx);
 		const double t2 = __dmul_rn(__dsub_rn(ra.src_b[a], ra.src_b[a - 1]), ra.ihy);
 		// d = 0; d += t1; d += t2
-		const long long b1 = __double_as_longlong(t1);
-		f = __dadd_rn(b1 == (long long)0x8000000000000000ull ? 0.0 : t1, t2);
+		f = __dadd_rn(plus_zero(t1), t2);
 	}
 	const double val = __dmul_rn(__dmul_rn(sxi, ra.helm ? ra.sy[j + gl] : sxi), f);
 	// val == 0 ? +0 : -val
-	const long long bv = __double_as_longlong(val);
-	return (bv << 1) == 0 ? 0.0 : __longlong_as_double(bv ^ (long long)0x8000000000000000ull);
+	return neg_or_plus_zero(val);
 }
 
 }  // namespace cg_dev
