@@ -55,7 +55,7 @@ __device__ __forceinline__ double neg_or_plus_zero(double x) {
 	return ((hi << 1) | lo) == 0u ? join_bits(0u, 0u) : join_bits(lo, hi ^ 0x80000000u);
 }
 
-__device__ __noinline__ double mul_p2_slow(double x, double s) {
+static __device__ __noinline__ double mul_p2_slow(double x, double s) {
 	return __dmul_rn(x, s);
 }
 
