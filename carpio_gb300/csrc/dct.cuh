@@ -12,8 +12,9 @@
 // (Makhoul 1980); its inverse runs the same steps backwards, and the DST-II
 // is the DCT-II of (-1)^n x read in reverse order (the order reversal lives
 // in the eigenvalue table). The FFT is an in-place radix-2 decimation in
-// time on bit-reversed input in shared memory, one block barrier per stage,
-// a batch of sequences at a time. Lengths are powers of two, N >= 2.
+// time on bit-reversed input in shared memory, three stages per pass in
+// registers and one block barrier per pass, a batch of sequences at a time.
+// Lengths are powers of two, N >= 2.
 #pragma once
 
 #include <cstdint>
@@ -59,27 +60,59 @@ __device__ __forceinline__ int dct_src(int m, int N) {
 	return m < (N >> 1) ? 2 * m : 2 * (N - 1 - m) + 1;
 }
 
+// K consecutive radix-2 stages s0 .. s0 + K - 1 of the in-place
+// decimation in time, fused in registers: a thread loads the 2^K elements
+// base + m h0 (h0 = 2^(s0 - 1)) of a group, runs the K stages' butterflies
+// on them (the same operations, in the same order per element, as K
+// separate stages) and stores them back. One block barrier per pass
+// instead of one per stage, and each element read and written once per
+// pass.
+template<int K>
+__device__ __forceinline__ void fft_pass(float2* buf, int B, int logN, int s0,
+		const float2* tw, int NS) {
+	constexpr int R = 1 << K;
+	const int h0 = 1 << (s0 - 1);
+	const int gps = 1 << (logN - K);   // groups per sequence
+	const int ng = B * gps;
+	for (int g = threadIdx.x; g < ng; g += blockDim.x) {
+		const int seq = g >> (logN - K);
+		const int w = g & (gps - 1);
+		const int pos = w & (h0 - 1);
+		const int base = ((w - pos) << K) + pos;
+		float2* sb = buf + seq * NS;
+		float2 v[R];
+#pragma unroll
+		for (int m = 0; m < R; ++m) v[m] = sb[dswz(base + m * h0)];
+#pragma unroll
+		for (int t = 0; t < K; ++t) {
+			const int sh = logN - (s0 + t);
+#pragma unroll
+			for (int m = 0; m < R; ++m) {
+				if (m & (1 << t)) continue;
+				// the element's position within the stage's half-span
+				const int pt = pos + (m & ((1 << t) - 1)) * h0;
+				const float2 x = cmulf(__ldg(tw + (pt << sh)), v[m + (1 << t)]);
+				const float2 a = v[m];
+				v[m] = make_float2(a.x + x.x, a.y + x.y);
+				v[m + (1 << t)] = make_float2(a.x - x.x, a.y - x.y);
+			}
+		}
+#pragma unroll
+		for (int m = 0; m < R; ++m) sb[dswz(base + m * h0)] = v[m];
+	}
+	__syncthreads();
+}
+
 // B sequences of N = 2^logN complex values in buf, NS apart (bit-reversed
-// order) -> their DFTs in natural order. Begins after the caller's barrier,
-// ends with one.
+// order) -> their DFTs in natural order: the logN radix-2 stages in passes
+// of three (then two or one). Begins after the caller's barrier, ends with
+// one.
 __device__ __forceinline__ void fft_stages(float2* buf, int B, int logN, const float2* tw,
 		int NS) {
-	const int halfN = 1 << (logN - 1), nb = B * halfN;
-	for (int s = 1; s <= logN; ++s) {
-		const int h = 1 << (s - 1);
-		for (int b = threadIdx.x; b < nb; b += blockDim.x) {
-			const int seq = b >> (logN - 1);
-			const int w = b & (halfN - 1);
-			const int pos = w & (h - 1);
-			const int e1 = ((w - pos) << 1) + pos, e2 = e1 + h;
-			const int i1 = seq * NS + dswz(e1), i2 = seq * NS + dswz(e2);
-			const float2 t = cmulf(__ldg(tw + (pos << (logN - s))), buf[i2]);
-			const float2 a = buf[i1];
-			buf[i1] = make_float2(a.x + t.x, a.y + t.y);
-			buf[i2] = make_float2(a.x - t.x, a.y - t.y);
-		}
-		__syncthreads();
-	}
+	int s = 1;
+	for (; logN - s + 1 >= 3; s += 3) fft_pass<3>(buf, B, logN, s, tw, NS);
+	if (logN - s + 1 == 2) fft_pass<2>(buf, B, logN, s, tw, NS);
+	else if (logN - s + 1 == 1) fft_pass<1>(buf, B, logN, s, tw, NS);
 }
 
 // Thread t of the block takes element m of sequence seq: seq-major
