@@ -233,6 +233,34 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
 // the same bits. `bank` alternates 0/1 on consecutive calls so a fast block
 // never overwrites partials a slow block is still reading.
 //
+// Thread 0's side of a grid all-reduce: arrive (release atomic on the
+// flip-bit word) and poll with acquire loads until every block has arrived,
+// bounded by the watchdog. Returns 0 on error (recorded in c.err).
+__device__ __forceinline__ int grid_arrive_wait(const GridCtl& c) {
+	int ok = 1;
+	const unsigned inc = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1) : 1u;
+	const unsigned old = atom_add_release_gpu(c.count, inc);
+	unsigned long long t0 = 0;
+	unsigned polls = 0;
+	while (((ld_acquire_gpu(c.count) ^ old) & 0x80000000u) == 0) {
+		if ((++polls & 63u) == 0) {
+			if (*(volatile int*)c.err) { ok = 0; break; }
+			unsigned long long t = globaltimer();
+			if (t0 == 0) t0 = t;
+			if (t - t0 > c.wait_ns || t > c.deadline) {
+				set_err(c, CARPIO_GPU_ETIMEOUT);
+				ok = 0;
+				break;
+			}
+		}
+	}
+	if (ok && blockIdx.x == 0 && globaltimer() > c.deadline) {
+		set_err(c, CARPIO_GPU_ETIMEOUT);
+		ok = 0;
+	}
+	return ok;
+}
+
 // One __syncthreads gathers the block's value; then warp 0 alone arrives at
 // the barrier (thread 0: release atomic on the flip-bit word, acquire polls
 // bounded by the watchdog), reads the blocks' partials in a fixed order and
@@ -266,26 +294,7 @@ __device__ __forceinline__ bool grid_allreduce(R (&v)[NV], const GridCtl& c,
 		if (lane == 0) {
 #pragma unroll
 			for (int m = 0; m < NV; ++m) part[m * gridDim.x + blockIdx.x] = (double)v[m];
-			const unsigned inc = blockIdx.x == 0 ? 0x80000000u - (gridDim.x - 1) : 1u;
-			const unsigned old = atom_add_release_gpu(c.count, inc);
-			unsigned long long t0 = 0;
-			unsigned polls = 0;
-			while (((ld_acquire_gpu(c.count) ^ old) & 0x80000000u) == 0) {
-				if ((++polls & 63u) == 0) {
-					if (*(volatile int*)c.err) { ok = 0; break; }
-					unsigned long long t = globaltimer();
-					if (t0 == 0) t0 = t;
-					if (t - t0 > c.wait_ns || t > c.deadline) {
-						set_err(c, CARPIO_GPU_ETIMEOUT);
-						ok = 0;
-						break;
-					}
-				}
-			}
-			if (ok && blockIdx.x == 0 && globaltimer() > c.deadline) {
-				set_err(c, CARPIO_GPU_ETIMEOUT);
-				ok = 0;
-			}
+			ok = grid_arrive_wait(c);
 		}
 		__syncwarp();
 		ok = __shfl_sync(0xffffffffu, ok, 0);
@@ -306,6 +315,65 @@ __device__ __forceinline__ bool grid_allreduce(R (&v)[NV], const GridCtl& c,
 	__syncthreads();
 #pragma unroll
 	for (int m = 0; m < NV; ++m) v[m] = s_res[bank][m];
+	const bool ok = s_ok[bank] != 0;
+	bank ^= 1;
+	return ok;
+}
+
+// grid_allreduce for FP64 values with the block's last stage in warp 0's
+// shuffles instead of thread 0's serial loop over the warps: an FP64 warp
+// instruction costs 64 cycles of its sub-partition, so the serial loop over
+// 16 warps' sums took 16 x 64 cycles a value. Same protocol, fixed order.
+template<int NV>
+__device__ __forceinline__ bool grid_allreduce_w0(double (&v)[NV], const GridCtl& c,
+		int& bank) {
+	static_assert(NV >= 1 && NV <= kMaxReduce, "partials");
+	__shared__ double s_w[NV][32];
+	__shared__ double s_r[2][NV];
+	__shared__ int s_ok[2];
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	const int nw = blockDim.x >> 5;
+#pragma unroll
+	for (int m = 0; m < NV; ++m) {
+		double x = v[m];
+#pragma unroll
+		for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+		if (lane == 0) s_w[m][warp] = x;
+	}
+	__syncthreads();
+	if (warp == 0) {
+		double* part = c.partials + (size_t)bank * kMaxReduce * gridDim.x;
+		double bs[NV];
+#pragma unroll
+		for (int m = 0; m < NV; ++m) {
+			double x = lane < nw ? s_w[m][lane] : 0.0;
+#pragma unroll
+			for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+			bs[m] = x;
+		}
+		int ok = 1;
+		if (lane == 0) {
+#pragma unroll
+			for (int m = 0; m < NV; ++m) part[m * gridDim.x + blockIdx.x] = bs[m];
+			ok = grid_arrive_wait(c);
+		}
+		__syncwarp();
+		ok = __shfl_sync(0xffffffffu, ok, 0);
+		if (ok) {
+#pragma unroll
+			for (int m = 0; m < NV; ++m) {
+				double acc = 0.0;
+				for (int b = lane; b < (int)gridDim.x; b += 32) acc += ldcg(&part[m * gridDim.x + b]);
+#pragma unroll
+				for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+				if (lane == 0) s_r[bank][m] = acc;
+			}
+		}
+		if (lane == 0) s_ok[bank] = ok;
+	}
+	__syncthreads();
+#pragma unroll
+	for (int m = 0; m < NV; ++m) v[m] = s_r[bank][m];
 	const bool ok = s_ok[bank] != 0;
 	bank ^= 1;
 	return ok;

@@ -459,21 +459,31 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 		}
 	};
 	// FP64 residual of the band (x64 complete on entry) and its norms; unless
-	// it meets the tolerance, the scaled FP32 residual into rs. One FMA per
-	// cell for the squares (the reference's nrm2 leaves the last element
-	// out: its square is taken off once, by the thread that holds it), the
-	// residual kept in FP32 (the scaling then costs no FP64 operation).
-	// fb (the first call of the spectral path, whose prologue leaves b
-	// uncentred): b's mean bmean is taken off here and ||b|| summed, in
-	// place of two separate passes; sx: the sum of x rides along for the
-	// epilogue's mean removal. Both are std::integral_constant tags, so that
-	// the optional terms are compiled in or out rather than issued
-	// predicated.
-	auto resid64 = [&](auto fbt, auto sxt, bool first) -> bool {
-		constexpr bool fb = decltype(fbt)::value;   // the fused first pass
-		constexpr bool sx = decltype(sxt)::value;   // sum x for the epilogue
-		double sums[5] = { 0, 0, 0, 0, 0 };   // (r, r), sum r, (b, b), sum x, last r^2
-		double rla = 0.0, bla = 0.0;
+	// it meets the tolerance, the scaled FP32 residual into rs (the residual
+	// is kept in FP32, so the scaling costs no FP64 operation). Tags
+	// (std::integral_constant, so that optional terms are compiled in or out
+	// rather than issued predicated):
+	// fb: the first call of the spectral path, whose prologue leaves b
+	//   uncentred: b's mean bmean is taken off here and ||b|| summed, in
+	//   place of two separate passes;
+	// sx: the sum of x rides along for the epilogue's mean removal;
+	// sp: the spectral path, whose M ignores the mean of r (the lambda = 0
+	//   mode maps to 0), so no sum of r; its scale is ||r|| itself.
+	// The reference's nrm2 leaves the last element out: on the spectral path
+	// its square is dropped in the loop (a zero factor), otherwise taken
+	// off once by the thread that holds it.
+	auto resid64 = [&](auto fbt, auto sxt, auto spt, bool first) -> bool {
+		constexpr bool fb = decltype(fbt)::value;
+		constexpr bool sx = decltype(sxt)::value;
+		constexpr bool spc = decltype(spt)::value;
+		// spectral: (r, r) without the last, [sum x], [(b, b) without the
+		// last]; else: (r, r), sum r, the last r^2
+		constexpr int NV = spc ? 1 + (sx ? 1 : 0) + (fb ? 1 : 0) : 3;
+		constexpr int IX = 1, IB = sx ? 2 : 1;
+		double sums[NV];
+#pragma unroll
+		for (int m = 0; m < NV; ++m) sums[m] = 0.0;
+		double rla = 0.0;
 		float* r32 = reinterpret_cast<float*>(v.r);
 #pragma unroll
 		for (int lr = 0; lr < RM; ++lr)
@@ -483,36 +493,44 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				if (lr < rows && j < ny) {
 					const int kk = (r0 + lr) * ny + j;
 					const int a = (r0 + lr + gl) * P + j + gl;
+					const bool last = a == la && !full;
 					double bb = v.b[a];
 					if (fb) {
 						bb = bb - bmean;
 						v.b[a] = bb;
-						sums[2] = fma(bb, bb, sums[2]);
+						sums[IB] = fma(bb, last ? 0.0 : bb, sums[IB]);
 					}
-					if (sx) sums[3] += ldcg(v.x + a);
+					if (sx) sums[IX] += ldcg(v.x + a);
 					const double rv = bb - op.apply(v.x, kk, a);
 					r32[a] = (float)rv;
-					sums[0] = fma(rv, rv, sums[0]);
-					sums[1] += rv;
-					if (a == la) { rla = rv; bla = bb; }
+					if (spc) {
+						sums[0] = fma(rv, last ? 0.0 : rv, sums[0]);
+					} else {
+						sums[0] = fma(rv, rv, sums[0]);
+						sums[1] += rv;
+						if (last) rla = rv;
+					}
 				}
 			}
-		if (!full) {
-			sums[4] = rla * rla;
-			if (fb) sums[2] -= bla * bla;
-		}
-		if (!grid_allreduce<double, 5>(sums, gc, bank)) return false;
+		if (!spc) sums[2] = rla * rla;
+		if (!grid_allreduce_w0<NV>(sums, gc, bank)) return false;
 		if (tid == 0) {
 			if (fb) {
-				const double nb = sqrt(fmax(sums[2], 0.0));
+				const double nb = sqrt(fmax(sums[IB], 0.0));
 				s_sc[3] = nb == 0.0 ? 1.0 : nb;
 			}
 			const double nrm = fb ? s_sc[3] : nrmb;
-			double mr = mean ? sums[1] / ncell : 0.0;
-			s_sc[0] = sqrt(fmax(sums[0] - sums[4], 0.0)) / nrm;
-			s_sc[1] = mr;
-			s_sc[2] = sqrt(mean ? fmax(sums[0] - sums[1] * mr, 0.0) : sums[0]);
-			s_xm = sums[3] / ncell;
+			if (spc) {
+				s_sc[0] = sqrt(fmax(sums[0], 0.0)) / nrm;
+				s_sc[1] = 0.0;
+				s_sc[2] = sqrt(fmax(sums[0], 0.0));
+			} else {
+				const double mr = mean ? sums[1] / ncell : 0.0;
+				s_sc[0] = sqrt(fmax(sums[0] - sums[2], 0.0)) / nrm;
+				s_sc[1] = mr;
+				s_sc[2] = sqrt(mean ? fmax(sums[0] - sums[1] * mr, 0.0) : sums[0]);
+			}
+			s_xm = sx ? sums[IX] / ncell : 0.0;
 		}
 		__syncthreads();
 		if (fb) nrmb = s_sc[3];
@@ -533,7 +551,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				const int j = tid + k * T;
 				if (lr < rows && j < ny) {
 					const int a = (r0 + lr + gl) * P + j + gl;
-					const float rv = (r32[a] - mr) * sc32;
+					const float rv = spc ? r32[a] * sc32 : (r32[a] - mr) * sc32;
 					rs[lr * ny + j] = rv;
 					rr = fmaf(rv, rv, rr);
 				}
@@ -544,7 +562,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	// resid64, then (unless converged) z = M r with the edges exchanged;
 	// returns gamma = (r, z) and rrn = (r, r) of the new FP32 residual
 	auto true_residual = [&](bool first, float& gamma) -> bool {
-		if (!resid64(std::false_type{}, std::false_type{}, first)) return false;
+		if (!resid64(std::false_type{}, std::false_type{}, std::false_type{}, first)) return false;
 		if (to.resid <= sc.tol) return true;
 		// (r, z) and (r, r) of the band: z = r without a preconditioner
 		float g[2] = { rr_band, rr_band };
@@ -582,7 +600,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 		// alpha = 1 up to FP32 rounding here; it is left out, with its two
 		// reductions and its halo exchange.
 		// (every call here is fused: the sum of x always rides along)
-		if (!resid64(std::true_type{}, std::true_type{}, true)) return;
+		if (!resid64(std::true_type{}, std::true_type{}, std::true_type{}, true)) return;
 		int it = 0;
 		while (!(to.resid <= sc.tol) && it < sc.max_iter) {
 			if (!dct_apply([&](int sq, int n, float val) {
@@ -592,7 +610,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				return;
 			++it;
 			if (!grid_sync(gc)) return;
-			if (!resid64(std::false_type{}, std::true_type{}, false)) return;
+			if (!resid64(std::false_type{}, std::true_type{}, std::true_type{}, false)) return;
 			++to.updates;
 		}
 		to.iters = it;
