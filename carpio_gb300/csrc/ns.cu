@@ -1434,42 +1434,6 @@ cudaError_t launch_bc(const Geo& geo, double* f0, const carpio_gpu_bc& b0,
 	return cudaGetLastError();
 }
 
-// Unused dynamic shared memory for the tiled predictor that caps its
-// blocks per SM where fewer give a better last wave: with b blocks per SM
-// the tiles run in ceil(tiles / (b SMs)) waves, and a wave that is half
-// full leaves half the SMs idle (2048 tiles at 1024^2: 3 per SM take 4.49
-// waves, i.e. 5, 90 % busy; 2 per SM take 6.74, i.e. 7, 96 %). The FP64
-// pipe is what bounds the kernel, so two blocks keep it as busy as three.
-size_t pred_smem_pad(const void* fn, long tiles) {
-	int per_sm = 0;
-	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kPredThreads, 0) != cudaSuccess
-			|| per_sm < 2)
-		return 0;
-	const long sms = cg_host::sm_count();
-	auto busy = [&](int b) {
-		const long slots = b * sms, waves = (tiles + slots - 1) / slots;
-		return (double)tiles / (double)(waves * slots);
-	};
-	int best = per_sm;
-	for (int b = per_sm - 1; b >= 2; --b)
-		if (busy(b) > busy(best) + 0.02) best = b;
-	if (best == per_sm) return 0;
-	cudaFuncAttributes fa;
-	int dev = 0, smem_sm = 0;
-	if (cudaFuncGetAttributes(&fa, fn) != cudaSuccess || cudaGetDevice(&dev) != cudaSuccess
-			|| cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev)
-			!= cudaSuccess)
-		return 0;
-	// per block at least a (best + 1)-th of the SM's shared memory, so that
-	// best + 1 blocks do not fit (1 KB a block is the runtime's reserve)
-	const long need = smem_sm / (best + 1) + 1 - (long)fa.sharedSizeBytes - 1024;
-	if (need <= 0) return 0;
-	if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)need)
-			!= cudaSuccess)
-		return 0;
-	return (size_t)need;
-}
-
 template<int SCH>
 cudaError_t launch_pred(const Geo& geo, int blocks, cudaStream_t s,
 		const double* u, const double* v, const double* uf, const double* vf,
@@ -1482,12 +1446,7 @@ cudaError_t launch_pred(const Geo& geo, int blocks, cudaStream_t s,
 		const dim3 grid((geo.ny + kPredTJ - 1) / kPredTJ, (geo.nx + kPredTI - 1) / kPredTI);
 		const FixedDiv rd = make_fixed_div(rho);
 		const int diff = muf ? 0 : (mu == 1.0 ? 2 : 1);
-		const size_t pad = pred_smem_pad(geo.p2 ? (diff == 0 ? (const void*)k_predictor_tiles<SCH, true, 0>
-				: diff == 1 ? (const void*)k_predictor_tiles<SCH, true, 1>
-				: (const void*)k_predictor_tiles<SCH, true, 2>)
-				: (diff == 0 ? (const void*)k_predictor_tiles<SCH, false, 0>
-				: (const void*)k_predictor_tiles<SCH, false, 1>), (long)grid.x * grid.y);
-#define PT(P, D) k_predictor_tiles<SCH, P, D><<<grid, kPredThreads, pad, s>>>(geo, u, v, uf, vf, \
+#define PT(P, D) k_predictor_tiles<SCH, P, D><<<grid, kPredThreads, 0, s>>>(geo, u, v, uf, vf, \
 		us, vs, ss, rd, mu, muf)
 		if (geo.p2) {
 			if (diff == 0) PT(true, 0);

@@ -757,38 +757,16 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_poisson_mixed_tile(
 	__shared__ double s_nb;
 	double bm = 0.0, normb = 1.0;
 	if (fused) {
-		// the band's cells in the layout of tile_solve (thread t: columns t,
-		// t + T, ...; every row), unrolled so that the cells' loads and FP64
-		// chains overlap; the boundary cells (row constant folds) after,
-		// out of line
 		double s[1] = { 0 };
-#pragma unroll
-		for (int lr = 0; lr < RM; ++lr)
-#pragma unroll
-			for (int k = 0; k < NC; ++k) {
-				const int j = tid + k * T, i = r0 + lr;
-				if (lr < rows && j < ny) {
-					const int a = (i + gl) * P + j + gl;
-					v.x[a] = ra.phi[a];
-					if (i > 0 && i < nx - 1 && j > 0 && j < ny - 1) {
-						const double bb = rhs_in<SRC>(sp, ra, i, j, a);
-						v.b[a] = bb;
-						s[0] += bb;
-					}
-				}
-			}
-#pragma unroll
-		for (int lr = 0; lr < RM; ++lr)
-#pragma unroll
-			for (int k = 0; k < NC; ++k) {
-				const int j = tid + k * T, i = r0 + lr;
-				if (lr < rows && j < ny && !(i > 0 && i < nx - 1 && j > 0 && j < ny - 1)) {
-					const int a = (i + gl) * P + j + gl;
-					const double bb = rhs_at_call<SRC>(sp, ra, i, j, a);
-					v.b[a] = bb;
-					s[0] += bb;
-				}
-			}
+		for (int t = tid; t < rows * ny; t += T) {
+			const int lr = t / ny, j = t - lr * ny, i = r0 + lr;
+			const int a = (i + gl) * P + j + gl;
+			const bool in = i > 0 && i < nx - 1 && j > 0 && j < ny - 1;
+			const double bb = in ? rhs_in<SRC>(sp, ra, i, j, a) : rhs_at_call<SRC>(sp, ra, i, j, a);
+			v.b[a] = bb;
+			v.x[a] = ra.phi[a];
+			s[0] += bb;
+		}
 		if (!grid_allreduce<double, 1>(s, gc, bank)) return;
 		bm = ra.mean ? s[0] / (double)sp.count() : 0.0;
 	} else {
