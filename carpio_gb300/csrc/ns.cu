@@ -898,28 +898,19 @@ struct DtRule {
 __global__ void __launch_bounds__(kThreads) k_restrict_time(Geo g,
 		const double* u, const double* v, StepScalars* ss, DtRule rule,
 		double* step_dt, int st) {
-	// the bits of the largest square so far: non-negative doubles order like
-	// their bit patterns, so the max is integer work
-	unsigned mlo = 0u, mhi = 0u;
+	double m = 0.0;
 	const long n = (long)g.nx * g.ny;
 	for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n;
 			k += (long)gridDim.x * blockDim.x) {
 		int i = (int)(k / g.ny), j = (int)(k - (long)i * g.ny);
 		int a = g.at(i, j);
-		// s = 0; s += u u; s += v v (u u is never -0: 0 + u u = u u)
-		const double s = u[a] * u[a] + v[a] * v[a];
+		double s = 0;
+		s += u[a] * u[a];
+		s += v[a] * v[a];
 		// max sqrt(s) = sqrt(max s): a correctly rounded sqrt is monotone,
-		// so one sqrt of the largest square gives the same bits; m =
-		// smax(m, s), where a NaN never wins (its bits lie above +inf's)
-		unsigned lo, hi;
-		split_bits(s, lo, hi);
-		const bool nan = hi > 0x7ff00000u || (hi == 0x7ff00000u && lo != 0u);
-		if (!nan && (hi > mhi || (hi == mhi && lo > mlo))) {
-			mhi = hi;
-			mlo = lo;
-		}
+		// so one sqrt of the largest square gives the same bits
+		m = smax(m, s);
 	}
-	double m = join_bits(mlo, mhi);
 	m = block_max(m);
 	__shared__ bool last;
 	if (threadIdx.x == 0) {
