@@ -105,6 +105,9 @@ struct StencilCoeffs {
 	// Dirichlet flags and the tables (eigenvalue parts [nx], [ny]; FFT
 	// twiddles [nx/2], [ny/2]; DCT factors [nx], [ny] as float2), packed
 	bool dct_ok = false;
+	// the stencil's coefficients exact in FP32: the spectral path's refinement
+	// residuals may run in double-float
+	bool dct_df = false;
 	int dct_lx = 0, dct_ly = 0, dct_fx = 0, dct_fy = 0;
 	DevBuf dctT;
 };

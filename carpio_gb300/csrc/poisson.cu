@@ -12,6 +12,7 @@
 #include "mixed.cuh"
 #include "mg.cuh"
 #include "dct.cuh"
+#include "dfloat.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -107,6 +108,9 @@ struct TileArgs {
 	int rows_max;
 	MgArgs mg;             // the multigrid preconditioner (mg.nlev > 0)
 	DctArgs dct;           // the spectral preconditioner (dct.on)
+	int df;                // spectral: x, b and the refinement residuals in
+	                       // double-float (FP32 pipe), the coefficients being
+	                       // exact in FP32
 };
 
 __device__ __forceinline__ int band_lo(int c, int C, int nx) {
@@ -559,6 +563,97 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 		rr_band = rr;
 		return true;
 	};
+	// The spectral path's residual in double-float (ta.df: x and b as hi + lo
+	// float pairs in the p and q vectors' memory, the coefficients exact in
+	// FP32): b - A x with TwoSum / TwoProd on the FP32 pipe, the FP32
+	// residual the pair's high part. fb (the first call): b centred (bmean)
+	// and the squares summed in FP64; later calls sum the squares of r
+	// scaled by 1 / rn0 in FP32 (so they stay in range). The last element's
+	// square is dropped (the reference's nrm2); the sum of x (double-float,
+	// for the epilogue) rides along.
+	float2* xdf = reinterpret_cast<float2*>(v.p);
+	float2* bdf = reinterpret_cast<float2*>(v.q);
+	auto resid_df = [&](auto fbt) -> bool {
+		constexpr bool fb = decltype(fbt)::value;
+		constexpr int NV = fb ? 3 : 2;   // (r, r), sum x, [(b, b)]
+		const float2 nbm = df_neg(df_from_double(bmean));
+		const float sc32 = (float)scale0;
+		double q2d = 0.0, b2d = 0.0;
+		float q2 = 0.f;
+		float2 sxa = make_float2(0.f, 0.f);
+		float* r32 = reinterpret_cast<float*>(v.r);
+#pragma unroll
+		for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+			for (int k = 0; k < NC; ++k) {
+				const int j = tid + k * T;
+				if (lr < rows && j < ny) {
+					const int a = (r0 + lr + gl) * P + j + gl, cc = lr * ny + j;
+					const bool last = a == la && !full;
+					float2 bb = bdf[a];
+					if (fb) {
+						bb = df_add(bb, nbm);
+						bdf[a] = bb;
+						const double bd = f2d_bits(bb.x);
+						b2d = fma(bd, last ? 0.0 : bd, b2d);
+					}
+					const float2 xc = xdf[a];
+					sxa = df_add(sxa, xc);
+					float2 ax = df_mul_f(xc, dd[cc]);
+					ax = df_add(ax, df_mul_f(xdf[a - P], axs[lr]));
+					ax = df_add(ax, df_mul_f(xdf[a + P], axs[lr + 1]));
+					ax = df_add(ax, df_mul_f(xdf[a - 1], ayl[k]));
+					ax = df_add(ax, df_mul_f(xdf[a + 1], ayr[k]));
+					const float rh = df_add(bb, df_neg(ax)).x;
+					r32[a] = rh;
+					if (fb) {
+						const double rd = f2d_bits(rh);
+						q2d = fma(rd, last ? 0.0 : rd, q2d);
+					} else {
+						const float rsc = __fmul_rn(rh, sc32);
+						q2 = __fmaf_rn(rsc, last ? 0.f : rsc, q2);
+					}
+				}
+			}
+		double sums[NV];
+		sums[0] = fb ? q2d : f2d_bits(q2);
+		sums[1] = df_to_double(sxa);
+		if (fb) sums[NV - 1] = b2d;
+		if (!grid_allreduce_w0<NV>(sums, gc, bank)) return false;
+		if (tid == 0) {
+			if (fb) {
+				const double nb = sqrt(fmax(sums[NV - 1], 0.0));
+				s_sc[3] = nb == 0.0 ? 1.0 : nb;
+			}
+			const double nrm = fb ? s_sc[3] : nrmb;
+			// later calls summed (r / rn0)^2
+			const double rn = fb ? sqrt(fmax(sums[0], 0.0)) : sqrt(fmax(sums[0], 0.0)) * rn0;
+			s_sc[0] = rn / nrm;
+			s_sc[2] = rn;
+			s_xm = sums[1] / ncell;
+		}
+		__syncthreads();
+		if (fb) nrmb = s_sc[3];
+		to.resid = s_sc[0];
+		to.xmean = s_xm;
+		if (to.resid <= sc.tol) return true;
+		if (fb) {
+			rn0 = s_sc[2];
+			scale0 = rn0 > 0.0 ? 1.0 / rn0 : 1.0;
+		}
+		const float s32 = (float)scale0;
+#pragma unroll
+		for (int lr = 0; lr < RM; ++lr)
+#pragma unroll
+			for (int k = 0; k < NC; ++k) {
+				const int j = tid + k * T;
+				if (lr < rows && j < ny) {
+					const int a = (r0 + lr + gl) * P + j + gl;
+					rs[lr * ny + j] = __fmul_rn(r32[a], s32);
+				}
+			}
+		return true;
+	};
 	// resid64, then (unless converged) z = M r with the edges exchanged;
 	// returns gamma = (r, z) and rrn = (r, r) of the new FP32 residual
 	auto true_residual = [&](bool first, float& gamma) -> bool {
@@ -593,6 +688,26 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 	to.iters = 0;
 	to.updates = 0;
 	to.done = 0;
+	if (use_dct && ta.df) {
+		// the same refinement with x, b and the residual in double-float
+		if (!resid_df(std::true_type{})) return;
+		const float2 rdf = df_from_double(rn0);
+		int it = 0;
+		while (!(to.resid <= sc.tol) && it < sc.max_iter) {
+			if (!dct_apply([&](int sq, int n, float val) {
+					const int a = (r0 + sq + gl) * P + n + gl;
+					xdf[a] = df_add(xdf[a], df_mul_f(rdf, val));
+				}))
+				return;
+			++it;
+			if (!grid_sync(gc)) return;
+			if (!resid_df(std::false_type{})) return;
+			++to.updates;
+		}
+		to.iters = it;
+		to.done = to.resid <= sc.tol ? 1 : 0;
+		return;
+	}
 	if (use_dct) {
 		// Iterative refinement with M = A^-1 to FP32 rounding: x += rn0 M r
 		// (r scaled by 1 / rn0), then the FP64 residual, until it meets the
@@ -758,14 +873,35 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_poisson_mixed_tile(
 	double bm = 0.0, normb = 1.0;
 	if (fused) {
 		double s[1] = { 0 };
+		// double-float: x and b as hi + lo float pairs in the p and q vectors'
+		// memory, with a zero first ghost layer around x (the wall faces'
+		// coefficients are 0, so the ghosts need only be finite)
+		float2* xdf = reinterpret_cast<float2*>(v.p);
+		float2* bdf = reinterpret_cast<float2*>(v.q);
 		for (int t = tid; t < rows * ny; t += T) {
 			const int lr = t / ny, j = t - lr * ny, i = r0 + lr;
 			const int a = (i + gl) * P + j + gl;
 			const bool in = i > 0 && i < nx - 1 && j > 0 && j < ny - 1;
 			const double bb = in ? rhs_in<SRC>(sp, ra, i, j, a) : rhs_at_call<SRC>(sp, ra, i, j, a);
-			v.b[a] = bb;
-			v.x[a] = ra.phi[a];
+			if (ta.df) {
+				bdf[a] = df_from_double(bb);
+				xdf[a] = df_from_double(ra.phi[a]);
+			} else {
+				v.b[a] = bb;
+				v.x[a] = ra.phi[a];
+			}
 			s[0] += bb;
+		}
+		if (ta.df) {
+			const float2 z = make_float2(0.f, 0.f);
+			for (int t = tid; t < 2 * rows; t += T) {
+				const int i = r0 + t / 2, j = (t & 1) ? ny : -1;
+				xdf[(i + gl) * P + j + gl] = z;
+			}
+			if (r0 == 0)
+				for (int j = tid; j < ny; j += T) xdf[(gl - 1) * P + j + gl] = z;
+			if (r0 + rows == nx)
+				for (int j = tid; j < ny; j += T) xdf[(nx + gl) * P + j + gl] = z;
 		}
 		if (!grid_allreduce<double, 1>(s, gc, bank)) return;
 		bm = ra.mean ? s[0] / (double)sp.count() : 0.0;
@@ -815,10 +951,12 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_poisson_mixed_tile(
 	finish(sc, to.done ? 0 : 1, to.iters, to.resid, to.updates + 1);
 	if (fused) {
 		const double xm = ra.mean ? to.xmean : 0.0;
+		const float2* xdf = reinterpret_cast<const float2*>(v.p);
 		for (int t = tid; t < rows * ny; t += T) {
 			const int lr = t / ny, j = t - lr * ny;
 			const int a = (r0 + lr + gl) * P + j + gl;
-			ra.phi[a] = ra.mean ? v.x[a] - xm : v.x[a];
+			const double xv = ta.df ? df_to_double(xdf[a]) : v.x[a];
+			ra.phi[a] = ra.mean ? xv - xm : xv;
 		}
 		return;
 	}
@@ -1106,6 +1244,7 @@ int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
 	// on both sides of each axis, and an operator that is the separable
 	// five-point one (uniform interior faces, the diagonal folded as above)
 	c.dct_ok = false;
+	c.dct_df = false;
 	auto pow2 = [](int n, int& lg) {
 		lg = 0;
 		while ((1 << lg) < n) ++lg;
@@ -1151,6 +1290,13 @@ int stencil_prepare(carpio_gpu_grid* g, const carpio_gpu_bc& bc, double beta,
 			for (int k = 0; k < ny; ++k) cplx(-pi * k / (2.0 * ny));
 			if ((rc = to_device(c.dctT, t.data(), sizeof(float) * t.size(), s))) return rc;
 			c.dct_ok = true;
+			bool ex = true;
+			auto f32 = [](double x) { return (double)(float)x == x && std::fabs(x) < 1e30; };
+			for (int i = 0; i <= nx && ex; ++i) ex = f32(ax[i]);
+			for (int j = 0; j <= ny && ex; ++j) ex = f32(ay[j]);
+			for (int i = 0; i < nx && ex; ++i)
+				for (int j = 0; j < ny && ex; ++j) ex = f32(D[(size_t)(i + gl) * g->P + (j + gl)]);
+			c.dct_df = ex;
 			c.dct_lx = lgx;
 			c.dct_ly = lgy;
 			c.dct_fx = bc.type[0] == 1;
@@ -1387,6 +1533,7 @@ int poisson_launch(carpio_gpu_grid* g, StencilCoeffs& c, PoissonWs& w,
 				d.ey = cp + nx / 2 + ny / 2 + nx;
 				d.G = w.dct.as<float>();
 				d.fb = (int)fb;
+				ta.df = c.dct_df ? 1 : 0;
 				smem = ssmem;
 				pdeg = 0;
 				spec = true;
