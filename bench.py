@@ -455,11 +455,13 @@ def main():
                                   else "k_poisson") + " (persistent projection solve)"}
     if a.precision == "mixed":
         out["roofline"]["note"] = (
-            "the Krylov vectors stay in shared memory and registers: DRAM "
+            "the solve's vectors stay in shared memory, registers and L2: DRAM "
             "traffic is `traffic`, far below the algorithmic bytes; the kernel "
-            "is bound by grid synchronisation latency and by its FP64 residual "
-            "passes (two all-reduces per FP32 iteration, the preconditioner's "
-            "grid barriers, three FP64 residuals and the prologue per solve)")
+            "is bound by grid synchronisation latency and its spectral "
+            "applications (with the spectral preconditioner: iterative "
+            "refinement, per refinement one application with two grid "
+            "barriers, a grid barrier and one residual all-reduce; the "
+            "residuals in double-float on the FP32 pipe)")
     # e2e through the public API with host buffers: the timed steps again,
     # from the same starting state, each step copying the whole state in
     # from pinned host memory and back out
