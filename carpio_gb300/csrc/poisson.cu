@@ -590,20 +590,22 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 				if (lr < rows && j < ny) {
 					const int a = (r0 + lr + gl) * P + j + gl, cc = lr * ny + j;
 					const bool last = a == la && !full;
-					float2 bb = bdf[a];
+					// L2 loads (ldcg): the neighbour bands' x was written by
+					// other SMs, whose stores no L1 here sees
+					float2 bb = ldcg(bdf + a);
 					if (fb) {
 						bb = df_add(bb, nbm);
 						bdf[a] = bb;
 						const double bd = f2d_bits(bb.x);
 						b2d = fma(bd, last ? 0.0 : bd, b2d);
 					}
-					const float2 xc = xdf[a];
+					const float2 xc = ldcg(xdf + a);
 					sxa = df_add(sxa, xc);
 					float2 ax = df_mul_f(xc, dd[cc]);
-					ax = df_add(ax, df_mul_f(xdf[a - P], axs[lr]));
-					ax = df_add(ax, df_mul_f(xdf[a + P], axs[lr + 1]));
-					ax = df_add(ax, df_mul_f(xdf[a - 1], ayl[k]));
-					ax = df_add(ax, df_mul_f(xdf[a + 1], ayr[k]));
+					ax = df_add(ax, df_mul_f(ldcg(xdf + a - P), axs[lr]));
+					ax = df_add(ax, df_mul_f(ldcg(xdf + a + P), axs[lr + 1]));
+					ax = df_add(ax, df_mul_f(ldcg(xdf + a - 1), ayl[k]));
+					ax = df_add(ax, df_mul_f(ldcg(xdf + a + 1), ayr[k]));
 					const float rh = df_add(bb, df_neg(ax)).x;
 					r32[a] = rh;
 					if (fb) {
@@ -696,7 +698,7 @@ __device__ void tile_solve(const GridSpace& sp, const StencilOp<double>& op,
 		while (!(to.resid <= sc.tol) && it < sc.max_iter) {
 			if (!dct_apply([&](int sq, int n, float val) {
 					const int a = (r0 + sq + gl) * P + n + gl;
-					xdf[a] = df_add(xdf[a], df_mul_f(rdf, val));
+					xdf[a] = df_add(ldcg(xdf + a), df_mul_f(rdf, val));
 				}))
 				return;
 			++it;
@@ -955,7 +957,7 @@ __global__ void __launch_bounds__(kTileThreads, 1) k_poisson_mixed_tile(
 		for (int t = tid; t < rows * ny; t += T) {
 			const int lr = t / ny, j = t - lr * ny;
 			const int a = (r0 + lr + gl) * P + j + gl;
-			const double xv = ta.df ? df_to_double(xdf[a]) : v.x[a];
+			const double xv = ta.df ? df_to_double(ldcg(xdf + a)) : v.x[a];
 			ra.phi[a] = ra.mean ? xv - xm : xv;
 		}
 		return;
