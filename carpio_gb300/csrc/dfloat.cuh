@@ -54,11 +54,6 @@ __device__ __forceinline__ float2 df_mul_f(float2 x, float c) {
 	return make_float2(s, t);
 }
 
-// x * y for a double-float y, x a float
-__device__ __forceinline__ float2 df_mul_df_f(float2 y, float x) {
-	return df_mul_f(y, x);
-}
-
 __device__ __noinline__ float2 df_from_double_slow(double d) {
 	const float h = __double2float_rn(d);
 	return make_float2(h, __double2float_rn(d - (double)h));

@@ -357,15 +357,10 @@ __device__ __forceinline__ double tvd_value(const Geo& g, const double* f, int f
 #undef S
 }
 
-// the stencil orientation of a cell from its velocity veo: 1 (veo >= 0), -1
-// (veo < 0), 0 (NaN: every offset 0)
-__device__ __forceinline__ int tvd_orient(double veo) {
-	return veo >= 0.0 ? 1 : (veo < 0.0 ? -1 : 0);
-}
-
-// tvd_orient((x + y) * 0.5) from s = x + y by its bits: the halving keeps
-// the sign and turns only -2^-1074 into -0 (round to nearest even), which
-// orients like a positive value
+// The stencil orientation of a cell from its velocity veo = (x + y) * 0.5:
+// 1 (veo >= 0), -1 (veo < 0), 0 (NaN: every offset 0), from s = x + y by
+// its bits: the halving keeps the sign and turns only -2^-1074 into -0
+// (round to nearest even), which orients like a positive value
 __device__ __forceinline__ int tvd_orient_sum(double s) {
 	unsigned lo, hi;
 	split_bits(s, lo, hi);

@@ -1667,7 +1667,6 @@ static int grid_from_axes(int nx, int ny, int gl, std::vector<double>&& cx,
 	g->cy = std::move(cy);
 	g->sy = std::move(sy);
 	cudaGetDevice(&g->device);
-	int rc = 0;
 	auto fail = [&](int code) {
 		carpio_gpu_grid_destroy(g);
 		return code;
@@ -1689,7 +1688,6 @@ static int grid_from_axes(int nx, int ny, int gl, std::vector<double>&& cx,
 			return fail(CARPIO_GPU_ECUDA);
 		}
 	}
-	(void)rc;
 	*out = g;
 	return 0;
 }
