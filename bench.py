@@ -67,8 +67,9 @@ def parse():
                     help="band-local Chebyshev degree of the FP32 CG (0 default, -1 none)")
     ap.add_argument("--poly-ratio", type=float, default=0.0)
     ap.add_argument("--precond", default="default",
-                    choices=["default", "chebyshev", "multigrid"],
-                    help="preconditioner of the on-chip FP32 CG")
+                    choices=["default", "spectral", "chebyshev", "multigrid"],
+                    help="the mixed solve's FP32 stage (default: spectral where it "
+                         "applies, else multigrid)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the FP64 comparison, Poisson, learned, batched, next-row and CPU legs")
     ap.add_argument("--oracle-steps", type=int, default=3,
@@ -112,7 +113,8 @@ def solver_desc(precision, inner_tol, n=1024):
         pre = None
     elif spectral_applies(n):
         pre = ("spectral: M = A^-1 through the DCT-II of both axes (FP32 FFTs "
-               "in shared memory, two grid barriers per application)")
+               "in shared memory, two grid barriers per application), iterative "
+               "refinement with double-float residuals")
     elif PRECOND[0] in ("multigrid", "default", "spectral"):
         pre = ("geometric multigrid V(1,1)-cycle (damped Jacobi, bilinear "
                "prolongation, restriction its transpose)")
